@@ -1,0 +1,281 @@
+/*
+ * rd_chain.h - C ABI of the GB300 radar chain.
+ *
+ * The chain is the bit-exact fixed-point pipeline that the reference model
+ * (fpga-professional-association/agilex-7-radar-detect, directory model/cpp)
+ * computes block by block and that rtl/top/benchmark_sim_top.sv wires
+ * together:
+ *
+ *   ADC -> polyphase FIR bank -> radix-2^2 FFT -> history / corner turn
+ *       -> bin alignment -> beamforming -> power + covariance -> CA/GO-CFAR
+ *       -> 176-bit detection events -> packet flits
+ *
+ * Every entry point computes on one GB300 (sm_103a) with hand-written CUDA
+ * kernels. There is no CPU fallback: when no device is usable the call returns
+ * RD_EDEVICE. Plain C types only; no exceptions cross this boundary.
+ *
+ * Conventions
+ *   - Samples are complex Q1.15 packed in one 32-bit word, real part in the
+ *     low half, imaginary in the high half (model/cpp/fxp/fxp.hpp:288-297,
+ *     fxp::Complex::packed).
+ *   - Flags are packed {sat_pos<<1 | sat_neg} (model/cpp/fxp/fxp.hpp:148-150).
+ *   - One host thread per rd_chain handle; several handles may coexist.
+ *   - rd_last_error() returns a thread-local description of the last failure.
+ */
+#ifndef RD_CHAIN_H_
+#define RD_CHAIN_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef uint32_t rd_cplx16; /* packed {im, re}, re in bits 15:0 */
+
+typedef enum rd_status {
+  RD_OK = 0,
+  RD_EINVAL = 1,    /* bad argument or geometry */
+  RD_ENOMEM = 2,    /* device memory or admission budget refused */
+  RD_ETIMEOUT = 3,  /* a bounded device wait gave up */
+  RD_EDEVICE = 4,   /* no usable CUDA device, or a CUDA call failed */
+  RD_ETRUNC = 5,    /* an output buffer was too small; counts say how much */
+  RD_EAGAIN = 6     /* request not finished yet (rd_chain_poll) */
+} rd_status;
+
+/* CFAR (model/cpp/cfar/cfar_model.hpp:89-90) */
+enum { RD_CFAR_CA = 0, RD_CFAR_GO = 1 };
+enum { RD_CFAR_EVENTS = 0, RD_CFAR_DENSE = 1 };
+/* CFAR event kinds (model/cpp/cfar/cfar_model.hpp:92-97) */
+enum { RD_EV_DETECT = 0, RD_EV_BIN = 1, RD_EV_SUPPRESSED = 2, RD_EV_SUMMARY = 3 };
+
+/* Covariance source vector and integrator mode
+ * (model/cpp/covariance/covar_model.hpp:157). */
+enum { RD_COV_OFF = 0, RD_COV_CHANNEL = 1, RD_COV_BEAM = 2 };
+enum { RD_COV_BLOCK = 0, RD_COV_EXP = 1 };
+
+/* Form of the beamforming / covariance contraction. Both are bit-exact. */
+enum { RD_FORM_CUDA_CORE = 0, RD_FORM_TENSOR = 1 };
+
+/* Stream geometry and block configuration. Zero-initialise, then fill;
+ * rd_config_default() gives the values the reference's defaults imply. */
+typedef struct rd_config {
+  uint32_t n_chan;       /* C antennas (ADC channels), 1..128 */
+  uint32_t n_fft;        /* N: FFT size = PFB phases, power of two, 8..1024 */
+  uint32_t taps;         /* T: PFB taps per phase, 1..64 */
+  uint32_t spc;          /* FFT samples per cycle = history lanes: 1 or 2 */
+  uint32_t scale_sched;  /* FFT per-sub-stage shift mask (fft_ref.hpp:155) */
+  uint32_t hist_frames;  /* H: history depth, power of two, >= 4 */
+  uint32_t n_beams;      /* B: beams, 1..128 */
+  /* CFAR (cfar_model.hpp:112-128) */
+  uint32_t cfar_enable;
+  uint32_t cfar_mode;     /* RD_CFAR_CA / RD_CFAR_GO */
+  uint32_t cfar_out_mode; /* RD_CFAR_EVENTS / RD_CFAR_DENSE */
+  uint32_t guard_lead, guard_lag, ref_lead, ref_lag;
+  uint32_t alpha;         /* UQ8.8 threshold multiplier */
+  uint32_t max_guard, max_ref; /* elaborated maxima (clamp_config) */
+  /* covariance (covar_model.hpp:159-169) */
+  uint32_t cov_source;    /* RD_COV_* */
+  uint32_t cov_mode;      /* RD_COV_BLOCK / RD_COV_EXP */
+  uint32_t cov_exp_k;     /* 0..15 */
+  uint32_t cov_window;    /* window length in frames (0 behaves as 1) */
+  uint32_t cov_acc_w;     /* integrator width in bits, 33..64 */
+  uint32_t cov_n_pairs;   /* 0: every (i<=j) pair of the source vector */
+  /* packets (packet_model.hpp:74-127) */
+  uint32_t packet_w;      /* payload bits per flit, 64..512, multiple of 32 */
+  uint32_t src_id, dest, vc;
+  /* engine */
+  uint32_t max_frames;    /* frames per internal launch (sizes device state) */
+  uint32_t form;          /* RD_FORM_* for beamforming and covariance */
+} rd_config;
+
+/* One CFAR event as the chain emits it. w[] holds the 176-bit event of
+ * model/cpp/cfar/cfar_model.hpp:75-84, little endian, bits 176..191 zero:
+ * kind[1:0] bin[17:2] frame_id[33:18] ref_cnt[40:34] alpha[56:41]
+ * det[72:57] sup[88:73] cut_power[128:89] noise_sum[175:129]. */
+typedef struct rd_event {
+  uint64_t w[3];
+  uint32_t frame;   /* stream frame index the event belongs to */
+  uint16_t beam;    /* beam (CFAR instance) that produced it */
+  uint8_t kind;     /* RD_EV_* (also bits 1:0 of w[0]) */
+  uint8_t framing;  /* bit0 sof, bit1 eof (cfar_model.hpp:190-192) */
+} rd_event;
+
+/* Header of one closed covariance window (covar_model.hpp:171-184). The
+ * accumulators of every (bin, pair) of the window are stored separately. */
+typedef struct rd_cov_window {
+  uint32_t window_id;     /* 16-bit window counter */
+  uint32_t sample_count;  /* samples in the window */
+  uint32_t end_frame;     /* stream frame that closed the window */
+  uint8_t flushed;
+  uint8_t truncated;
+  uint8_t sat_flags;      /* OR of every integrator step's flags in it */
+  uint8_t pad;
+} rd_cov_window;
+
+/* Results of one process call. Every pointer may be NULL (that output is
+ * skipped); counts are always filled. When a capacity is too small the call
+ * fills what fits and returns RD_ETRUNC. */
+typedef struct rd_output {
+  rd_event* events;       uint64_t cap_events;   uint64_t n_events;
+  uint32_t* flits;        uint64_t cap_flits;    uint64_t n_flits;
+  /* flit f occupies flit_words u32 words starting at flits[f*flit_words] */
+  uint32_t flit_words;
+  rd_cov_window* cov_windows; uint32_t cap_cov_windows; uint32_t n_cov_windows;
+  /* [cap_cov_windows][n_fft][n_pairs][2] int64 (re, im) */
+  int64_t* cov_acc;
+  /* optional per-frame taps, [n_frames] outer: */
+  rd_cplx16* tap_pfb;      /* [frames][C][N] PFB output, phase order */
+  rd_cplx16* tap_spectrum; /* [frames][N][C] natural-bin spectra (history) */
+  rd_cplx16* tap_beams;    /* [frames][B][N] beamformer output */
+  uint32_t* tap_power;     /* [frames][B][N] power cells (<= 2^31) */
+  uint64_t n_frames;       /* frames processed by this call */
+} rd_output;
+
+/* Cumulative per-stream statistics. */
+typedef struct rd_stats {
+  uint64_t frames;
+  uint32_t pfb_flags;        /* OR over every PFB output */
+  uint64_t pfb_sat_samples;  /* PFB outputs with any flag set */
+  uint32_t fft_stage_flags[11]; /* OR per FFT sub-stage (fft_ref.hpp:230) */
+  uint32_t bf_flags;
+  uint64_t bf_sat_samples;
+  uint32_t cov_flags;
+  uint64_t cov_sat_steps;
+  /* history (history_model.hpp:364-384) */
+  uint32_t hist_frames_done, hist_write_beats, hist_reads, hist_collisions;
+  uint32_t hist_errors, hist_overwrites, hist_skew;
+  /* align (align_model.hpp:209-215) */
+  uint32_t align_beats, align_missing, align_dup, align_orphan, align_timeout;
+  uint32_t align_fault;
+  /* CFAR */
+  uint64_t cfar_det, cfar_sup, cfar_frames;
+  /* packets */
+  uint64_t packets, flits;
+  uint32_t next_seq;         /* per-VC packet sequence number (16 bits) */
+} rd_stats;
+
+typedef struct rd_chain rd_chain;
+
+/* ---- configuration ------------------------------------------------------ */
+void rd_config_default(rd_config* cfg);
+rd_status rd_config_validate(const rd_config* cfg);
+uint32_t rd_flit_words(uint32_t packet_w);           /* ceil((W+5)/32) */
+uint32_t rd_detection_flits(uint32_t packet_w);       /* 1 + ceil(176/W) */
+uint32_t rd_cov_pairs(const rd_config* cfg);          /* pairs in the table */
+
+/* ---- chain lifecycle (replaces composing model/cpp block objects by hand:
+ *      pfb::PfbModel pfb_model.hpp:207, fft::Engine fft_ref.hpp:246,
+ *      hist::Model history_model.hpp:191, algn::Model align_model.hpp:207,
+ *      bf::BeamformerModel beamformer_model.hpp:255, covar::Integrator
+ *      covar_model.hpp:186, cfar::run_frame cfar_model.hpp:295) ---------- */
+rd_status rd_chain_create(const rd_config* cfg, rd_chain** out);
+void rd_chain_destroy(rd_chain* ch);
+
+/* PFB coefficients, n_fft*taps, phase-major tap-minor (pfb_model.hpp:108).
+ * Takes effect at the next frame; the delay lines are kept, as
+ * pfb::PfbModel::swap_coeff does (pfb_model.hpp:229-233). */
+rd_status rd_chain_set_coeff(rd_chain* ch, const rd_cplx16* coeff);
+/* Beam weights, n_beams*n_chan, beam-major (beamformer_model.hpp:137-139).
+ * Takes effect at the next frame (BeamformerModel::swap_weights :276). */
+rd_status rd_chain_set_weights(rd_chain* ch, const rd_cplx16* w);
+/* Covariance pair table (covar_model.hpp:306-309): x[i], y[i] index the
+ * source vector. Only legal before the first frame. */
+rd_status rd_chain_set_pairs(rd_chain* ch, const uint32_t* x, const uint32_t* y,
+                             uint32_t n_pairs);
+
+/* Process n samples per channel (a multiple of n_fft) from HOST memory laid
+ * out [n_chan][ld]. Copies in, runs, copies the results out. Synchronous. */
+rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n,
+                           uint64_t ld, rd_output* out);
+
+/* The same on DEVICE memory, asynchronous on `stream` (a cudaStream_t, NULL
+ * for the legacy default stream). Results stay on the device until
+ * rd_chain_fetch(). */
+rd_status rd_chain_process_device(rd_chain* ch, const rd_cplx16* adc_dev,
+                                  uint64_t n, uint64_t ld, void* stream);
+/* Copies the results of the last rd_chain_process_device to the host. */
+rd_status rd_chain_fetch(rd_chain* ch, rd_output* out);
+/* Number of kernels the last process call launched. */
+uint64_t rd_chain_last_launches(const rd_chain* ch);
+
+/* Emits every open covariance window as a flushed, truncated result
+ * (covar::Integrator::step with flush=1, covar_model.hpp:226-249). */
+rd_status rd_chain_flush_cov(rd_chain* ch, rd_output* out);
+
+rd_status rd_chain_stats(const rd_chain* ch, rd_stats* st);
+
+/* hist::Model::read (history_model.hpp:283-337): the antenna vector of
+ * natural bin `bin`, `frame_off` frames back from the newest complete one. */
+rd_status rd_chain_read_history(rd_chain* ch, uint32_t bin, uint32_t frame_off,
+                                rd_cplx16* vec, uint32_t* frame_id,
+                                uint32_t* flags);
+
+/* ---- per-block entry points (the model/cpp call surface, on the GPU) ---- */
+
+/* pfb::PfbModel::step over `beats` beats (pfb_model.hpp:242-251).
+ * state: [taps-1][phases] delay line, state[k] = x[n-1-k]; updated in place.
+ * flags_out: [beats][phases] bytes, (f_re << 2) | f_im, may be NULL. */
+rd_status rd_pfb_run(uint32_t phases, uint32_t taps, const rd_cplx16* coeff,
+                     rd_cplx16* state, const rd_cplx16* in, uint32_t beats,
+                     rd_cplx16* out, uint8_t* flags_out);
+
+/* fft::transform (fft_ref.hpp:409-412) on `frames` independent frames.
+ * out: beat order, bins: natural order (either may be NULL),
+ * stage_flags: [frames][log2 n_fft] packed flags (may be NULL). */
+rd_status rd_fft_run(uint32_t n_fft, uint32_t spc, uint32_t scale_sched,
+                     int reorder, const rd_cplx16* in, uint32_t frames,
+                     rd_cplx16* out, rd_cplx16* bins, uint8_t* stage_flags);
+
+/* bf::dot / BeamformerModel::step (beamformer_model.hpp:162-179,283-303) for
+ * n_vec antenna vectors x[n_vec][n_ant] -> y[n_vec][n_beams].
+ * acc: [n_vec][n_beams][2] exact accumulators (may be NULL);
+ * flags: [n_vec][n_beams] bytes (f_re << 2) | f_im (may be NULL). */
+rd_status rd_bf_run(uint32_t n_ant, uint32_t n_beams, const rd_cplx16* w,
+                    const rd_cplx16* x, uint64_t n_vec, rd_cplx16* y,
+                    int64_t* acc, uint8_t* flags, uint32_t form);
+
+/* covar::power and covar::cross_power (covar_model.hpp:99-151) elementwise:
+ * power[i] = |x[i]|^2, cross[i] = x[i] * conj(y[i]) as (re, im) int64. */
+rd_status rd_power_run(const rd_cplx16* x, uint64_t n, int64_t* power);
+rd_status rd_cross_power_run(const rd_cplx16* x, const rd_cplx16* y, uint64_t n,
+                             int64_t* cross);
+
+/* cfar::run_frame (cfar_model.hpp:295-340) on `frames` frames of n cells
+ * each (raw signed power, clamped as clamp_cell does). Events of frame i
+ * carry frame_ids[i]; beam field = frame index i. */
+rd_status rd_cfar_run(const int64_t* cells, uint32_t n, uint32_t frames,
+                      const rd_config* cfg, const uint32_t* frame_ids,
+                      rd_event* events, uint64_t cap, uint64_t* n_events);
+
+/* Detection packet flits for n events (packet_model.hpp:122-260 and the DMA
+ * tap of rtl/top/benchmark_sim_top.sv:1818-1936): header flit then payload
+ * flits LS word first; seq = (seq0 + i) mod 2^16. */
+rd_status rd_packetize(const rd_event* ev, uint64_t n, uint32_t packet_w,
+                       uint32_t src_id, uint32_t dest, uint32_t vc,
+                       uint32_t seq0, uint32_t* flits);
+
+/* fxp primitives (model/cpp/fxp/fxp_ops.hpp:109-177) evaluated on the GPU:
+ * op codes RD_OP_*; a, b, y int64; sh, w unsigned; flags packed. */
+enum {
+  RD_OP_SAT = 0, RD_OP_TRUNC, RD_OP_ROUND_EVEN, RD_OP_ROUND_HALF_UP,
+  RD_OP_ROUND, RD_OP_ROUND_SAT, RD_OP_ADD_SAT, RD_OP_SUB_SAT, RD_OP_NEG_SAT,
+  RD_OP_MUL_Q15, RD_OP_MUL_Q15_RS, RD_OP_CMUL_RE, RD_OP_CMUL_IM,
+  RD_OP_ACC_W, RD_OP_GROWTH_BITS
+};
+rd_status rd_fxp_apply(const uint32_t* op, const int64_t* a, const int64_t* b,
+                       const uint32_t* sh, const uint32_t* w, uint64_t n,
+                       int64_t* y, uint8_t* flags);
+
+/* ---- diagnostics ---------------------------------------------------------- */
+const char* rd_last_error(void);
+/* 1 when a usable sm_100+ device is present. */
+int rd_device_ok(void);
+const char* rd_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RD_CHAIN_H_ */
