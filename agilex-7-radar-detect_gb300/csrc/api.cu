@@ -1,0 +1,1029 @@
+// api.cu - the C ABI of include/rd_chain.h: chain state, the launch sequence
+// per chunk of frames, the history / align bookkeeping that needs no device
+// work, and the per-block entry points.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "fxp.cuh"
+#include "rd_internal.h"
+
+using namespace rd;
+
+namespace {
+
+thread_local std::string g_err;
+
+rd_status fail(rd_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return st;
+}
+
+#define CK(call)                                                                    \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess)                                                          \
+      return fail(RD_EDEVICE, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                  __FILE__, __LINE__);                                              \
+  } while (0)
+
+bool is_pow2(uint32_t v) { return v && !(v & (v - 1)); }
+
+void sat_bump(uint32_t* c, uint64_t by) {
+  const uint64_t v = (uint64_t)*c + by;
+  *c = v > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)v;
+}
+
+unsigned clog2(unsigned v) {
+  unsigned w = 0;
+  while ((1u << w) < v) ++w;
+  return w;
+}
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t want) {
+    if (want <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(want, 1) * sizeof(T));
+    if (e == cudaSuccess) n = std::max<size_t>(want, 1);
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host mirror of the history model's state machine (history_model.hpp:191-467)
+// for the chain's write pattern: every antenna writes one whole frame, in
+// order, then the align stage reads every bin at frame_off 0. Only the
+// counters and pointers live here; the samples live in the device ring.
+// ---------------------------------------------------------------------------
+struct HistMirror {
+  unsigned n_ant = 0, n = 0, lanes = 1, frames_max = 4, depth = 4;
+  uint32_t frames_done = 0;
+  unsigned done_slot = 0;
+  uint32_t c_overwrite = 0, c_skew = 0, c_wbeat = 0, c_read = 0, c_collision = 0, c_error = 0;
+
+  unsigned readable() const {
+    const unsigned dm2 = depth <= 2 ? 0u : depth - 2u;
+    return frames_done >= dm2 ? dm2 : (unsigned)frames_done;
+  }
+  // every antenna finished the next frame (write_beat x M each, then settle_)
+  void write_frame() {
+    sat_bump(&c_wbeat, (uint64_t)n_ant * (n / lanes));
+    if (frames_done >= depth) sat_bump(&c_overwrite, 1);
+    frames_done += 1;
+    if (frames_done != 1) done_slot = (done_slot + 1 == depth) ? 0u : done_slot + 1u;
+  }
+  struct Read {
+    unsigned slot;
+    uint32_t frame_id;
+    unsigned flags;
+    bool valid_data;
+  };
+  // read() (history_model.hpp:283-337) without touching the counters
+  Read locate(unsigned bin, unsigned frame_off) const {
+    const unsigned depth_mask = (1u << clog2(frames_max + 1)) - 1u;
+    unsigned slot_w = clog2(frames_max);
+    if (slot_w == 0) slot_w = 1;
+    const unsigned slot_mask = (1u << slot_w) - 1u;
+    const unsigned ext_mask = (1u << (slot_w + 1)) - 1u;
+    const unsigned bin_p = bin & 0xFFFFu, off_p = frame_off & 0xFFFFu;
+    const unsigned rd = readable();
+    const bool oor = (bin_p >= n) || (rd == 0) || (off_p >= rd);
+    const unsigned off_clamped = rd == 0 ? 0u : rd - 1u;
+    const unsigned off_safe = oor ? off_clamped : (off_p & depth_mask);
+    const unsigned off_ext = off_safe & ext_mask, done_ext = done_slot & ext_mask;
+    const unsigned slot = (done_ext >= off_ext) ? ((done_ext - off_ext) & slot_mask)
+                                                : (((done_ext - off_ext + depth) & ext_mask) & slot_mask);
+    const unsigned write_slot = (done_slot + 1 == depth) ? 0u : (done_slot + 1) & slot_mask;
+    const bool collision = (frames_done != 0) && (slot == write_slot);
+    const uint32_t fid = (uint32_t)(frames_done - 1u - off_safe);
+    const bool stale = (uint32_t)(frames_done - fid) > depth;
+    Read r;
+    r.slot = slot;
+    r.frame_id = fid;
+    r.flags = (oor ? 1u : 0u) | (collision ? 2u : 0u) | (stale ? 4u : 0u);
+    r.valid_data = frames_done != 0;
+    return r;
+  }
+  void count_reads(unsigned flags, uint64_t k) {
+    sat_bump(&c_read, k);
+    if (flags & 2u) sat_bump(&c_collision, k);
+    if (flags & 1u) sat_bump(&c_error, k);
+  }
+};
+
+namespace {
+struct Scratch {
+  std::vector<void*> ptrs;
+  ~Scratch() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  template <typename T>
+  cudaError_t alloc(T** p, size_t n) {
+    cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T));
+    if (e == cudaSuccess) ptrs.push_back(*p);
+    return e;
+  }
+};
+}  // namespace
+
+struct rd_chain {
+  rd_config cfg;
+  uint32_t R = 0;            // ring frames
+  uint32_t S = 0, P = 0;     // covariance source length, pairs
+  bool pairs_custom = false;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+
+  DevBuf<uint32_t> coeff_t, weights, tail[2], ring, power, beams_bn, stage;
+  int tail_cur = 0;
+  DevBuf<uint32_t> px, py;
+  DevBuf<long long> acc_re, acc_im, cov_out;
+  DevBuf<unsigned> sticky, satcnt, win_flags;
+  DevBuf<uint32_t> counts, detsup, mask;
+  DevBuf<unsigned long long> offsets;
+  DevBuf<rd_event> events;
+  DevBuf<uint32_t> flits;
+  DevBuf<uint32_t> tap_pfb;
+  DevBuf<DevStats> stats;
+
+  // host-side state
+  uint64_t frame = 0;        // frames processed so far
+  uint32_t cov_count = 0;    // samples in the open covariance window
+  uint32_t cov_window_id = 0;
+  HistMirror hist;
+  rd_stats host_st{};        // host-owned counters (history, align, packets)
+  uint32_t align_seq = 0;
+  // results of the last call
+  uint64_t call_frames = 0;
+  std::vector<rd_cov_window> call_windows;
+  uint64_t call_cap_events = 0;
+  uint64_t launches = 0;
+};
+
+extern "C" {
+
+const char* rd_last_error(void) { return g_err.c_str(); }
+const char* rd_version(void) { return "rdgb 0.1 sm_103a"; }
+
+int rd_device_ok(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return 0;
+  }
+  int dev = 0, major = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  return major >= 10 ? 1 : 0;
+}
+
+void rd_config_default(rd_config* c) {
+  std::memset(c, 0, sizeof(*c));
+  c->n_chan = 4;
+  c->n_fft = 64;
+  c->taps = 4;
+  c->spc = 2;
+  c->scale_sched = 0xFFFFFFFFu;
+  c->hist_frames = 8;
+  c->n_beams = 2;
+  c->cfar_enable = 1;  // cfar_model.hpp:112-128 defaults
+  c->cfar_mode = RD_CFAR_CA;
+  c->cfar_out_mode = RD_CFAR_EVENTS;
+  c->guard_lead = c->guard_lag = 2;
+  c->ref_lead = c->ref_lag = 8;
+  c->alpha = 1u << 8;
+  c->max_guard = 2;
+  c->max_ref = 8;
+  c->cov_source = RD_COV_CHANNEL;
+  c->cov_mode = RD_COV_BLOCK;
+  c->cov_window = 256;
+  c->cov_acc_w = 64;
+  c->packet_w = 64;
+  c->max_frames = 1024;
+  c->form = RD_FORM_CUDA_CORE;
+}
+
+uint32_t rd_flit_words(uint32_t packet_w) { return (packet_w + 5u + 31u) / 32u; }
+uint32_t rd_detection_flits(uint32_t packet_w) {
+  return packet_w ? 1u + (176u + packet_w - 1u) / packet_w : 0u;
+}
+
+uint32_t rd_cov_pairs(const rd_config* c) {
+  if (c->cov_source == RD_COV_OFF) return 0;
+  if (c->cov_n_pairs) return c->cov_n_pairs;
+  const uint32_t s = c->cov_source == RD_COV_CHANNEL ? c->n_chan : c->n_beams;
+  return s * (s + 1) / 2;
+}
+
+rd_status rd_config_validate(const rd_config* c) {
+  if (!c) return fail(RD_EINVAL, "null config");
+  if (c->n_chan < 1 || c->n_chan > 128) return fail(RD_EINVAL, "n_chan %u not in 1..128", c->n_chan);
+  if (c->n_beams < 1 || c->n_beams > 128) return fail(RD_EINVAL, "n_beams %u not in 1..128", c->n_beams);
+  if (!is_pow2(c->n_fft) || c->n_fft < 8 || c->n_fft > 1024)
+    return fail(RD_EINVAL, "n_fft %u must be a power of two in 8..1024", c->n_fft);
+  if (c->spc != 1 && c->spc != 2) return fail(RD_EINVAL, "spc %u must be 1 or 2", c->spc);
+  if (c->n_fft / c->spc < 4) return fail(RD_EINVAL, "n_fft/spc must be >= 4");
+  if (c->taps < 1 || c->taps > 64) return fail(RD_EINVAL, "taps %u not in 1..64", c->taps);
+  if (!is_pow2(c->hist_frames) || c->hist_frames < 4 || c->hist_frames > 65536)
+    return fail(RD_EINVAL, "hist_frames %u must be a power of two >= 4", c->hist_frames);
+  if (c->packet_w < 64 || c->packet_w > 512 || (c->packet_w % 32) != 0)
+    return fail(RD_EINVAL, "packet_w %u must be a multiple of 32 in 64..512", c->packet_w);
+  if (c->max_guard > 31 || c->max_ref > 63) return fail(RD_EINVAL, "CFAR maxima out of range");
+  if (c->cov_source > RD_COV_BEAM || c->cov_mode > RD_COV_EXP)
+    return fail(RD_EINVAL, "bad covariance source/mode");
+  if (c->cov_source != RD_COV_OFF) {
+    if (c->cov_acc_w < 33 || c->cov_acc_w > 64) return fail(RD_EINVAL, "cov_acc_w must be 33..64");
+    if (c->cov_exp_k > 15) return fail(RD_EINVAL, "cov_exp_k must be 0..15");
+    if (c->cov_window > 65535) return fail(RD_EINVAL, "cov_window must fit 16 bits");
+  }
+  if (c->max_frames < 1 || c->max_frames > 65536) return fail(RD_EINVAL, "max_frames 1..65536");
+  if (c->form > RD_FORM_TENSOR) return fail(RD_EINVAL, "bad form");
+  if (c->vc > 3 || c->src_id > 31 || c->dest > 15) return fail(RD_EINVAL, "packet header field out of range");
+  return RD_OK;
+}
+
+static rd_status upload_pairs(rd_chain* ch, const uint32_t* x, const uint32_t* y, uint32_t n) {
+  CK(ch->px.ensure(n));
+  CK(ch->py.ensure(n));
+  CK(cudaMemcpy(ch->px.p, x, n * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ch->py.p, y, n * 4, cudaMemcpyHostToDevice));
+  const size_t k = (size_t)ch->cfg.n_fft * n;
+  CK(ch->acc_re.ensure(k));
+  CK(ch->acc_im.ensure(k));
+  CK(ch->sticky.ensure(k));
+  CK(ch->satcnt.ensure(2 * k));
+  CK(cudaMemset(ch->acc_re.p, 0, k * 8));
+  CK(cudaMemset(ch->acc_im.p, 0, k * 8));
+  CK(cudaMemset(ch->sticky.p, 0, k * 4));
+  CK(cudaMemset(ch->satcnt.p, 0, k * 8));
+  ch->P = n;
+  return RD_OK;
+}
+
+rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
+  if (!out) return fail(RD_EINVAL, "null out");
+  *out = nullptr;
+  rd_status st = rd_config_validate(cfg);
+  if (st != RD_OK) return st;
+  if (!rd_device_ok()) return fail(RD_EDEVICE, "no CUDA device of compute capability 10.x or newer");
+  rd_chain* ch = new rd_chain();
+  ch->cfg = *cfg;
+  const rd_config& c = ch->cfg;
+  const uint32_t N = c.n_fft, C = c.n_chan, B = c.n_beams, T = c.taps, F = c.max_frames;
+  ch->R = F + c.hist_frames;
+  auto bad = [&](cudaError_t e) {
+    if (e == cudaSuccess) return false;
+    fail(e == cudaErrorMemoryAllocation ? RD_ENOMEM : RD_EDEVICE, "allocation failed: %s",
+         cudaGetErrorString(e));
+    return true;
+  };
+  const uint32_t D = T > 1 ? T - 1 : 1;
+  if (bad(cudaStreamCreateWithFlags(&ch->stream, cudaStreamNonBlocking)) ||
+      bad(ch->coeff_t.ensure((size_t)T * N)) || bad(ch->weights.ensure((size_t)B * C)) ||
+      bad(ch->tail[0].ensure((size_t)C * D * N)) || bad(ch->tail[1].ensure((size_t)C * D * N)) ||
+      bad(ch->ring.ensure((size_t)ch->R * N * C)) || bad(ch->power.ensure((size_t)F * B * N)) ||
+      bad(ch->counts.ensure((size_t)F * B)) || bad(ch->detsup.ensure((size_t)F * B * 2)) ||
+      bad(ch->mask.ensure((size_t)F * B * ((N + 31) / 32))) ||
+      bad(ch->offsets.ensure((size_t)F * B)) || bad(ch->stats.ensure(1))) {
+    rd_chain_destroy(ch);
+    return RD_ENOMEM;
+  }
+  ch->own_stream = true;
+  cudaMemset(ch->coeff_t.p, 0, (size_t)T * N * 4);
+  cudaMemset(ch->weights.p, 0, (size_t)B * C * 4);
+  cudaMemset(ch->tail[0].p, 0, (size_t)C * D * N * 4);
+  cudaMemset(ch->tail[1].p, 0, (size_t)C * D * N * 4);
+  cudaMemset(ch->ring.p, 0, (size_t)ch->R * N * C * 4);
+  cudaMemset(ch->stats.p, 0, sizeof(DevStats));
+  if (c.cov_source != RD_COV_OFF) {
+    ch->S = c.cov_source == RD_COV_CHANNEL ? C : B;
+    const uint32_t np = rd_cov_pairs(&c);
+    std::vector<uint32_t> x, y;
+    for (uint32_t i = 0; i < ch->S; ++i)
+      for (uint32_t j = i; j < ch->S; ++j) {
+        x.push_back(i);
+        y.push_back(j);
+      }
+    x.resize(np);
+    y.resize(np);
+    st = upload_pairs(ch, x.data(), y.data(), np);
+    if (st != RD_OK) {
+      rd_chain_destroy(ch);
+      return st;
+    }
+    if (c.cov_source == RD_COV_BEAM && bad(ch->beams_bn.ensure((size_t)F * N * B))) {
+      rd_chain_destroy(ch);
+      return RD_ENOMEM;
+    }
+  }
+  ch->hist.n_ant = C;
+  ch->hist.n = N;
+  ch->hist.lanes = c.spc;
+  ch->hist.frames_max = c.hist_frames;
+  ch->hist.depth = c.hist_frames;
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    rd_chain_destroy(ch);
+    return fail(RD_EDEVICE, "device sync failed at create");
+  }
+  *out = ch;
+  return RD_OK;
+}
+
+void rd_chain_destroy(rd_chain* ch) {
+  if (!ch) return;
+  if (ch->stream) cudaStreamSynchronize(ch->stream);
+  ch->coeff_t.release(); ch->weights.release(); ch->tail[0].release(); ch->tail[1].release();
+  ch->ring.release(); ch->power.release(); ch->beams_bn.release(); ch->stage.release();
+  ch->px.release(); ch->py.release(); ch->acc_re.release(); ch->acc_im.release();
+  ch->cov_out.release(); ch->sticky.release(); ch->satcnt.release(); ch->win_flags.release();
+  ch->counts.release(); ch->detsup.release(); ch->mask.release(); ch->offsets.release();
+  ch->events.release(); ch->flits.release(); ch->tap_pfb.release(); ch->stats.release();
+  if (ch->own_stream && ch->stream) cudaStreamDestroy(ch->stream);
+  delete ch;
+}
+
+rd_status rd_chain_set_coeff(rd_chain* ch, const rd_cplx16* coeff) {
+  if (!ch || !coeff) return fail(RD_EINVAL, "null argument");
+  const uint32_t N = ch->cfg.n_fft, T = ch->cfg.taps;
+  std::vector<uint32_t> t((size_t)T * N);
+  for (uint32_t p = 0; p < N; ++p)
+    for (uint32_t k = 0; k < T; ++k) t[(size_t)k * N + p] = coeff[(size_t)p * T + k];
+  CK(cudaMemcpyAsync(ch->coeff_t.p, t.data(), t.size() * 4, cudaMemcpyHostToDevice, ch->stream));
+  CK(cudaStreamSynchronize(ch->stream));
+  return RD_OK;
+}
+
+rd_status rd_chain_set_weights(rd_chain* ch, const rd_cplx16* w) {
+  if (!ch || !w) return fail(RD_EINVAL, "null argument");
+  CK(cudaMemcpyAsync(ch->weights.p, w, (size_t)ch->cfg.n_beams * ch->cfg.n_chan * 4,
+                     cudaMemcpyHostToDevice, ch->stream));
+  CK(cudaStreamSynchronize(ch->stream));
+  return RD_OK;
+}
+
+rd_status rd_chain_set_pairs(rd_chain* ch, const uint32_t* x, const uint32_t* y, uint32_t n) {
+  if (!ch || !x || !y || n == 0) return fail(RD_EINVAL, "null argument");
+  if (ch->cfg.cov_source == RD_COV_OFF) return fail(RD_EINVAL, "covariance is off");
+  if (ch->frame != 0) return fail(RD_EINVAL, "pairs can only be set before the first frame");
+  for (uint32_t i = 0; i < n; ++i)
+    if (x[i] >= ch->S || y[i] >= ch->S) return fail(RD_EINVAL, "pair %u out of range", i);
+  ch->pairs_custom = true;
+  return upload_pairs(ch, x, y, n);
+}
+
+__global__ void k_call_begin(DevStats* s) { s->events_call = 0; }
+__global__ void k_call_end(DevStats* s) {
+  s->scan_scratch[0] = s->events_call;  // events of the call just finished
+  s->events_total += s->events_call;
+}
+
+// Launch sequence for one chunk of F frames whose channel-c samples start at
+// adc + c*ld. tap_pfb (device) is optional.
+static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint32_t F,
+                           uint32_t* d_tap_pfb) {
+  const rd_config& c = ch->cfg;
+  const uint32_t N = c.n_fft, C = c.n_chan, B = c.n_beams;
+  cudaStream_t s = ch->stream;
+  DevStats* st = ch->stats.p;
+
+  FrontParams fp{};
+  fp.adc = adc;
+  fp.ld = ld;
+  fp.tail = ch->tail[ch->tail_cur].p;
+  fp.coeff_t = ch->coeff_t.p;
+  fp.ring = ch->ring.p;
+  fp.ring_frames = ch->R;
+  fp.g0 = ch->frame;
+  fp.tap_pfb = d_tap_pfb;
+  fp.F = F;
+  fp.C = C;
+  fp.N = N;
+  fp.T = c.taps;
+  fp.spc = c.spc;
+  fp.sched = c.scale_sched;
+  fp.stats = st;
+  launch_front(fp, s);
+  launch_tail_update(adc, ld, ch->tail[ch->tail_cur].p, ch->tail[ch->tail_cur ^ 1].p, F, C, N,
+                     c.taps, s);
+  ch->tail_cur ^= (c.taps > 1) ? 1 : 0;
+  ch->launches += (c.taps > 1) ? 2 : 1;
+
+  BeamParams bp{};
+  bp.ring = ch->ring.p;
+  bp.ring_frames = ch->R;
+  bp.g0 = ch->frame;
+  bp.weights = ch->weights.p;
+  bp.power = ch->power.p;
+  bp.beams_bn = ch->beams_bn.p;
+  bp.F = F;
+  bp.C = C;
+  bp.N = N;
+  bp.B = B;
+  bp.stats = st;
+  launch_beam(bp, s);
+  ch->launches++;
+
+  if (c.cov_source != RD_COV_OFF && ch->P) {
+    const uint32_t wl = c.cov_window ? c.cov_window : 1u;
+    const uint32_t n_win = (ch->cov_count + F) / wl;
+    const uint32_t w0 = (uint32_t)ch->call_windows.size();
+    CovParams cp{};
+    cp.ring = ch->ring.p;
+    cp.ring_frames = ch->R;
+    cp.g0 = ch->frame;
+    cp.beams_bn = ch->beams_bn.p;
+    cp.S = ch->S;
+    cp.src_beam = c.cov_source == RD_COV_BEAM;
+    cp.px = ch->px.p;
+    cp.py = ch->py.p;
+    cp.P = ch->P;
+    cp.F = F;
+    cp.N = N;
+    cp.acc_re = ch->acc_re.p;
+    cp.acc_im = ch->acc_im.p;
+    cp.sticky = ch->sticky.p;
+    cp.satcnt = ch->satcnt.p;
+    cp.count0 = ch->cov_count;
+    cp.wl = wl;
+    cp.exp_mode = c.cov_mode == RD_COV_EXP;
+    cp.exp_k = c.cov_exp_k;
+    cp.acc_w = c.cov_acc_w;
+    const size_t per = (size_t)N * ch->P * 2;
+    cp.out = ch->cov_out.p ? ch->cov_out.p + (size_t)w0 * per : nullptr;
+    cp.win_flags = ch->win_flags.p ? ch->win_flags.p + w0 : nullptr;
+    cp.n_windows = n_win;
+    cp.stats = st;
+    launch_cov(cp, s);
+    ch->launches++;
+    // window headers, known on the host (covar_model.hpp:229-235)
+    uint32_t cnt = ch->cov_count;
+    for (uint32_t f = 0; f < F; ++f) {
+      if (++cnt >= wl) {
+        rd_cov_window h{};
+        h.window_id = ch->cov_window_id;
+        h.sample_count = cnt;
+        h.end_frame = (uint32_t)(ch->frame + f);
+        h.flushed = 0;
+        h.truncated = cnt != wl;
+        ch->call_windows.push_back(h);
+        ch->cov_window_id = (ch->cov_window_id + 1u) & 0xFFFFu;
+        cnt = 0;
+      }
+    }
+    ch->cov_count = cnt;
+  }
+
+  CfarParams fp2{};
+  fp2.power_u32 = ch->power.p;
+  fp2.frames = F * B;
+  fp2.n = N;
+  fp2.beams = B;
+  fp2.g0 = ch->frame;
+  fp2.enable = c.cfar_enable != 0;
+  fp2.go = c.cfar_mode == RD_CFAR_GO;
+  fp2.dense = c.cfar_out_mode == RD_CFAR_DENSE;
+  fp2.gl = std::min(c.guard_lead, c.max_guard);  // clamp_config, cfar_model.hpp:134-141
+  fp2.gg = std::min(c.guard_lag, c.max_guard);
+  fp2.rl = std::min(c.ref_lead, c.max_ref);
+  fp2.rg = std::min(c.ref_lag, c.max_ref);
+  fp2.alpha = c.alpha;
+  fp2.counts = ch->counts.p;
+  fp2.detsup = ch->detsup.p;
+  fp2.mask = ch->mask.p;
+  fp2.offsets = ch->offsets.p;
+  fp2.events = ch->events.p;
+  fp2.cap = ch->call_cap_events;
+  fp2.flits = ch->flits.p;
+  fp2.packet_w = c.packet_w;
+  fp2.src_id = c.src_id;
+  fp2.dest = c.dest;
+  fp2.vc = c.vc;
+  fp2.flit_words = rd_flit_words(c.packet_w);
+  fp2.nfl = rd_detection_flits(c.packet_w);
+  fp2.stats = st;
+  launch_cfar_decide(fp2, s);
+  launch_cfar_scan(fp2, s);
+  launch_cfar_emit(fp2, s);
+  ch->launches += 3;
+
+  // host bookkeeping of the history and align counters, frame by frame
+  for (uint32_t f = 0; f < F; ++f) {
+    ch->hist.write_frame();
+    const HistMirror::Read r = ch->hist.locate(0, 0);
+    ch->hist.count_reads(r.flags, N);
+    sat_bump(&ch->host_st.align_beats, N / 2);
+    ch->align_seq = (ch->align_seq + N / 2) & 0xFFFFu;
+    if (r.flags) ch->host_st.align_fault |= 8u;  // kUserHist (align_model.hpp:343-355)
+  }
+  ch->frame += F;
+  return RD_OK;
+}
+
+static rd_status begin_call(rd_chain* ch, uint64_t frames, uint64_t cap_events) {
+  const rd_config& c = ch->cfg;
+  ch->call_frames = frames;
+  ch->call_windows.clear();
+  ch->launches = 0;
+  const uint64_t worst = frames * c.n_beams * (c.n_fft + 1ull);
+  ch->call_cap_events = std::min<uint64_t>(cap_events, worst);
+  const uint32_t nfl = rd_detection_flits(c.packet_w), words = rd_flit_words(c.packet_w);
+  CK(ch->events.ensure(ch->call_cap_events));
+  CK(ch->flits.ensure(ch->call_cap_events * nfl * words));
+  if (c.cov_source != RD_COV_OFF && ch->P) {
+    const uint32_t wl = c.cov_window ? c.cov_window : 1u;
+    const uint64_t n_win = (ch->cov_count + frames) / wl;
+    const size_t per = (size_t)c.n_fft * ch->P * 2;
+    CK(ch->cov_out.ensure(std::max<uint64_t>(n_win, 1) * per));
+    CK(ch->win_flags.ensure(std::max<uint64_t>(n_win, 1)));
+    CK(cudaMemsetAsync(ch->win_flags.p, 0, std::max<uint64_t>(n_win, 1) * 4, ch->stream));
+  }
+  k_call_begin<<<1, 1, 0, ch->stream>>>(ch->stats.p);
+  ch->launches++;
+  return RD_OK;
+}
+
+static rd_status end_call(rd_chain* ch) {
+  k_call_end<<<1, 1, 0, ch->stream>>>(ch->stats.p);
+  ch->launches++;
+  CK(cudaGetLastError());
+  return RD_OK;
+}
+
+static uint64_t default_cap(const rd_config& c, uint64_t frames) {
+  return frames * c.n_beams * (2ull + c.n_fft / 16u);
+}
+
+rd_status rd_chain_process_device(rd_chain* ch, const rd_cplx16* adc_dev, uint64_t n,
+                                  uint64_t ld, void* stream) {
+  if (!ch || !adc_dev) return fail(RD_EINVAL, "null argument");
+  const rd_config& c = ch->cfg;
+  if (n % c.n_fft) return fail(RD_EINVAL, "n=%llu is not a multiple of n_fft", (unsigned long long)n);
+  if (ld < n) return fail(RD_EINVAL, "ld < n");
+  cudaStream_t user = (cudaStream_t)stream;
+  cudaEvent_t ev_in;
+  if (user) {  // order the chain after the caller's stream
+    CK(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
+    CK(cudaEventRecord(ev_in, user));
+    CK(cudaStreamWaitEvent(ch->stream, ev_in, 0));
+    cudaEventDestroy(ev_in);
+  }
+  const uint64_t frames = n / c.n_fft;
+  rd_status st = begin_call(ch, frames, std::max<uint64_t>(ch->events.n, default_cap(c, frames)));
+  if (st != RD_OK) return st;
+  for (uint64_t f = 0; f < frames; f += c.max_frames) {
+    const uint32_t F = (uint32_t)std::min<uint64_t>(c.max_frames, frames - f);
+    st = run_chunk(ch, adc_dev + f * c.n_fft, ld, F, nullptr);
+    if (st != RD_OK) return st;
+  }
+  st = end_call(ch);
+  if (st != RD_OK) return st;
+  if (user) {  // and the caller's stream after the chain
+    cudaEvent_t ev_out;
+    CK(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming));
+    CK(cudaEventRecord(ev_out, ch->stream));
+    CK(cudaStreamWaitEvent(user, ev_out, 0));
+    cudaEventDestroy(ev_out);
+  }
+  return RD_OK;
+}
+
+uint64_t rd_chain_last_launches(const rd_chain* ch) { return ch ? ch->launches : 0; }
+
+rd_status rd_chain_fetch(rd_chain* ch, rd_output* out) {
+  if (!ch || !out) return fail(RD_EINVAL, "null argument");
+  const rd_config& c = ch->cfg;
+  CK(cudaStreamSynchronize(ch->stream));
+  DevStats ds;
+  CK(cudaMemcpy(&ds, ch->stats.p, sizeof(ds), cudaMemcpyDeviceToHost));
+  const uint64_t n_ev = ds.scan_scratch[0];
+  const uint32_t nfl = rd_detection_flits(c.packet_w), words = rd_flit_words(c.packet_w);
+  bool trunc = n_ev > ch->call_cap_events;
+  const uint64_t avail = std::min<uint64_t>(n_ev, ch->call_cap_events);
+  out->n_events = n_ev;
+  out->n_flits = n_ev * nfl;
+  out->flit_words = words;
+  out->n_frames = ch->call_frames;
+  if (out->events) {
+    const uint64_t k = std::min<uint64_t>(avail, out->cap_events);
+    if (k < n_ev) trunc = true;
+    if (k) CK(cudaMemcpy(out->events, ch->events.p, k * sizeof(rd_event), cudaMemcpyDeviceToHost));
+  }
+  if (out->flits) {
+    const uint64_t k = std::min<uint64_t>(avail, out->cap_flits / nfl);
+    if (k < n_ev) trunc = true;
+    if (k) CK(cudaMemcpy(out->flits, ch->flits.p, k * nfl * words * 4, cudaMemcpyDeviceToHost));
+  }
+  const uint32_t nw = (uint32_t)ch->call_windows.size();
+  out->n_cov_windows = nw;
+  if (nw) {
+    const uint32_t k = std::min<uint32_t>(nw, out->cap_cov_windows);
+    if (k < nw) trunc = true;
+    std::vector<unsigned> wf(nw);
+    CK(cudaMemcpy(wf.data(), ch->win_flags.p, nw * 4, cudaMemcpyDeviceToHost));
+    if (out->cov_windows)
+      for (uint32_t w = 0; w < k; ++w) {
+        out->cov_windows[w] = ch->call_windows[w];
+        out->cov_windows[w].sat_flags = (uint8_t)wf[w];
+      }
+    if (out->cov_acc && k)
+      CK(cudaMemcpy(out->cov_acc, ch->cov_out.p, (size_t)k * c.n_fft * ch->P * 2 * 8,
+                    cudaMemcpyDeviceToHost));
+  }
+  return trunc ? fail(RD_ETRUNC, "output capacity exceeded") : RD_OK;
+}
+
+rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint64_t ld,
+                           rd_output* out) {
+  if (!ch || !adc || !out) return fail(RD_EINVAL, "null argument");
+  const rd_config& c = ch->cfg;
+  if (n % c.n_fft) return fail(RD_EINVAL, "n=%llu is not a multiple of n_fft", (unsigned long long)n);
+  if (ld < n) return fail(RD_EINVAL, "ld < n");
+  const uint32_t N = c.n_fft, C = c.n_chan, B = c.n_beams;
+  const uint64_t frames = n / N;
+  const uint64_t sld = (uint64_t)c.max_frames * N;
+  CK(ch->stage.ensure((size_t)C * sld));
+  const bool taps = out->tap_pfb || out->tap_spectrum || out->tap_beams || out->tap_power;
+  if (taps) {
+    CK(ch->tap_pfb.ensure((size_t)c.max_frames * C * N));
+    if (out->tap_beams && !ch->beams_bn.p) CK(ch->beams_bn.ensure((size_t)c.max_frames * N * B));
+  }
+  const uint64_t cap = out->events ? out->cap_events : default_cap(c, frames);
+  rd_status st = begin_call(ch, frames, std::max<uint64_t>(cap, 1));
+  if (st != RD_OK) return st;
+  std::vector<uint32_t> hb;
+  for (uint64_t f = 0; f < frames; f += c.max_frames) {
+    const uint32_t F = (uint32_t)std::min<uint64_t>(c.max_frames, frames - f);
+    CK(cudaMemcpy2DAsync(ch->stage.p, sld * 4, adc + f * N, ld * 4, (size_t)F * N * 4, C,
+                         cudaMemcpyHostToDevice, ch->stream));
+    const uint64_t g0 = ch->frame;
+    st = run_chunk(ch, ch->stage.p, sld, F, taps ? ch->tap_pfb.p : nullptr);
+    if (st != RD_OK) return st;
+    if (taps) {  // debug taps: copied out chunk by chunk
+      CK(cudaStreamSynchronize(ch->stream));
+      const size_t fcn = (size_t)F * C * N, fbn = (size_t)F * B * N;
+      if (out->tap_pfb)
+        CK(cudaMemcpy(out->tap_pfb + f * C * N, ch->tap_pfb.p, fcn * 4, cudaMemcpyDeviceToHost));
+      if (out->tap_spectrum) {
+        for (uint32_t k = 0; k < F; ++k) {
+          const uint64_t slot = (g0 + k) % ch->R;
+          CK(cudaMemcpy(out->tap_spectrum + (f + k) * N * C, ch->ring.p + slot * N * C,
+                        (size_t)N * C * 4, cudaMemcpyDeviceToHost));
+        }
+      }
+      if (out->tap_power)
+        CK(cudaMemcpy(out->tap_power + f * B * N, ch->power.p, fbn * 4, cudaMemcpyDeviceToHost));
+      if (out->tap_beams && ch->beams_bn.p) {
+        hb.resize(fbn);
+        CK(cudaMemcpy(hb.data(), ch->beams_bn.p, fbn * 4, cudaMemcpyDeviceToHost));
+        for (uint32_t k = 0; k < F; ++k)
+          for (uint32_t b = 0; b < B; ++b)
+            for (uint32_t i = 0; i < N; ++i)
+              out->tap_beams[((f + k) * B + b) * N + i] = hb[((size_t)k * N + i) * B + b];
+      }
+    }
+  }
+  st = end_call(ch);
+  if (st != RD_OK) return st;
+  return rd_chain_fetch(ch, out);
+}
+
+__global__ void k_cov_flush(long long* acc_re, long long* acc_im, unsigned* sticky,
+                            unsigned* satcnt, uint64_t n, long long* out, int emit) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (emit) {
+    out[2 * i] = acc_re[i];
+    out[2 * i + 1] = acc_im[i];
+  }
+  acc_re[i] = 0;
+  acc_im[i] = 0;
+  sticky[i] = 0;
+  satcnt[2 * i] = 0;
+  satcnt[2 * i + 1] = 0;
+}
+__global__ void k_cov_flush_stats(DevStats* s) {
+  s->cov_flags = 0;
+  s->cov_sat_steps = 0;
+}
+
+rd_status rd_chain_flush_cov(rd_chain* ch, rd_output* out) {
+  if (!ch || !out) return fail(RD_EINVAL, "null argument");
+  out->n_cov_windows = 0;
+  const rd_config& c = ch->cfg;
+  if (c.cov_source == RD_COV_OFF || !ch->P) return RD_OK;
+  const uint64_t n = (uint64_t)c.n_fft * ch->P;
+  const bool emit = ch->cov_count != 0;
+  if (emit && out->cap_cov_windows < 1) return fail(RD_ETRUNC, "no room for the flushed window");
+  CK(ch->cov_out.ensure(n * 2));
+  k_cov_flush<<<(unsigned)((n + 255) / 256), 256, 0, ch->stream>>>(
+      ch->acc_re.p, ch->acc_im.p, ch->sticky.p, ch->satcnt.p, n, ch->cov_out.p, emit ? 1 : 0);
+  k_cov_flush_stats<<<1, 1, 0, ch->stream>>>(ch->stats.p);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ch->stream));
+  if (emit) {
+    rd_cov_window h{};
+    const uint32_t wl = c.cov_window ? c.cov_window : 1u;
+    h.window_id = ch->cov_window_id;
+    h.sample_count = ch->cov_count;
+    h.end_frame = (uint32_t)ch->frame;
+    h.flushed = 1;
+    h.truncated = ch->cov_count != wl;
+    if (out->cov_windows) out->cov_windows[0] = h;
+    if (out->cov_acc) CK(cudaMemcpy(out->cov_acc, ch->cov_out.p, n * 16, cudaMemcpyDeviceToHost));
+    out->n_cov_windows = 1;
+  }
+  ch->cov_count = 0;
+  ch->cov_window_id = 0;
+  return RD_OK;
+}
+
+rd_status rd_chain_stats(const rd_chain* ch, rd_stats* st) {
+  if (!ch || !st) return fail(RD_EINVAL, "null argument");
+  CK(cudaStreamSynchronize(ch->stream));
+  DevStats ds;
+  CK(cudaMemcpy(&ds, ch->stats.p, sizeof(ds), cudaMemcpyDeviceToHost));
+  *st = ch->host_st;
+  st->frames = ch->frame;
+  st->pfb_flags = ds.pfb_flags;
+  st->pfb_sat_samples = ds.pfb_sat;
+  for (int g = 0; g < 11; ++g) st->fft_stage_flags[g] = (ds.fft_flags >> (2 * g)) & 3u;
+  st->bf_flags = ds.bf_flags;
+  st->bf_sat_samples = ds.bf_sat;
+  st->cov_flags = ds.cov_flags;
+  st->cov_sat_steps = ds.cov_sat_steps;
+  st->hist_frames_done = ch->hist.frames_done;
+  st->hist_write_beats = ch->hist.c_wbeat;
+  st->hist_reads = ch->hist.c_read;
+  st->hist_collisions = ch->hist.c_collision;
+  st->hist_errors = ch->hist.c_error;
+  st->hist_overwrites = ch->hist.c_overwrite;
+  st->hist_skew = ch->hist.c_skew;
+  st->cfar_det = ds.cfar_det;
+  st->cfar_sup = ds.cfar_sup;
+  st->cfar_frames = ch->frame * ch->cfg.n_beams;
+  st->packets = ds.events_total;
+  st->flits = ds.events_total * rd_detection_flits(ch->cfg.packet_w);
+  st->next_seq = (uint32_t)(ds.events_total & 0xFFFFu);
+  return RD_OK;
+}
+
+rd_status rd_chain_read_history(rd_chain* ch, uint32_t bin, uint32_t frame_off, rd_cplx16* vec,
+                                uint32_t* frame_id, uint32_t* flags) {
+  if (!ch || !vec || !frame_id || !flags) return fail(RD_EINVAL, "null argument");
+  const HistMirror::Read r = ch->hist.locate(bin, frame_off);
+  const uint32_t C = ch->cfg.n_chan, N = ch->cfg.n_fft;
+  if (r.valid_data) {
+    // the slot holds the newest frame written to it, which is frame_id
+    // whenever frame_off is in range or clamped (history_model.hpp:294-305)
+    const uint64_t slot = (uint64_t)r.frame_id % ch->R;
+    CK(cudaStreamSynchronize(ch->stream));
+    CK(cudaMemcpy(vec, ch->ring.p + (slot * N + ((bin & 0xFFFFu) % N)) * C, (size_t)C * 4,
+                  cudaMemcpyDeviceToHost));
+  } else {
+    std::memset(vec, 0, (size_t)C * 4);
+  }
+  *frame_id = r.frame_id;
+  *flags = r.flags;
+  ch->hist.count_reads(r.flags, 1);
+  return RD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Per-block entry points: copy in, one kernel, copy out.
+// ---------------------------------------------------------------------------
+
+rd_status rd_pfb_run(uint32_t phases, uint32_t taps, const rd_cplx16* coeff, rd_cplx16* state,
+                     const rd_cplx16* in, uint32_t beats, rd_cplx16* out, uint8_t* flags_out) {
+  if (!coeff || !state || !in || !out || phases == 0 || taps == 0 || taps > 64)
+    return fail(RD_EINVAL, "bad argument");
+  if (!rd_device_ok()) return fail(RD_EDEVICE, "no usable CUDA device");
+  Scratch sc;
+  uint32_t *dc, *ds, *dn, *di, *dout;
+  uint8_t* df = nullptr;
+  const size_t D = taps > 1 ? taps - 1 : 1;
+  CK(sc.alloc(&dc, (size_t)phases * taps));
+  CK(sc.alloc(&ds, D * phases));
+  CK(sc.alloc(&dn, D * phases));
+  CK(sc.alloc(&di, (size_t)beats * phases));
+  CK(sc.alloc(&dout, (size_t)beats * phases));
+  if (flags_out) CK(sc.alloc(&df, (size_t)beats * phases));
+  CK(cudaMemcpy(dc, coeff, (size_t)phases * taps * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ds, state, D * phases * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(di, in, (size_t)beats * phases * 4, cudaMemcpyHostToDevice));
+  launch_pfb_block(phases, taps, dc, ds, di, beats, dout, df, 0);
+  launch_tail_update(di, 0, ds, dn, beats, 1, phases, taps, 0);
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(out, dout, (size_t)beats * phases * 4, cudaMemcpyDeviceToHost));
+  if (flags_out) CK(cudaMemcpy(flags_out, df, (size_t)beats * phases, cudaMemcpyDeviceToHost));
+  if (taps > 1) CK(cudaMemcpy(state, dn, D * phases * 4, cudaMemcpyDeviceToHost));
+  return RD_OK;
+}
+
+rd_status rd_fft_run(uint32_t n_fft, uint32_t spc, uint32_t sched, int reorder,
+                     const rd_cplx16* in, uint32_t frames, rd_cplx16* out, rd_cplx16* bins,
+                     uint8_t* stage_flags) {
+  if (!in || !is_pow2(n_fft) || n_fft < 8 || n_fft > 1024 || (spc != 1 && spc != 2) ||
+      n_fft / spc < 4)
+    return fail(RD_EINVAL, "invalid FFT geometry (fft_ref.hpp:216-219)");
+  if (!rd_device_ok()) return fail(RD_EDEVICE, "no usable CUDA device");
+  Scratch sc;
+  uint32_t *di, *dout = nullptr, *dbins = nullptr;
+  uint8_t* dsf = nullptr;
+  const size_t n = (size_t)frames * n_fft;
+  const unsigned stages = clog2(n_fft);
+  CK(sc.alloc(&di, n));
+  if (out) CK(sc.alloc(&dout, n));
+  if (bins) CK(sc.alloc(&dbins, n));
+  if (stage_flags) CK(sc.alloc(&dsf, (size_t)frames * stages));
+  CK(cudaMemcpy(di, in, n * 4, cudaMemcpyHostToDevice));
+  launch_fft_block(n_fft, spc, sched, reorder, di, frames, dout, dbins, dsf, 0);
+  CK(cudaGetLastError());
+  if (out) CK(cudaMemcpy(out, dout, n * 4, cudaMemcpyDeviceToHost));
+  if (bins) CK(cudaMemcpy(bins, dbins, n * 4, cudaMemcpyDeviceToHost));
+  if (stage_flags) CK(cudaMemcpy(stage_flags, dsf, (size_t)frames * stages, cudaMemcpyDeviceToHost));
+  return RD_OK;
+}
+
+rd_status rd_bf_run(uint32_t n_ant, uint32_t n_beams, const rd_cplx16* w, const rd_cplx16* x,
+                    uint64_t n_vec, rd_cplx16* y, int64_t* acc, uint8_t* flags, uint32_t form) {
+  if (!w || !x || !y || n_ant == 0 || n_beams == 0 || form > RD_FORM_TENSOR)
+    return fail(RD_EINVAL, "bad argument");
+  if (!rd_device_ok()) return fail(RD_EDEVICE, "no usable CUDA device");
+  Scratch sc;
+  uint32_t *dw, *dx, *dy;
+  long long* dacc = nullptr;
+  uint8_t* df = nullptr;
+  CK(sc.alloc(&dw, (size_t)n_ant * n_beams));
+  CK(sc.alloc(&dx, n_vec * n_ant));
+  CK(sc.alloc(&dy, n_vec * n_beams));
+  if (acc) CK(sc.alloc(&dacc, n_vec * n_beams * 2));
+  if (flags) CK(sc.alloc(&df, n_vec * n_beams));
+  CK(cudaMemcpy(dw, w, (size_t)n_ant * n_beams * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dx, x, n_vec * n_ant * 4, cudaMemcpyHostToDevice));
+  launch_bf_block(n_ant, n_beams, dw, dx, n_vec, dy, dacc, df, 0);
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(y, dy, n_vec * n_beams * 4, cudaMemcpyDeviceToHost));
+  if (acc) CK(cudaMemcpy(acc, dacc, n_vec * n_beams * 16, cudaMemcpyDeviceToHost));
+  if (flags) CK(cudaMemcpy(flags, df, n_vec * n_beams, cudaMemcpyDeviceToHost));
+  return RD_OK;
+}
+
+rd_status rd_power_run(const rd_cplx16* x, uint64_t n, int64_t* power) {
+  if (!x || !power) return fail(RD_EINVAL, "null argument");
+  if (!rd_device_ok()) return fail(RD_EDEVICE, "no usable CUDA device");
+  Scratch sc;
+  uint32_t* dx;
+  long long* dp;
+  CK(sc.alloc(&dx, n));
+  CK(sc.alloc(&dp, n));
+  CK(cudaMemcpy(dx, x, n * 4, cudaMemcpyHostToDevice));
+  launch_power_block(dx, n, dp, 0);
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(power, dp, n * 8, cudaMemcpyDeviceToHost));
+  return RD_OK;
+}
+
+rd_status rd_cross_power_run(const rd_cplx16* x, const rd_cplx16* y, uint64_t n, int64_t* cross) {
+  if (!x || !y || !cross) return fail(RD_EINVAL, "null argument");
+  if (!rd_device_ok()) return fail(RD_EDEVICE, "no usable CUDA device");
+  Scratch sc;
+  uint32_t *dx, *dy;
+  long long* dc;
+  CK(sc.alloc(&dx, n));
+  CK(sc.alloc(&dy, n));
+  CK(sc.alloc(&dc, 2 * n));
+  CK(cudaMemcpy(dx, x, n * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dy, y, n * 4, cudaMemcpyHostToDevice));
+  launch_cross_block(dx, dy, n, dc, 0);
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(cross, dc, n * 16, cudaMemcpyDeviceToHost));
+  return RD_OK;
+}
+
+rd_status rd_cfar_run(const int64_t* cells, uint32_t n, uint32_t frames, const rd_config* cfg,
+                      const uint32_t* frame_ids, rd_event* events, uint64_t cap,
+                      uint64_t* n_events) {
+  if (!cells || !cfg || !frame_ids || !n_events || n == 0 || n > 65535)
+    return fail(RD_EINVAL, "bad argument");
+  if (!rd_device_ok()) return fail(RD_EDEVICE, "no usable CUDA device");
+  Scratch sc;
+  long long* dc;
+  uint32_t *dfid, *dcnt, *dds, *dmask;
+  unsigned long long* doff;
+  rd_event* dev = nullptr;
+  DevStats* dst;
+  const size_t words = (n + 31) / 32;
+  CK(sc.alloc(&dc, (size_t)frames * n));
+  CK(sc.alloc(&dfid, frames));
+  CK(sc.alloc(&dcnt, frames));
+  CK(sc.alloc(&dds, (size_t)frames * 2));
+  CK(sc.alloc(&dmask, (size_t)frames * words));
+  CK(sc.alloc(&doff, frames));
+  CK(sc.alloc(&dst, 1));
+  CK(sc.alloc(&dev, std::max<uint64_t>(cap, 1)));
+  CK(cudaMemcpy(dc, cells, (size_t)frames * n * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dfid, frame_ids, (size_t)frames * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemset(dst, 0, sizeof(DevStats)));
+  CfarParams p{};
+  p.cells_i64 = (const int64_t*)dc;
+  p.frames = frames;
+  p.n = n;
+  p.beams = 1;
+  p.frame_ids = dfid;
+  p.enable = cfg->cfar_enable != 0;
+  p.go = cfg->cfar_mode == RD_CFAR_GO;
+  p.dense = cfg->cfar_out_mode == RD_CFAR_DENSE;
+  p.gl = std::min(cfg->guard_lead, cfg->max_guard);
+  p.gg = std::min(cfg->guard_lag, cfg->max_guard);
+  p.rl = std::min(cfg->ref_lead, cfg->max_ref);
+  p.rg = std::min(cfg->ref_lag, cfg->max_ref);
+  p.alpha = cfg->alpha;
+  p.counts = dcnt;
+  p.detsup = dds;
+  p.mask = dmask;
+  p.offsets = doff;
+  p.events = dev;
+  p.cap = cap;
+  p.stats = dst;
+  launch_cfar_decide(p, 0);
+  launch_cfar_scan(p, 0);
+  launch_cfar_emit(p, 0);
+  CK(cudaGetLastError());
+  DevStats hs;
+  CK(cudaMemcpy(&hs, dst, sizeof(hs), cudaMemcpyDeviceToHost));
+  *n_events = hs.events_call;
+  const uint64_t k = std::min<uint64_t>(hs.events_call, cap);
+  if (k && events) CK(cudaMemcpy(events, dev, k * sizeof(rd_event), cudaMemcpyDeviceToHost));
+  return hs.events_call > cap ? fail(RD_ETRUNC, "event capacity exceeded") : RD_OK;
+}
+
+rd_status rd_packetize(const rd_event* ev, uint64_t n, uint32_t packet_w, uint32_t src_id,
+                       uint32_t dest, uint32_t vc, uint32_t seq0, uint32_t* flits) {
+  if (!ev || !flits || packet_w < 64 || packet_w > 512 || (packet_w % 32) != 0)
+    return fail(RD_EINVAL, "bad argument");
+  if (!rd_device_ok()) return fail(RD_EDEVICE, "no usable CUDA device");
+  Scratch sc;
+  rd_event* de;
+  uint32_t* df;
+  const size_t nw = (size_t)n * rd_detection_flits(packet_w) * rd_flit_words(packet_w);
+  CK(sc.alloc(&de, n));
+  CK(sc.alloc(&df, nw));
+  CK(cudaMemcpy(de, ev, n * sizeof(rd_event), cudaMemcpyHostToDevice));
+  launch_packetize(de, n, packet_w, src_id, dest, vc, seq0, df, 0);
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(flits, df, nw * 4, cudaMemcpyDeviceToHost));
+  return RD_OK;
+}
+
+rd_status rd_fxp_apply(const uint32_t* op, const int64_t* a, const int64_t* b, const uint32_t* sh,
+                       const uint32_t* w, uint64_t n, int64_t* y, uint8_t* flags) {
+  if (!op || !a || !b || !sh || !w || !y || !flags) return fail(RD_EINVAL, "null argument");
+  if (!rd_device_ok()) return fail(RD_EDEVICE, "no usable CUDA device");
+  Scratch sc;
+  uint32_t *dop, *dsh, *dw;
+  long long *da, *db, *dy;
+  uint8_t* df;
+  CK(sc.alloc(&dop, n));
+  CK(sc.alloc(&dsh, n));
+  CK(sc.alloc(&dw, n));
+  CK(sc.alloc(&da, n));
+  CK(sc.alloc(&db, n));
+  CK(sc.alloc(&dy, n));
+  CK(sc.alloc(&df, n));
+  CK(cudaMemcpy(dop, op, n * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dsh, sh, n * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dw, w, n * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(da, a, n * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(db, b, n * 8, cudaMemcpyHostToDevice));
+  launch_fxp(dop, (const int64_t*)da, (const int64_t*)db, dsh, dw, n, (int64_t*)dy, df, 0);
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(y, dy, n * 8, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(flags, df, n, cudaMemcpyDeviceToHost));
+  return RD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,610 @@
+// k_backend.cu - beamforming, power, covariance integration, CA/GO-CFAR,
+// event packing and packet flits.
+#include <cuda_runtime.h>
+
+#include "fxp.cuh"
+#include "rd_internal.h"
+
+namespace rd {
+
+// ---------------------------------------------------------------------------
+// Beamforming + power (CUDA-core integer form).
+//
+// Y[f][b][bin] = round_sat(sum_a X[f][bin][a] * W[b][a], 15, 16), the exact
+// int64 dot product of bf::dot (beamformer_model.hpp:162-179), then
+// power = re^2 + im^2 (covar_model.hpp:99-102), the CFAR cell. A CTA owns 64
+// bins of one frame; the 256 threads split as 64 bins x 4 beam groups and each
+// keeps BPT beams' accumulators in registers. The spectrum tile is staged in
+// shared memory with a padded row so the 64 bin-threads of a warp pair read
+// distinct banks; every weight read is a warp-wide broadcast.
+// ---------------------------------------------------------------------------
+template <int BPT>
+__global__ void __launch_bounds__(256) k_beam(BeamParams p) {
+  extern __shared__ uint32_t sm[];
+  const unsigned C = p.C, B = p.B, N = p.N;
+  const unsigned xs = C + 1;  // padded row
+  uint32_t* s_w = sm;
+  uint32_t* s_x = sm + B * C;
+  const unsigned tid = threadIdx.x;
+  const unsigned bin0 = blockIdx.x * 64u;
+  const uint64_t f = blockIdx.y;
+  const uint64_t slot = (p.g0 + f) % p.ring_frames;
+  for (unsigned k = tid; k < B * C; k += 256u) s_w[k] = p.weights[k];
+  const uint32_t* xsrc = p.ring + (slot * N + bin0) * C;
+  const unsigned nb = (N - bin0) < 64u ? (N - bin0) : 64u;
+  for (unsigned k = tid; k < nb * C; k += 256u) s_x[(k / C) * xs + (k % C)] = xsrc[k];
+  __syncthreads();
+  const unsigned bl = tid & 63u, bg = tid >> 6;
+  const unsigned bin = bin0 + bl;
+  long long ar[BPT], ai[BPT];
+#pragma unroll
+  for (int j = 0; j < BPT; ++j) ar[j] = ai[j] = 0;
+  if (bl < nb) {
+    const uint32_t* xr = s_x + bl * xs;
+    for (unsigned a = 0; a < C; ++a) {
+      const cplx x = unpack(xr[a]);
+#pragma unroll
+      for (int j = 0; j < BPT; ++j) {
+        const unsigned b = bg + 4u * j;
+        if (b < B) {
+          const cplx w = unpack(s_w[b * C + a]);
+          ar[j] += (long long)((int32_t)x.re * w.re - (int32_t)x.im * w.im);
+          ai[j] += (long long)((int32_t)x.re * w.im) + (long long)((int32_t)x.im * w.re);
+        }
+      }
+    }
+  }
+  unsigned fl_any = 0;
+  unsigned long long nsat = 0;
+#pragma unroll
+  for (int j = 0; j < BPT; ++j) {
+    const unsigned b = bg + 4u * j;
+    if (b < B && bl < nb) {
+      unsigned fr = 0, fi = 0;
+      const int32_t yr = q15_out64(ar[j], &fr), yi = q15_out64(ai[j], &fi);
+      if (fr | fi) {
+        fl_any |= fr | fi;
+        ++nsat;
+      }
+      cplx y;
+      y.re = (int16_t)yr;
+      y.im = (int16_t)yi;
+      p.power[(f * B + b) * N + bin] = power_u32(y);
+      if (p.beams_bn) p.beams_bn[(f * N + bin) * B + b] = pack(y);
+    }
+  }
+  const unsigned a = __reduce_or_sync(0xffffffffu, fl_any);
+  for (int o = 16; o > 0; o >>= 1) nsat += __shfl_xor_sync(0xffffffffu, nsat, o);
+  if ((tid & 31u) == 0u) {
+    if (a) atomicOr(&p.stats->bf_flags, a);
+    if (nsat) atomicAdd(&p.stats->bf_sat, nsat);
+  }
+}
+
+static bool g_beam_attr_set = false;
+
+void launch_beam(const BeamParams& p, cudaStream_t s) {
+  const unsigned bpt = (p.B + 3u) / 4u;
+  const dim3 grid((p.N + 63u) / 64u, p.F);
+  const size_t smem = ((size_t)p.B * p.C + 64u * (p.C + 1u)) * sizeof(uint32_t);
+  if (!g_beam_attr_set) {
+    cudaFuncSetAttribute(k_beam<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_beam<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_beam<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_beam<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_beam<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_beam<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    g_beam_attr_set = true;
+  }
+  if (bpt <= 1) k_beam<1><<<grid, 256, smem, s>>>(p);
+  else if (bpt <= 2) k_beam<2><<<grid, 256, smem, s>>>(p);
+  else if (bpt <= 4) k_beam<4><<<grid, 256, smem, s>>>(p);
+  else if (bpt <= 8) k_beam<8><<<grid, 256, smem, s>>>(p);
+  else if (bpt <= 16) k_beam<16><<<grid, 256, smem, s>>>(p);
+  else k_beam<32><<<grid, 256, smem, s>>>(p);
+}
+
+// ---------------------------------------------------------------------------
+// Covariance: one covar::Integrator pair (re, im) per (bin, pair), stepped
+// once per frame with X[x] * conj(X[y]) (covar_model.hpp:119-151, 204-262).
+// A CTA owns one bin and up to 256 pairs; the frame's source vector is staged
+// in shared memory (double-buffered, one barrier per frame) and the integrator
+// state lives in registers for the whole chunk. Window count and id are the
+// same for every integrator of the stream (they all step on every frame), so
+// the host tracks them and passes where windows close.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void integ_step(long long& acc, long long x, unsigned exp_mode,
+                                           unsigned k, unsigned acc_w, unsigned& sticky,
+                                           unsigned& satcnt) {
+  const long long raw =
+      exp_mode ? add_wrap(acc, asr64(sub_wrap(x, acc), k)) : add_wrap(acc, x);
+  const unsigned fl = sat_flags64(raw, acc_w);
+  acc = sat64(raw, acc_w);
+  sticky |= fl;
+  if (fl && satcnt != 0xFFFFFFFFu) ++satcnt;
+}
+
+__global__ void __launch_bounds__(256) k_cov(CovParams p) {
+  __shared__ uint32_t s_src[2][128];
+  const unsigned tid = threadIdx.x;
+  const unsigned bin = blockIdx.x;
+  const unsigned q = blockIdx.y * 256u + tid;
+  const bool live = q < p.P;
+  const size_t k = (size_t)bin * p.P + q;
+  long long are = 0, aim = 0;
+  unsigned st_re = 0, st_im = 0, sc_re = 0, sc_im = 0, xi = 0, yi = 0;
+  if (live) {
+    are = p.acc_re[k];
+    aim = p.acc_im[k];
+    st_re = p.sticky[k] >> 2;
+    st_im = p.sticky[k] & 3u;
+    sc_re = p.satcnt[2 * k];
+    sc_im = p.satcnt[2 * k + 1];
+    xi = p.px[q];
+    yi = p.py[q];
+  }
+  unsigned count = p.count0, w = 0;
+  unsigned wflags = 0;
+  for (uint32_t f = 0; f < p.F; ++f) {
+    uint32_t* buf = s_src[f & 1u];
+    if (tid < p.S) {
+      buf[tid] = p.src_beam ? p.beams_bn[((size_t)f * p.N + bin) * p.S + tid]
+                            : p.ring[(((p.g0 + f) % p.ring_frames) * p.N + bin) * p.S + tid];
+    }
+    __syncthreads();
+    if (live) {
+      const cplx X = unpack(buf[xi]), Y = unpack(buf[yi]);
+      // X * conj(Y) through the operand-swap wiring: b = {Y.im, Y.re},
+      // re = im(X*b), im = -re(X*b) (covar_model.hpp:137-145)
+      const long long cre = (long long)((int32_t)X.re * Y.re) + (long long)((int32_t)X.im * Y.im);
+      const long long cim = (long long)((int32_t)X.im * Y.re) - (long long)((int32_t)X.re * Y.im);
+      integ_step(are, cre, p.exp_mode, p.exp_k, p.acc_w, st_re, sc_re);
+      integ_step(aim, cim, p.exp_mode, p.exp_k, p.acc_w, st_im, sc_im);
+    }
+    if (++count >= p.wl) {
+      if (live && w < p.n_windows) {
+        long long* o = p.out + (((size_t)w * p.N + bin) * p.P + q) * 2;
+        o[0] = are;
+        o[1] = aim;
+        wflags |= st_re | st_im;
+      }
+      if (!p.exp_mode) are = aim = 0;
+      count = 0;
+      if (wflags) atomicOr(&p.win_flags[w], wflags);
+      wflags = 0;
+      ++w;
+    }
+  }
+  if (live) {
+    p.acc_re[k] = are;
+    p.acc_im[k] = aim;
+    p.sticky[k] = (st_re << 2) | st_im;
+    const unsigned old_re = p.satcnt[2 * k], old_im = p.satcnt[2 * k + 1];
+    p.satcnt[2 * k] = sc_re;
+    p.satcnt[2 * k + 1] = sc_im;
+    const unsigned long long d = (unsigned long long)(sc_re - old_re) + (sc_im - old_im);
+    if (d) atomicAdd(&p.stats->cov_sat_steps, d);
+    if (st_re | st_im) atomicOr(&p.stats->cov_flags, st_re | st_im);
+  }
+}
+
+void launch_cov(const CovParams& p, cudaStream_t s) {
+  if (p.P == 0 || p.F == 0) return;
+  const dim3 grid(p.N, (p.P + 255u) / 256u);
+  k_cov<<<grid, 256, 0, s>>>(p);
+}
+
+// ---------------------------------------------------------------------------
+// CFAR (cfar_model.hpp:243-340). One warp per CFAR frame (frame x beam).
+// Pass 1 (decide): prefix sums of the frame's cells in shared memory, the
+// lead/lag reference sums of every cell as prefix differences (the same
+// integers the model's per-cell loops add), the CA or GO decision, and a
+// ballot bitmask of the cells that emit an event. Pass 2 (scan): exclusive
+// offsets of every frame's event count. Pass 3 (emit): each warp rebuilds its
+// frame's sums only when it has events, packs the 176-bit events in bin order
+// followed by the SUMMARY, and writes the packet flits next to them.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t cell_at(const CfarParams& p, uint64_t u, unsigned i) {
+  if (p.power_u32) return p.power_u32[u * p.n + i];
+  const long long v = p.cells_i64[u * p.n + i];
+  return v < 0 ? 0ull : (uint64_t)v;  // clamp_cell (cfar_model.hpp:238-240)
+}
+
+// Inclusive prefix sums pre[1..n] of frame u (pre[0] = 0), warp-cooperative.
+__device__ __forceinline__ void warp_prefix(const CfarParams& p, uint64_t u, uint64_t* pre) {
+  const unsigned lane = threadIdx.x & 31u;
+  uint64_t carry = 0;
+  if (lane == 0) pre[0] = 0;
+  for (unsigned r = 0; r * 32u < p.n; ++r) {
+    const unsigned i = r * 32u + lane;
+    uint64_t v = i < p.n ? cell_at(p, u, i) : 0ull;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t t = __shfl_up_sync(0xffffffffu, v, o);
+      if ((int)lane >= o) v += t;
+    }
+    if (i < p.n) pre[i + 1] = carry + v;
+    carry += __shfl_sync(0xffffffffu, v, 31);
+  }
+  __syncwarp();
+}
+
+struct CellDecision {
+  bool emit, detected, evaluable;
+  uint64_t sum;
+  unsigned n;
+};
+
+__device__ __forceinline__ CellDecision decide_cell(const CfarParams& p, const uint64_t* pre,
+                                                    unsigned i, uint64_t cut) {
+  CellDecision d;
+  const long long hi = (long long)i + p.gl + p.rl;
+  const long long lo = (long long)i - (long long)p.gg - (long long)p.rg;
+  const bool ok = hi < (long long)p.n && lo >= 0;
+  uint64_t sl = 0, sg = 0;
+  if (ok) {
+    sl = pre[i + p.gl + p.rl + 1] - pre[i + p.gl + 1];
+    sg = pre[i - p.gg] - pre[i - p.gg - p.rg];
+  }
+  if (p.go) {
+    const bool lead = (sl * p.rg) >= (sg * p.rl);
+    d.sum = lead ? sl : sg;
+    d.n = lead ? p.rl : p.rg;
+  } else {
+    d.sum = sl + sg;
+    d.n = p.rl + p.rg;
+  }
+  const bool usable = p.go ? (p.rl != 0u && p.rg != 0u) : (p.rl + p.rg) != 0u;
+  d.evaluable = ok && p.enable && usable;
+  d.detected = d.evaluable && ((cut * d.n) << 8) > ((uint64_t)p.alpha * d.sum);
+  d.emit = d.detected || p.dense;
+  return d;
+}
+
+__global__ void __launch_bounds__(128) k_cfar_decide(CfarParams p) {
+  extern __shared__ uint64_t s_pre[];
+  const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  const uint64_t u = (uint64_t)blockIdx.x * 4u + warp;
+  uint64_t* pre = s_pre + (size_t)warp * (p.n + 1u);
+  if (u >= p.frames) return;
+  warp_prefix(p, u, pre);
+  const unsigned words = (p.n + 31u) / 32u;
+  unsigned emitted = 0, det = 0, sup = 0;
+  for (unsigned r = 0; r < words; ++r) {
+    const unsigned i = r * 32u + lane;
+    bool em = false;
+    if (i < p.n) {
+      const CellDecision d = decide_cell(p, pre, i, pre[i + 1] - pre[i]);
+      em = d.emit;
+      det += d.detected;
+      sup += !d.evaluable;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, em);
+    if (lane == 0) p.mask[u * words + r] = m;
+    emitted += __popc(m);
+  }
+  det = __reduce_add_sync(0xffffffffu, det);
+  sup = __reduce_add_sync(0xffffffffu, sup);
+  if (lane == 0) {
+    p.counts[u] = emitted + 1u;  // + SUMMARY
+    p.detsup[2 * u] = det;
+    p.detsup[2 * u + 1] = sup;
+    atomicAdd(&p.stats->cfar_det, (unsigned long long)det);
+    atomicAdd(&p.stats->cfar_sup, (unsigned long long)sup);
+  }
+}
+
+// Exclusive scan of counts -> offsets (+ the call's running event count).
+__global__ void __launch_bounds__(1024) k_cfar_scan(CfarParams p) {
+  __shared__ unsigned long long s_part[1024];
+  const unsigned tid = threadIdx.x;
+  const uint64_t per = (p.frames + 1023u) / 1024u;
+  const uint64_t lo = tid * per, hi = (lo + per) < p.frames ? (lo + per) : p.frames;
+  unsigned long long sum = 0;
+  for (uint64_t i = lo; i < hi; ++i) sum += p.counts[i];
+  s_part[tid] = sum;
+  __syncthreads();
+  for (unsigned o = 1; o < 1024u; o <<= 1) {
+    const unsigned long long t = tid >= o ? s_part[tid - o] : 0ull;
+    __syncthreads();
+    s_part[tid] += t;
+    __syncthreads();
+  }
+  const unsigned long long base = p.stats->events_call;
+  unsigned long long run = base + s_part[tid] - sum;
+  for (uint64_t i = lo; i < hi; ++i) {
+    p.offsets[i] = run;
+    run += p.counts[i];
+  }
+  __syncthreads();
+  if (tid == 1023u) p.stats->events_call = base + s_part[1023];
+}
+
+__device__ __forceinline__ void set_field(uint64_t* w, unsigned lsb, unsigned n, uint64_t v) {
+  v &= (n >= 64) ? ~0ull : ((1ull << n) - 1ull);
+  const unsigned wi = lsb >> 6, sh = lsb & 63u;
+  w[wi] |= v << sh;
+  if (sh + n > 64u) w[wi + 1] |= v >> (64u - sh);
+}
+
+// 176-bit event of cfar_model.hpp:75-84 (fields masked to their widths)
+__device__ __forceinline__ void make_event(rd_event* e, unsigned kind, unsigned bin,
+                                           unsigned fid, unsigned refc, unsigned alpha,
+                                           unsigned det, unsigned sup, uint64_t cut,
+                                           uint64_t sum, bool sof, bool eof, uint32_t frame,
+                                           uint16_t beam) {
+  uint64_t w[3] = {0, 0, 0};
+  set_field(w, 0, 2, kind);
+  set_field(w, 2, 16, bin);
+  set_field(w, 18, 16, fid);
+  set_field(w, 34, 7, refc);
+  set_field(w, 41, 16, alpha);
+  set_field(w, 57, 16, det);
+  set_field(w, 73, 16, sup);
+  set_field(w, 89, 40, cut);
+  set_field(w, 129, 47, sum);
+  e->w[0] = w[0];
+  e->w[1] = w[1];
+  e->w[2] = w[2];
+  e->frame = frame;
+  e->beam = beam;
+  e->kind = (uint8_t)kind;
+  e->framing = (uint8_t)((sof ? 1u : 0u) | (eof ? 2u : 0u));
+}
+
+// 32 bits of a bit string of `nbits` starting at signed bit s (zeros outside).
+__device__ __forceinline__ uint32_t bits32(const uint64_t* w, int s, int nbits) {
+  uint32_t r = 0;
+  for (int j = 0; j < 32; ++j) {
+    const int b = s + j;
+    if (b >= 0 && b < nbits && ((w[b >> 6] >> (b & 63)) & 1ull)) r |= 1u << j;
+  }
+  return r;
+}
+
+// One detection packet: the header flit (packet_model.hpp:150-159, sof) and
+// payload flits carrying the event LS word first (benchmark_sim_top.sv:
+// 1818-1936); flit = data << 5 | eof << 4 | sof << 3 | vc << 1 | odd parity.
+__device__ void write_packet(const rd_event* e, uint32_t* out, unsigned pw, unsigned words,
+                             unsigned nfl, unsigned src, unsigned dest, unsigned vc,
+                             unsigned seq) {
+  for (unsigned f = 0; f < nfl; ++f) {
+    uint32_t* o = out + (size_t)f * words;
+    uint64_t hdr[3] = {0, 0, 0};
+    const uint64_t* data;
+    int dbits, off;
+    if (f == 0) {
+      hdr[0] = (uint64_t)(dest & 0xFu) | ((uint64_t)(src & 0x1Fu) << 4) |
+               ((uint64_t)(vc & 3u) << 9) | ((uint64_t)0u << 11) |
+               ((uint64_t)(nfl & 0x3Fu) << 14) | ((uint64_t)(seq & 0xFFFFu) << 20);
+      data = hdr;
+      dbits = 36;
+      off = 0;
+    } else {
+      data = e->w;
+      dbits = 176;
+      off = (int)((f - 1) * pw);
+    }
+    unsigned pop = 0;
+    for (unsigned k = 0; k < words; ++k) {
+      // flit bit j carries data bit off + j - 5, for 5 <= j < 5 + pw
+      uint32_t v = bits32(data, off + (int)(32 * k) - 5, dbits);
+      const int lo = 32 * (int)k, hi = lo + 32;
+      if (lo < 5) v &= ~0x1Fu;
+      const int top = 5 + (int)pw;  // first bit past the data
+      if (hi > top) v &= (top <= lo) ? 0u : ((1u << (top - lo)) - 1u);
+      if (k == 0)
+        v |= ((vc & 3u) << 1) | ((f == 0 ? 1u : 0u) << 3) | ((f + 1 == nfl ? 1u : 0u) << 4);
+      pop += __popc(v);
+      o[k] = v;
+    }
+    if ((pop & 1u) == 0u) o[0] |= 1u;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_cfar_emit(CfarParams p) {
+  extern __shared__ uint64_t s_pre[];
+  const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  const uint64_t u = (uint64_t)blockIdx.x * 4u + warp;
+  uint64_t* pre = s_pre + (size_t)warp * (p.n + 1u);
+  if (u >= p.frames) return;
+  const unsigned words = (p.n + 31u) / 32u;
+  const uint32_t cnt = p.counts[u];
+  const uint64_t base = p.offsets[u];
+  const uint64_t frame = p.frame_ids ? p.frame_ids[u] : (p.g0 + u / p.beams);
+  const unsigned fid = p.frame_ids ? p.frame_ids[u] : (unsigned)(frame & 0xFFFFu);
+  const uint16_t beam = (uint16_t)(p.frame_ids ? u : (u % p.beams));
+  const unsigned long long seq0 = p.stats->events_total;
+  if (cnt > 1u) {
+    warp_prefix(p, u, pre);
+    unsigned before = 0;
+    for (unsigned r = 0; r < words; ++r) {
+      const uint32_t m = p.mask[u * words + r];
+      const unsigned i = r * 32u + lane;
+      if ((m >> lane) & 1u) {
+        const uint64_t cut = pre[i + 1] - pre[i];
+        const CellDecision d = decide_cell(p, pre, i, cut);
+        const uint64_t idx = base + before + __popc(m & ((1u << lane) - 1u));
+        const unsigned kind = d.detected ? 0u : (!d.evaluable ? 2u : 1u);
+        if (idx < p.cap) {
+          rd_event ev;
+          make_event(&ev, kind, i, fid, d.evaluable ? d.n : 0u, p.alpha, 0, 0, cut,
+                     d.evaluable ? d.sum : 0ull, idx == base, false, (uint32_t)frame, beam);
+          p.events[idx] = ev;
+          if (p.flits)
+            write_packet(&ev, p.flits + idx * p.nfl * p.flit_words, p.packet_w, p.flit_words,
+                         p.nfl, p.src_id, p.dest, p.vc, (unsigned)((seq0 + idx) & 0xFFFFu));
+        }
+      }
+      before += __popc(m);
+    }
+  }
+  if (lane == 0) {
+    const uint64_t idx = base + cnt - 1u;
+    if (idx < p.cap) {
+      rd_event ev;
+      make_event(&ev, 3u, p.n, fid, 0, p.alpha, p.detsup[2 * u], p.detsup[2 * u + 1], 0, 0,
+                 cnt == 1u, true, (uint32_t)frame, beam);
+      p.events[idx] = ev;
+      if (p.flits)
+        write_packet(&ev, p.flits + idx * p.nfl * p.flit_words, p.packet_w, p.flit_words, p.nfl,
+                     p.src_id, p.dest, p.vc, (unsigned)((seq0 + idx) & 0xFFFFu));
+    }
+  }
+}
+
+static size_t cfar_smem(const CfarParams& p) { return 4u * (p.n + 1u) * sizeof(uint64_t); }
+static bool g_cfar_attr_set = false;
+static void cfar_attrs() {
+  if (g_cfar_attr_set) return;
+  cudaFuncSetAttribute(k_cfar_decide, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  cudaFuncSetAttribute(k_cfar_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  g_cfar_attr_set = true;
+}
+
+void launch_cfar_decide(const CfarParams& p, cudaStream_t s) {
+  if (!p.frames) return;
+  cfar_attrs();
+  k_cfar_decide<<<(unsigned)((p.frames + 3u) / 4u), 128, cfar_smem(p), s>>>(p);
+}
+void launch_cfar_scan(const CfarParams& p, cudaStream_t s) {
+  if (!p.frames) return;
+  k_cfar_scan<<<1, 1024, 0, s>>>(p);
+}
+void launch_cfar_emit(const CfarParams& p, cudaStream_t s) {
+  if (!p.frames) return;
+  cfar_attrs();
+  k_cfar_emit<<<(unsigned)((p.frames + 3u) / 4u), 128, cfar_smem(p), s>>>(p);
+}
+
+// ---------------------------------------------------------------------------
+// Per-block entry points
+// ---------------------------------------------------------------------------
+__global__ void k_bf_block(uint32_t A, uint32_t B, const uint32_t* w, const uint32_t* x,
+                           uint64_t nv, uint32_t* y, long long* acc, uint8_t* flags) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv * B) return;
+  const uint64_t v = i / B;
+  const uint32_t b = (uint32_t)(i % B);
+  long long ar = 0, ai = 0;
+  for (uint32_t a = 0; a < A; ++a) {
+    const cplx xv = unpack(x[v * A + a]), wv = unpack(w[(size_t)b * A + a]);
+    ar += cmul_re_raw(xv, wv);
+    ai += cmul_im_raw(xv, wv);
+  }
+  unsigned fr = 0, fi = 0;
+  const int32_t yr = q15_out64(ar, &fr), yi = q15_out64(ai, &fi);
+  y[i] = pack2(yr, yi);
+  if (acc) {
+    acc[2 * i] = ar;
+    acc[2 * i + 1] = ai;
+  }
+  if (flags) flags[i] = (uint8_t)((fr << 2) | fi);
+}
+void launch_bf_block(uint32_t n_ant, uint32_t n_beams, const uint32_t* w, const uint32_t* x,
+                     uint64_t n_vec, uint32_t* y, long long* acc, uint8_t* flags, cudaStream_t s) {
+  const uint64_t n = n_vec * n_beams;
+  if (n) k_bf_block<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n_ant, n_beams, w, x, n_vec, y,
+                                                                 acc, flags);
+}
+
+__global__ void k_power_block(const uint32_t* x, uint64_t n, long long* p) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = (long long)power_u32(unpack(x[i]));
+}
+void launch_power_block(const uint32_t* x, uint64_t n, long long* p, cudaStream_t s) {
+  if (n) k_power_block<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, n, p);
+}
+
+__global__ void k_cross_block(const uint32_t* x, const uint32_t* y, uint64_t n, long long* c) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const cplx X = unpack(x[i]), Y = unpack(y[i]);
+  const cplx b = {Y.im, Y.re};
+  c[2 * i] = cmul_im_raw(X, b);
+  c[2 * i + 1] = neg_wrap(cmul_re_raw(X, b));
+}
+void launch_cross_block(const uint32_t* x, const uint32_t* y, uint64_t n, long long* c,
+                        cudaStream_t s) {
+  if (n) k_cross_block<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, y, n, c);
+}
+
+__global__ void k_packetize(const rd_event* ev, uint64_t n, uint32_t pw, uint32_t src,
+                            uint32_t dest, uint32_t vc, uint32_t seq0, uint32_t* flits,
+                            uint32_t words, uint32_t nfl) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const rd_event e = ev[i];
+  write_packet(&e, flits + i * nfl * words, pw, words, nfl, src, dest, vc,
+               (unsigned)((seq0 + i) & 0xFFFFu));
+}
+void launch_packetize(const rd_event* ev, uint64_t n, uint32_t packet_w, uint32_t src,
+                      uint32_t dest, uint32_t vc, uint32_t seq0, uint32_t* flits, cudaStream_t s) {
+  const uint32_t words = (packet_w + 5u + 31u) / 32u;
+  const uint32_t nfl = 1u + (176u + packet_w - 1u) / packet_w;
+  if (n) k_packetize<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(ev, n, packet_w, src, dest, vc,
+                                                                  seq0, flits, words, nfl);
+}
+
+__device__ __forceinline__ unsigned growth_bits(unsigned n) {
+  return n <= 1u ? 0u : 32u - __clz(n - 1u);
+}
+
+// fxp_ops.hpp:109-177 dispatch over the device primitives
+__global__ void k_fxp(const uint32_t* op, const int64_t* a, const int64_t* b, const uint32_t* sh,
+                      const uint32_t* wv, uint64_t n, int64_t* y, uint8_t* flags) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const long long A = a[i], Bv = b[i];
+  const unsigned S = sh[i], W = wv[i];
+  long long r = 0;
+  unsigned f = 0;
+  switch (op[i]) {
+    case RD_OP_SAT: r = sat64(A, W); f = sat_flags64(A, W); break;
+    case RD_OP_TRUNC: r = asr64(A, S); break;
+    case RD_OP_ROUND_EVEN:
+    case RD_OP_ROUND: r = round_even64(A, S); break;
+    case RD_OP_ROUND_HALF_UP: r = round_half_up64(A, S); break;
+    case RD_OP_ROUND_SAT: {
+      const long long q = round_even64(A, S);
+      r = sat64(q, W);
+      f = sat_flags64(q, W);
+      break;
+    }
+    case RD_OP_ADD_SAT: r = sat64(add_wrap(A, Bv), W); f = sat_flags64(add_wrap(A, Bv), W); break;
+    case RD_OP_SUB_SAT: r = sat64(sub_wrap(A, Bv), W); f = sat_flags64(sub_wrap(A, Bv), W); break;
+    case RD_OP_NEG_SAT: r = sat64(neg_wrap(A), W); f = sat_flags64(neg_wrap(A), W); break;
+    case RD_OP_MUL_Q15:
+      r = (long long)((int32_t)(int16_t)(uint16_t)(A & 0xFFFF) * (int16_t)(uint16_t)(Bv & 0xFFFF));
+      break;
+    case RD_OP_MUL_Q15_RS: {
+      const int32_t pr = (int32_t)(int16_t)(uint16_t)(A & 0xFFFF) * (int16_t)(uint16_t)(Bv & 0xFFFF);
+      const int32_t q = rne15_32(pr);
+      r = sat16(q);
+      f = flags16(q);
+      break;
+    }
+    case RD_OP_CMUL_RE:
+    case RD_OP_CMUL_IM: {
+      const cplx ca = unpack((uint32_t)(A & 0xFFFFFFFFll)), cb = unpack((uint32_t)(Bv & 0xFFFFFFFFll));
+      unsigned fl = 0;
+      const cplx o = cmul_q15(ca, cb, &fl);
+      // flags of the selected component only
+      const long long raw = op[i] == RD_OP_CMUL_RE ? cmul_re_raw(ca, cb) : cmul_im_raw(ca, cb);
+      const long long q = rne15_64(raw);
+      f = (q > 32767 ? 2u : 0u) | (q < -32768 ? 1u : 0u);
+      r = op[i] == RD_OP_CMUL_RE ? o.re : o.im;
+      break;
+    }
+    case RD_OP_ACC_W: r = (long long)(W + growth_bits((uint32_t)(A & 0xFFFFFFFFll))); break;
+    case RD_OP_GROWTH_BITS: r = (long long)growth_bits((uint32_t)(A & 0xFFFFFFFFll)); break;
+    default: r = 0; break;
+  }
+  y[i] = r;
+  flags[i] = (uint8_t)f;
+}
+void launch_fxp(const uint32_t* op, const int64_t* a, const int64_t* b, const uint32_t* sh,
+                const uint32_t* w, uint64_t n, int64_t* y, uint8_t* flags, cudaStream_t s) {
+  if (n) k_fxp<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(op, a, b, sh, w, n, y, flags);
+}
+
+}  // namespace rd

@@ -1,0 +1,318 @@
+// k_frontend.cu - polyphase FIR bank + streaming radix-2^2 FFT + corner turn.
+//
+// One CTA owns a block of (frame, channel) items. For each item, thread e
+// holds one FFT element: it first computes the PFB output of phase
+// p(e) (pfb_model.hpp:139-177: exact int64 accumulation of T products, one
+// round_sat), which is exactly the lane-q, index-i input of the
+// decimation-in-time FFT (fft_ref.hpp:261-266, lane q = p mod spc). It then
+// runs every BF2I/BF2II sub-stage of its lane (fft_ref.hpp:334-365) and the
+// group twiddles (:368-377), exchanging partners through warp shuffles when
+// the butterfly span is below 32 and through shared memory above, then the
+// radix-2 DIT merge (:380-406). The natural-order spectrum of the item lands
+// in a shared-memory tile [frame][bin][channel] that is written to the
+// history ring coalesced - the corner turn of history_model.hpp:147-159
+// (bin-major, antenna-minor) without a second pass over HBM.
+#include <cuda_runtime.h>
+
+#include "fxp.cuh"
+#include "rd_internal.h"
+
+namespace rd {
+
+__device__ const uint32_t g_tw[1024] = {
+#include "twiddle_q15.inc"
+};
+
+const uint32_t* twiddles_device() {
+  const uint32_t* p = nullptr;
+  cudaGetSymbolAddress((void**)&p, g_tw);
+  return p;
+}
+
+// Exchange with element e ^ h of the same item (h uniform over the block).
+__device__ __forceinline__ uint32_t xchg(uint32_t val, unsigned h, uint32_t* xs) {
+  if (h < 32) return __shfl_xor_sync(0xffffffffu, val, h);
+  xs[threadIdx.x] = val;
+  __syncthreads();
+  const uint32_t r = xs[threadIdx.x ^ h];
+  __syncthreads();
+  return r;
+}
+
+// One FFT element. e = q*m + i is the thread's (lane, position) in the
+// item; returns its value after the last sub-stage; *pos = i (position).
+// Stage flags of sub-stage g accumulate into *sf bits [2g+1:2g].
+__device__ __forceinline__ uint32_t fft_elem(uint32_t v, unsigned e, unsigned nl,
+                                             unsigned spc, unsigned sched,
+                                             const uint32_t* tw, uint32_t* xs,
+                                             unsigned* sf) {
+  const unsigned m = 1u << nl;
+  const unsigned q = e >> nl, i = e & (m - 1u);
+  for (unsigned s = 0; s < nl; ++s) {
+    const unsigned half = 1u << (nl - 1u - s);
+    const unsigned sh = (sched >> s) & 1u;
+    const bool hi = (i & half) != 0u;
+    const bool k1 = (s & 1u) && ((i >> (nl - s)) & 1u);
+    unsigned fl = 0;
+    const cplx cur = unpack(v);
+    const cplx mine = (hi && k1) ? neg_j(cur, &fl) : cur;
+    const cplx o = unpack(xchg(pack(mine), half, xs));
+    cplx r;
+    if (!hi) {
+      r.re = (int16_t)quant1((int32_t)mine.re + o.re, sh, &fl);
+      r.im = (int16_t)quant1((int32_t)mine.im + o.im, sh, &fl);
+    } else {
+      r.re = (int16_t)quant1((int32_t)o.re - mine.re, sh, &fl);
+      r.im = (int16_t)quant1((int32_t)o.im - mine.im, sh, &fl);
+    }
+    if ((s & 1u) && s + 1u < nl) {
+      const unsigned l2l = nl - s + 1u;
+      r = cmul_tw(r, unpack(tw[r22_tw_exp(l2l, i) << (10u - l2l)]), &fl);
+    }
+    *sf |= fl << (2u * s);
+    v = pack(r);
+  }
+  if (spc == 2) {
+    const unsigned sh = (sched >> nl) & 1u;
+    unsigned fl = 0;
+    const cplx cur = unpack(v);
+    cplx mine = cur;
+    if (q == 1u) mine = cmul_tw(cur, unpack(tw[bitrev(i, nl) << (10u - (nl + 1u))]), &fl);
+    const cplx o = unpack(xchg(pack(mine), m, xs));
+    cplx r;
+    if (q == 0u) {
+      r.re = (int16_t)quant1((int32_t)mine.re + o.re, sh, &fl);
+      r.im = (int16_t)quant1((int32_t)mine.im + o.im, sh, &fl);
+    } else {
+      r.re = (int16_t)quant1((int32_t)o.re - mine.re, sh, &fl);
+      r.im = (int16_t)quant1((int32_t)o.im - mine.im, sh, &fl);
+    }
+    *sf |= fl << (2u * nl);
+    v = pack(r);
+  }
+  return v;
+}
+
+// natural bin of the element e after fft_elem (fft_ref.hpp:291-296)
+__device__ __forceinline__ unsigned fft_bin(unsigned e, unsigned nl) {
+  const unsigned m = 1u << nl;
+  return bitrev(e & (m - 1u), nl) + (e >> nl) * m;
+}
+
+__device__ __forceinline__ void reduce_stats(DevStats* st, unsigned pfl, unsigned long long psat,
+                                             unsigned sf) {
+  const unsigned a = __reduce_or_sync(0xffffffffu, pfl);
+  const unsigned b = __reduce_or_sync(0xffffffffu, sf);
+  unsigned long long c = psat;
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31u) == 0u) {
+    if (a) atomicOr(&st->pfb_flags, a);
+    if (b) atomicOr(&st->fft_flags, b);
+    if (c) atomicAdd(&st->pfb_sat, c);
+  }
+}
+
+template <int TT>
+__global__ void __launch_bounds__(1024) k_front(FrontParams p, unsigned FB, unsigned CB) {
+  extern __shared__ uint32_t sm[];
+  uint32_t* s_tw = sm;
+  uint32_t* s_x = sm + 1024;
+  uint32_t* s_tile = s_x + blockDim.x;
+  const unsigned tid = threadIdx.x, nth = blockDim.x;
+  for (unsigned k = tid; k < 1024u; k += nth) s_tw[k] = g_tw[k];
+
+  const unsigned N = p.N, spc = p.spc;
+  const unsigned T = TT ? (unsigned)TT : p.T;
+  const unsigned m = N / spc, nl = ilog2(m);
+  const unsigned ipp = nth / N;
+  const unsigned item = tid / N, e = tid % N;
+  const unsigned ph = spc == 2u ? 2u * (e & (m - 1u)) + (e >> nl) : e;
+  uint32_t h[TT ? TT : 1];
+  if (TT) {
+#pragma unroll
+    for (int k = 0; k < (TT ? TT : 1); ++k) h[k] = p.coeff_t[(size_t)k * N + ph];
+  }
+  const uint64_t f0 = (uint64_t)blockIdx.x * FB;
+  const unsigned c0 = blockIdx.y * CB;
+  unsigned pfl = 0, sf = 0;
+  unsigned long long psat = 0;
+  __syncthreads();
+
+  const unsigned n_items = FB * CB;
+  for (unsigned base = 0; base < n_items; base += ipp) {
+    const unsigned it = base + item;
+    const unsigned fb = it / CB, cc = it % CB;
+    const uint64_t f = f0 + fb;
+    const unsigned c = c0 + cc;
+    const bool ok = it < n_items && f < p.F && c < p.C;
+    uint32_t v = 0;
+    if (ok) {
+      long long are = 0, aim = 0;
+      const uint32_t* xc = p.adc + (size_t)c * p.ld + ph;
+      const uint32_t* tc = p.tail + (size_t)c * (T > 1u ? T - 1u : 1u) * N + ph;
+#pragma unroll
+      for (int k = 0; k < (TT ? TT : 64); ++k) {
+        if (!TT && (unsigned)k >= T) break;
+        const long long fr = (long long)f - k;
+        const uint32_t xw = fr >= 0 ? __ldg(xc + (size_t)fr * N) : __ldg(tc + (size_t)(-fr - 1) * N);
+        const uint32_t hw = TT ? h[TT ? k : 0] : __ldg(p.coeff_t + (size_t)k * N + ph);
+        const cplx x = unpack(xw), hk = unpack(hw);
+        are += (long long)((int32_t)x.re * hk.re - (int32_t)x.im * hk.im);
+        aim += (long long)((int32_t)x.re * hk.im) + (long long)((int32_t)x.im * hk.re);
+      }
+      unsigned fr = 0, fi = 0;
+      const int32_t yr = q15_out64(are, &fr);
+      const int32_t yi = q15_out64(aim, &fi);
+      if (fr | fi) {
+        pfl |= fr | fi;
+        ++psat;
+      }
+      v = pack2(yr, yi);
+      if (p.tap_pfb) p.tap_pfb[((size_t)f * p.C + c) * N + ph] = v;
+    }
+    unsigned sfi = 0;
+    const uint32_t r = fft_elem(v, e, nl, spc, p.sched, s_tw, s_x, &sfi);
+    if (ok) {
+      sf |= sfi;
+      s_tile[((size_t)fb * N + fft_bin(e, nl)) * CB + cc] = r;
+    }
+  }
+  __syncthreads();
+  const unsigned tile_n = FB * N * CB;
+  for (unsigned t = tid; t < tile_n; t += nth) {
+    const unsigned fb = t / (N * CB), rem = t % (N * CB);
+    const unsigned bin = rem / CB, cc = rem % CB;
+    const uint64_t f = f0 + fb;
+    const unsigned c = c0 + cc;
+    if (f < p.F && c < p.C) {
+      const uint64_t slot = (p.g0 + f) % p.ring_frames;
+      p.ring[(slot * N + bin) * p.C + c] = s_tile[t];
+    }
+  }
+  reduce_stats(p.stats, pfl, psat, sf);
+}
+
+void launch_front(const FrontParams& p, cudaStream_t s) {
+  const unsigned nth = p.N > 256u ? p.N : 256u;
+  const unsigned ipp = nth / p.N;
+  unsigned CB = 8192u / p.N;
+  if (CB < 1u) CB = 1u;
+  if (CB > p.C) CB = p.C;
+  unsigned FB = ipp / CB;
+  if (FB < 1u) FB = 1u;
+  while (FB * CB * p.N > 8192u && FB > 1u) FB >>= 1;
+  const dim3 grid((p.F + FB - 1) / FB, (p.C + CB - 1) / CB);
+  const size_t smem = (1024u + nth + (size_t)FB * p.N * CB) * sizeof(uint32_t);
+  switch (p.T) {
+    case 4: k_front<4><<<grid, nth, smem, s>>>(p, FB, CB); break;
+    case 8: k_front<8><<<grid, nth, smem, s>>>(p, FB, CB); break;
+    case 16: k_front<16><<<grid, nth, smem, s>>>(p, FB, CB); break;
+    default: k_front<0><<<grid, nth, smem, s>>>(p, FB, CB); break;
+  }
+}
+
+// New delay line after a chunk of F frames: tail'[c][k] = frame F-1-k of the
+// chunk when it exists, else tail[c][k-F] (pfb_model.hpp:170-175).
+__global__ void k_tail(const uint32_t* adc, uint64_t ld, const uint32_t* old_tail,
+                       uint32_t* new_tail, uint32_t F, uint32_t C, uint32_t N, uint32_t D) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t n = (uint64_t)C * D * N;
+  if (i >= n) return;
+  const uint32_t p = (uint32_t)(i % N);
+  const uint32_t k = (uint32_t)((i / N) % D);
+  const uint32_t c = (uint32_t)(i / ((uint64_t)N * D));
+  new_tail[i] = (k < F) ? adc[(size_t)c * ld + (size_t)(F - 1 - k) * N + p]
+                        : old_tail[((size_t)c * D + (k - F)) * N + p];
+}
+
+void launch_tail_update(const uint32_t* adc, uint64_t ld, const uint32_t* old_tail,
+                        uint32_t* new_tail, uint32_t F, uint32_t C, uint32_t N, uint32_t T,
+                        cudaStream_t s) {
+  if (T <= 1) return;
+  const uint32_t D = T - 1;
+  const uint64_t n = (uint64_t)C * D * N;
+  k_tail<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(adc, ld, old_tail, new_tail, F, C, N, D);
+}
+
+// ---- per-block entry points ---------------------------------------------
+
+// pfb::PfbModel::step over `beats` beats, one thread per (beat, phase).
+__global__ void k_pfb_block(uint32_t P, uint32_t T, const uint32_t* coeff, const uint32_t* state,
+                            const uint32_t* in, uint32_t beats, uint32_t* out, uint8_t* flags) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint64_t)beats * P) return;
+  const uint32_t t = (uint32_t)(i / P), ph = (uint32_t)(i % P);
+  long long are = 0, aim = 0;
+  for (uint32_t k = 0; k < T; ++k) {
+    const uint32_t xw = k <= t ? in[(size_t)(t - k) * P + ph] : state[(size_t)(k - t - 1) * P + ph];
+    const cplx x = unpack(xw), h = unpack(coeff[(size_t)ph * T + k]);
+    are += (long long)((int32_t)x.re * h.re - (int32_t)x.im * h.im);
+    aim += (long long)((int32_t)x.re * h.im) + (long long)((int32_t)x.im * h.re);
+  }
+  unsigned fr = 0, fi = 0;
+  const int32_t yr = q15_out64(are, &fr), yi = q15_out64(aim, &fi);
+  out[i] = pack2(yr, yi);
+  if (flags) flags[i] = (uint8_t)((fr << 2) | fi);
+}
+
+void launch_pfb_block(uint32_t phases, uint32_t taps, const uint32_t* coeff,
+                      const uint32_t* state, const uint32_t* in, uint32_t beats, uint32_t* out,
+                      uint8_t* flags, cudaStream_t s) {
+  const uint64_t n = (uint64_t)beats * phases;
+  if (n) k_pfb_block<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(phases, taps, coeff, state, in,
+                                                                  beats, out, flags);
+}
+
+// fft::transform on independent frames; one item of N threads per frame.
+__global__ void k_fft_block(uint32_t N, uint32_t spc, uint32_t sched, int reorder,
+                            const uint32_t* in, uint32_t frames, uint32_t* out, uint32_t* bins,
+                            uint8_t* stage_flags) {
+  extern __shared__ uint32_t sm[];
+  uint32_t* s_tw = sm;
+  uint32_t* s_x = sm + 1024;
+  uint32_t* s_fl = s_x + blockDim.x;
+  const unsigned tid = threadIdx.x, nth = blockDim.x;
+  for (unsigned k = tid; k < 1024u; k += nth) s_tw[k] = g_tw[k];
+  const unsigned ipp = nth / N, item = tid / N, e = tid % N;
+  if (tid < ipp) s_fl[tid] = 0;
+  const unsigned m = N / spc, nl = ilog2(m);
+  const unsigned q = e >> nl, i = e & (m - 1u);
+  const unsigned ph = spc == 2u ? 2u * i + q : e;
+  const unsigned stages = ilog2(N);
+  __syncthreads();
+  for (uint64_t f0 = (uint64_t)blockIdx.x * ipp; f0 < frames; f0 += (uint64_t)gridDim.x * ipp) {
+    const uint64_t f = f0 + item;
+    const bool ok = f < frames;
+    const uint32_t v = ok ? in[f * N + ph] : 0u;
+    unsigned sf = 0;
+    const uint32_t r = fft_elem(v, e, nl, spc, sched, s_tw, s_x, &sf);
+    if (ok) {
+      const unsigned j = bitrev(i, nl);
+      if (bins) bins[f * N + (spc == 2u ? j + q * m : j)] = r;
+      if (out) {
+        const unsigned o = reorder ? (spc == 2u ? 2u * j + q : j) : (spc == 2u ? 2u * i + q : i);
+        out[f * N + o] = r;
+      }
+      if (sf) atomicOr(&s_fl[item], sf);
+    }
+    __syncthreads();
+    if (ok && e < stages && stage_flags) stage_flags[f * stages + e] = (uint8_t)((s_fl[item] >> (2u * e)) & 3u);
+    __syncthreads();
+    if (e == 0u) s_fl[item] = 0;
+    __syncthreads();
+  }
+}
+
+void launch_fft_block(uint32_t n, uint32_t spc, uint32_t sched, int reorder, const uint32_t* in,
+                      uint32_t frames, uint32_t* out, uint32_t* bins, uint8_t* stage_flags,
+                      cudaStream_t s) {
+  const unsigned nth = n > 256u ? n : 256u;
+  const unsigned ipp = nth / n;
+  unsigned grid = (frames + ipp - 1) / ipp;
+  if (grid > 4096u) grid = 4096u;
+  if (grid == 0u) return;
+  const size_t smem = (1024u + nth + ipp) * sizeof(uint32_t);
+  k_fft_block<<<grid, nth, smem, s>>>(n, spc, sched, reorder, in, frames, out, bins, stage_flags);
+}
+
+}  // namespace rd

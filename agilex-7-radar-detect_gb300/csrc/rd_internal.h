@@ -1,0 +1,129 @@
+// rd_internal.h - launch interfaces between the host ABI (api.cu) and the
+// kernel translation units (k_frontend.cu, k_backend.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/rd_chain.h"
+
+namespace rd {
+
+// Device-side cumulative statistics of one stream (zeroed at create).
+struct DevStats {
+  unsigned pfb_flags;
+  unsigned fft_flags;       // 2 bits per sub-stage g at bits [2g+1:2g]
+  unsigned bf_flags;
+  unsigned cov_flags;
+  unsigned long long pfb_sat;
+  unsigned long long bf_sat;
+  unsigned long long cov_sat_steps;
+  unsigned long long cfar_det;
+  unsigned long long cfar_sup;
+  unsigned long long events_total;   // events emitted so far (packet seq base)
+  unsigned long long events_call;    // events of the current call
+  unsigned long long scan_scratch[4];
+};
+
+// ---- front end: PFB + FFT + corner turn into the spectrum ring ------------
+struct FrontParams {
+  const uint32_t* adc;      // chunk frame 0 of channel 0; channel c at +c*ld
+  uint64_t ld;
+  const uint32_t* tail;     // [C][T-1][N]: tail[c][k][p] = frame -1-k
+  const uint32_t* coeff_t;  // [T][N] (tap-major copy of the phase-major bank)
+  uint32_t* ring;           // [R][N][C]
+  uint32_t ring_frames;     // R
+  uint64_t g0;              // stream frame index of chunk frame 0
+  uint32_t* tap_pfb;        // [F][C][N] chunk-relative, or null
+  uint32_t F, C, N, T, spc, sched;
+  DevStats* stats;
+};
+void launch_front(const FrontParams& p, cudaStream_t s);
+void launch_tail_update(const uint32_t* adc, uint64_t ld, const uint32_t* old_tail,
+                        uint32_t* new_tail, uint32_t F, uint32_t C, uint32_t N,
+                        uint32_t T, cudaStream_t s);
+
+// ---- per-block front-end kernels ------------------------------------------
+void launch_pfb_block(uint32_t phases, uint32_t taps, const uint32_t* coeff,
+                      const uint32_t* state, const uint32_t* in, uint32_t beats,
+                      uint32_t* out, uint8_t* flags, cudaStream_t s);
+void launch_fft_block(uint32_t n, uint32_t spc, uint32_t sched, int reorder,
+                      const uint32_t* in, uint32_t frames, uint32_t* out,
+                      uint32_t* bins, uint8_t* stage_flags, cudaStream_t s);
+
+// ---- back end ----------------------------------------------------------------
+struct BeamParams {
+  const uint32_t* ring;     // [R][N][C]
+  uint32_t ring_frames;
+  uint64_t g0;
+  const uint32_t* weights;  // [B][C]
+  uint32_t* power;          // [F][B][N]
+  uint32_t* beams_bn;       // [F][N][B] beam samples (null unless needed)
+  uint32_t F, C, N, B;
+  DevStats* stats;
+};
+void launch_beam(const BeamParams& p, cudaStream_t s);
+
+struct CovParams {
+  const uint32_t* ring;     // channel source: [R][N][C]
+  uint32_t ring_frames;
+  uint64_t g0;
+  const uint32_t* beams_bn; // beam source: [F][N][B]
+  uint32_t S;               // source vector length
+  uint32_t src_beam;        // 1: beams_bn, 0: ring
+  const uint32_t* px;
+  const uint32_t* py;
+  uint32_t P, F, N;
+  long long* acc_re;        // [N][P] integrator state
+  long long* acc_im;
+  unsigned* sticky;         // [N][P] (re << 2 | im)
+  unsigned* satcnt;         // [N][P][2]
+  uint32_t count0;          // samples already in the open window
+  uint32_t wl;              // effective window length
+  uint32_t exp_mode, exp_k, acc_w;
+  long long* out;           // [n_windows][N][P][2]
+  unsigned* win_flags;      // [n_windows]
+  uint32_t n_windows;       // windows that close in this chunk
+  DevStats* stats;
+};
+void launch_cov(const CovParams& p, cudaStream_t s);
+
+struct CfarParams {
+  const uint32_t* power_u32;  // [frames][n] (chain) ...
+  const int64_t* cells_i64;   // ... or raw signed cells (per-block entry)
+  uint32_t frames, n;         // CFAR frames (frame*beam) and cells per frame
+  uint32_t beams;             // frame index = u / beams, beam = u % beams
+  uint64_t g0;                // stream frame of chunk frame 0
+  const uint32_t* frame_ids;  // per CFAR frame (per-block entry) or null
+  int enable, go, dense;
+  uint32_t gl, gg, rl, rg, alpha;  // clamped geometry
+  uint32_t* counts;           // [frames] events per CFAR frame
+  uint32_t* detsup;           // [frames][2]
+  uint32_t* mask;             // [frames][ceil(n/32)] emitted-cell bitmask
+  unsigned long long* offsets;// [frames] exclusive offsets (from the scan)
+  rd_event* events;           // output, capacity cap
+  uint64_t cap;
+  uint32_t* flits;            // output flits or null
+  uint32_t packet_w, src_id, dest, vc, flit_words, nfl;
+  DevStats* stats;
+};
+void launch_cfar_decide(const CfarParams& p, cudaStream_t s);
+void launch_cfar_scan(const CfarParams& p, cudaStream_t s);
+void launch_cfar_emit(const CfarParams& p, cudaStream_t s);
+
+void launch_bf_block(uint32_t n_ant, uint32_t n_beams, const uint32_t* w,
+                     const uint32_t* x, uint64_t n_vec, uint32_t* y, long long* acc,
+                     uint8_t* flags, cudaStream_t s);
+void launch_power_block(const uint32_t* x, uint64_t n, long long* p, cudaStream_t s);
+void launch_cross_block(const uint32_t* x, const uint32_t* y, uint64_t n, long long* c,
+                        cudaStream_t s);
+void launch_packetize(const rd_event* ev, uint64_t n, uint32_t packet_w, uint32_t src,
+                      uint32_t dest, uint32_t vc, uint32_t seq0, uint32_t* flits,
+                      cudaStream_t s);
+void launch_fxp(const uint32_t* op, const int64_t* a, const int64_t* b, const uint32_t* sh,
+                const uint32_t* w, uint64_t n, int64_t* y, uint8_t* flags, cudaStream_t s);
+
+// Q1.15 twiddle table in device global memory (k_frontend.cu)
+const uint32_t* twiddles_device();
+
+}  // namespace rd

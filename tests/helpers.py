@@ -1,0 +1,67 @@
+"""Shared helpers of the parity tests."""
+from __future__ import annotations
+
+import numpy as np
+
+from rdgb import abi, scenario as sc
+
+CHAIN_KEYS = ("events", "flits", "cov_windows", "cov_acc")
+TAP_KEYS = ("tap_pfb", "tap_spectrum", "tap_beams", "tap_power")
+STAT_KEYS = ("frames", "pfb_flags", "pfb_sat_samples", "fft_stage_flags", "bf_flags",
+             "bf_sat_samples", "cov_flags", "cov_sat_steps", "hist_frames_done",
+             "hist_write_beats", "hist_reads", "hist_collisions", "hist_errors",
+             "hist_overwrites", "hist_skew", "align_beats", "align_missing", "align_dup",
+             "align_orphan", "align_timeout", "align_fault", "cfar_det", "cfar_sup",
+             "cfar_frames", "packets", "flits", "next_seq")
+
+
+def cfg_from_fixture(z) -> abi.RdConfig:
+    c = abi.RdConfig()
+    for name, _ in abi.RdConfig._fields_:
+        setattr(c, name, int(z[f"cfg_{name}"]))
+    return c
+
+
+def diff(a: dict, b: dict, keys=CHAIN_KEYS) -> list[str]:
+    bad = []
+    for k in keys:
+        if k not in a or k not in b:
+            continue
+        if not np.array_equal(np.asarray(a[k]), np.asarray(b[k])):
+            bad.append(k)
+    return bad
+
+
+def diff_stats(a: dict, b: dict) -> list[str]:
+    return [k for k in STAT_KEYS if a[k] != b[k]]
+
+
+def fixture_stats(z, i: int) -> dict:
+    keys = list(z[f"c{i}_stats_keys"])
+    vals = list(z[f"c{i}_stats_vals"])
+    d = {str(k): int(v) for k, v in zip(keys, vals)}
+    d["fft_stage_flags"] = [int(v) for v in z[f"c{i}_fft_stage_flags"]]
+    return d
+
+
+def scenario_inputs(name: str, frames: int, **over):
+    p = sc.preset(name, **over)
+    cfg = sc.make_config(p, max_frames=over.get("max_frames", None) if False else None)
+    px, py = sc.pair_table(p)
+    coeff = sc.coefficients(p.n_fft, p.taps)
+    w = sc.steering_weights(p.n_chan, p.n_beams)
+    x = sc.adc(p, frames * p.n_fft)
+    return p, cfg, (px, py), coeff, w, x
+
+
+def event_fields(ev: np.ndarray) -> dict:
+    """Decodes the 176-bit events (cfar_model.hpp:75-84) into columns."""
+    w = ev["w"].astype(object)
+    v = [int(a) | (int(b) << 64) | (int(c) << 128) for a, b, c in w]
+
+    def f(lsb, n):
+        return np.array([(x >> lsb) & ((1 << n) - 1) for x in v], dtype=np.int64)
+
+    return {"kind": f(0, 2), "bin": f(2, 16), "frame_id": f(18, 16), "ref_cnt": f(34, 7),
+            "alpha": f(41, 16), "det": f(57, 16), "sup": f(73, 16), "cut": f(89, 40),
+            "sum": f(129, 47)}

@@ -1,0 +1,171 @@
+"""Chain parity on the GPU, through the C ABI: the committed fixtures made by
+the reference's own model headers, and the CPU oracle on seeded inputs,
+including chunking across launches, multiple calls, device-resident input,
+history reads and the covariance flush. Bit-exact."""
+import numpy as np
+import pytest
+
+from conftest import load_chain_fixture
+from helpers import (CHAIN_KEYS, TAP_KEYS, cfg_from_fixture, diff, diff_stats, event_fields,
+                     fixture_stats)
+from rdgb import abi, chain as gc, scenario as sc
+
+pytestmark = pytest.mark.gpu
+
+FIXTURES = ["tiny", "tiny_calls", "ref_tiny", "medium_slice", "tiny_go_dense", "tiny_sat"]
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_chain_fixture(gpulib, name):
+    z = load_chain_fixture(name)
+    cfg = cfg_from_fixture(z)
+    ch = gc.Chain(cfg, z["coeff"], z["weights"], (z["px"], z["py"]))
+    n_fft = cfg.n_fft
+    f0 = 0
+    for i, nf in enumerate(z["calls"]):
+        taps = f"c{i}_tap_pfb" in z
+        r = ch.process(z["adc"][:, f0 * n_fft:(f0 + nf) * n_fft], taps=taps,
+                       cap_events=int(nf) * cfg.n_beams * (n_fft + 1))
+        want = {k[len(f"c{i}_"):]: z[k] for k in z.files if k.startswith(f"c{i}_")}
+        assert diff(r, want, CHAIN_KEYS + TAP_KEYS) == [], (name, i)
+        assert diff_stats(ch.stats(), fixture_stats(z, i)) == [], (name, i)
+        f0 += nf
+    fl = ch.flush_cov()
+    assert np.array_equal(fl["cov_windows"], z["flush_cov_windows"])
+    assert np.array_equal(fl["cov_acc"], z["flush_cov_acc"])
+
+
+@pytest.mark.parametrize("name", ["tiny", "ref_tiny"])
+def test_history_reads_fixture(gpulib, name):
+    z = load_chain_fixture(name)
+    cfg = cfg_from_fixture(z)
+    ch = gc.Chain(cfg, z["coeff"], z["weights"], (z["px"], z["py"]))
+    ch.process(z["adc"])
+    p = {"tiny": sc.preset("tiny"), "ref_tiny": sc.preset("ref_tiny")}[name]
+    got = [ch.read_history(b, off) for off in range(0, min(p.hist_frames, 6))
+           for b in (0, 1, p.n_fft - 1)]
+    assert np.array_equal(np.array([g[0] for g in got]), z["hist_vec"])
+    assert np.array_equal(np.array([g[1] for g in got], np.uint32), z["hist_fid"])
+    assert np.array_equal(np.array([g[2] for g in got], np.uint32), z["hist_flags"])
+
+
+def _random_cfg(rng, name, max_frames):
+    p = sc.preset(name)
+    cfg = sc.make_config(p, max_frames=max_frames)
+    cfg.cfar_mode = int(rng.integers(0, 2))
+    cfg.cfar_out_mode = int(rng.integers(0, 2)) if p.n_fft <= 64 else 0
+    cfg.alpha = int(rng.integers(200, 4096))
+    cfg.scale_sched = int(rng.integers(0, 2**32)) | 0xFFFFFF00
+    cfg.cov_window = int(rng.integers(1, 40))
+    if rng.integers(0, 2):
+        cfg.cov_mode, cfg.cov_exp_k, cfg.cov_acc_w = abi.RD_COV_EXP, int(rng.integers(0, 16)), 40
+    return p, cfg
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_chain_random_vs_oracle(gpulib, port, seed):
+    rng = np.random.default_rng(100 + seed)
+    name = ["tiny", "ref_tiny", "tiny", "medium", "ref_tiny", "tiny"][seed]
+    p, cfg = _random_cfg(rng, name, max_frames=int(rng.integers(3, 40)))
+    px, py = sc.pair_table(p)
+    coeff = sc.coefficients(p.n_fft, p.taps) if seed % 2 else \
+        rng.integers(0, 2**32, size=p.n_fft * p.taps, dtype=np.uint64).astype(np.uint32)
+    w = sc.steering_weights(p.n_chan, p.n_beams)
+    g = gc.Chain(cfg, coeff, w, (px, py))
+    o = port.chain(cfg, coeff, w, px, py)
+    start = 0
+    for call in range(3):
+        nf = int(rng.integers(1, 70 if p.n_fft <= 64 else 25))
+        x = sc.adc(p, nf * p.n_fft, start=start * p.n_fft)
+        rg = g.process(x, taps=True, cap_events=nf * p.n_beams * (p.n_fft + 1))
+        ro = o.process(x, taps=True, threads=4)
+        assert diff(rg, ro, CHAIN_KEYS + TAP_KEYS) == [], (seed, call)
+        assert diff_stats(g.stats(), o.stats()) == [], (seed, call)
+        start += nf
+    fg, fo = g.flush_cov(), o.flush_cov()
+    assert diff(fg, fo, ("cov_windows", "cov_acc")) == []
+
+
+def test_chain_medium_cpi_vs_oracle(gpulib, port):
+    p = sc.preset("medium")
+    cfg = sc.make_config(p, max_frames=100)
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    x = sc.adc(p, p.cpi_samples)
+    rg = gc.Chain(cfg, coeff, w, (px, py)).process(x)
+    ro = port.chain(cfg, coeff, w, px, py).process(x, taps=False, threads=8)
+    assert diff(rg, ro) == []
+    assert len(rg["cov_windows"]) == 1 and rg["cov_windows"][0]["sample_count"] == 256
+    assert (event_fields(rg["events"][:50])["alpha"] == p.alpha).all()
+
+
+def test_chain_full_geometry_slice_vs_oracle(gpulib, port):
+    # the full workload's geometry (64 ch, 1024-point PFB x 16 taps, 64 beams,
+    # 2080 covariance pairs), 20 frames with an 8-frame window
+    p = sc.preset("full", cov_window=8)
+    cfg = sc.make_config(p, max_frames=12)
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    x = sc.adc(p, 20 * p.n_fft)
+    g = gc.Chain(cfg, coeff, w, (px, py))
+    rg = g.process(x, taps=True)
+    o = port.chain(cfg, coeff, w, px, py)
+    ro = o.process(x, taps=True, threads=8)
+    assert diff(rg, ro, CHAIN_KEYS + TAP_KEYS) == []
+    assert diff_stats(g.stats(), o.stats()) == []
+
+
+def test_device_input_and_chunking_invariance(gpulib):
+    torch = pytest.importorskip("torch")
+    p = sc.preset("medium")
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    n = 2 * p.cpi_samples
+    x = sc.adc(p, n)
+    d = torch.from_numpy(x.view(np.int32)).cuda()
+    results = []
+    for mf in (512, 100, 37):
+        cfg = sc.make_config(p, max_frames=mf)
+        ch = gc.Chain(cfg, coeff, w, (px, py))
+        ch.process_device(d.data_ptr(), n, n, torch.cuda.current_stream().cuda_stream)
+        results.append((ch.fetch(n // p.n_fft), ch.stats()))
+        ch.close()
+    host = gc.Chain(sc.make_config(p, max_frames=512), coeff, w, (px, py)).process(x)
+    for r, st in results:
+        assert diff(r, host) == []
+        assert diff_stats(st, results[0][1]) == []
+
+
+def test_zero_input(gpulib):
+    p = sc.preset("tiny")
+    cfg = sc.make_config(p)
+    px, py = sc.pair_table(p)
+    ch = gc.Chain(cfg, sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams),
+                  (px, py))
+    r = ch.process(np.zeros((p.n_chan, 64 * p.n_fft), np.uint32), taps=True)
+    assert not r["tap_power"].any() and not r["tap_spectrum"].any()
+    f = event_fields(r["events"])
+    assert (f["kind"] == 3).all() and len(r["events"]) == 64 * p.n_beams
+    assert not r["cov_acc"].any() if len(r["cov_acc"]) else True
+
+
+def test_empty_call_and_bad_sizes(gpulib):
+    p = sc.preset("tiny")
+    cfg = sc.make_config(p)
+    ch = gc.Chain(cfg, sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams))
+    r = ch.process(np.zeros((p.n_chan, 0), np.uint32))
+    assert r["n_frames"] == 0 and len(r["events"]) == 0
+    with pytest.raises(RuntimeError, match="RD_EINVAL"):
+        ch.process(np.zeros((p.n_chan, p.n_fft + 3), np.uint32))
+
+
+def test_event_truncation_reports(gpulib, port):
+    p = sc.preset("tiny")
+    cfg = sc.make_config(p)
+    cfg.cfar_out_mode = abi.RD_CFAR_DENSE
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    x = sc.adc(p, 10 * p.n_fft)
+    ch = gc.Chain(cfg, coeff, w, (px, py))
+    with pytest.raises(RuntimeError, match="RD_ETRUNC"):
+        ch.process(x, cap_events=5)

@@ -1,0 +1,165 @@
+"""CPU oracle pinning: the plain-C restatement (oracle/orc_port.c) against the
+reference's own golden vectors, against chain fixtures produced by the
+reference's model headers, and against those headers directly on seeded
+random cases. No GPU."""
+import numpy as np
+import pytest
+
+from conftest import load_chain_fixture
+from helpers import CHAIN_KEYS, TAP_KEYS, cfg_from_fixture, diff, diff_stats, fixture_stats
+from rdgb import abi, scenario as sc
+from rdgb.twiddle import DIGEST, TWIDDLES
+
+
+def test_twiddle_table(port):
+    # fft_twiddle_table.hpp:40-43: digest c756048fbc00d64f, axis points exact
+    assert DIGEST == "c756048fbc00d64f"
+    t = port.twiddles()
+    assert np.array_equal(t, np.array(TWIDDLES, np.uint32))
+    re, im = sc.unpack(t)
+    assert (re[0], im[0]) == (32767, 0)
+    assert (re[256], im[256]) == (0, -32768)
+    assert (re[512], im[512]) == (-32768, 0)
+
+
+def test_twiddle_matches_reference(refo):
+    assert np.array_equal(refo.twiddles(), np.array(TWIDDLES, np.uint32))
+
+
+def test_fxp_ops_vectors(port, blockvec):
+    z = blockvec
+    y, fl = port.fxp(z["fxp_op"], z["fxp_a"], z["fxp_b"], z["fxp_sh"], z["fxp_w"])
+    assert len(y) == 1457
+    assert np.array_equal(y, z["fxp_y"])
+    assert np.array_equal(fl, z["fxp_flags"])
+
+
+def test_cmult_vectors(port, blockvec):
+    z = blockvec
+    a, b = z["cmult_a"], z["cmult_b"]
+    n = len(a)
+    ops = np.concatenate([np.full(n, abi.OP_CODE["cmul_re"]), np.full(n, abi.OP_CODE["cmul_im"])])
+    y, fl = port.fxp(ops, np.concatenate([a, a]).astype(np.int64),
+                     np.concatenate([b, b]).astype(np.int64), np.zeros(2 * n), np.zeros(2 * n))
+    yre, yim = sc.unpack(z["cmult_y"])
+    assert np.array_equal(y[:n], yre) and np.array_equal(y[n:], yim)
+    assert np.array_equal(fl[:n], z["cmult_f_re"]) and np.array_equal(fl[n:], z["cmult_f_im"])
+    # X * conj(Y) with Y = conj(b) is the exact 33-bit product p of cmult.vec
+    bre, bim = sc.unpack(b)
+    c = port.cross_power(a, sc.pack(bre, -bim)).reshape(n, 2)
+    ok = bim != -32768  # conj of -32768j is not representable
+    assert np.array_equal(c[ok, 0], z["cmult_p_re"][ok])
+    assert np.array_equal(c[ok, 1], z["cmult_p_im"][ok])
+
+
+def test_fft64_vectors(port, blockvec):
+    z = blockvec
+    n, spc = int(z["fft_n"]), int(z["fft_spc"])
+    for r in range(len(z["fft_sched"])):
+        out, _, sf = port.fft(n, spc, int(z["fft_sched"][r]), int(z["fft_reorder"][r]), z["fft_x"][r])
+        assert np.array_equal(out, z["fft_y"][r]), f"record {r}"
+        assert np.array_equal(sf, z["fft_stage_flags"][r]), f"record {r} flags"
+
+
+def test_fft_reorder_property(port):
+    # test_fft_ref.cpp check 2: reorder on/off relate by bitrev of the beat
+    rng = np.random.default_rng(1)
+    for n, spc in ((64, 2), (256, 2), (1024, 1), (16, 2), (8, 2)):
+        x = rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
+        o1, b1, _ = port.fft(n, spc, 0xFFFFFFFF, 1, x)
+        o0, b0, _ = port.fft(n, spc, 0xFFFFFFFF, 0, x)
+        assert np.array_equal(b1, b0)
+        m, nl = n // spc, int(np.log2(n // spc))
+        for j in range(m):
+            src = int(format(j, f"0{nl}b")[::-1], 2)
+            assert np.array_equal(o1[j * spc:(j + 1) * spc], o0[src * spc:(src + 1) * spc])
+
+
+@pytest.mark.parametrize("idx", range(10))
+def test_pfb_vectors(port, blockvec, idx):
+    z = blockvec
+    name = str(z["pfb_sets"][idx])
+    P, T = int(z[f"{name}_P"]), int(z[f"{name}_T"])
+    x = z[f"{name}_x"]
+    y, fl, _ = port.pfb(P, T, z[f"{name}_coeff"], np.zeros((T - 1) * P, np.uint32), x)
+    assert np.array_equal(y.reshape(x.shape), z[f"{name}_y"]), name
+    assert np.array_equal((fl >> 2).reshape(x.shape), z[f"{name}_f_re"]), name
+    assert np.array_equal((fl & 3).reshape(x.shape), z[f"{name}_f_im"]), name
+
+
+def test_pfb_state_carry(port):
+    # two calls with the returned delay line equal one call (swap-free stream)
+    rng = np.random.default_rng(2)
+    P, T = 8, 16
+    c = rng.integers(0, 2**32, size=P * T, dtype=np.uint64).astype(np.uint32)
+    x = rng.integers(0, 2**32, size=40 * P, dtype=np.uint64).astype(np.uint32)
+    y_all, _, _ = port.pfb(P, T, c, np.zeros((T - 1) * P, np.uint32), x)
+    y1, _, st = port.pfb(P, T, c, np.zeros((T - 1) * P, np.uint32), x[:3 * P])
+    y2, _, _ = port.pfb(P, T, c, st, x[3 * P:])
+    assert np.array_equal(np.concatenate([y1, y2]), y_all)
+
+
+CHAIN_FIXTURES = ["tiny", "tiny_calls", "ref_tiny", "medium_slice", "tiny_go_dense", "tiny_sat"]
+
+
+@pytest.mark.parametrize("name", CHAIN_FIXTURES)
+def test_port_chain_fixture(port, name):
+    z = load_chain_fixture(name)
+    cfg = cfg_from_fixture(z)
+    ch = port.chain(cfg, z["coeff"], z["weights"], z["px"], z["py"])
+    n_fft = cfg.n_fft
+    f0 = 0
+    for i, nf in enumerate(z["calls"]):
+        r = ch.process(z["adc"][:, f0 * n_fft:(f0 + nf) * n_fft], taps=f"c{i}_tap_pfb" in z,
+                       threads=4)
+        want = {k[len(f"c{i}_"):]: z[k] for k in z.files if k.startswith(f"c{i}_")}
+        assert diff(r, want, CHAIN_KEYS + TAP_KEYS) == []
+        assert diff_stats(ch.stats(), fixture_stats(z, i)) == []
+        f0 += nf
+    fl = ch.flush_cov()
+    assert np.array_equal(fl["cov_windows"], z["flush_cov_windows"])
+    assert np.array_equal(fl["cov_acc"], z["flush_cov_acc"])
+
+
+def test_port_matches_reference_random(port, refo):
+    rng = np.random.default_rng(11)
+    for trial in range(4):
+        name = ["tiny", "ref_tiny", "tiny", "medium"][trial]
+        p = sc.preset(name)
+        cfg = sc.make_config(p)
+        cfg.cfar_mode = int(rng.integers(0, 2))
+        cfg.cfar_out_mode = int(rng.integers(0, 2)) if name != "medium" else 0
+        cfg.alpha = int(rng.integers(0, 4096))
+        cfg.guard_lead, cfg.guard_lag = (int(v) for v in rng.integers(0, 4, 2))
+        cfg.ref_lead, cfg.ref_lag = (int(v) for v in rng.integers(0, 9, 2))
+        cfg.scale_sched = int(rng.integers(0, 2**32))
+        px, py = sc.pair_table(p)
+        coeff = rng.integers(0, 2**32, size=p.n_fft * p.taps, dtype=np.uint64).astype(np.uint32)
+        w = rng.integers(0, 2**32, size=p.n_chan * p.n_beams, dtype=np.uint64).astype(np.uint32)
+        frames = 20 if name == "medium" else 50
+        x = rng.integers(0, 2**32, size=(p.n_chan, frames * p.n_fft), dtype=np.uint64).astype(np.uint32)
+        a = port.chain(cfg, coeff, w, px, py)
+        b = refo.chain(cfg, coeff, w, px, py)
+        ra, rb = a.process(x, taps=True, threads=3), b.process(x, taps=True)
+        assert diff(ra, rb, CHAIN_KEYS + TAP_KEYS) == [], trial
+        assert diff_stats(a.stats(), b.stats()) == [], trial
+
+
+def test_history_reads(port, refo):
+    p = sc.preset("tiny")
+    cfg = sc.make_config(p)
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    a = port.chain(cfg, coeff, w, px, py)
+    b = refo.chain(cfg, coeff, w, px, py)
+    # before any frame: out of range, frame id wraps, zeros
+    va, fa, ga = a.read_history(3, 0)
+    vb, fb, gb = b.read_history(3, 0)
+    assert (np.array_equal(va, vb), fa, ga) == (True, fb, gb)
+    x = sc.adc(p, 11 * p.n_fft)
+    a.process(x), b.process(x)
+    for off in range(0, 10):
+        for bin_ in (0, 5, 15, 16, 70000):
+            assert [np.asarray(v).tolist() for v in a.read_history(bin_, off)] == \
+                   [np.asarray(v).tolist() for v in b.read_history(bin_, off)]
+    assert a.stats()["hist_reads"] == b.stats()["hist_reads"]
