@@ -927,8 +927,8 @@ rd_status rd_cross_power_run(const rd_cplx16* x, const rd_cplx16* y, uint64_t n,
 rd_status rd_cfar_run(const int64_t* cells, uint32_t n, uint32_t frames, const rd_config* cfg,
                       const uint32_t* frame_ids, rd_event* events, uint64_t cap,
                       uint64_t* n_events) {
-  if (!cells || !cfg || !frame_ids || !n_events || n == 0 || n > 65535)
-    return fail(RD_EINVAL, "bad argument");
+  if (!cells || !cfg || !frame_ids || !n_events || n == 0 || n > 4096)
+    return fail(RD_EINVAL, "bad argument (frames of 1..4096 cells)");
   if (!rd_device_ok()) return fail(RD_EDEVICE, "no usable CUDA device");
   Scratch sc;
   long long* dc;
