@@ -182,6 +182,51 @@ struct rd_chain {
   std::vector<rd_cov_window> call_windows;
   uint64_t call_cap_events = 0;
   uint64_t launches = 0;
+  // stage timing (rd_chain_set_profiling)
+  bool profiling = false;
+  struct Pending {
+    int id;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> pool;
+  double ktime[8] = {0};
+  uint64_t klaunch[8] = {0};
+  cudaEvent_t ev_get() {
+    if (!pool.empty()) {
+      cudaEvent_t e = pool.back();
+      pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+  }
+};
+
+static const char* kKernelNames[8] = {"k_front", "k_tail", "k_beam", "k_cov",
+                                      "k_cfar_decide", "k_cfar_scan", "k_cfar_emit", "k_call"};
+enum { KT_FRONT = 0, KT_TAIL, KT_BEAM, KT_COV, KT_DECIDE, KT_SCAN, KT_EMIT, KT_CALL };
+
+// Brackets one kernel launch with events on the chain's stream when stage
+// timing is on.
+struct KTimer {
+  rd_chain* ch;
+  int id;
+  cudaEvent_t a = nullptr;
+  KTimer(rd_chain* c, int i) : ch(c), id(i) {
+    if (ch->profiling) {
+      a = ch->ev_get();
+      cudaEventRecord(a, ch->stream);
+    }
+  }
+  ~KTimer() {
+    if (a) {
+      cudaEvent_t b = ch->ev_get();
+      cudaEventRecord(b, ch->stream);
+      ch->pending.push_back({id, a, b});
+    }
+  }
 };
 
 extern "C" {
@@ -362,6 +407,11 @@ void rd_chain_destroy(rd_chain* ch) {
   ch->cov_out.release(); ch->sticky.release(); ch->satcnt.release(); ch->win_flags.release();
   ch->counts.release(); ch->detsup.release(); ch->mask.release(); ch->offsets.release();
   ch->events.release(); ch->flits.release(); ch->tap_pfb.release(); ch->stats.release();
+  for (const rd_chain::Pending& p : ch->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (cudaEvent_t e : ch->pool) cudaEventDestroy(e);
   if (ch->own_stream && ch->stream) cudaStreamDestroy(ch->stream);
   delete ch;
 }
@@ -426,9 +476,15 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   fp.spc = c.spc;
   fp.sched = c.scale_sched;
   fp.stats = st;
-  launch_front(fp, s);
-  launch_tail_update(adc, ld, ch->tail[ch->tail_cur].p, ch->tail[ch->tail_cur ^ 1].p, F, C, N,
-                     c.taps, s);
+  {
+    KTimer t(ch, KT_FRONT);
+    launch_front(fp, s);
+  }
+  if (c.taps > 1) {
+    KTimer t(ch, KT_TAIL);
+    launch_tail_update(adc, ld, ch->tail[ch->tail_cur].p, ch->tail[ch->tail_cur ^ 1].p, F, C,
+                       N, c.taps, s);
+  }
   ch->tail_cur ^= (c.taps > 1) ? 1 : 0;
   ch->launches += (c.taps > 1) ? 2 : 1;
 
@@ -444,7 +500,10 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   bp.N = N;
   bp.B = B;
   bp.stats = st;
-  launch_beam(bp, s);
+  {
+    KTimer t(ch, KT_BEAM);
+    launch_beam(bp, s);
+  }
   ch->launches++;
 
   if (c.cov_source != RD_COV_OFF && ch->P) {
@@ -477,7 +536,10 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
     cp.win_flags = ch->win_flags.p ? ch->win_flags.p + w0 : nullptr;
     cp.n_windows = n_win;
     cp.stats = st;
-    launch_cov(cp, s);
+    {
+      KTimer t(ch, KT_COV);
+      launch_cov(cp, s);
+    }
     ch->launches++;
     // window headers, known on the host (covar_model.hpp:229-235)
     uint32_t cnt = ch->cov_count;
@@ -525,9 +587,18 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   fp2.flit_words = rd_flit_words(c.packet_w);
   fp2.nfl = rd_detection_flits(c.packet_w);
   fp2.stats = st;
-  launch_cfar_decide(fp2, s);
-  launch_cfar_scan(fp2, s);
-  launch_cfar_emit(fp2, s);
+  {
+    KTimer t(ch, KT_DECIDE);
+    launch_cfar_decide(fp2, s);
+  }
+  {
+    KTimer t(ch, KT_SCAN);
+    launch_cfar_scan(fp2, s);
+  }
+  {
+    KTimer t(ch, KT_EMIT);
+    launch_cfar_emit(fp2, s);
+  }
   ch->launches += 3;
 
   // host bookkeeping of the history and align counters, frame by frame
@@ -758,6 +829,41 @@ rd_status rd_chain_flush_cov(rd_chain* ch, rd_output* out) {
   }
   ch->cov_count = 0;
   ch->cov_window_id = 0;
+  return RD_OK;
+}
+
+rd_status rd_chain_set_profiling(rd_chain* ch, int on) {
+  if (!ch) return fail(RD_EINVAL, "null chain");
+  ch->profiling = on != 0;
+  return RD_OK;
+}
+
+rd_status rd_chain_kernel_times(rd_chain* ch, rd_kernel_time* out, uint32_t cap, uint32_t* n) {
+  if (!ch || !n) return fail(RD_EINVAL, "null argument");
+  CK(cudaStreamSynchronize(ch->stream));
+  for (const rd_chain::Pending& p : ch->pending) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, p.a, p.b));
+    ch->ktime[p.id] += ms;
+    ch->klaunch[p.id] += 1;
+    ch->pool.push_back(p.a);
+    ch->pool.push_back(p.b);
+  }
+  ch->pending.clear();
+  uint32_t k = 0;
+  for (int i = 0; i < 8; ++i) {
+    if (!ch->klaunch[i]) continue;
+    if (out && k < cap) {
+      std::memset(&out[k], 0, sizeof(out[k]));
+      std::strncpy(out[k].name, kKernelNames[i], sizeof(out[k].name) - 1);
+      out[k].launches = ch->klaunch[i];
+      out[k].total_ms = ch->ktime[i];
+    }
+    ++k;
+    ch->klaunch[i] = 0;
+    ch->ktime[i] = 0;
+  }
+  *n = k;
   return RD_OK;
 }
 

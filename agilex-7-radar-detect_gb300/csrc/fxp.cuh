@@ -138,13 +138,15 @@ RD_HD cplx cmul_tw(cplx a, cplx w, unsigned* fl) {
   o.im = (int16_t)sat16(ri);
   return o;
 }
-// -j * c with a saturating negate (fft_ref.hpp:322-331)
+// -j * c with a saturating negate (fft_ref.hpp:322-331). -(-32768) is the
+// only input that leaves the 16-bit range; it is selected explicitly so the
+// saturation and its sat_pos flag never depend on how the negate is lowered.
 RD_HD cplx neg_j(cplx c, unsigned* fl) {
-  const int32_t n = -(int32_t)c.re;
-  *fl |= flags16(n);
+  const bool over = c.re == (int16_t)-32768;
+  *fl |= over ? 2u : 0u;
   cplx o;
   o.re = c.im;
-  o.im = (int16_t)sat16(n);
+  o.im = over ? (int16_t)32767 : (int16_t)(-(int32_t)c.re);
   return o;
 }
 // covar::power (covar_model.hpp:99-102): re^2 + im^2 in [0, 2^31]

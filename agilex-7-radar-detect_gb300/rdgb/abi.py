@@ -81,6 +81,10 @@ class RdOutput(C.Structure):
     ]
 
 
+class RdKernelTime(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("total_ms", C.c_double)]
+
+
 class RdStats(C.Structure):
     _fields_ = [
         ("frames", C.c_uint64), ("pfb_flags", C.c_uint32), ("pfb_sat_samples", C.c_uint64),
@@ -142,6 +146,8 @@ def declare_rd(lib) -> None:
     _proto(lib, "rd_chain_fetch", I32, [VP, P(RdOutput)])
     _proto(lib, "rd_chain_last_launches", U64, [VP])
     _proto(lib, "rd_chain_flush_cov", I32, [VP, P(RdOutput)])
+    _proto(lib, "rd_chain_set_profiling", I32, [VP, I32])
+    _proto(lib, "rd_chain_kernel_times", I32, [VP, P(RdKernelTime), U32, P(U32)])
     _proto(lib, "rd_chain_stats", I32, [VP, P(RdStats)])
     _proto(lib, "rd_chain_read_history", I32, [VP, U32, U32, VP, P(U32), P(U32)])
     _proto(lib, "rd_pfb_run", I32, [U32, U32, VP, VP, VP, U32, VP, VP])
@@ -163,7 +169,7 @@ EXPORTED = [
     "rd_cov_pairs", "rd_chain_create", "rd_chain_destroy", "rd_chain_set_coeff",
     "rd_chain_set_weights", "rd_chain_set_pairs", "rd_chain_process",
     "rd_chain_process_device", "rd_chain_fetch", "rd_chain_last_launches",
-    "rd_chain_flush_cov", "rd_chain_stats", "rd_chain_read_history", "rd_pfb_run",
+    "rd_chain_flush_cov", "rd_chain_set_profiling", "rd_chain_kernel_times", "rd_chain_stats", "rd_chain_read_history", "rd_pfb_run",
     "rd_fft_run", "rd_bf_run", "rd_power_run", "rd_cross_power_run", "rd_cfar_run",
     "rd_packetize", "rd_fxp_apply", "rd_last_error", "rd_device_ok", "rd_version",
 ]

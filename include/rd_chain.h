@@ -200,6 +200,19 @@ rd_status rd_chain_fetch(rd_chain* ch, rd_output* out);
 /* Number of kernels the last process call launched. */
 uint64_t rd_chain_last_launches(const rd_chain* ch);
 
+/* Stage timing: when enabled, every kernel the chain launches is bracketed by
+ * CUDA events on the chain's stream. rd_chain_kernel_times() waits for the
+ * stream and returns, per kernel, the launches and the summed device time
+ * since the last call (then resets). */
+typedef struct rd_kernel_time {
+  char name[32];
+  uint64_t launches;
+  double total_ms;
+} rd_kernel_time;
+rd_status rd_chain_set_profiling(rd_chain* ch, int on);
+rd_status rd_chain_kernel_times(rd_chain* ch, rd_kernel_time* out, uint32_t cap,
+                                uint32_t* n);
+
 /* Emits every open covariance window as a flushed, truncated result
  * (covar::Integrator::step with flush=1, covar_model.hpp:226-249). */
 rd_status rd_chain_flush_cov(rd_chain* ch, rd_output* out);
