@@ -158,7 +158,7 @@ struct rd_chain {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
 
-  DevBuf<uint32_t> coeff_t, weights, tail[2], ring, power, beams_bn, stage;
+  DevBuf<uint32_t> coeff_t, weights, tail[2], ring, power, beams_bn, stage, tw_pos;
   int tail_cur = 0;
   DevBuf<uint32_t> px, py;
   DevBuf<long long> acc_re, acc_im, cov_out;
@@ -385,6 +385,16 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
       return RD_ENOMEM;
     }
   }
+  {
+    std::vector<uint32_t> tp(5u * N);
+    uint32_t words = 0;
+    twiddle_positions(N, c.spc, tp.data(), &words);
+    if (bad(ch->tw_pos.ensure(words ? words : 1))) {
+      rd_chain_destroy(ch);
+      return RD_ENOMEM;
+    }
+    if (words) cudaMemcpy(ch->tw_pos.p, tp.data(), words * 4, cudaMemcpyHostToDevice);
+  }
   ch->hist.n_ant = C;
   ch->hist.n = N;
   ch->hist.lanes = c.spc;
@@ -403,6 +413,7 @@ void rd_chain_destroy(rd_chain* ch) {
   if (ch->stream) cudaStreamSynchronize(ch->stream);
   ch->coeff_t.release(); ch->weights.release(); ch->tail[0].release(); ch->tail[1].release();
   ch->ring.release(); ch->power.release(); ch->beams_bn.release(); ch->stage.release();
+  ch->tw_pos.release();
   ch->px.release(); ch->py.release(); ch->acc_re.release(); ch->acc_im.release();
   ch->cov_out.release(); ch->sticky.release(); ch->satcnt.release(); ch->win_flags.release();
   ch->counts.release(); ch->detsup.release(); ch->mask.release(); ch->offsets.release();
@@ -459,6 +470,7 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   const uint32_t N = c.n_fft, C = c.n_chan, B = c.n_beams;
   cudaStream_t s = ch->stream;
   DevStats* st = ch->stats.p;
+  const uint32_t ring_base = (uint32_t)(ch->frame % ch->R);
 
   FrontParams fp{};
   fp.adc = adc;
@@ -467,7 +479,9 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   fp.coeff_t = ch->coeff_t.p;
   fp.ring = ch->ring.p;
   fp.ring_frames = ch->R;
+  fp.ring_base = ring_base;
   fp.g0 = ch->frame;
+  fp.tw_pos = ch->tw_pos.p;
   fp.tap_pfb = d_tap_pfb;
   fp.F = F;
   fp.C = C;
@@ -491,6 +505,7 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   BeamParams bp{};
   bp.ring = ch->ring.p;
   bp.ring_frames = ch->R;
+  bp.ring_base = ring_base;
   bp.g0 = ch->frame;
   bp.weights = ch->weights.p;
   bp.power = ch->power.p;
@@ -513,7 +528,12 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
     CovParams cp{};
     cp.ring = ch->ring.p;
     cp.ring_frames = ch->R;
+    cp.ring_base = ring_base;
     cp.g0 = ch->frame;
+    // no step can saturate: exponential mode, or a block window whose worst
+    // sum (wl terms of magnitude <= 2^31) fits acc_w (covar_model.hpp:82-90)
+    cp.exact = (c.cov_mode == RD_COV_EXP) || c.cov_acc_w >= 64 ||
+               (uint64_t)wl <= ((1ull << (c.cov_acc_w - 32)) - 1ull);
     cp.beams_bn = ch->beams_bn.p;
     cp.S = ch->S;
     cp.src_beam = c.cov_source == RD_COV_BEAM;
@@ -654,9 +674,11 @@ rd_status rd_chain_process_device(rd_chain* ch, const rd_cplx16* adc_dev, uint64
   const rd_config& c = ch->cfg;
   if (n % c.n_fft) return fail(RD_EINVAL, "n=%llu is not a multiple of n_fft", (unsigned long long)n);
   if (ld < n) return fail(RD_EINVAL, "ld < n");
-  cudaStream_t user = (cudaStream_t)stream;
-  cudaEvent_t ev_in;
-  if (user) {  // order the chain after the caller's stream
+  // NULL means the legacy default stream; the chain's own stream does not
+  // synchronise with it implicitly, so the order is made explicit both ways.
+  cudaStream_t user = stream ? (cudaStream_t)stream : cudaStreamLegacy;
+  {  // order the chain after the caller's stream
+    cudaEvent_t ev_in;
     CK(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
     CK(cudaEventRecord(ev_in, user));
     CK(cudaStreamWaitEvent(ch->stream, ev_in, 0));
@@ -672,7 +694,7 @@ rd_status rd_chain_process_device(rd_chain* ch, const rd_cplx16* adc_dev, uint64
   }
   st = end_call(ch);
   if (st != RD_OK) return st;
-  if (user) {  // and the caller's stream after the chain
+  {  // and the caller's stream after the chain
     cudaEvent_t ev_out;
     CK(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming));
     CK(cudaEventRecord(ev_out, ch->stream));
@@ -966,7 +988,13 @@ rd_status rd_fft_run(uint32_t n_fft, uint32_t spc, uint32_t sched, int reorder,
   if (bins) CK(sc.alloc(&dbins, n));
   if (stage_flags) CK(sc.alloc(&dsf, (size_t)frames * stages));
   CK(cudaMemcpy(di, in, n * 4, cudaMemcpyHostToDevice));
-  launch_fft_block(n_fft, spc, sched, reorder, di, frames, dout, dbins, dsf, 0);
+  std::vector<uint32_t> tp(5u * n_fft);
+  uint32_t words = 0;
+  twiddle_positions(n_fft, spc, tp.data(), &words);
+  uint32_t* dtw;
+  CK(sc.alloc(&dtw, words ? words : 1));
+  if (words) CK(cudaMemcpy(dtw, tp.data(), words * 4, cudaMemcpyHostToDevice));
+  launch_fft_block(n_fft, spc, sched, reorder, dtw, di, frames, dout, dbins, dsf, 0);
   CK(cudaGetLastError());
   if (out) CK(cudaMemcpy(out, dout, n * 4, cudaMemcpyDeviceToHost));
   if (bins) CK(cudaMemcpy(bins, dbins, n * 4, cudaMemcpyDeviceToHost));

@@ -28,9 +28,10 @@ __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
   const unsigned tid = threadIdx.x;
   const unsigned bin0 = blockIdx.x * 64u;
   const uint64_t f = blockIdx.y;
-  const uint64_t slot = (p.g0 + f) % p.ring_frames;
+  unsigned slot = p.ring_base + (unsigned)f;
+  if (slot >= p.ring_frames) slot -= p.ring_frames;
   for (unsigned k = tid; k < B * C; k += 256u) s_w[k] = p.weights[k];
-  const uint32_t* xsrc = p.ring + (slot * N + bin0) * C;
+  const uint32_t* xsrc = p.ring + ((size_t)slot * N + bin0) * C;
   const unsigned nb = (N - bin0) < 64u ? (N - bin0) : 64u;
   for (unsigned k = tid; k < nb * C; k += 256u) s_x[(k / C) * xs + (k % C)] = xsrc[k];
   __syncthreads();
@@ -107,11 +108,17 @@ void launch_beam(const BeamParams& p, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // Covariance: one covar::Integrator pair (re, im) per (bin, pair), stepped
 // once per frame with X[x] * conj(X[y]) (covar_model.hpp:119-151, 204-262).
-// A CTA owns one bin and up to 256 pairs; the frame's source vector is staged
-// in shared memory (double-buffered, one barrier per frame) and the integrator
-// state lives in registers for the whole chunk. Window count and id are the
-// same for every integrator of the stream (they all step on every frame), so
-// the host tracks them and passes where windows close.
+// A CTA owns BT bins x QB pairs. The source vectors of FB frames are staged in
+// shared memory per barrier: the next batch is loaded into registers while
+// the current one is integrated, so the loop carries no exposed load latency.
+// Integrator state lives in registers for the whole chunk. Window count and
+// id are the same for every integrator of the stream (they all step on every
+// frame), so the host tracks them and passes where windows close.
+//
+// EXACT: no step can saturate - exponential mode (the accumulator stays
+// between its old value and the input, |.| <= 2^31, inside any acc_w >= 33)
+// or block mode with window * 2^31 <= 2^(acc_w-1) - 1 (covar_pkg's
+// window_max_exact) - so the sum is a plain int64 sum and the flags stay 0.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void integ_step(long long& acc, long long x, unsigned exp_mode,
                                            unsigned k, unsigned acc_w, unsigned& sticky,
@@ -124,74 +131,137 @@ __device__ __forceinline__ void integ_step(long long& acc, long long x, unsigned
   if (fl && satcnt != 0xFFFFFFFFu) ++satcnt;
 }
 
-__global__ void __launch_bounds__(256) k_cov(CovParams p) {
-  __shared__ uint32_t s_src[2][128];
-  const unsigned tid = threadIdx.x;
-  const unsigned bin = blockIdx.x;
-  const unsigned q = blockIdx.y * 256u + tid;
-  const bool live = q < p.P;
+constexpr unsigned kCovPre = 16;  // prefetch registers per thread
+
+template <bool EXACT>
+__global__ void __launch_bounds__(256) k_cov(CovParams p, unsigned BT, unsigned QB, unsigned FB) {
+  extern __shared__ uint32_t s_src[];  // [FB][BT][S]
+  const unsigned tid = threadIdx.x, nth = blockDim.x;
+  const unsigned S = p.S, row = BT * S, per_batch = FB * row;
+  const unsigned bin0 = blockIdx.x * BT;
+  const unsigned bl = tid / QB, q = blockIdx.y * QB + tid % QB;
+  const unsigned bin = bin0 + bl;
+  const bool live = bl < BT && bin < p.N && q < p.P;
   const size_t k = (size_t)bin * p.P + q;
   long long are = 0, aim = 0;
   unsigned st_re = 0, st_im = 0, sc_re = 0, sc_im = 0, xi = 0, yi = 0;
   if (live) {
     are = p.acc_re[k];
     aim = p.acc_im[k];
-    st_re = p.sticky[k] >> 2;
-    st_im = p.sticky[k] & 3u;
-    sc_re = p.satcnt[2 * k];
-    sc_im = p.satcnt[2 * k + 1];
-    xi = p.px[q];
-    yi = p.py[q];
+    if (!EXACT) {
+      st_re = p.sticky[k] >> 2;
+      st_im = p.sticky[k] & 3u;
+      sc_re = p.satcnt[2 * k];
+      sc_im = p.satcnt[2 * k + 1];
+    }
+    xi = bl * S + p.px[q];
+    yi = bl * S + p.py[q];
   }
+  uint32_t pre[kCovPre];
+  auto load = [&](unsigned fbase) {
+#pragma unroll
+    for (unsigned j = 0; j < kCovPre; ++j) {
+      const unsigned w = tid + j * nth;
+      uint32_t v = 0;
+      if (w < per_batch) {
+        const unsigned fl = w / row, r = w % row;
+        const unsigned f = fbase + fl, b = bin0 + r / S, a = r % S;
+        if (f < p.F && b < p.N) {
+          if (p.src_beam) {
+            v = __ldg(p.beams_bn + ((size_t)f * p.N + b) * S + a);
+          } else {
+            unsigned slot = p.ring_base + f;
+            if (slot >= p.ring_frames) slot -= p.ring_frames;
+            v = __ldg(p.ring + ((size_t)slot * p.N + b) * S + a);
+          }
+        }
+      }
+      pre[j] = v;
+    }
+  };
+  auto store = [&]() {
+#pragma unroll
+    for (unsigned j = 0; j < kCovPre; ++j) {
+      const unsigned w = tid + j * nth;
+      if (w < per_batch) s_src[w] = pre[j];
+    }
+  };
   unsigned count = p.count0, w = 0;
-  unsigned wflags = 0;
-  for (uint32_t f = 0; f < p.F; ++f) {
-    uint32_t* buf = s_src[f & 1u];
-    if (tid < p.S) {
-      buf[tid] = p.src_beam ? p.beams_bn[((size_t)f * p.N + bin) * p.S + tid]
-                            : p.ring[(((p.g0 + f) % p.ring_frames) * p.N + bin) * p.S + tid];
+  load(0);
+  store();
+  __syncthreads();
+  for (unsigned fbase = 0; fbase < p.F; fbase += FB) {
+    if (fbase + FB < p.F) load(fbase + FB);
+    const unsigned nf = (p.F - fbase) < FB ? (p.F - fbase) : FB;
+    for (unsigned fl = 0; fl < nf; ++fl) {
+      if (live) {
+        const cplx X = unpack(s_src[fl * row + xi]), Y = unpack(s_src[fl * row + yi]);
+        // X * conj(Y) through the operand-swap wiring: b = {Y.im, Y.re},
+        // re = im(X*b), im = -re(X*b) (covar_model.hpp:137-145)
+        const long long cre = (long long)((int32_t)X.re * Y.re) + (long long)((int32_t)X.im * Y.im);
+        const long long cim = (long long)((int32_t)X.im * Y.re) - (long long)((int32_t)X.re * Y.im);
+        if (EXACT) {
+          if (p.exp_mode) {
+            are += (cre - are) >> p.exp_k;
+            aim += (cim - aim) >> p.exp_k;
+          } else {
+            are += cre;
+            aim += cim;
+          }
+        } else {
+          integ_step(are, cre, p.exp_mode, p.exp_k, p.acc_w, st_re, sc_re);
+          integ_step(aim, cim, p.exp_mode, p.exp_k, p.acc_w, st_im, sc_im);
+        }
+      }
+      if (++count >= p.wl) {  // uniform over the block
+        if (live && w < p.n_windows) {
+          long long* o = p.out + (((size_t)w * p.N + bin) * p.P + q) * 2;
+          o[0] = are;
+          o[1] = aim;
+          if (!EXACT && (st_re | st_im)) atomicOr(&p.win_flags[w], st_re | st_im);
+        }
+        if (!p.exp_mode) are = aim = 0;
+        count = 0;
+        ++w;
+      }
     }
     __syncthreads();
-    if (live) {
-      const cplx X = unpack(buf[xi]), Y = unpack(buf[yi]);
-      // X * conj(Y) through the operand-swap wiring: b = {Y.im, Y.re},
-      // re = im(X*b), im = -re(X*b) (covar_model.hpp:137-145)
-      const long long cre = (long long)((int32_t)X.re * Y.re) + (long long)((int32_t)X.im * Y.im);
-      const long long cim = (long long)((int32_t)X.im * Y.re) - (long long)((int32_t)X.re * Y.im);
-      integ_step(are, cre, p.exp_mode, p.exp_k, p.acc_w, st_re, sc_re);
-      integ_step(aim, cim, p.exp_mode, p.exp_k, p.acc_w, st_im, sc_im);
-    }
-    if (++count >= p.wl) {
-      if (live && w < p.n_windows) {
-        long long* o = p.out + (((size_t)w * p.N + bin) * p.P + q) * 2;
-        o[0] = are;
-        o[1] = aim;
-        wflags |= st_re | st_im;
-      }
-      if (!p.exp_mode) are = aim = 0;
-      count = 0;
-      if (wflags) atomicOr(&p.win_flags[w], wflags);
-      wflags = 0;
-      ++w;
-    }
+    store();
+    __syncthreads();
   }
   if (live) {
     p.acc_re[k] = are;
     p.acc_im[k] = aim;
-    p.sticky[k] = (st_re << 2) | st_im;
-    const unsigned old_re = p.satcnt[2 * k], old_im = p.satcnt[2 * k + 1];
-    p.satcnt[2 * k] = sc_re;
-    p.satcnt[2 * k + 1] = sc_im;
-    const unsigned long long d = (unsigned long long)(sc_re - old_re) + (sc_im - old_im);
-    if (d) atomicAdd(&p.stats->cov_sat_steps, d);
-    if (st_re | st_im) atomicOr(&p.stats->cov_flags, st_re | st_im);
+    if (!EXACT) {
+      p.sticky[k] = (st_re << 2) | st_im;
+      const unsigned old_re = p.satcnt[2 * k], old_im = p.satcnt[2 * k + 1];
+      p.satcnt[2 * k] = sc_re;
+      p.satcnt[2 * k + 1] = sc_im;
+      const unsigned long long d = (unsigned long long)(sc_re - old_re) + (sc_im - old_im);
+      if (d) atomicAdd(&p.stats->cov_sat_steps, d);
+      if (st_re | st_im) atomicOr(&p.stats->cov_flags, st_re | st_im);
+    }
   }
 }
 
 void launch_cov(const CovParams& p, cudaStream_t s) {
   if (p.P == 0 || p.F == 0) return;
-  const dim3 grid(p.N, (p.P + 255u) / 256u);
-  k_cov<<<grid, 256, 0, s>>>(p);
+  unsigned QB, BT;
+  if (p.P >= 256u) {
+    QB = 256u;
+    BT = 1u;
+  } else {
+    QB = p.P;
+    BT = 256u / p.P;
+  }
+  unsigned nth = ((BT * QB + 31u) / 32u) * 32u;
+  unsigned FB = (kCovPre * nth) / (BT * p.S);
+  if (FB > 32u) FB = 32u;
+  if (FB < 1u) FB = 1u;
+  const dim3 grid((p.N + BT - 1u) / BT, (p.P + QB - 1u) / QB);
+  const size_t smem = (size_t)FB * BT * p.S * sizeof(uint32_t);
+  if (p.exact) k_cov<true><<<grid, nth, smem, s>>>(p, BT, QB, FB);
+  else k_cov<false><<<grid, nth, smem, s>>>(p, BT, QB, FB);
 }
 
 // ---------------------------------------------------------------------------
@@ -351,47 +421,41 @@ __device__ __forceinline__ void make_event(rd_event* e, unsigned kind, unsigned 
   e->framing = (uint8_t)((sof ? 1u : 0u) | (eof ? 2u : 0u));
 }
 
-// 32 bits of a bit string of `nbits` starting at signed bit s (zeros outside).
-__device__ __forceinline__ uint32_t bits32(const uint64_t* w, int s, int nbits) {
-  uint32_t r = 0;
-  for (int j = 0; j < 32; ++j) {
-    const int b = s + j;
-    if (b >= 0 && b < nbits && ((w[b >> 6] >> (b & 63)) & 1ull)) r |= 1u << j;
-  }
-  return r;
+// 32 bits of the zero-padded 192-bit string w[0..2] starting at signed bit s.
+__device__ __forceinline__ uint32_t ext32(const uint64_t* w, int s) {
+  if (s >= 192 || s <= -32) return 0u;
+  if (s < 0) return (uint32_t)(w[0] << (-s));
+  const int lo = s >> 6, sh = s & 63;
+  uint64_t v = w[lo] >> sh;
+  if (sh && lo < 2) v |= w[lo + 1] << (64 - sh);
+  return (uint32_t)v;
 }
 
 // One detection packet: the header flit (packet_model.hpp:150-159, sof) and
 // payload flits carrying the event LS word first (benchmark_sim_top.sv:
 // 1818-1936); flit = data << 5 | eof << 4 | sof << 3 | vc << 1 | odd parity.
+// Each 32-bit flit word is cut from the payload bit string with two shifts.
 __device__ void write_packet(const rd_event* e, uint32_t* out, unsigned pw, unsigned words,
                              unsigned nfl, unsigned src, unsigned dest, unsigned vc,
                              unsigned seq) {
+  const uint64_t hdr[3] = {(uint64_t)(dest & 0xFu) | ((uint64_t)(src & 0x1Fu) << 4) |
+                               ((uint64_t)(vc & 3u) << 9) | ((uint64_t)0u << 11) |
+                               ((uint64_t)(nfl & 0x3Fu) << 14) | ((uint64_t)(seq & 0xFFFFu) << 20),
+                           0ull, 0ull};
+  const int top = 5 + (int)pw;  // first flit bit past the data
   for (unsigned f = 0; f < nfl; ++f) {
     uint32_t* o = out + (size_t)f * words;
-    uint64_t hdr[3] = {0, 0, 0};
-    const uint64_t* data;
-    int dbits, off;
-    if (f == 0) {
-      hdr[0] = (uint64_t)(dest & 0xFu) | ((uint64_t)(src & 0x1Fu) << 4) |
-               ((uint64_t)(vc & 3u) << 9) | ((uint64_t)0u << 11) |
-               ((uint64_t)(nfl & 0x3Fu) << 14) | ((uint64_t)(seq & 0xFFFFu) << 20);
-      data = hdr;
-      dbits = 36;
-      off = 0;
-    } else {
-      data = e->w;
-      dbits = 176;
-      off = (int)((f - 1) * pw);
-    }
+    const uint64_t* data = f == 0 ? hdr : e->w;
+    const int off = f == 0 ? 0 : (int)((f - 1) * pw);
+    // payload bits past this flit's slice belong to the next flit
+    const int last = f == 0 ? 36 : (off + (int)pw < 176 ? off + (int)pw : 176);
     unsigned pop = 0;
     for (unsigned k = 0; k < words; ++k) {
-      // flit bit j carries data bit off + j - 5, for 5 <= j < 5 + pw
-      uint32_t v = bits32(data, off + (int)(32 * k) - 5, dbits);
-      const int lo = 32 * (int)k, hi = lo + 32;
+      const int lo = 32 * (int)k;
+      uint32_t v = ext32(data, off + lo - 5);
       if (lo < 5) v &= ~0x1Fu;
-      const int top = 5 + (int)pw;  // first bit past the data
-      if (hi > top) v &= (top <= lo) ? 0u : ((1u << (top - lo)) - 1u);
+      const int lim = 5 + (last - off) < top ? 5 + (last - off) : top;  // flit bits in use
+      if (lo + 32 > lim) v &= (lim <= lo) ? 0u : ((1u << (lim - lo)) - 1u);
       if (k == 0)
         v |= ((vc & 3u) << 1) | ((f == 0 ? 1u : 0u) << 3) | ((f + 1 == nfl ? 1u : 0u) << 4);
       pop += __popc(v);

@@ -22,11 +22,36 @@ namespace rd {
 __device__ const uint32_t g_tw[1024] = {
 #include "twiddle_q15.inc"
 };
+static const uint32_t h_tw[1024] = {
+#include "twiddle_q15.inc"
+};
 
 const uint32_t* twiddles_device() {
   const uint32_t* p = nullptr;
   cudaGetSymbolAddress((void**)&p, g_tw);
   return p;
+}
+
+static unsigned host_bitrev(unsigned v, unsigned w) {
+  unsigned r = 0;
+  for (unsigned i = 0; i < w; ++i)
+    if ((v >> i) & 1u) r |= 1u << (w - 1 - i);
+  return r;
+}
+
+void twiddle_positions(uint32_t n, uint32_t spc, uint32_t* out, uint32_t* words) {
+  const unsigned m = n / spc, nl = ilog2(m);
+  const unsigned n_tw = (nl - 1u) / 2u;
+  for (unsigned k = 0; k < n_tw; ++k) {
+    const unsigned s = 2u * k + 1u, l2l = nl - s + 1u;
+    for (unsigned i = 0; i < m; ++i) out[k * m + i] = h_tw[r22_tw_exp(l2l, i) << (10u - l2l)];
+  }
+  unsigned total = n_tw * m;
+  if (spc == 2) {
+    for (unsigned i = 0; i < m; ++i) out[total + i] = h_tw[host_bitrev(i, nl) << (10u - nl - 1u)];
+    total += m;
+  }
+  *words = total;
 }
 
 // Exchange with element e ^ h of the same item (h uniform over the block).
@@ -39,12 +64,13 @@ __device__ __forceinline__ uint32_t xchg(uint32_t val, unsigned h, uint32_t* xs)
   return r;
 }
 
-// One FFT element. e = q*m + i is the thread's (lane, position) in the
-// item; returns its value after the last sub-stage; *pos = i (position).
-// Stage flags of sub-stage g accumulate into *sf bits [2g+1:2g].
+// One FFT element. e = q*m + i is the thread's (lane, position) in the item;
+// returns its value after the last sub-stage. twp holds the per-position
+// twiddles (twiddle_positions). Stage flags of sub-stage g accumulate into
+// *sf bits [2g+1:2g].
 __device__ __forceinline__ uint32_t fft_elem(uint32_t v, unsigned e, unsigned nl,
                                              unsigned spc, unsigned sched,
-                                             const uint32_t* tw, uint32_t* xs,
+                                             const uint32_t* twp, uint32_t* xs,
                                              unsigned* sf) {
   const unsigned m = 1u << nl;
   const unsigned q = e >> nl, i = e & (m - 1u);
@@ -65,10 +91,7 @@ __device__ __forceinline__ uint32_t fft_elem(uint32_t v, unsigned e, unsigned nl
       r.re = (int16_t)quant1((int32_t)o.re - mine.re, sh, &fl);
       r.im = (int16_t)quant1((int32_t)o.im - mine.im, sh, &fl);
     }
-    if ((s & 1u) && s + 1u < nl) {
-      const unsigned l2l = nl - s + 1u;
-      r = cmul_tw(r, unpack(tw[r22_tw_exp(l2l, i) << (10u - l2l)]), &fl);
-    }
+    if ((s & 1u) && s + 1u < nl) r = cmul_tw(r, unpack(twp[(s >> 1) * m + i]), &fl);
     *sf |= fl << (2u * s);
     v = pack(r);
   }
@@ -77,7 +100,7 @@ __device__ __forceinline__ uint32_t fft_elem(uint32_t v, unsigned e, unsigned nl
     unsigned fl = 0;
     const cplx cur = unpack(v);
     cplx mine = cur;
-    if (q == 1u) mine = cmul_tw(cur, unpack(tw[bitrev(i, nl) << (10u - (nl + 1u))]), &fl);
+    if (q == 1u) mine = cmul_tw(cur, unpack(twp[((nl - 1u) / 2u) * m + i]), &fl);
     const cplx o = unpack(xchg(pack(mine), m, xs));
     cplx r;
     if (q == 0u) {
@@ -112,14 +135,23 @@ __device__ __forceinline__ void reduce_stats(DevStats* st, unsigned pfl, unsigne
   }
 }
 
-template <int TT>
-__global__ void __launch_bounds__(1024) k_front(FrontParams p, unsigned FB, unsigned CB) {
+// PFB input x[f-k] of phase `ph` of channel c (delay line for f-k < 0)
+__device__ __forceinline__ uint32_t pfb_in(const FrontParams& p, unsigned T, unsigned c,
+                                           long long fr, unsigned ph) {
+  return fr >= 0 ? __ldg(p.adc + (size_t)c * p.ld + (size_t)fr * p.N + ph)
+                 : __ldg(p.tail + ((size_t)c * (T - 1u) + (size_t)(-fr - 1)) * p.N + ph);
+}
+
+template <int TT, int MAXT>
+__global__ void __launch_bounds__(MAXT) k_front(FrontParams p, unsigned FB, unsigned CB,
+                                               unsigned twn) {
   extern __shared__ uint32_t sm[];
-  uint32_t* s_tw = sm;
-  uint32_t* s_x = sm + 1024;
-  uint32_t* s_tile = s_x + blockDim.x;
   const unsigned tid = threadIdx.x, nth = blockDim.x;
-  for (unsigned k = tid; k < 1024u; k += nth) s_tw[k] = g_tw[k];
+  uint32_t* s_tw = sm;
+  uint32_t* s_x = sm + twn;
+  uint32_t* s_tile = s_x + nth;
+  const unsigned cbp = CB + 1u;  // padded row: bit-reversed bins hit distinct banks
+  for (unsigned k = tid; k < twn; k += nth) s_tw[k] = p.tw_pos[k];
 
   const unsigned N = p.N, spc = p.spc;
   const unsigned T = TT ? (unsigned)TT : p.T;
@@ -127,38 +159,62 @@ __global__ void __launch_bounds__(1024) k_front(FrontParams p, unsigned FB, unsi
   const unsigned ipp = nth / N;
   const unsigned item = tid / N, e = tid % N;
   const unsigned ph = spc == 2u ? 2u * (e & (m - 1u)) + (e >> nl) : e;
-  uint32_t h[TT ? TT : 1];
+  constexpr int TR = TT ? TT : 1;
+  uint32_t h[TR];
+  uint32_t xn[TR];  // inputs of the next item (prefetched)
   if (TT) {
 #pragma unroll
-    for (int k = 0; k < (TT ? TT : 1); ++k) h[k] = p.coeff_t[(size_t)k * N + ph];
+    for (int k = 0; k < TR; ++k) h[k] = p.coeff_t[(size_t)k * N + ph];
   }
-  const uint64_t f0 = (uint64_t)blockIdx.x * FB;
+  const unsigned f0 = blockIdx.x * FB;
   const unsigned c0 = blockIdx.y * CB;
+  const unsigned n_items = FB * CB;
   unsigned pfl = 0, sf = 0;
   unsigned long long psat = 0;
+
+  auto item_ok = [&](unsigned it, unsigned& f, unsigned& c) {
+    f = f0 + it / CB;
+    c = c0 + it % CB;
+    return it < n_items && f < p.F && c < p.C;
+  };
+  if (TT) {
+    unsigned f, c;
+    if (item_ok(item, f, c)) {
+#pragma unroll
+      for (int k = 0; k < TR; ++k) xn[k] = pfb_in(p, T, c, (long long)f - k, ph);
+    }
+  }
   __syncthreads();
 
-  const unsigned n_items = FB * CB;
   for (unsigned base = 0; base < n_items; base += ipp) {
     const unsigned it = base + item;
-    const unsigned fb = it / CB, cc = it % CB;
-    const uint64_t f = f0 + fb;
-    const unsigned c = c0 + cc;
-    const bool ok = it < n_items && f < p.F && c < p.C;
+    unsigned f, c;
+    const bool ok = item_ok(it, f, c);
     uint32_t v = 0;
     if (ok) {
       long long are = 0, aim = 0;
-      const uint32_t* xc = p.adc + (size_t)c * p.ld + ph;
-      const uint32_t* tc = p.tail + (size_t)c * (T > 1u ? T - 1u : 1u) * N + ph;
+      if (TT) {
+        uint32_t xc[TR];
 #pragma unroll
-      for (int k = 0; k < (TT ? TT : 64); ++k) {
-        if (!TT && (unsigned)k >= T) break;
-        const long long fr = (long long)f - k;
-        const uint32_t xw = fr >= 0 ? __ldg(xc + (size_t)fr * N) : __ldg(tc + (size_t)(-fr - 1) * N);
-        const uint32_t hw = TT ? h[TT ? k : 0] : __ldg(p.coeff_t + (size_t)k * N + ph);
-        const cplx x = unpack(xw), hk = unpack(hw);
-        are += (long long)((int32_t)x.re * hk.re - (int32_t)x.im * hk.im);
-        aim += (long long)((int32_t)x.re * hk.im) + (long long)((int32_t)x.im * hk.re);
+        for (int k = 0; k < TR; ++k) xc[k] = xn[k];
+        unsigned f2, c2;  // issue the next item's loads before the math
+        if (item_ok(it + ipp, f2, c2)) {
+#pragma unroll
+          for (int k = 0; k < TR; ++k) xn[k] = pfb_in(p, T, c2, (long long)f2 - k, ph);
+        }
+#pragma unroll
+        for (int k = 0; k < TR; ++k) {
+          const cplx x = unpack(xc[k]), hk = unpack(h[k]);
+          are += (long long)((int32_t)x.re * hk.re - (int32_t)x.im * hk.im);
+          aim += (long long)((int32_t)x.re * hk.im) + (long long)((int32_t)x.im * hk.re);
+        }
+      } else {
+        for (unsigned k = 0; k < T; ++k) {
+          const cplx x = unpack(pfb_in(p, T, c, (long long)f - k, ph));
+          const cplx hk = unpack(__ldg(p.coeff_t + (size_t)k * N + ph));
+          are += (long long)((int32_t)x.re * hk.re - (int32_t)x.im * hk.im);
+          aim += (long long)((int32_t)x.re * hk.im) + (long long)((int32_t)x.im * hk.re);
+        }
       }
       unsigned fr = 0, fi = 0;
       const int32_t yr = q15_out64(are, &fr);
@@ -174,7 +230,7 @@ __global__ void __launch_bounds__(1024) k_front(FrontParams p, unsigned FB, unsi
     const uint32_t r = fft_elem(v, e, nl, spc, p.sched, s_tw, s_x, &sfi);
     if (ok) {
       sf |= sfi;
-      s_tile[((size_t)fb * N + fft_bin(e, nl)) * CB + cc] = r;
+      s_tile[((f - f0) * N + fft_bin(e, nl)) * cbp + (c - c0)] = r;
     }
   }
   __syncthreads();
@@ -182,15 +238,17 @@ __global__ void __launch_bounds__(1024) k_front(FrontParams p, unsigned FB, unsi
   for (unsigned t = tid; t < tile_n; t += nth) {
     const unsigned fb = t / (N * CB), rem = t % (N * CB);
     const unsigned bin = rem / CB, cc = rem % CB;
-    const uint64_t f = f0 + fb;
-    const unsigned c = c0 + cc;
+    const unsigned f = f0 + fb, c = c0 + cc;
     if (f < p.F && c < p.C) {
-      const uint64_t slot = (p.g0 + f) % p.ring_frames;
-      p.ring[(slot * N + bin) * p.C + c] = s_tile[t];
+      unsigned slot = p.ring_base + f;
+      if (slot >= p.ring_frames) slot -= p.ring_frames;
+      p.ring[((size_t)slot * N + bin) * p.C + c] = s_tile[(fb * N + bin) * cbp + cc];
     }
   }
   reduce_stats(p.stats, pfl, psat, sf);
 }
+
+static bool g_front_attr = false;
 
 void launch_front(const FrontParams& p, cudaStream_t s) {
   const unsigned nth = p.N > 256u ? p.N : 256u;
@@ -201,13 +259,36 @@ void launch_front(const FrontParams& p, cudaStream_t s) {
   unsigned FB = ipp / CB;
   if (FB < 1u) FB = 1u;
   while (FB * CB * p.N > 8192u && FB > 1u) FB >>= 1;
+  const unsigned m = p.N / p.spc, nl = ilog2(m);
+  const unsigned twn = ((nl - 1u) / 2u) * m + (p.spc == 2u ? m : 0u);
   const dim3 grid((p.F + FB - 1) / FB, (p.C + CB - 1) / CB);
-  const size_t smem = (1024u + nth + (size_t)FB * p.N * CB) * sizeof(uint32_t);
-  switch (p.T) {
-    case 4: k_front<4><<<grid, nth, smem, s>>>(p, FB, CB); break;
-    case 8: k_front<8><<<grid, nth, smem, s>>>(p, FB, CB); break;
-    case 16: k_front<16><<<grid, nth, smem, s>>>(p, FB, CB); break;
-    default: k_front<0><<<grid, nth, smem, s>>>(p, FB, CB); break;
+  const size_t smem = (twn + nth + (size_t)FB * p.N * (CB + 1u)) * sizeof(uint32_t);
+  if (!g_front_attr) {
+    const int lim = 96 * 1024;
+    cudaFuncSetAttribute(k_front<0, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_front<4, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_front<8, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_front<16, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_front<0, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_front<4, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_front<8, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_front<16, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    g_front_attr = true;
+  }
+  if (nth <= 256u) {
+    switch (p.T) {
+      case 4: k_front<4, 256><<<grid, nth, smem, s>>>(p, FB, CB, twn); break;
+      case 8: k_front<8, 256><<<grid, nth, smem, s>>>(p, FB, CB, twn); break;
+      case 16: k_front<16, 256><<<grid, nth, smem, s>>>(p, FB, CB, twn); break;
+      default: k_front<0, 256><<<grid, nth, smem, s>>>(p, FB, CB, twn); break;
+    }
+  } else {
+    switch (p.T) {
+      case 4: k_front<4, 1024><<<grid, nth, smem, s>>>(p, FB, CB, twn); break;
+      case 8: k_front<8, 1024><<<grid, nth, smem, s>>>(p, FB, CB, twn); break;
+      case 16: k_front<16, 1024><<<grid, nth, smem, s>>>(p, FB, CB, twn); break;
+      default: k_front<0, 1024><<<grid, nth, smem, s>>>(p, FB, CB, twn); break;
+    }
   }
 }
 
@@ -265,14 +346,15 @@ void launch_pfb_block(uint32_t phases, uint32_t taps, const uint32_t* coeff,
 
 // fft::transform on independent frames; one item of N threads per frame.
 __global__ void k_fft_block(uint32_t N, uint32_t spc, uint32_t sched, int reorder,
-                            const uint32_t* in, uint32_t frames, uint32_t* out, uint32_t* bins,
+                            const uint32_t* tw_pos, unsigned twn, const uint32_t* in,
+                            uint32_t frames, uint32_t* out, uint32_t* bins,
                             uint8_t* stage_flags) {
   extern __shared__ uint32_t sm[];
   uint32_t* s_tw = sm;
-  uint32_t* s_x = sm + 1024;
+  uint32_t* s_x = sm + twn;
   uint32_t* s_fl = s_x + blockDim.x;
   const unsigned tid = threadIdx.x, nth = blockDim.x;
-  for (unsigned k = tid; k < 1024u; k += nth) s_tw[k] = g_tw[k];
+  for (unsigned k = tid; k < twn; k += nth) s_tw[k] = tw_pos[k];
   const unsigned ipp = nth / N, item = tid / N, e = tid % N;
   if (tid < ipp) s_fl[tid] = 0;
   const unsigned m = N / spc, nl = ilog2(m);
@@ -303,16 +385,19 @@ __global__ void k_fft_block(uint32_t N, uint32_t spc, uint32_t sched, int reorde
   }
 }
 
-void launch_fft_block(uint32_t n, uint32_t spc, uint32_t sched, int reorder, const uint32_t* in,
-                      uint32_t frames, uint32_t* out, uint32_t* bins, uint8_t* stage_flags,
-                      cudaStream_t s) {
+void launch_fft_block(uint32_t n, uint32_t spc, uint32_t sched, int reorder,
+                      const uint32_t* tw_pos, const uint32_t* in, uint32_t frames, uint32_t* out,
+                      uint32_t* bins, uint8_t* stage_flags, cudaStream_t s) {
   const unsigned nth = n > 256u ? n : 256u;
   const unsigned ipp = nth / n;
   unsigned grid = (frames + ipp - 1) / ipp;
   if (grid > 4096u) grid = 4096u;
   if (grid == 0u) return;
-  const size_t smem = (1024u + nth + ipp) * sizeof(uint32_t);
-  k_fft_block<<<grid, nth, smem, s>>>(n, spc, sched, reorder, in, frames, out, bins, stage_flags);
+  const unsigned m = n / spc, nl = ilog2(m);
+  const unsigned twn = ((nl - 1u) / 2u) * m + (spc == 2u ? m : 0u);
+  const size_t smem = (twn + nth + ipp) * sizeof(uint32_t);
+  k_fft_block<<<grid, nth, smem, s>>>(n, spc, sched, reorder, tw_pos, twn, in, frames, out, bins,
+                                      stage_flags);
 }
 
 }  // namespace rd

@@ -33,7 +33,9 @@ struct FrontParams {
   const uint32_t* coeff_t;  // [T][N] (tap-major copy of the phase-major bank)
   uint32_t* ring;           // [R][N][C]
   uint32_t ring_frames;     // R
+  uint32_t ring_base;       // ring slot of chunk frame 0 (g0 mod R)
   uint64_t g0;              // stream frame index of chunk frame 0
+  const uint32_t* tw_pos;   // per-position twiddles, twiddle_positions()
   uint32_t* tap_pfb;        // [F][C][N] chunk-relative, or null
   uint32_t F, C, N, T, spc, sched;
   DevStats* stats;
@@ -48,13 +50,24 @@ void launch_pfb_block(uint32_t phases, uint32_t taps, const uint32_t* coeff,
                       const uint32_t* state, const uint32_t* in, uint32_t beats,
                       uint32_t* out, uint8_t* flags, cudaStream_t s);
 void launch_fft_block(uint32_t n, uint32_t spc, uint32_t sched, int reorder,
-                      const uint32_t* in, uint32_t frames, uint32_t* out,
-                      uint32_t* bins, uint8_t* stage_flags, cudaStream_t s);
+                      const uint32_t* tw_pos, const uint32_t* in, uint32_t frames,
+                      uint32_t* out, uint32_t* bins, uint8_t* stage_flags, cudaStream_t s);
+
+// Per-position twiddle tables of an (n_fft, spc) transform: for the k-th
+// twiddle sub-stage s (odd s with s + 1 < log2(n/spc)), entry [k][i] is the
+// twiddle lane position i multiplies by, kTw[r22_tw_exp(l2l, i) << (10-l2l)]
+// with l2l = log2(n/spc) - s + 1 (fft_ref.hpp:123-133, 368-377); then, for
+// spc = 2, the merge twiddle of position i, kTw[bitrev(i) << (10-l2l-1)]
+// (fft_ref.hpp:139-147, 380-406). Indexing by position keeps shared-memory
+// reads bank-conflict free.
+void twiddle_positions(uint32_t n, uint32_t spc, uint32_t* out /* 5 * n words */,
+                       uint32_t* words);
 
 // ---- back end ----------------------------------------------------------------
 struct BeamParams {
   const uint32_t* ring;     // [R][N][C]
   uint32_t ring_frames;
+  uint32_t ring_base;       // ring slot of chunk frame 0
   uint64_t g0;
   const uint32_t* weights;  // [B][C]
   uint32_t* power;          // [F][B][N]
@@ -67,7 +80,9 @@ void launch_beam(const BeamParams& p, cudaStream_t s);
 struct CovParams {
   const uint32_t* ring;     // channel source: [R][N][C]
   uint32_t ring_frames;
+  uint32_t ring_base;       // ring slot of chunk frame 0
   uint64_t g0;
+  uint32_t exact;           // 1: no step can saturate (see launch_cov)
   const uint32_t* beams_bn; // beam source: [F][N][B]
   uint32_t S;               // source vector length
   uint32_t src_beam;        // 1: beams_bn, 0: ring

@@ -228,7 +228,8 @@ def run_gpu(a, rank: int, world: int, local: int) -> None:
     dev = host.cuda()
     samples = p.n_chan * n
     chain = gc.Chain(cfg, coeff, w, pairs)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sh = stream.cuda_stream
 
     for _ in range(a.warmup):

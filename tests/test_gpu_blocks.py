@@ -198,7 +198,7 @@ def test_cfar_directed(gpulib, port):
     n = 128
     cells = np.full(n, 100, np.int64)
     cells[60] = 100 * 9          # injected target: CUT*N*256 vs alpha*sum
-    cells[70], cells[72] = 5000, 5000   # closely spaced pair
+    cells[100], cells[102] = 5000, 5000  # closely spaced pair, outside bin 60's window
     # threshold flip: alpha exactly at the boundary and one LSB below
     for alpha, want in ((9 * 256 - 1, True), (9 * 256, False)):
         cfg = cfar_cfg(abi.RD_CFAR_CA, abi.RD_CFAR_EVENTS, 2, 2, 8, 8, alpha)
