@@ -159,6 +159,7 @@ struct rd_chain {
   bool own_stream = false;
 
   DevBuf<uint32_t> coeff_t, weights, tail[2], ring, power, beams_bn, stage, tw_pos;
+  DevBuf<int4> w_limbs;
   int tail_cur = 0;
   DevBuf<uint32_t> px, py;
   DevBuf<long long> acc_re, acc_im, cov_out;
@@ -349,6 +350,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
   const uint32_t D = T > 1 ? T - 1 : 1;
   if (bad(cudaStreamCreateWithFlags(&ch->stream, cudaStreamNonBlocking)) ||
       bad(ch->coeff_t.ensure((size_t)T * N)) || bad(ch->weights.ensure((size_t)B * C)) ||
+      bad(ch->w_limbs.ensure((size_t)B * C)) ||
       bad(ch->tail[0].ensure((size_t)C * D * N)) || bad(ch->tail[1].ensure((size_t)C * D * N)) ||
       bad(ch->ring.ensure((size_t)ch->R * N * C)) || bad(ch->power.ensure((size_t)F * B * N)) ||
       bad(ch->counts.ensure((size_t)F * B)) || bad(ch->detsup.ensure((size_t)F * B * 2)) ||
@@ -360,6 +362,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
   ch->own_stream = true;
   cudaMemset(ch->coeff_t.p, 0, (size_t)T * N * 4);
   cudaMemset(ch->weights.p, 0, (size_t)B * C * 4);
+  cudaMemset(ch->w_limbs.p, 0, (size_t)B * C * sizeof(int4));
   cudaMemset(ch->tail[0].p, 0, (size_t)C * D * N * 4);
   cudaMemset(ch->tail[1].p, 0, (size_t)C * D * N * 4);
   cudaMemset(ch->ring.p, 0, (size_t)ch->R * N * C * 4);
@@ -411,7 +414,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
 void rd_chain_destroy(rd_chain* ch) {
   if (!ch) return;
   if (ch->stream) cudaStreamSynchronize(ch->stream);
-  ch->coeff_t.release(); ch->weights.release(); ch->tail[0].release(); ch->tail[1].release();
+  ch->coeff_t.release(); ch->weights.release(); ch->w_limbs.release(); ch->tail[0].release(); ch->tail[1].release();
   ch->ring.release(); ch->power.release(); ch->beams_bn.release(); ch->stage.release();
   ch->tw_pos.release();
   ch->px.release(); ch->py.release(); ch->acc_re.release(); ch->acc_im.release();
@@ -440,8 +443,15 @@ rd_status rd_chain_set_coeff(rd_chain* ch, const rd_cplx16* coeff) {
 
 rd_status rd_chain_set_weights(rd_chain* ch, const rd_cplx16* w) {
   if (!ch || !w) return fail(RD_EINVAL, "null argument");
-  CK(cudaMemcpyAsync(ch->weights.p, w, (size_t)ch->cfg.n_beams * ch->cfg.n_chan * 4,
-                     cudaMemcpyHostToDevice, ch->stream));
+  const size_t n = (size_t)ch->cfg.n_beams * ch->cfg.n_chan;
+  std::vector<int4> limbs(n);
+  for (size_t i = 0; i < n; ++i) {  // w = 256 * wh + wl, wl in [0, 255]
+    const int re = (int16_t)(uint16_t)(w[i] & 0xFFFFu), im = (int16_t)(uint16_t)(w[i] >> 16);
+    limbs[i] = make_int4(re >> 8, im >> 8, re & 255, im & 255);
+  }
+  CK(cudaMemcpyAsync(ch->weights.p, w, n * 4, cudaMemcpyHostToDevice, ch->stream));
+  CK(cudaMemcpyAsync(ch->w_limbs.p, limbs.data(), n * sizeof(int4), cudaMemcpyHostToDevice,
+                     ch->stream));
   CK(cudaStreamSynchronize(ch->stream));
   return RD_OK;
 }
@@ -508,6 +518,7 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   bp.ring_base = ring_base;
   bp.g0 = ch->frame;
   bp.weights = ch->weights.p;
+  bp.w_limbs = ch->w_limbs.p;
   bp.power = ch->power.p;
   bp.beams_bn = ch->beams_bn.p;
   bp.F = F;

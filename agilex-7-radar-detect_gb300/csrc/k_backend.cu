@@ -18,19 +18,24 @@ namespace rd {
 // shared memory with a padded row so the 64 bin-threads of a warp pair read
 // distinct banks; every weight read is a warp-wide broadcast.
 // ---------------------------------------------------------------------------
+// The weights arrive split into limbs, w = wh * 256 + wl with wh in
+// [-128, 127] and wl in [0, 255] (set at rd_chain_set_weights), so every
+// product term is exact in int32: |x * wh| <= 2^22, |x * wl| < 2^23, and a
+// 64-channel block of complex terms stays below 2^31. Blocks are combined in
+// int64 as acc = 256 * acc_h + acc_l - the same integer bf::dot sums.
 template <int BPT>
 __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
   extern __shared__ uint32_t sm[];
   const unsigned C = p.C, B = p.B, N = p.N;
   const unsigned xs = C + 1;  // padded row
-  uint32_t* s_w = sm;
-  uint32_t* s_x = sm + B * C;
+  int4* s_w = reinterpret_cast<int4*>(sm);          // [B][C] limbs
+  uint32_t* s_x = sm + 4u * B * C;
   const unsigned tid = threadIdx.x;
   const unsigned bin0 = blockIdx.x * 64u;
   const uint64_t f = blockIdx.y;
   unsigned slot = p.ring_base + (unsigned)f;
   if (slot >= p.ring_frames) slot -= p.ring_frames;
-  for (unsigned k = tid; k < B * C; k += 256u) s_w[k] = p.weights[k];
+  for (unsigned k = tid; k < B * C; k += 256u) s_w[k] = p.w_limbs[k];
   const uint32_t* xsrc = p.ring + ((size_t)slot * N + bin0) * C;
   const unsigned nb = (N - bin0) < 64u ? (N - bin0) : 64u;
   for (unsigned k = tid; k < nb * C; k += 256u) s_x[(k / C) * xs + (k % C)] = xsrc[k];
@@ -42,16 +47,30 @@ __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
   for (int j = 0; j < BPT; ++j) ar[j] = ai[j] = 0;
   if (bl < nb) {
     const uint32_t* xr = s_x + bl * xs;
-    for (unsigned a = 0; a < C; ++a) {
-      const cplx x = unpack(xr[a]);
+    for (unsigned a0 = 0; a0 < C; a0 += 64u) {
+      const unsigned a1 = (a0 + 64u) < C ? (a0 + 64u) : C;
+      int hr[BPT], hi[BPT], lr[BPT], li[BPT];
+#pragma unroll
+      for (int j = 0; j < BPT; ++j) hr[j] = hi[j] = lr[j] = li[j] = 0;
+      for (unsigned a = a0; a < a1; ++a) {
+        const uint32_t xv = xr[a];
+        const int x_re = (int)(int16_t)(uint16_t)(xv & 0xFFFFu), x_im = (int)xv >> 16;
+#pragma unroll
+        for (int j = 0; j < BPT; ++j) {
+          const unsigned b = bg + 4u * j;
+          if (BPT == 1 || b < B) {
+            const int4 w = s_w[b * C + a];  // {wh.re, wh.im, wl.re, wl.im}
+            hr[j] += x_re * w.x - x_im * w.y;
+            hi[j] += x_re * w.y + x_im * w.x;
+            lr[j] += x_re * w.z - x_im * w.w;
+            li[j] += x_re * w.w + x_im * w.z;
+          }
+        }
+      }
 #pragma unroll
       for (int j = 0; j < BPT; ++j) {
-        const unsigned b = bg + 4u * j;
-        if (b < B) {
-          const cplx w = unpack(s_w[b * C + a]);
-          ar[j] += (long long)((int32_t)x.re * w.re - (int32_t)x.im * w.im);
-          ai[j] += (long long)((int32_t)x.re * w.im) + (long long)((int32_t)x.im * w.re);
-        }
+        ar[j] += (long long)hr[j] * 256 + lr[j];
+        ai[j] += (long long)hi[j] * 256 + li[j];
       }
     }
   }
@@ -87,14 +106,14 @@ static bool g_beam_attr_set = false;
 void launch_beam(const BeamParams& p, cudaStream_t s) {
   const unsigned bpt = (p.B + 3u) / 4u;
   const dim3 grid((p.N + 63u) / 64u, p.F);
-  const size_t smem = ((size_t)p.B * p.C + 64u * (p.C + 1u)) * sizeof(uint32_t);
+  const size_t smem = ((size_t)4u * p.B * p.C + 64u * (p.C + 1u)) * sizeof(uint32_t);
   if (!g_beam_attr_set) {
-    cudaFuncSetAttribute(k_beam<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    cudaFuncSetAttribute(k_beam<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    cudaFuncSetAttribute(k_beam<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    cudaFuncSetAttribute(k_beam<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    cudaFuncSetAttribute(k_beam<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    cudaFuncSetAttribute(k_beam<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_beam<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_beam<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_beam<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_beam<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_beam<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_beam<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     g_beam_attr_set = true;
   }
   if (bpt <= 1) k_beam<1><<<grid, 256, smem, s>>>(p);
@@ -133,7 +152,12 @@ __device__ __forceinline__ void integ_step(long long& acc, long long x, unsigned
 
 constexpr unsigned kCovPre = 16;  // prefetch registers per thread
 
-template <bool EXACT>
+// MODE: 0 = exact block mode, 1 = exact exponential mode, 2 = saturating
+// (either mode, sequential). In exact block mode the chunk's frames are split
+// at window boundaries across blockIdx.z (windows are independent there): the
+// first segment carries the open window's accumulator in, the last one
+// carries its accumulator out, every other one starts from zero.
+template <int MODE>
 __global__ void __launch_bounds__(256) k_cov(CovParams p, unsigned BT, unsigned QB, unsigned FB) {
   extern __shared__ uint32_t s_src[];  // [FB][BT][S]
   const unsigned tid = threadIdx.x, nth = blockDim.x;
@@ -143,12 +167,21 @@ __global__ void __launch_bounds__(256) k_cov(CovParams p, unsigned BT, unsigned 
   const unsigned bin = bin0 + bl;
   const bool live = bl < BT && bin < p.N && q < p.P;
   const size_t k = (size_t)bin * p.P + q;
+  // this CTA's frame segment
+  const unsigned z = blockIdx.z, nz = gridDim.z;
+  const unsigned first = p.wl - p.count0;  // frames until the open window closes
+  const unsigned lo = z == 0 ? 0u : first + (z - 1u) * p.wl;
+  const unsigned hi_ = z == 0 ? first : first + z * p.wl;
+  const unsigned hi = (nz == 1u || hi_ > p.F) ? p.F : hi_;
+  const bool carry_in = z == 0, carry_out = z + 1u == nz;
   long long are = 0, aim = 0;
   unsigned st_re = 0, st_im = 0, sc_re = 0, sc_im = 0, xi = 0, yi = 0;
   if (live) {
-    are = p.acc_re[k];
-    aim = p.acc_im[k];
-    if (!EXACT) {
+    if (carry_in) {
+      are = p.acc_re[k];
+      aim = p.acc_im[k];
+    }
+    if (MODE == 2) {
       st_re = p.sticky[k] >> 2;
       st_im = p.sticky[k] & 3u;
       sc_re = p.satcnt[2 * k];
@@ -166,7 +199,7 @@ __global__ void __launch_bounds__(256) k_cov(CovParams p, unsigned BT, unsigned 
       if (w < per_batch) {
         const unsigned fl = w / row, r = w % row;
         const unsigned f = fbase + fl, b = bin0 + r / S, a = r % S;
-        if (f < p.F && b < p.N) {
+        if (f < hi && b < p.N) {
           if (p.src_beam) {
             v = __ldg(p.beams_bn + ((size_t)f * p.N + b) * S + a);
           } else {
@@ -186,31 +219,36 @@ __global__ void __launch_bounds__(256) k_cov(CovParams p, unsigned BT, unsigned 
       if (w < per_batch) s_src[w] = pre[j];
     }
   };
-  unsigned count = p.count0, w = 0;
-  load(0);
+  unsigned count = carry_in ? p.count0 : 0u;
+  unsigned w = carry_in ? 0u : z;  // window index of this segment's close
+  load(lo);
   store();
   __syncthreads();
-  for (unsigned fbase = 0; fbase < p.F; fbase += FB) {
-    if (fbase + FB < p.F) load(fbase + FB);
-    const unsigned nf = (p.F - fbase) < FB ? (p.F - fbase) : FB;
+  for (unsigned fbase = lo; fbase < hi; fbase += FB) {
+    if (fbase + FB < hi) load(fbase + FB);
+    const unsigned nf = (hi - fbase) < FB ? (hi - fbase) : FB;
     for (unsigned fl = 0; fl < nf; ++fl) {
       if (live) {
-        const cplx X = unpack(s_src[fl * row + xi]), Y = unpack(s_src[fl * row + yi]);
+        const uint32_t xv = s_src[fl * row + xi], yv = s_src[fl * row + yi];
+        const int xr = (int)(int16_t)(uint16_t)(xv & 0xFFFFu), xm = (int)xv >> 16;
+        const int yr = (int)(int16_t)(uint16_t)(yv & 0xFFFFu), ym = (int)yv >> 16;
         // X * conj(Y) through the operand-swap wiring: b = {Y.im, Y.re},
         // re = im(X*b), im = -re(X*b) (covar_model.hpp:137-145)
-        const long long cre = (long long)((int32_t)X.re * Y.re) + (long long)((int32_t)X.im * Y.im);
-        const long long cim = (long long)((int32_t)X.im * Y.re) - (long long)((int32_t)X.re * Y.im);
-        if (EXACT) {
-          if (p.exp_mode) {
+        if (MODE == 0) {
+          are += (long long)xr * yr;
+          are += (long long)xm * ym;
+          aim += (long long)xm * yr;
+          aim -= (long long)xr * ym;
+        } else {
+          const long long cre = (long long)xr * yr + (long long)xm * ym;
+          const long long cim = (long long)xm * yr - (long long)xr * ym;
+          if (MODE == 1) {
             are += (cre - are) >> p.exp_k;
             aim += (cim - aim) >> p.exp_k;
           } else {
-            are += cre;
-            aim += cim;
+            integ_step(are, cre, p.exp_mode, p.exp_k, p.acc_w, st_re, sc_re);
+            integ_step(aim, cim, p.exp_mode, p.exp_k, p.acc_w, st_im, sc_im);
           }
-        } else {
-          integ_step(are, cre, p.exp_mode, p.exp_k, p.acc_w, st_re, sc_re);
-          integ_step(aim, cim, p.exp_mode, p.exp_k, p.acc_w, st_im, sc_im);
         }
       }
       if (++count >= p.wl) {  // uniform over the block
@@ -218,9 +256,9 @@ __global__ void __launch_bounds__(256) k_cov(CovParams p, unsigned BT, unsigned 
           long long* o = p.out + (((size_t)w * p.N + bin) * p.P + q) * 2;
           o[0] = are;
           o[1] = aim;
-          if (!EXACT && (st_re | st_im)) atomicOr(&p.win_flags[w], st_re | st_im);
+          if (MODE == 2 && (st_re | st_im)) atomicOr(&p.win_flags[w], st_re | st_im);
         }
-        if (!p.exp_mode) are = aim = 0;
+        if (MODE != 1 && !(MODE == 2 && p.exp_mode)) are = aim = 0;
         count = 0;
         ++w;
       }
@@ -229,10 +267,10 @@ __global__ void __launch_bounds__(256) k_cov(CovParams p, unsigned BT, unsigned 
     store();
     __syncthreads();
   }
-  if (live) {
+  if (live && carry_out) {
     p.acc_re[k] = are;
     p.acc_im[k] = aim;
-    if (!EXACT) {
+    if (MODE == 2) {
       p.sticky[k] = (st_re << 2) | st_im;
       const unsigned old_re = p.satcnt[2 * k], old_im = p.satcnt[2 * k + 1];
       p.satcnt[2 * k] = sc_re;
@@ -254,14 +292,22 @@ void launch_cov(const CovParams& p, cudaStream_t s) {
     QB = p.P;
     BT = 256u / p.P;
   }
-  unsigned nth = ((BT * QB + 31u) / 32u) * 32u;
+  const unsigned nth = ((BT * QB + 31u) / 32u) * 32u;
   unsigned FB = (kCovPre * nth) / (BT * p.S);
   if (FB > 32u) FB = 32u;
   if (FB < 1u) FB = 1u;
-  const dim3 grid((p.N + BT - 1u) / BT, (p.P + QB - 1u) / QB);
+  const int mode = !p.exact ? 2 : (p.exp_mode ? 1 : 0);
+  // segments: the open window, every whole window, the trailing partial one
+  unsigned nz = 1;
+  if (mode == 0) {
+    const unsigned first = p.wl - p.count0;
+    nz = first >= p.F ? 1u : 1u + (p.F - first + p.wl - 1u) / p.wl;
+  }
+  const dim3 grid((p.N + BT - 1u) / BT, (p.P + QB - 1u) / QB, nz);
   const size_t smem = (size_t)FB * BT * p.S * sizeof(uint32_t);
-  if (p.exact) k_cov<true><<<grid, nth, smem, s>>>(p, BT, QB, FB);
-  else k_cov<false><<<grid, nth, smem, s>>>(p, BT, QB, FB);
+  if (mode == 0) k_cov<0><<<grid, nth, smem, s>>>(p, BT, QB, FB);
+  else if (mode == 1) k_cov<1><<<grid, nth, smem, s>>>(p, BT, QB, FB);
+  else k_cov<2><<<grid, nth, smem, s>>>(p, BT, QB, FB);
 }
 
 // ---------------------------------------------------------------------------

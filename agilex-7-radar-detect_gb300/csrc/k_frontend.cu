@@ -251,6 +251,7 @@ __global__ void __launch_bounds__(MAXT) k_front(FrontParams p, unsigned FB, unsi
 static bool g_front_attr = false;
 
 void launch_front(const FrontParams& p, cudaStream_t s) {
+  if (launch_front_fast(p, s)) return;
   const unsigned nth = p.N > 256u ? p.N : 256u;
   const unsigned ipp = nth / p.N;
   unsigned CB = 8192u / p.N;

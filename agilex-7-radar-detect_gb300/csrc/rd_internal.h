@@ -41,6 +41,9 @@ struct FrontParams {
   DevStats* stats;
 };
 void launch_front(const FrontParams& p, cudaStream_t s);
+// The geometry-specialised kernel (k_front_fast.cu); false when the geometry
+// has no specialisation.
+bool launch_front_fast(const FrontParams& p, cudaStream_t s);
 void launch_tail_update(const uint32_t* adc, uint64_t ld, const uint32_t* old_tail,
                         uint32_t* new_tail, uint32_t F, uint32_t C, uint32_t N,
                         uint32_t T, cudaStream_t s);
@@ -70,6 +73,7 @@ struct BeamParams {
   uint32_t ring_base;       // ring slot of chunk frame 0
   uint64_t g0;
   const uint32_t* weights;  // [B][C]
+  const int4* w_limbs;      // [B][C] {wh.re, wh.im, wl.re, wl.im}, w = 256 wh + wl
   uint32_t* power;          // [F][B][N]
   uint32_t* beams_bn;       // [F][N][B] beam samples (null unless needed)
   uint32_t F, C, N, B;
