@@ -40,6 +40,20 @@ rd_status fail(rd_status st, const char* fmt, ...) {
 
 bool is_pow2(uint32_t v) { return v && !(v & (v - 1)); }
 
+}  // namespace
+
+rd_status rd::set_error(rd_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return st;
+}
+
+namespace {
+
 void sat_bump(uint32_t* c, uint64_t by) {
   const uint64_t v = (uint64_t)*c + by;
   *c = v > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)v;

@@ -142,6 +142,9 @@ void launch_packetize(const rd_event* ev, uint64_t n, uint32_t packet_w, uint32_
 void launch_fxp(const uint32_t* op, const int64_t* a, const int64_t* b, const uint32_t* sh,
                 const uint32_t* w, uint64_t n, int64_t* y, uint8_t* flags, cudaStream_t s);
 
+// Records a formatted message for rd_last_error() and returns st (api.cu).
+rd_status set_error(rd_status st, const char* fmt, ...);
+
 // Q1.15 twiddle table in device global memory (k_frontend.cu)
 const uint32_t* twiddles_device();
 

@@ -26,6 +26,7 @@ RD_EV_DETECT, RD_EV_BIN, RD_EV_SUPPRESSED, RD_EV_SUMMARY = 0, 1, 2, 3
 RD_COV_OFF, RD_COV_CHANNEL, RD_COV_BEAM = 0, 1, 2
 RD_COV_BLOCK, RD_COV_EXP = 0, 1
 RD_FORM_CUDA_CORE, RD_FORM_TENSOR = 0, 1
+RD_STATIC_CFAR_MAX_FRAMES, RD_STATIC_CFAR_MAX_CELLS = 4096, 1024
 
 OPS = ["sat", "trunc", "round_even", "round_half_up", "round", "round_sat",
        "add_sat", "sub_sat", "neg_sat", "mul_q15", "mul_q15_rs", "cmul_re",
@@ -156,6 +157,7 @@ def declare_rd(lib) -> None:
     _proto(lib, "rd_power_run", I32, [VP, U64, VP])
     _proto(lib, "rd_cross_power_run", I32, [VP, VP, U64, VP])
     _proto(lib, "rd_cfar_run", I32, [VP, U32, U32, P(RdConfig), VP, VP, U64, P(U64)])
+    _proto(lib, "rd_cfar_run_static", I32, [VP, U32, U32, P(RdConfig), VP, VP, U64, VP, VP])
     _proto(lib, "rd_packetize", I32, [VP, U64, U32, U32, U32, U32, U32, VP])
     _proto(lib, "rd_fxp_apply", I32, [VP, VP, VP, VP, VP, U64, VP, VP])
     _proto(lib, "rd_last_error", C.c_char_p, [])
@@ -170,7 +172,7 @@ EXPORTED = [
     "rd_chain_set_weights", "rd_chain_set_pairs", "rd_chain_process",
     "rd_chain_process_device", "rd_chain_fetch", "rd_chain_last_launches",
     "rd_chain_flush_cov", "rd_chain_set_profiling", "rd_chain_kernel_times", "rd_chain_stats", "rd_chain_read_history", "rd_pfb_run",
-    "rd_fft_run", "rd_bf_run", "rd_power_run", "rd_cross_power_run", "rd_cfar_run",
+    "rd_fft_run", "rd_bf_run", "rd_power_run", "rd_cross_power_run", "rd_cfar_run", "rd_cfar_run_static",
     "rd_packetize", "rd_fxp_apply", "rd_last_error", "rd_device_ok", "rd_version",
 ]
 

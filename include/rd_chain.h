@@ -262,6 +262,25 @@ rd_status rd_cfar_run(const int64_t* cells, uint32_t n, uint32_t frames,
                       const rd_config* cfg, const uint32_t* frame_ids,
                       rd_event* events, uint64_t cap, uint64_t* n_events);
 
+/* cfar::run_frame like rd_cfar_run, but on caller-provided DEVICE buffers and
+ * without allocating anything. It has no counterpart in the reference: it is
+ * for callers that are handed device memory but may not call cudaMalloc
+ * (code inside another framework's memory pool, real-time loops where an
+ * allocation would synchronise the device, processes whose allocator is
+ * locked after start-up). Its scratch is a static device array shared by
+ * every call on a device: at most RD_STATIC_CFAR_MAX_FRAMES frames of at most
+ * RD_STATIC_CFAR_MAX_CELLS cells (larger sizes return RD_EINVAL); calls whose
+ * work overlaps on the GPU race on it. The first call on each device looks up
+ * the scratch address and should come before any stream capture. cells,
+ * frame_ids, events and n_events (one uint64) are device pointers; the call
+ * is asynchronous on `stream` (a cudaStream_t, NULL = legacy stream). */
+#define RD_STATIC_CFAR_MAX_FRAMES 4096u
+#define RD_STATIC_CFAR_MAX_CELLS 1024u
+rd_status rd_cfar_run_static(const int64_t* cells, uint32_t n, uint32_t frames,
+                             const rd_config* cfg, const uint32_t* frame_ids,
+                             rd_event* events, uint64_t cap, uint64_t* n_events,
+                             void* stream);
+
 /* Detection packet flits for n events (packet_model.hpp:122-260 and the DMA
  * tap of rtl/top/benchmark_sim_top.sv:1818-1936): header flit then payload
  * flits LS word first; seq = (seq0 + i) mod 2^16. */
