@@ -174,6 +174,7 @@ struct rd_chain {
 
   DevBuf<uint32_t> coeff_t, weights, tail[2], ring, power, beams_bn, stage, tw_pos;
   DevBuf<int4> w_limbs;
+  DevBuf<uint32_t> w_frag;  // tensor form: mma fragments of the limb-split weights
   int tail_cur = 0;
   DevBuf<uint32_t> px, py;
   DevBuf<long long> acc_re, acc_im, cov_out;
@@ -322,6 +323,8 @@ rd_status rd_config_validate(const rd_config* c) {
   }
   if (c->max_frames < 1 || c->max_frames > 65536) return fail(RD_EINVAL, "max_frames 1..65536");
   if (c->form > RD_FORM_TENSOR) return fail(RD_EINVAL, "bad form");
+  if (c->form == RD_FORM_TENSOR && c->n_chan > RD_TC_MAX_CHAN)
+    return fail(RD_EINVAL, "the tensor form takes at most %u channels", RD_TC_MAX_CHAN);
   if (c->vc > 3 || c->src_id > 31 || c->dest > 15) return fail(RD_EINVAL, "packet header field out of range");
   return RD_OK;
 }
@@ -365,6 +368,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
   if (bad(cudaStreamCreateWithFlags(&ch->stream, cudaStreamNonBlocking)) ||
       bad(ch->coeff_t.ensure((size_t)T * N)) || bad(ch->weights.ensure((size_t)B * C)) ||
       bad(ch->w_limbs.ensure((size_t)B * C)) ||
+      (c.form == RD_FORM_TENSOR && bad(ch->w_frag.ensure(beam_tc_fragment_words(C, B)))) ||
       bad(ch->tail[0].ensure((size_t)C * D * N)) || bad(ch->tail[1].ensure((size_t)C * D * N)) ||
       bad(ch->ring.ensure((size_t)ch->R * N * C)) || bad(ch->power.ensure((size_t)F * B * N)) ||
       bad(ch->counts.ensure((size_t)F * B)) || bad(ch->detsup.ensure((size_t)F * B * 2)) ||
@@ -377,6 +381,8 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
   cudaMemset(ch->coeff_t.p, 0, (size_t)T * N * 4);
   cudaMemset(ch->weights.p, 0, (size_t)B * C * 4);
   cudaMemset(ch->w_limbs.p, 0, (size_t)B * C * sizeof(int4));
+  if (c.form == RD_FORM_TENSOR)
+    cudaMemset(ch->w_frag.p, 0, (size_t)beam_tc_fragment_words(C, B) * 4);
   cudaMemset(ch->tail[0].p, 0, (size_t)C * D * N * 4);
   cudaMemset(ch->tail[1].p, 0, (size_t)C * D * N * 4);
   cudaMemset(ch->ring.p, 0, (size_t)ch->R * N * C * 4);
@@ -428,7 +434,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
 void rd_chain_destroy(rd_chain* ch) {
   if (!ch) return;
   if (ch->stream) cudaStreamSynchronize(ch->stream);
-  ch->coeff_t.release(); ch->weights.release(); ch->w_limbs.release(); ch->tail[0].release(); ch->tail[1].release();
+  ch->coeff_t.release(); ch->weights.release(); ch->w_limbs.release(); ch->w_frag.release(); ch->tail[0].release(); ch->tail[1].release();
   ch->ring.release(); ch->power.release(); ch->beams_bn.release(); ch->stage.release();
   ch->tw_pos.release();
   ch->px.release(); ch->py.release(); ch->acc_re.release(); ch->acc_im.release();
@@ -466,6 +472,13 @@ rd_status rd_chain_set_weights(rd_chain* ch, const rd_cplx16* w) {
   CK(cudaMemcpyAsync(ch->weights.p, w, n * 4, cudaMemcpyHostToDevice, ch->stream));
   CK(cudaMemcpyAsync(ch->w_limbs.p, limbs.data(), n * sizeof(int4), cudaMemcpyHostToDevice,
                      ch->stream));
+  std::vector<uint32_t> frag;
+  if (ch->cfg.form == RD_FORM_TENSOR) {
+    frag.resize(beam_tc_fragment_words(ch->cfg.n_chan, ch->cfg.n_beams));
+    beam_tc_fragments(w, ch->cfg.n_chan, ch->cfg.n_beams, frag.data());
+    CK(cudaMemcpyAsync(ch->w_frag.p, frag.data(), frag.size() * 4, cudaMemcpyHostToDevice,
+                       ch->stream));
+  }
   CK(cudaStreamSynchronize(ch->stream));
   return RD_OK;
 }
@@ -533,6 +546,7 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   bp.g0 = ch->frame;
   bp.weights = ch->weights.p;
   bp.w_limbs = ch->w_limbs.p;
+  bp.w_frag = ch->w_frag.p;
   bp.power = ch->power.p;
   bp.beams_bn = ch->beams_bn.p;
   bp.F = F;
@@ -542,7 +556,10 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   bp.stats = st;
   {
     KTimer t(ch, KT_BEAM);
-    launch_beam(bp, s);
+    if (c.form == RD_FORM_TENSOR)
+      launch_beam_tc(bp, s);
+    else
+      launch_beam(bp, s);
   }
   ch->launches++;
 
@@ -1031,6 +1048,8 @@ rd_status rd_bf_run(uint32_t n_ant, uint32_t n_beams, const rd_cplx16* w, const 
                     uint64_t n_vec, rd_cplx16* y, int64_t* acc, uint8_t* flags, uint32_t form) {
   if (!w || !x || !y || n_ant == 0 || n_beams == 0 || form > RD_FORM_TENSOR)
     return fail(RD_EINVAL, "bad argument");
+  if (form == RD_FORM_TENSOR && n_ant > RD_TC_MAX_CHAN)
+    return fail(RD_EINVAL, "the tensor form takes at most %u antennas", RD_TC_MAX_CHAN);
   if (!rd_device_ok()) return fail(RD_EDEVICE, "no usable CUDA device");
   Scratch sc;
   uint32_t *dw, *dx, *dy;
@@ -1043,7 +1062,32 @@ rd_status rd_bf_run(uint32_t n_ant, uint32_t n_beams, const rd_cplx16* w, const 
   if (flags) CK(sc.alloc(&df, n_vec * n_beams));
   CK(cudaMemcpy(dw, w, (size_t)n_ant * n_beams * 4, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(dx, x, n_vec * n_ant * 4, cudaMemcpyHostToDevice));
-  launch_bf_block(n_ant, n_beams, dw, dx, n_vec, dy, dacc, df, 0);
+  if (form == RD_FORM_TENSOR) {
+    // the vectors as a one-bin "ring" of n_vec frames, in launches of < 2^31 rows
+    std::vector<uint32_t> frag(beam_tc_fragment_words(n_ant, n_beams));
+    beam_tc_fragments(w, n_ant, n_beams, frag.data());
+    uint32_t* dfrag;
+    CK(sc.alloc(&dfrag, frag.size()));
+    CK(cudaMemcpy(dfrag, frag.data(), frag.size() * 4, cudaMemcpyHostToDevice));
+    const uint64_t step = 1ull << 30;
+    for (uint64_t v0 = 0; v0 < n_vec; v0 += step) {
+      const uint32_t F = (uint32_t)(n_vec - v0 < step ? n_vec - v0 : step);
+      BeamParams bp{};
+      bp.ring = dx + v0 * n_ant;
+      bp.ring_frames = F;
+      bp.w_frag = dfrag;
+      bp.y_rows = dy + v0 * n_beams;
+      bp.acc_rows = dacc ? dacc + v0 * n_beams * 2 : nullptr;
+      bp.flag_rows = df ? df + v0 * n_beams : nullptr;
+      bp.F = F;
+      bp.C = n_ant;
+      bp.N = 1;
+      bp.B = n_beams;
+      launch_beam_tc(bp, 0);
+    }
+  } else {
+    launch_bf_block(n_ant, n_beams, dw, dx, n_vec, dy, dacc, df, 0);
+  }
   CK(cudaGetLastError());
   CK(cudaMemcpy(y, dy, n_vec * n_beams * 4, cudaMemcpyDeviceToHost));
   if (acc) CK(cudaMemcpy(acc, dacc, n_vec * n_beams * 16, cudaMemcpyDeviceToHost));

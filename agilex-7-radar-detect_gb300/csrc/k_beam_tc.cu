@@ -1,0 +1,298 @@
+// k_beam_tc.cu - beamforming on the tensor cores, exact.
+//
+// Y[r][b] = sum_a X[r][a] W[b][a] (bf::dot, beamformer_model.hpp:162-179) as a
+// real fp16 GEMM with fp32 accumulation that is exact by construction:
+//
+//   x = 256 xh + xl,  w = 256 wh + wl,  xh, wh in [-128, 127], xl, wl in [0, 255]
+//
+// every limb is an integer of magnitude <= 256, exact in fp16; every product
+// is an integer of magnitude < 2^16, exact in fp32; and the three scale
+// classes of the complex product
+//
+//   class 16: xh*wh          class 8: xh*wl + xl*wh          class 0: xl*wl
+//
+// each sum at most 4 C terms of magnitude <= 128 * 255, which for C <= 128 is
+// below 2^24: every partial sum the tensor core forms, in any order, is an
+// integer that fp32 holds exactly. The epilogue recombines
+// acc = 2^16 c16 + 2^8 c8 + c0 in int64 - the integer bf::dot sums - then
+// round_sat and covar::power (covar_model.hpp:99-102).
+//
+// GEMM: rows r = (frame, bin) of the spectrum ring; K = 4 limb parts x C
+// channels, k = 4a + {xre_hi, xim_hi, xre_lo, xim_lo}; N = 6 columns per beam
+// {re16, re8, re0, im16, im8, im0}. Three m16n8 tiles cover four beams, laid
+// out so that column 2t + e of tile j is class 2j + e of beam t: the lane of
+// the accumulator fragment that holds columns 2t, 2t+1 then holds all six
+// classes of beam t for its two rows after the three tiles, and every lane
+// finishes two outputs without exchanging data. The weight matrix is built on
+// the host in mma fragment order (set_weights). mma.sync m16n8k16 f16 -> f32.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstring>
+
+#include "fxp.cuh"
+#include "rd_internal.h"
+
+namespace rd {
+
+constexpr unsigned kTcRows = 128u;  // rows per CTA: 8 warps x 16
+constexpr unsigned kTcBeams = 16u;  // beams per group: 4 tile triples
+constexpr unsigned kTcTiles = 12u;  // m16n8 tiles per group
+
+__device__ __forceinline__ uint32_t hsub2(uint32_t a, uint32_t b) {
+  uint32_t d;
+  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+
+// fp16x2 limb words of a packed sample v = {im, re}: hi = (re >> 8, im >> 8),
+// lo = (re & 255, im & 255). The fp16 number with bits 0x6400 | u is 1024 + u
+// for u < 1024, so placing a byte under that exponent and subtracting the
+// bias gives the byte's value exactly; the high byte is made unsigned by
+// flipping the sign bit first (bias 1024 + 128).
+__device__ __forceinline__ void limb_words(uint32_t v, uint32_t& hi, uint32_t& lo) {
+  hi = hsub2((((v ^ 0x80008000u) >> 8) & 0x00FF00FFu) | 0x64006400u, 0x64806480u);
+  lo = hsub2((v & 0x00FF00FFu) | 0x64006400u, 0x64006400u);
+}
+
+__device__ __forceinline__ void mma_f16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
+                                        uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 "
+      "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// ---- host: weight operand -----------------------------------------------------
+static int wlimb(const uint32_t* w, uint32_t C, uint32_t B, uint32_t b, uint32_t a, int part) {
+  if (b >= B || a >= C) return 0;
+  const uint32_t v = w[(size_t)b * C + a];
+  const int re = (int16_t)(uint16_t)(v & 0xFFFFu), im = (int16_t)(uint16_t)(v >> 16);
+  switch (part) {
+    case 0: return re >> 8;    // wrh
+    case 1: return im >> 8;    // wih
+    case 2: return re & 255;   // wrl
+    default: return im & 255;  // wil
+  }
+}
+
+// W'[k = 4a + part][class] of beam b, class in {re16, re8, re0, im16, im8, im0}:
+// re = xr wr - xi wi, im = xr wi + xi wr, split by limb scale.
+static int wprime(const uint32_t* w, uint32_t C, uint32_t B, uint32_t b, uint32_t k, int cls) {
+  const uint32_t a = k / 4;
+  const int part = (int)(k % 4);  // 0 xrh, 1 xih, 2 xrl, 3 xil
+  const int wrh = wlimb(w, C, B, b, a, 0), wih = wlimb(w, C, B, b, a, 1);
+  const int wrl = wlimb(w, C, B, b, a, 2), wil = wlimb(w, C, B, b, a, 3);
+  switch (cls) {
+    case 0: return part == 0 ? wrh : part == 1 ? -wih : 0;                       // re16
+    case 1: return part == 0 ? wrl : part == 1 ? -wil : part == 2 ? wrh : -wih;  // re8
+    case 2: return part == 2 ? wrl : part == 3 ? -wil : 0;                       // re0
+    case 3: return part == 0 ? wih : part == 1 ? wrh : 0;                        // im16
+    case 4: return part == 0 ? wil : part == 1 ? wrl : part == 2 ? wih : wrh;    // im8
+    default: return part == 2 ? wil : part == 3 ? wrl : 0;                       // im0
+  }
+}
+
+// IEEE binary16 bits of an integer |v| <= 2048 (exact)
+static uint16_t host_f16(int v) {
+  if (v == 0) return 0;
+  const unsigned sign = v < 0 ? 0x8000u : 0u;
+  const unsigned m = (unsigned)(v < 0 ? -v : v);
+  int e = 0;
+  while ((m >> (e + 1)) != 0) ++e;  // m in [2^e, 2^(e+1))
+  const unsigned mant = (m << (10 - e)) & 0x3FFu;
+  return (uint16_t)(sign | (unsigned)(e + 15) << 10 | mant);
+}
+
+uint32_t beam_tc_fragment_words(uint32_t C, uint32_t B) {
+  const uint32_t KS = (C + 3u) / 4u, G = (B + kTcBeams - 1u) / kTcBeams;
+  return G * KS * kTcTiles * 64u;
+}
+
+// Fragment order: [group][k-step][tile j][lane] x 2 words. Lane (g', t') of
+// tile j holds B[k = 2t' + {0,1}][n = g'] and B[k = 2t' + 8 + {0,1}][n = g'];
+// column n of tile j (triple j / 3, sub-tile j % 3) is class 2 (j % 3) +
+// (n & 1) of beam 16 group + 4 (j / 3) + (n >> 1).
+void beam_tc_fragments(const uint32_t* w, uint32_t C, uint32_t B, uint32_t* out) {
+  const uint32_t KS = (C + 3u) / 4u, G = (B + kTcBeams - 1u) / kTcBeams;
+  for (uint32_t g = 0; g < G; ++g)
+    for (uint32_t kk = 0; kk < KS; ++kk)
+      for (uint32_t j = 0; j < kTcTiles; ++j)
+        for (uint32_t l = 0; l < 32; ++l) {
+          const uint32_t n = l >> 2, tig = l & 3;
+          const uint32_t b = g * kTcBeams + (j / 3) * 4 + (n >> 1);
+          const int cls = (int)(2 * (j % 3) + (n & 1));
+          uint32_t* o = out + (((size_t)(g * KS + kk) * kTcTiles + j) * 64 + l * 2);
+          for (int h = 0; h < 2; ++h) {
+            const uint32_t k0 = kk * 16 + tig * 2 + (uint32_t)h * 8;
+            const uint16_t lo = host_f16(wprime(w, C, B, b, k0, cls));
+            const uint16_t hi = host_f16(wprime(w, C, B, b, k0 + 1, cls));
+            o[h] = (uint32_t)lo | ((uint32_t)hi << 16);
+          }
+        }
+}
+
+// ---- device ---------------------------------------------------------------------
+// One CTA: 128 rows of the ring, all beams in groups of 16. The rows are
+// converted once into fp16 limb words in shared memory, row stride S = 8 ks
+// + 4 words (ks = ceil(C / 4) k16 steps): word 2a of a row holds channel a's
+// (re, im) high limbs and word 2a + 1 its low limbs, so the A fragment of
+// k-step kk is words 8 kk + t and 8 kk + 4 + t, bank-conflict free.
+__global__ void __launch_bounds__(256, 2) k_beam_tc(BeamParams p) {
+  extern __shared__ __align__(16) uint32_t sm[];
+  const unsigned C = p.C, B = p.B, N = p.N;
+  const unsigned ks = (C + 3u) / 4u;
+  const unsigned S = 8u * ks + 4u;
+  uint32_t* s_x = sm;                                                      // [128][S]
+  unsigned long long* s_off = reinterpret_cast<unsigned long long*>(sm + kTcRows * S);
+  uint32_t* s_f = reinterpret_cast<uint32_t*>(s_off + kTcRows);            // chunk frame
+  uint32_t* s_bin = s_f + kTcRows;
+  const unsigned tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+  const unsigned gid = lane >> 2, tig = lane & 3u;
+  const uint64_t rows = (uint64_t)p.F * N;
+  const uint64_t r0 = (uint64_t)blockIdx.x * kTcRows;
+
+  if (tid < kTcRows) {
+    const uint64_t r = r0 + tid;
+    unsigned long long off = ~0ull;
+    unsigned f = 0, bin = 0;
+    if (r < rows) {
+      f = (unsigned)(r / N);
+      bin = (unsigned)(r - (uint64_t)f * N);
+      unsigned slot = p.ring_base + f;
+      if (slot >= p.ring_frames) slot -= p.ring_frames;
+      off = ((unsigned long long)slot * N + bin) * C;
+    }
+    s_off[tid] = off;
+    s_f[tid] = f;
+    s_bin[tid] = bin;
+  }
+  __syncthreads();
+  // stage: 4 channels per item (channels >= C and rows >= rows read as 0,
+  // whose limbs are 0)
+  const bool vec = (C & 3u) == 0u;
+  for (unsigned k = tid; k < kTcRows * ks; k += 256u) {
+    const unsigned rr = k / ks, j = k - rr * ks;
+    const unsigned long long off = s_off[rr];
+    uint32_t v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+    if (off != ~0ull) {
+      if (vec) {
+        const uint4 t = __ldg(reinterpret_cast<const uint4*>(p.ring + off) + j);
+        v0 = t.x, v1 = t.y, v2 = t.z, v3 = t.w;
+      } else {
+        const unsigned a = 4u * j;
+        v0 = p.ring[off + a];
+        if (a + 1u < C) v1 = p.ring[off + a + 1u];
+        if (a + 2u < C) v2 = p.ring[off + a + 2u];
+        if (a + 3u < C) v3 = p.ring[off + a + 3u];
+      }
+    }
+    uint4 w0, w1;
+    limb_words(v0, w0.x, w0.y);
+    limb_words(v1, w0.z, w0.w);
+    limb_words(v2, w1.x, w1.y);
+    limb_words(v3, w1.z, w1.w);
+    uint4* dst = reinterpret_cast<uint4*>(s_x + rr * S + 8u * j);
+    dst[0] = w0;
+    dst[1] = w1;
+  }
+  __syncthreads();
+
+  const uint32_t* xa0 = s_x + (warp * 16u + gid) * S + tig;
+  const uint32_t* xa1 = xa0 + 8u * S;
+  const unsigned rr0 = warp * 16u + gid;
+  const unsigned long long off0 = s_off[rr0], off1 = s_off[rr0 + 8u];
+  const unsigned f0 = s_f[rr0], f1 = s_f[rr0 + 8u];
+  const unsigned bin0 = s_bin[rr0], bin1 = s_bin[rr0 + 8u];
+  const unsigned G = (B + kTcBeams - 1u) / kTcBeams;
+  unsigned fl_any = 0;
+  unsigned long long nsat = 0;
+  for (unsigned grp = 0; grp < G; ++grp) {
+    float d[kTcTiles][4];
+#pragma unroll
+    for (int j = 0; j < (int)kTcTiles; ++j) d[j][0] = d[j][1] = d[j][2] = d[j][3] = 0.f;
+    const uint2* wf = reinterpret_cast<const uint2*>(p.w_frag) +
+                      (size_t)grp * ks * kTcTiles * 32u + lane;
+#pragma unroll 1
+    for (unsigned kk = 0; kk < ks; ++kk) {
+      const uint32_t af[4] = {xa0[8u * kk], xa1[8u * kk], xa0[8u * kk + 4u], xa1[8u * kk + 4u]};
+      const uint2* wk = wf + (size_t)kk * kTcTiles * 32u;
+#pragma unroll
+      for (int j = 0; j < (int)kTcTiles; ++j) {
+        const uint2 bw = __ldg(wk + j * 32);
+        mma_f16(d[j], af, bw.x, bw.y);
+      }
+    }
+    // epilogue: lane t of each quad holds beam 4 t3 + t of the group for
+    // rows g (h = 0) and g + 8 (h = 1)
+#pragma unroll
+    for (int t3 = 0; t3 < 4; ++t3) {
+      const unsigned b = grp * kTcBeams + (unsigned)t3 * 4u + tig;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const float* c0 = d[3 * t3];
+        const float* c1 = d[3 * t3 + 1];
+        const float* c2 = d[3 * t3 + 2];
+        const long long re_v = (long long)__float2int_rn(c0[2 * h]) * 65536 +
+                               (long long)__float2int_rn(c0[2 * h + 1]) * 256 +
+                               (long long)__float2int_rn(c1[2 * h]);
+        const long long im_v = (long long)__float2int_rn(c1[2 * h + 1]) * 65536 +
+                               (long long)__float2int_rn(c2[2 * h]) * 256 +
+                               (long long)__float2int_rn(c2[2 * h + 1]);
+        const unsigned long long off = h ? off1 : off0;
+        if (b < B && off != ~0ull) {
+          unsigned fr = 0, fi = 0;
+          const int32_t yr = q15_out64(re_v, &fr), yi = q15_out64(im_v, &fi);
+          if (fr | fi) {
+            fl_any |= fr | fi;
+            ++nsat;
+          }
+          cplx y;
+          y.re = (int16_t)yr;
+          y.im = (int16_t)yi;
+          const uint64_t f = h ? f1 : f0, bin = h ? bin1 : bin0;
+          const uint64_t r = r0 + rr0 + 8u * (unsigned)h;
+          if (p.power) p.power[(f * B + b) * N + bin] = power_u32(y);
+          if (p.beams_bn) p.beams_bn[(f * N + bin) * B + b] = pack(y);
+          if (p.y_rows) p.y_rows[r * B + b] = pack(y);
+          if (p.acc_rows) {
+            p.acc_rows[(r * B + b) * 2] = re_v;
+            p.acc_rows[(r * B + b) * 2 + 1] = im_v;
+          }
+          if (p.flag_rows) p.flag_rows[r * B + b] = (uint8_t)((fr << 2) | fi);
+        }
+      }
+    }
+  }
+  const unsigned a = __reduce_or_sync(0xffffffffu, fl_any);
+  for (int o = 16; o > 0; o >>= 1) nsat += __shfl_xor_sync(0xffffffffu, nsat, o);
+  if (lane == 0u && p.stats) {
+    if (a) atomicOr(&p.stats->bf_flags, a);
+    if (nsat) atomicAdd(&p.stats->bf_sat, nsat);
+  }
+}
+
+size_t beam_tc_smem(uint32_t C) {
+  const size_t S = 8u * ((C + 3u) / 4u) + 4u;
+  return (kTcRows * S + 4u * kTcRows) * sizeof(uint32_t);
+}
+
+// the dynamic shared-memory opt-in is per device
+static std::atomic<bool> g_tc_attr[64];
+
+void launch_beam_tc(const BeamParams& p, cudaStream_t s) {
+  const uint64_t rows = (uint64_t)p.F * p.N;
+  if (!rows) return;
+  const size_t smem = beam_tc_smem(p.C);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64 || !g_tc_attr[dev].load()) {
+    cudaFuncSetAttribute(k_beam_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)beam_tc_smem(RD_TC_MAX_CHAN));
+    if (dev >= 0 && dev < 64) g_tc_attr[dev].store(true);
+  }
+  k_beam_tc<<<(unsigned)((rows + kTcRows - 1u) / kTcRows), 256, smem, s>>>(p);
+}
+
+}  // namespace rd

@@ -74,12 +74,21 @@ struct BeamParams {
   uint64_t g0;
   const uint32_t* weights;  // [B][C]
   const int4* w_limbs;      // [B][C] {wh.re, wh.im, wl.re, wl.im}, w = 256 wh + wl
-  uint32_t* power;          // [F][B][N]
+  const uint32_t* w_frag;   // tensor form: beam_tc_fragments() of the weights
+  uint32_t* power;          // [F][B][N] (or null)
   uint32_t* beams_bn;       // [F][N][B] beam samples (null unless needed)
+  uint32_t* y_rows;         // per-block entry: [rows][B] y, acc, flags (or null)
+  long long* acc_rows;
+  uint8_t* flag_rows;
   uint32_t F, C, N, B;
-  DevStats* stats;
+  DevStats* stats;          // may be null
 };
 void launch_beam(const BeamParams& p, cudaStream_t s);
+// Tensor-core form (k_beam_tc.cu): mma fragments of the limb-split weights.
+void launch_beam_tc(const BeamParams& p, cudaStream_t s);
+uint32_t beam_tc_fragment_words(uint32_t C, uint32_t B);
+size_t beam_tc_smem(uint32_t C);
+void beam_tc_fragments(const uint32_t* w, uint32_t C, uint32_t B, uint32_t* out);
 
 struct CovParams {
   const uint32_t* ring;     // channel source: [R][N][C]

@@ -55,8 +55,15 @@ enum { RD_EV_DETECT = 0, RD_EV_BIN = 1, RD_EV_SUPPRESSED = 2, RD_EV_SUMMARY = 3 
 enum { RD_COV_OFF = 0, RD_COV_CHANNEL = 1, RD_COV_BEAM = 2 };
 enum { RD_COV_BLOCK = 0, RD_COV_EXP = 1 };
 
-/* Form of the beamforming / covariance contraction. Both are bit-exact. */
+/* Form of the beamforming contraction. Both are bit-exact.
+ * RD_FORM_CUDA_CORE: int32 limb multiply-accumulate on the CUDA cores.
+ * RD_FORM_TENSOR: the int16 samples and weights split into 8-bit limbs held
+ * exactly in fp16, multiplied on the tensor cores with fp32 accumulation
+ * whose every partial sum is an integer below 2^24 (hence n_chan <=
+ * RD_TC_MAX_CHAN), recombined in int64. Covariance always runs on the CUDA
+ * cores. */
 enum { RD_FORM_CUDA_CORE = 0, RD_FORM_TENSOR = 1 };
+#define RD_TC_MAX_CHAN 128u
 
 /* Stream geometry and block configuration. Zero-initialise, then fill;
  * rd_config_default() gives the values the reference's defaults imply. */
@@ -87,7 +94,7 @@ typedef struct rd_config {
   uint32_t src_id, dest, vc;
   /* engine */
   uint32_t max_frames;    /* frames per internal launch (sizes device state) */
-  uint32_t form;          /* RD_FORM_* for beamforming and covariance */
+  uint32_t form;          /* RD_FORM_* of the beamformer */
 } rd_config;
 
 /* One CFAR event as the chain emits it. w[] holds the 176-bit event of
@@ -244,7 +251,8 @@ rd_status rd_fft_run(uint32_t n_fft, uint32_t spc, uint32_t scale_sched,
 /* bf::dot / BeamformerModel::step (beamformer_model.hpp:162-179,283-303) for
  * n_vec antenna vectors x[n_vec][n_ant] -> y[n_vec][n_beams].
  * acc: [n_vec][n_beams][2] exact accumulators (may be NULL);
- * flags: [n_vec][n_beams] bytes (f_re << 2) | f_im (may be NULL). */
+ * flags: [n_vec][n_beams] bytes (f_re << 2) | f_im (may be NULL).
+ * form: RD_FORM_*; RD_FORM_TENSOR needs n_ant <= RD_TC_MAX_CHAN. */
 rd_status rd_bf_run(uint32_t n_ant, uint32_t n_beams, const rd_cplx16* w,
                     const rd_cplx16* x, uint64_t n_vec, rd_cplx16* y,
                     int64_t* acc, uint8_t* flags, uint32_t form);

@@ -54,6 +54,21 @@ def test_config_validation(lib):
         assert lib.rd_last_error()
 
 
+def test_tensor_form_channel_limit(lib):
+    # the tensor form's exactness bound: at most RD_TC_MAX_CHAN channels
+    assert abi.RD_TC_MAX_CHAN == 128
+    cfg = sc.make_config(sc.preset("tiny"), form=abi.RD_FORM_TENSOR)
+    assert lib.rd_config_validate(C.byref(cfg)) == abi.RD_OK
+    cfg.n_chan = abi.RD_TC_MAX_CHAN + 1
+    assert lib.rd_config_validate(C.byref(cfg)) == abi.RD_EINVAL
+    n = abi.RD_TC_MAX_CHAN + 1
+    w = np.zeros(n, np.uint32)
+    y = np.zeros(1, np.uint32)
+    st = lib.rd_bf_run(n, 1, w.ctypes.data, w.ctypes.data, 1, y.ctypes.data, None, None,
+                       abi.RD_FORM_TENSOR)
+    assert st == abi.RD_EINVAL and b"tensor form" in lib.rd_last_error()
+
+
 def test_geometry_helpers(lib):
     # packet_model.hpp:118-127: 1 + ceil(176 / W) flits of W + 5 bits
     assert [lib.rd_detection_flits(w) for w in (64, 128, 512)] == [4, 3, 2]

@@ -1,0 +1,108 @@
+"""The tensor-core form of the beamformer (RD_FORM_TENSOR) on the GPU, through
+the C ABI: bit-exact against the CPU oracle and against the CUDA-core form,
+per block (bf::dot, beamformer_model.hpp:162-179) and inside the chain
+(the committed fixtures made by the reference's model headers, seeded random
+chains, the full workload's geometry). The limb split makes every partial sum
+an integer below 2^24, so any difference at all is a bug, not rounding."""
+import numpy as np
+import pytest
+
+from conftest import load_chain_fixture
+from helpers import CHAIN_KEYS, TAP_KEYS, cfg_from_fixture, diff, diff_stats, fixture_stats
+from rdgb import abi, chain as gc, scenario as sc
+
+pytestmark = pytest.mark.gpu
+TC = abi.RD_FORM_TENSOR
+
+
+def rnd(rng, n):
+    return rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
+
+
+@pytest.mark.parametrize("A,B", [(1, 1), (4, 2), (16, 16), (64, 64), (5, 3), (63, 17),
+                                 (65, 16), (128, 7), (127, 33), (2, 100)])
+def test_bf_tensor_random_vs_oracle(gpulib, port, A, B):
+    rng = np.random.default_rng(7 * A + B)
+    w, x = rnd(rng, A * B), rnd(rng, 301 * A)
+    want = port.bf(A, B, w, x)
+    for a, b in zip(gc.bf(A, B, w, x, form=TC), want):
+        assert np.array_equal(a, b)
+    for a, b in zip(gc.bf(A, B, w, x, form=TC), gc.bf(A, B, w, x)):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("A", [64, 128])
+def test_bf_tensor_extremes(gpulib, port, A):
+    # every limb at its extreme: -32768 (high limb -128, low 0), 32767
+    # (127, 255), -1 (-1, 255), and mixed signs; at 128 channels the class
+    # sums come within 0.4 % of 2^24, the most the fp32 accumulation holds
+    B = 16
+    vals = np.array([-32768, 32767, -1, 0, 255, -256, 128, -129], np.int64)
+    rng = np.random.default_rng(11 + A)
+    for trial in range(6):
+        wr, wi = rng.choice(vals, A * B), rng.choice(vals, A * B)
+        xr, xi = rng.choice(vals, 97 * A), rng.choice(vals, 97 * A)
+        if trial == 0:
+            wr[:] = wi[:] = -32768
+            xr[:] = xi[:] = -32768
+        if trial == 1:
+            wr[:], wi[:] = 32767, -32768
+            xr[:], xi[:] = -32768, 32767
+        if trial == 2:  # the largest class-8 and class-0 sums: low limbs 255, high -128
+            wr[:], wi[:] = -32768 + 255, 32767
+            xr[:], xi[:] = -32768 + 255, -32768 + 255
+        w, x = sc.pack(wr, wi), sc.pack(xr, xi)
+        got, want = gc.bf(A, B, w, x, form=TC), port.bf(A, B, w, x)
+        for a, b in zip(got, want):
+            assert np.array_equal(a, b), trial
+
+
+@pytest.mark.parametrize("name", ["tiny", "ref_tiny", "medium_slice", "tiny_sat"])
+def test_chain_tensor_fixture(gpulib, name):
+    z = load_chain_fixture(name)
+    cfg = cfg_from_fixture(z)
+    cfg.form = TC
+    ch = gc.Chain(cfg, z["coeff"], z["weights"], (z["px"], z["py"]))
+    n_fft, f0 = cfg.n_fft, 0
+    for i, nf in enumerate(z["calls"]):
+        taps = f"c{i}_tap_pfb" in z
+        r = ch.process(z["adc"][:, f0 * n_fft:(f0 + nf) * n_fft], taps=taps,
+                       cap_events=int(nf) * cfg.n_beams * (n_fft + 1))
+        want = {k[len(f"c{i}_"):]: z[k] for k in z.files if k.startswith(f"c{i}_")}
+        assert diff(r, want, CHAIN_KEYS + TAP_KEYS) == [], (name, i)
+        assert diff_stats(ch.stats(), fixture_stats(z, i)) == [], (name, i)
+        f0 += nf
+
+
+def test_chain_tensor_full_geometry_vs_oracle(gpulib, port):
+    # 64 channels, 1024 bins, 64 beams: four beam groups, one channel block
+    p = sc.preset("full", cov_window=8)
+    cfg = sc.make_config(p, max_frames=12, form=TC)
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    x = sc.adc(p, 20 * p.n_fft)
+    g = gc.Chain(cfg, coeff, w, (px, py))
+    rg = g.process(x, taps=True)
+    o = port.chain(cfg, coeff, w, px, py)
+    ro = o.process(x, taps=True, threads=8)
+    assert diff(rg, ro, CHAIN_KEYS + TAP_KEYS) == []
+    assert diff_stats(g.stats(), o.stats()) == []
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_chain_tensor_equals_cuda_core(gpulib, seed):
+    # random weights over the full int16 range and a medium CPI: both forms
+    # give identical outputs and statistics
+    rng = np.random.default_rng(300 + seed)
+    p = sc.preset("medium")
+    px, py = sc.pair_table(p)
+    coeff = sc.coefficients(p.n_fft, p.taps)
+    w = rnd(rng, p.n_chan * p.n_beams) if seed else sc.steering_weights(p.n_chan, p.n_beams)
+    x = sc.adc(p, p.cpi_samples // 4, start=seed * 1000 * p.n_fft)
+    outs = []
+    for form in (abi.RD_FORM_CUDA_CORE, TC):
+        cfg = sc.make_config(p, max_frames=int(rng.integers(20, 200)), form=form)
+        ch = gc.Chain(cfg, coeff, w, (px, py))
+        outs.append((ch.process(x, taps=True), ch.stats()))
+    assert diff(outs[0][0], outs[1][0], CHAIN_KEYS + TAP_KEYS) == []
+    assert diff_stats(outs[0][1], outs[1][1]) == []
