@@ -123,12 +123,16 @@ def kernel_bytes(cfg, name: str, frames: int) -> float:
 
 
 def profile_traffic(kernel: str) -> float | None:
-    """dram read+write bytes per launch from the committed ncu summary, when
-    one exists for this kernel on this workload."""
-    f = ROOT / "profiles" / f"{kernel}_medium.json"
+    """dram read+write bytes per launch of `kernel` at the bench's launch size,
+    from the committed ncu summary of the medium chain (a line
+    `traffic <kernel> dram_bytes_per_launch=<bytes>`), or None."""
+    import re
+    f = ROOT / "profiles" / "kernels_medium_ncu_full.md"
     if f.exists():
-        d = json.loads(f.read_text())
-        return d.get("dram_bytes_per_launch_scaled")
+        m = re.search(rf"^traffic {re.escape(kernel)} dram_bytes_per_launch=(\d+)$",
+                      f.read_text(), re.M)
+        if m:
+            return float(m.group(1))
     return None
 
 
