@@ -175,9 +175,18 @@ struct rd_chain {
   DevBuf<uint32_t> coeff_t, weights, tail[2], ring, power, beams_bn, stage, tw_pos;
   DevBuf<int4> w_limbs;
   DevBuf<uint32_t> w_frag;  // tensor form: mma fragments of the limb-split weights
+  // tensor form of the exact covariance: plan, unit lists and pair map
+  CovTcHost cov_tc{};
+  bool cov_tc_ok = false;
+  DevBuf<uint32_t> ct_units;
+  DevBuf<int32_t> ct_pq;
   int tail_cur = 0;
   DevBuf<uint32_t> px, py;
+  // integrator state [2][N][P]: each launch reads one copy and writes the
+  // other, so the CTA that carries a window in never races the CTA that
+  // carries the next one out
   DevBuf<long long> acc_re, acc_im, cov_out;
+  uint32_t acc_cur = 0;
   DevBuf<unsigned> sticky, satcnt, win_flags;
   DevBuf<uint32_t> counts, detsup, mask;
   DevBuf<unsigned long long> offsets;
@@ -335,15 +344,28 @@ static rd_status upload_pairs(rd_chain* ch, const uint32_t* x, const uint32_t* y
   CK(cudaMemcpy(ch->px.p, x, n * 4, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ch->py.p, y, n * 4, cudaMemcpyHostToDevice));
   const size_t k = (size_t)ch->cfg.n_fft * n;
-  CK(ch->acc_re.ensure(k));
-  CK(ch->acc_im.ensure(k));
+  CK(ch->acc_re.ensure(2 * k));
+  CK(ch->acc_im.ensure(2 * k));
   CK(ch->sticky.ensure(k));
   CK(ch->satcnt.ensure(2 * k));
-  CK(cudaMemset(ch->acc_re.p, 0, k * 8));
-  CK(cudaMemset(ch->acc_im.p, 0, k * 8));
+  CK(cudaMemset(ch->acc_re.p, 0, 2 * k * 8));
+  CK(cudaMemset(ch->acc_im.p, 0, 2 * k * 8));
+  ch->acc_cur = 0;
   CK(cudaMemset(ch->sticky.p, 0, k * 4));
   CK(cudaMemset(ch->satcnt.p, 0, k * 8));
   ch->P = n;
+  ch->cov_tc_ok = false;
+  if (ch->cfg.form == RD_FORM_TENSOR && cov_tc_plan(ch->S, x, y, n, &ch->cov_tc)) {
+    CK(ch->ct_units.ensure(ch->cov_tc.units.size()));
+    CK(ch->ct_pq.ensure(ch->cov_tc.pq.size()));
+    CK(cudaMemcpy(ch->ct_units.p, ch->cov_tc.units.data(), ch->cov_tc.units.size() * 4,
+                  cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ch->ct_pq.p, ch->cov_tc.pq.data(), ch->cov_tc.pq.size() * 4,
+                  cudaMemcpyHostToDevice));
+    ch->cov_tc.plan.units = ch->ct_units.p;
+    ch->cov_tc.plan.pq = ch->ct_pq.p;
+    ch->cov_tc_ok = true;
+  }
   return RD_OK;
 }
 
@@ -436,7 +458,7 @@ void rd_chain_destroy(rd_chain* ch) {
   if (ch->stream) cudaStreamSynchronize(ch->stream);
   ch->coeff_t.release(); ch->weights.release(); ch->w_limbs.release(); ch->w_frag.release(); ch->tail[0].release(); ch->tail[1].release();
   ch->ring.release(); ch->power.release(); ch->beams_bn.release(); ch->stage.release();
-  ch->tw_pos.release();
+  ch->tw_pos.release(); ch->ct_units.release(); ch->ct_pq.release();
   ch->px.release(); ch->py.release(); ch->acc_re.release(); ch->acc_im.release();
   ch->cov_out.release(); ch->sticky.release(); ch->satcnt.release(); ch->win_flags.release();
   ch->counts.release(); ch->detsup.release(); ch->mask.release(); ch->offsets.release();
@@ -584,8 +606,11 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
     cp.P = ch->P;
     cp.F = F;
     cp.N = N;
-    cp.acc_re = ch->acc_re.p;
-    cp.acc_im = ch->acc_im.p;
+    const size_t nk = (size_t)N * ch->P;
+    cp.acc_re = ch->acc_re.p + ch->acc_cur * nk;
+    cp.acc_im = ch->acc_im.p + ch->acc_cur * nk;
+    cp.acc_re_out = ch->acc_re.p + (ch->acc_cur ^ 1u) * nk;
+    cp.acc_im_out = ch->acc_im.p + (ch->acc_cur ^ 1u) * nk;
     cp.sticky = ch->sticky.p;
     cp.satcnt = ch->satcnt.p;
     cp.count0 = ch->cov_count;
@@ -600,8 +625,12 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
     cp.stats = st;
     {
       KTimer t(ch, KT_COV);
-      launch_cov(cp, s);
+      if (ch->cov_tc_ok && cp.exact && !cp.exp_mode)
+        launch_cov_tc(cp, ch->cov_tc.plan, s);
+      else
+        launch_cov(cp, s);
     }
+    ch->acc_cur ^= 1u;
     ch->launches++;
     // window headers, known on the host (covar_model.hpp:229-235)
     uint32_t cnt = ch->cov_count;
@@ -875,7 +904,7 @@ rd_status rd_chain_flush_cov(rd_chain* ch, rd_output* out) {
   if (emit && out->cap_cov_windows < 1) return fail(RD_ETRUNC, "no room for the flushed window");
   CK(ch->cov_out.ensure(n * 2));
   k_cov_flush<<<(unsigned)((n + 255) / 256), 256, 0, ch->stream>>>(
-      ch->acc_re.p, ch->acc_im.p, ch->sticky.p, ch->satcnt.p, n, ch->cov_out.p, emit ? 1 : 0);
+      ch->acc_re.p + ch->acc_cur * (size_t)n, ch->acc_im.p + ch->acc_cur * (size_t)n, ch->sticky.p, ch->satcnt.p, n, ch->cov_out.p, emit ? 1 : 0);
   k_cov_flush_stats<<<1, 1, 0, ch->stream>>>(ch->stats.p);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ch->stream));

@@ -268,8 +268,8 @@ __global__ void __launch_bounds__(256) k_cov(CovParams p, unsigned BT, unsigned 
     __syncthreads();
   }
   if (live && carry_out) {
-    p.acc_re[k] = are;
-    p.acc_im[k] = aim;
+    p.acc_re_out[k] = are;
+    p.acc_im_out[k] = aim;
     if (MODE == 2) {
       p.sticky[k] = (st_re << 2) | st_im;
       const unsigned old_re = p.satcnt[2 * k], old_im = p.satcnt[2 * k + 1];

@@ -32,37 +32,13 @@
 
 #include "fxp.cuh"
 #include "rd_internal.h"
+#include "tc.cuh"
 
 namespace rd {
 
 constexpr unsigned kTcRows = 128u;  // rows per CTA: 8 warps x 16
 constexpr unsigned kTcBeams = 16u;  // beams per group: 4 tile triples
 constexpr unsigned kTcTiles = 12u;  // m16n8 tiles per group
-
-__device__ __forceinline__ uint32_t hsub2(uint32_t a, uint32_t b) {
-  uint32_t d;
-  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
-  return d;
-}
-
-// fp16x2 limb words of a packed sample v = {im, re}: hi = (re >> 8, im >> 8),
-// lo = (re & 255, im & 255). The fp16 number with bits 0x6400 | u is 1024 + u
-// for u < 1024, so placing a byte under that exponent and subtracting the
-// bias gives the byte's value exactly; the high byte is made unsigned by
-// flipping the sign bit first (bias 1024 + 128).
-__device__ __forceinline__ void limb_words(uint32_t v, uint32_t& hi, uint32_t& lo) {
-  hi = hsub2((((v ^ 0x80008000u) >> 8) & 0x00FF00FFu) | 0x64006400u, 0x64806480u);
-  lo = hsub2((v & 0x00FF00FFu) | 0x64006400u, 0x64006400u);
-}
-
-__device__ __forceinline__ void mma_f16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
-                                        uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 "
-      "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
 
 // ---- host: weight operand -----------------------------------------------------
 static int wlimb(const uint32_t* w, uint32_t C, uint32_t B, uint32_t b, uint32_t a, int part) {
@@ -234,12 +210,8 @@ __global__ void __launch_bounds__(256, 2) k_beam_tc(BeamParams p) {
         const float* c0 = d[3 * t3];
         const float* c1 = d[3 * t3 + 1];
         const float* c2 = d[3 * t3 + 2];
-        const long long re_v = (long long)__float2int_rn(c0[2 * h]) * 65536 +
-                               (long long)__float2int_rn(c0[2 * h + 1]) * 256 +
-                               (long long)__float2int_rn(c1[2 * h]);
-        const long long im_v = (long long)__float2int_rn(c1[2 * h + 1]) * 65536 +
-                               (long long)__float2int_rn(c2[2 * h]) * 256 +
-                               (long long)__float2int_rn(c2[2 * h + 1]);
+        const long long re_v = fold3(c0[2 * h], c0[2 * h + 1], c1[2 * h]);
+        const long long im_v = fold3(c1[2 * h + 1], c2[2 * h], c2[2 * h + 1]);
         const unsigned long long off = h ? off1 : off0;
         if (b < B && off != ~0ull) {
           unsigned fr = 0, fi = 0;

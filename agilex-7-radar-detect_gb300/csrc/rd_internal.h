@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "../../include/rd_chain.h"
 
 namespace rd {
@@ -102,8 +104,10 @@ struct CovParams {
   const uint32_t* px;
   const uint32_t* py;
   uint32_t P, F, N;
-  long long* acc_re;        // [N][P] integrator state
+  long long* acc_re;        // [N][P] integrator state carried in
   long long* acc_im;
+  long long* acc_re_out;    // [N][P] integrator state carried out (another copy)
+  long long* acc_im_out;
   unsigned* sticky;         // [N][P] (re << 2 | im)
   unsigned* satcnt;         // [N][P][2]
   uint32_t count0;          // samples already in the open window
@@ -115,6 +119,25 @@ struct CovParams {
   DevStats* stats;
 };
 void launch_cov(const CovParams& p, cudaStream_t s);
+
+// Tensor-core form of the exact block covariance (k_cov_tc.cu). The plan is
+// built once per pair table on the host: S <= 128 and no repeated pair.
+struct CovTcPlan {
+  uint32_t Sp, log2_sp;     // channels padded to a power of two >= 16
+  uint32_t NB;              // bins per CTA
+  uint32_t UPW, G;          // units per warp, CTA groups per bin block
+  const uint32_t* units;    // [G][8 warps][UPW]: bin << 16 | m-tile << 8 | triple, or ~0
+  const int32_t* pq;        // [S][S]: pair index of (x, y), or -1
+};
+struct CovTcHost {
+  CovTcPlan plan;
+  std::vector<uint32_t> units;
+  std::vector<int32_t> pq;
+};
+bool cov_tc_plan(uint32_t S, const uint32_t* px, const uint32_t* py, uint32_t P,
+                 CovTcHost* out);
+size_t cov_tc_smem(const CovTcPlan& t);
+void launch_cov_tc(const CovParams& p, const CovTcPlan& t, cudaStream_t s);
 
 struct CfarParams {
   const uint32_t* power_u32;  // [frames][n] (chain) ...

@@ -1,0 +1,49 @@
+// tc.cuh - exact integer arithmetic on the fp16 tensor cores: 8-bit limbs of
+// the packed Q1.15 samples as fp16 pairs, and the mma.sync m16n8k16
+// f16 x f16 -> f32 instruction. A limb (and its negation) is an integer of
+// magnitude <= 256, exact in fp16; a product of two limbs is below 2^16, exact
+// in fp32; and a kernel that keeps every accumulated sum below 2^24 in
+// magnitude gets exact integers out of the fp32 accumulators.
+#pragma once
+
+#include <stdint.h>
+
+namespace rd {
+
+__device__ __forceinline__ uint32_t hsub2(uint32_t a, uint32_t b) {
+  uint32_t d;
+  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+
+// fp16x2 limb words of a packed sample v = {im, re}: hi = (re >> 8, im >> 8),
+// lo = (re & 255, im & 255), the real part in the low half. The fp16 number
+// with bits 0x6400 | u is 1024 + u for u < 1024, so placing a byte under that
+// exponent and subtracting the bias gives the byte's value exactly; the high
+// byte is made unsigned by flipping the sign bit first (bias 1024 + 128).
+__device__ __forceinline__ void limb_words(uint32_t v, uint32_t& hi, uint32_t& lo) {
+  hi = hsub2((((v ^ 0x80008000u) >> 8) & 0x00FF00FFu) | 0x64006400u, 0x64806480u);
+  lo = hsub2((v & 0x00FF00FFu) | 0x64006400u, 0x64006400u);
+}
+
+// (-b, a) from the fp16 pair (a, b): the halves swapped, the new low half negated
+__device__ __forceinline__ uint32_t negswap(uint32_t w) {
+  return __byte_perm(w, 0u, 0x1032) ^ 0x00008000u;
+}
+
+__device__ __forceinline__ void mma_f16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
+                                        uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 "
+      "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// 2^16 c16 + 2^8 c8 + c0 from three fp32 accumulators holding exact integers
+__device__ __forceinline__ long long fold3(float c16, float c8, float c0) {
+  return (long long)__float2int_rn(c16) * 65536 + (long long)__float2int_rn(c8) * 256 +
+         (long long)__float2int_rn(c0);
+}
+
+}  // namespace rd

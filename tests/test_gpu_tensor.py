@@ -106,3 +106,55 @@ def test_chain_tensor_equals_cuda_core(gpulib, seed):
         outs.append((ch.process(x, taps=True), ch.stats()))
     assert diff(outs[0][0], outs[1][0], CHAIN_KEYS + TAP_KEYS) == []
     assert diff_stats(outs[0][1], outs[1][1]) == []
+
+
+def _cov_chain_pair(p, cfg_over, pairs, x, coeff=None, w=None):
+    coeff = sc.coefficients(p.n_fft, p.taps) if coeff is None else coeff
+    w = sc.steering_weights(p.n_chan, p.n_beams) if w is None else w
+    outs = []
+    for form in (abi.RD_FORM_CUDA_CORE, TC):
+        cfg = sc.make_config(p, max_frames=64, form=form)
+        for k, v in cfg_over.items():
+            setattr(cfg, k, v)
+        ch = gc.Chain(cfg, coeff, w, pairs)
+        r = ch.process(x, taps=True)
+        outs.append((r, ch.stats(), ch.flush_cov()))
+    return outs
+
+
+@pytest.mark.parametrize("window", [1, 7, 64, 200, 1000])
+def test_cov_tensor_windows_and_custom_pairs(gpulib, window):
+    # the covariance on the tensor cores against the CUDA-core form: windows
+    # shorter and longer than a launch, a pair table with lower-triangle,
+    # diagonal and repeated-channel pairs, both sources
+    rng = np.random.default_rng(window)
+    p = sc.preset("medium")
+    x = sc.adc(p, 300 * p.n_fft, start=window * p.n_fft)
+    S = p.n_chan
+    px = rng.integers(0, S, 40).astype(np.uint32)
+    py = rng.integers(0, S, 40).astype(np.uint32)
+    keep = np.unique(px * S + py, return_index=True)[1]
+    px, py = px[np.sort(keep)], py[np.sort(keep)]
+    for src in (abi.RD_COV_CHANNEL, abi.RD_COV_BEAM):
+        a, b = _cov_chain_pair(p, {"cov_window": window, "cov_source": src, "cov_acc_w": 64},
+                               (px, py), x)
+        assert diff(a[0], b[0], CHAIN_KEYS + TAP_KEYS) == [], src
+        assert diff_stats(a[1], b[1]) == [], src
+        assert diff(a[2], b[2], ("cov_windows", "cov_acc")) == [], src
+
+
+def test_cov_tensor_saturated_spectrum(gpulib):
+    # a full-scale square wave on every channel drives the FFT into
+    # saturation, so the covariance sees samples at -32768 and 32767: the
+    # largest limb products the 128-frame fp32 accumulation has to hold
+    p = sc.preset("full", cov_window=256)
+    n = 300 * p.n_fft
+    t = np.arange(n)
+    sq = np.where((t // 3) % 2 == 0, 32767, -32768)
+    x = np.tile(sc.pack(sq, -sq), (p.n_chan, 1))
+    px, py = sc.pair_table(p)
+    a, b = _cov_chain_pair(p, {"cov_acc_w": 64, "scale_sched": 0}, (px, py), x)
+    re, im = sc.unpack(a[0]["tap_spectrum"])
+    assert (re == -32768).any() and (im == 32767).any()
+    assert diff(a[0], b[0], CHAIN_KEYS + TAP_KEYS) == []
+    assert diff_stats(a[1], b[1]) == []
