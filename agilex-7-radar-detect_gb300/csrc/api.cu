@@ -167,6 +167,7 @@ struct Scratch {
 struct rd_chain {
   rd_config cfg;
   uint32_t R = 0;            // ring frames
+  uint32_t launch_frames = 0;  // frames per launch (<= max_frames)
   uint32_t S = 0, P = 0;     // covariance source length, pairs
   bool pairs_custom = false;
   cudaStream_t stream = nullptr;
@@ -380,6 +381,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
   const rd_config& c = ch->cfg;
   const uint32_t N = c.n_fft, C = c.n_chan, B = c.n_beams, T = c.taps, F = c.max_frames;
   ch->R = F + c.hist_frames;
+  ch->launch_frames = F;
   auto bad = [&](cudaError_t e) {
     if (e == cudaSuccess) return false;
     fail(e == cudaErrorMemoryAllocation ? RD_ENOMEM : RD_EDEVICE, "allocation failed: %s",
@@ -445,7 +447,10 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
   ch->hist.lanes = c.spc;
   ch->hist.frames_max = c.hist_frames;
   ch->hist.depth = c.hist_frames;
-  if (cudaDeviceSynchronize() != cudaSuccess) {
+  // the set-up copies ran on the legacy stream; wait for them without
+  // synchronising the device (other chains may be running)
+  if (cudaStreamSynchronize(cudaStreamLegacy) != cudaSuccess ||
+      cudaStreamSynchronize(ch->stream) != cudaSuccess) {
     rd_chain_destroy(ch);
     return fail(RD_EDEVICE, "device sync failed at create");
   }
@@ -719,8 +724,10 @@ static rd_status begin_call(rd_chain* ch, uint64_t frames, uint64_t cap_events) 
     const uint32_t wl = c.cov_window ? c.cov_window : 1u;
     const uint64_t n_win = (ch->cov_count + frames) / wl;
     const size_t per = (size_t)c.n_fft * ch->P * 2;
-    CK(ch->cov_out.ensure(std::max<uint64_t>(n_win, 1) * per));
-    CK(ch->win_flags.ensure(std::max<uint64_t>(n_win, 1)));
+    // one window of headroom: a call may close one more window than a
+    // same-sized call that started on an empty window
+    CK(ch->cov_out.ensure((n_win + 1) * per));
+    CK(ch->win_flags.ensure(n_win + 1));
     CK(cudaMemsetAsync(ch->win_flags.p, 0, std::max<uint64_t>(n_win, 1) * 4, ch->stream));
   }
   k_call_begin<<<1, 1, 0, ch->stream>>>(ch->stats.p);
@@ -735,7 +742,10 @@ static rd_status end_call(rd_chain* ch) {
   return RD_OK;
 }
 
+// Events of a call: every cell of every (frame, beam) in dense output,
+// else room for one detection in 16 cells plus the summaries.
 static uint64_t default_cap(const rd_config& c, uint64_t frames) {
+  if (c.cfar_out_mode == RD_CFAR_DENSE) return frames * c.n_beams * (c.n_fft + 1ull);
   return frames * c.n_beams * (2ull + c.n_fft / 16u);
 }
 
@@ -758,8 +768,8 @@ rd_status rd_chain_process_device(rd_chain* ch, const rd_cplx16* adc_dev, uint64
   const uint64_t frames = n / c.n_fft;
   rd_status st = begin_call(ch, frames, std::max<uint64_t>(ch->events.n, default_cap(c, frames)));
   if (st != RD_OK) return st;
-  for (uint64_t f = 0; f < frames; f += c.max_frames) {
-    const uint32_t F = (uint32_t)std::min<uint64_t>(c.max_frames, frames - f);
+  for (uint64_t f = 0; f < frames; f += ch->launch_frames) {
+    const uint32_t F = (uint32_t)std::min<uint64_t>(ch->launch_frames, frames - f);
     st = run_chunk(ch, adc_dev + f * c.n_fft, ld, F, nullptr);
     if (st != RD_OK) return st;
   }
@@ -839,8 +849,8 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
   rd_status st = begin_call(ch, frames, std::max<uint64_t>(cap, 1));
   if (st != RD_OK) return st;
   std::vector<uint32_t> hb;
-  for (uint64_t f = 0; f < frames; f += c.max_frames) {
-    const uint32_t F = (uint32_t)std::min<uint64_t>(c.max_frames, frames - f);
+  for (uint64_t f = 0; f < frames; f += ch->launch_frames) {
+    const uint32_t F = (uint32_t)std::min<uint64_t>(ch->launch_frames, frames - f);
     CK(cudaMemcpy2DAsync(ch->stage.p, sld * 4, adc + f * N, ld * 4, (size_t)F * N * 4, C,
                          cudaMemcpyHostToDevice, ch->stream));
     const uint64_t g0 = ch->frame;
@@ -958,6 +968,86 @@ rd_status rd_chain_kernel_times(rd_chain* ch, rd_kernel_time* out, uint32_t cap,
   }
   *n = k;
   return RD_OK;
+}
+
+rd_status rd_chain_set_launch_frames(rd_chain* ch, uint32_t frames) {
+  if (!ch) return fail(RD_EINVAL, "null argument");
+  if (frames == 0 || frames > ch->cfg.max_frames)
+    return fail(RD_EINVAL, "launch frames %u outside 1..%u", frames, ch->cfg.max_frames);
+  ch->launch_frames = frames;
+  return RD_OK;
+}
+
+rd_status rd_chain_reset(rd_chain* ch, void* stream) {
+  if (!ch) return fail(RD_EINVAL, "null argument");
+  const rd_config& c = ch->cfg;
+  cudaStream_t s = stream ? (cudaStream_t)stream : cudaStreamLegacy;
+  const uint32_t D = c.taps > 1 ? c.taps - 1 : 1;
+  const size_t tail = (size_t)c.n_chan * D * c.n_fft * 4;
+  // the chain's own stream may still be running the previous call (under
+  // stream capture the graph's own dependencies order the replays instead)
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(s, &cap));
+  if (cap == cudaStreamCaptureStatusNone) {
+    cudaEvent_t ev;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    CK(cudaEventRecord(ev, ch->stream));
+    CK(cudaStreamWaitEvent(s, ev, 0));
+    cudaEventDestroy(ev);
+  }
+  CK(cudaMemsetAsync(ch->tail[0].p, 0, tail, s));
+  CK(cudaMemsetAsync(ch->tail[1].p, 0, tail, s));
+  CK(cudaMemsetAsync(ch->stats.p, 0, sizeof(DevStats), s));
+  if (ch->P) {
+    const size_t k = (size_t)c.n_fft * ch->P;
+    CK(cudaMemsetAsync(ch->acc_re.p, 0, 2 * k * 8, s));
+    CK(cudaMemsetAsync(ch->acc_im.p, 0, 2 * k * 8, s));
+    CK(cudaMemsetAsync(ch->sticky.p, 0, k * 4, s));
+    CK(cudaMemsetAsync(ch->satcnt.p, 0, 2 * k * 4, s));
+  }
+  ch->tail_cur = 0;
+  ch->acc_cur = 0;
+  ch->frame = 0;
+  ch->cov_count = 0;
+  ch->cov_window_id = 0;
+  const HistMirror h0 = ch->hist;
+  ch->hist = HistMirror{};
+  ch->hist.n_ant = h0.n_ant;
+  ch->hist.n = h0.n;
+  ch->hist.lanes = h0.lanes;
+  ch->hist.frames_max = h0.frames_max;
+  ch->hist.depth = h0.depth;
+  ch->host_st = rd_stats{};
+  ch->align_seq = 0;
+  ch->call_frames = 0;
+  ch->call_windows.clear();
+  return RD_OK;
+}
+
+uint64_t rd_chain_footprint(const rd_config* cfg, uint64_t frames_per_call) {
+  if (!cfg || rd_config_validate(cfg) != RD_OK) return 0;
+  const rd_config& c = *cfg;
+  const uint64_t N = c.n_fft, C = c.n_chan, B = c.n_beams, T = c.taps, F = c.max_frames;
+  const uint64_t R = F + c.hist_frames, D = T > 1 ? T - 1 : 1;
+  uint64_t b = 0;
+  b += T * N * 4 + B * C * (4 + 16);                         // coefficients, weights
+  if (c.form == RD_FORM_TENSOR) b += (uint64_t)beam_tc_fragment_words(c.n_chan, c.n_beams) * 4;
+  b += 2 * C * D * N * 4 + R * N * C * 4;                    // delay lines, spectrum ring
+  b += F * B * N * 4 + F * B * (4 + 8 + 8) + F * B * ((N + 31) / 32) * 4;  // power, CFAR
+  b += sizeof(DevStats) + 5 * N * 4;
+  if (c.cov_source != RD_COV_OFF) {
+    const uint64_t S = c.cov_source == RD_COV_CHANNEL ? C : B;
+    const uint64_t P = rd_cov_pairs(cfg);
+    b += P * 8 + N * P * (2 * 2 * 8 + 4 + 8);                // pairs, state
+    if (c.form == RD_FORM_TENSOR) b += S * S * 4 + 4096;      // pair map, unit lists
+    if (c.cov_source == RD_COV_BEAM) b += F * N * B * 4;
+    const uint64_t wl = c.cov_window ? c.cov_window : 1;
+    b += (frames_per_call / wl + 1) * (N * P * 16 + 4);       // closed windows of a call
+  }
+  const uint64_t cap = frames_per_call * B * (2 + N / 16);    // default event capacity
+  b += cap * (sizeof(rd_event) + (uint64_t)rd_detection_flits(c.packet_w) *
+                                     rd_flit_words(c.packet_w) * 4);
+  return b;
 }
 
 rd_status rd_chain_stats(const rd_chain* ch, rd_stats* st) {

@@ -1,0 +1,283 @@
+// batch.cu - rd_batch_*: many independent scenarios of uneven geometry run
+// together. Each scenario is a chain (the same launch sequence a single
+// stream uses); a run resets every chain and processes one input per
+// scenario. The scenarios are spread largest-first over concurrent streams
+// so that small ones fill the SMs the large ones leave idle, and the whole
+// run - resets, launches, cross-stream ordering - is captured once into a
+// CUDA graph and replayed, so the host issues one launch per run. The
+// autotuner times the (streams, frames-per-launch) candidates with graph
+// replays and keeps the fastest.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "rd_internal.h"
+
+namespace {
+
+#define BK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return rd::set_error(RD_EDEVICE, "%s failed: %s", #call, cudaGetErrorString(e_));   \
+  } while (0)
+
+#define BS(call)                      \
+  do {                                \
+    rd_status s_ = (call);            \
+    if (s_ != RD_OK) return s_;       \
+  } while (0)
+
+}  // namespace
+
+struct rd_batch {
+  std::vector<rd_chain*> chains;
+  std::vector<rd_config> cfgs;
+  rd_batch_options opt{};
+  std::vector<cudaStream_t> streams;  // worker streams (32 at most)
+  cudaStream_t root = nullptr;        // capture origin
+  cudaEvent_t ev = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  // what the graph was captured with
+  std::vector<const rd_cplx16*> cap_adc;
+  std::vector<uint64_t> cap_n;
+  rd_batch_options cap_opt{};
+  bool warmed = false;
+  cudaStream_t last = nullptr;        // the stream of the last run
+};
+
+namespace {
+
+constexpr uint32_t kMaxStreams = 32;
+
+void drop_graph(rd_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+}
+
+// Enqueues one full run on `root`: fork to the worker streams, reset and
+// process every scenario on its stream, join back.
+rd_status enqueue(rd_batch* b, const rd_cplx16* const* adc, const uint64_t* n, cudaStream_t root,
+                  const rd_batch_options& o) {
+  const uint32_t ns = std::max(1u, std::min<uint32_t>(o.n_streams, (uint32_t)b->streams.size()));
+  for (size_t i = 0; i < b->chains.size(); ++i) {
+    const uint32_t lf = std::max(1u, std::min(o.launch_frames ? o.launch_frames : b->cfgs[i].max_frames,
+                                              b->cfgs[i].max_frames));
+    BS(rd_chain_set_launch_frames(b->chains[i], lf));
+  }
+  // largest first onto the least-loaded stream (cost ~ samples x channels x beams)
+  std::vector<uint32_t> order(b->chains.size());
+  std::iota(order.begin(), order.end(), 0u);
+  auto cost = [&](uint32_t i) {
+    const rd_config& c = b->cfgs[i];
+    return (double)n[i] * c.n_chan * (1.0 + c.n_beams / 16.0);
+  };
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t c) { return cost(a) > cost(c); });
+  std::vector<double> load(ns, 0.0);
+  std::vector<std::vector<uint32_t>> per(ns);
+  for (uint32_t i : order) {
+    const uint32_t k = (uint32_t)(std::min_element(load.begin(), load.end()) - load.begin());
+    load[k] += cost(i);
+    per[k].push_back(i);
+  }
+  BK(cudaEventRecord(b->ev, root));
+  for (uint32_t k = 0; k < ns; ++k) BK(cudaStreamWaitEvent(b->streams[k], b->ev, 0));
+  for (uint32_t k = 0; k < ns; ++k)
+    for (uint32_t i : per[k]) {
+      BS(rd_chain_reset(b->chains[i], b->streams[k]));
+      BS(rd_chain_process_device(b->chains[i], adc[i], n[i], n[i], b->streams[k]));
+    }
+  for (uint32_t k = 0; k < ns; ++k) {
+    BK(cudaEventRecord(b->ev, b->streams[k]));
+    BK(cudaStreamWaitEvent(root, b->ev, 0));
+  }
+  return RD_OK;
+}
+
+rd_status capture(rd_batch* b, const rd_cplx16* const* adc, const uint64_t* n,
+                  const rd_batch_options& o) {
+  drop_graph(b);
+  cudaGraph_t g = nullptr;
+  BK(cudaStreamBeginCapture(b->root, cudaStreamCaptureModeRelaxed));
+  rd_status st = enqueue(b, adc, n, b->root, o);
+  cudaError_t e = cudaStreamEndCapture(b->root, &g);
+  if (st != RD_OK) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  if (e != cudaSuccess)
+    return rd::set_error(RD_EDEVICE, "graph capture failed: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&b->exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    b->exec = nullptr;
+    return rd::set_error(RD_EDEVICE, "graph instantiation failed: %s", cudaGetErrorString(e));
+  }
+  b->cap_adc.assign(adc, adc + b->chains.size());
+  b->cap_n.assign(n, n + b->chains.size());
+  b->cap_opt = o;
+  return RD_OK;
+}
+
+bool same_inputs(const rd_batch* b, const rd_cplx16* const* adc, const uint64_t* n) {
+  for (size_t i = 0; i < b->chains.size(); ++i)
+    if (b->cap_adc[i] != adc[i] || b->cap_n[i] != n[i]) return false;
+  return true;
+}
+
+// One run with options o on stream s (graph or eager); the first run of a
+// batch is eager so that every chain sizes its buffers outside a capture.
+rd_status run_with(rd_batch* b, const rd_cplx16* const* adc, const uint64_t* n, cudaStream_t s,
+                   const rd_batch_options& o) {
+  BK(cudaEventRecord(b->ev, s));
+  BK(cudaStreamWaitEvent(b->root, b->ev, 0));
+  if (!o.use_graph || !b->warmed) {
+    BS(enqueue(b, adc, n, b->root, o));
+    b->warmed = true;
+    drop_graph(b);
+  } else {
+    const bool reuse = b->exec && same_inputs(b, adc, n) && b->cap_opt.n_streams == o.n_streams &&
+                       b->cap_opt.launch_frames == o.launch_frames;
+    if (!reuse) BS(capture(b, adc, n, o));
+    BK(cudaGraphLaunch(b->exec, b->root));
+  }
+  BK(cudaEventRecord(b->ev, b->root));
+  BK(cudaStreamWaitEvent(s, b->ev, 0));
+  b->last = s;
+  return RD_OK;
+}
+
+}  // namespace
+
+rd_status rd_batch_create(uint32_t n, const rd_config* cfgs, const rd_cplx16* const* coeff,
+                          const rd_cplx16* const* weights, const rd_batch_options* opt,
+                          rd_batch** out) {
+  if (!out || !cfgs || !coeff || !weights || n == 0)
+    return rd::set_error(RD_EINVAL, "rd_batch_create: bad argument");
+  *out = nullptr;
+  rd_batch* b = new rd_batch();
+  b->opt = opt ? *opt : rd_batch_options{0, 0, 1};
+  if (b->opt.n_streams == 0) b->opt.n_streams = 16;
+  b->cfgs.assign(cfgs, cfgs + n);
+  for (uint32_t i = 0; i < n; ++i) {
+    rd_chain* ch = nullptr;
+    rd_status st = rd_chain_create(&cfgs[i], &ch);
+    if (st == RD_OK) st = rd_chain_set_coeff(ch, coeff[i]);
+    if (st == RD_OK) st = rd_chain_set_weights(ch, weights[i]);
+    if (st != RD_OK) {
+      if (ch) rd_chain_destroy(ch);
+      rd_batch_destroy(b);
+      return st;
+    }
+    b->chains.push_back(ch);
+  }
+  b->streams.resize(kMaxStreams);
+  for (cudaStream_t& s : b->streams)
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+      s = nullptr;
+      rd_batch_destroy(b);
+      return rd::set_error(RD_EDEVICE, "rd_batch_create: stream creation failed");
+    }
+  if (cudaStreamCreateWithFlags(&b->root, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming) != cudaSuccess) {
+    rd_batch_destroy(b);
+    return rd::set_error(RD_EDEVICE, "rd_batch_create: stream creation failed");
+  }
+  *out = b;
+  return RD_OK;
+}
+
+void rd_batch_destroy(rd_batch* b) {
+  if (!b) return;
+  if (b->root) cudaStreamSynchronize(b->root);
+  drop_graph(b);
+  for (rd_chain* ch : b->chains) rd_chain_destroy(ch);
+  for (cudaStream_t s : b->streams)
+    if (s) cudaStreamDestroy(s);
+  if (b->root) cudaStreamDestroy(b->root);
+  if (b->ev) cudaEventDestroy(b->ev);
+  delete b;
+}
+
+rd_status rd_batch_run(rd_batch* b, const rd_cplx16* const* adc_dev, const uint64_t* n_samples,
+                       void* stream) {
+  if (!b || !adc_dev || !n_samples) return rd::set_error(RD_EINVAL, "rd_batch_run: bad argument");
+  cudaStream_t s = stream ? (cudaStream_t)stream : cudaStreamLegacy;
+  return run_with(b, adc_dev, n_samples, s, b->opt);
+}
+
+rd_status rd_batch_run_sequential(rd_batch* b, const rd_cplx16* const* adc_dev,
+                                  const uint64_t* n_samples, void* stream) {
+  if (!b || !adc_dev || !n_samples)
+    return rd::set_error(RD_EINVAL, "rd_batch_run_sequential: bad argument");
+  cudaStream_t s = stream ? (cudaStream_t)stream : cudaStreamLegacy;
+  for (size_t i = 0; i < b->chains.size(); ++i) {
+    BS(rd_chain_set_launch_frames(b->chains[i], b->cfgs[i].max_frames));
+    BS(rd_chain_reset(b->chains[i], s));
+    BS(rd_chain_process_device(b->chains[i], adc_dev[i], n_samples[i], n_samples[i], s));
+  }
+  b->last = s;
+  return RD_OK;
+}
+
+rd_status rd_batch_fetch(rd_batch* b, uint32_t i, rd_output* out) {
+  if (!b || i >= b->chains.size()) return rd::set_error(RD_EINVAL, "rd_batch_fetch: bad index");
+  if (b->last) BK(cudaStreamSynchronize(b->last));
+  return rd_chain_fetch(b->chains[i], out);
+}
+
+rd_status rd_batch_tune(rd_batch* b, const rd_cplx16* const* adc_dev, const uint64_t* n_samples,
+                        uint32_t reps, rd_batch_options* chosen, double* best_ms) {
+  if (!b || !adc_dev || !n_samples) return rd::set_error(RD_EINVAL, "rd_batch_tune: bad argument");
+  if (reps == 0) reps = 3;
+  uint32_t maxf = 0;
+  for (const rd_config& c : b->cfgs) maxf = std::max(maxf, c.max_frames);
+  const uint32_t n = (uint32_t)b->chains.size();
+  std::vector<uint32_t> stream_c, frame_c;
+  for (uint32_t s : {1u, 4u, 8u, 16u, 32u})
+    if (s <= std::max(1u, n)) stream_c.push_back(s);
+  for (uint32_t f : {128u, 256u, 512u, 1024u, 4096u})
+    if (f <= maxf) frame_c.push_back(f);
+  if (frame_c.empty()) frame_c.push_back(maxf);
+  cudaEvent_t t0, t1;
+  BK(cudaEventCreate(&t0));
+  BK(cudaEventCreate(&t1));
+  cudaStream_t s = b->root;
+  rd_batch_options best = b->opt;
+  double best_t = 1e30;
+  if (!b->warmed) {  // size every chain's buffers before the first capture
+    rd_batch_options o = b->opt;
+    o.use_graph = 0;
+    BS(run_with(b, adc_dev, n_samples, s, o));
+  }
+  for (uint32_t ns : stream_c)
+    for (uint32_t lf : frame_c) {
+      rd_batch_options o{ns, lf, 1};
+      BS(run_with(b, adc_dev, n_samples, s, o));  // capture + first replay
+      std::vector<float> ts;
+      for (uint32_t r = 0; r < reps; ++r) {
+        BK(cudaEventRecord(t0, s));
+        BS(run_with(b, adc_dev, n_samples, s, o));
+        BK(cudaEventRecord(t1, s));
+        BK(cudaEventSynchronize(t1));
+        float ms = 0;
+        BK(cudaEventElapsedTime(&ms, t0, t1));
+        ts.push_back(ms);
+      }
+      std::sort(ts.begin(), ts.end());
+      const double med = ts[ts.size() / 2];
+      if (med < best_t) {
+        best_t = med;
+        best = o;
+      }
+    }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  b->opt = best;
+  drop_graph(b);
+  if (chosen) *chosen = best;
+  if (best_ms) *best_ms = best_t;
+  return RD_OK;
+}

@@ -1,0 +1,441 @@
+// server.cu - rd_server_*: a request loop over many streams whose chain state
+// stays on the device between requests.
+//
+// Admission. The server reserves its request slots (one device input buffer
+// each) against the HBM budget at create; a stream is admitted at open when
+// its chain's footprint (rd_chain_footprint) fits what is left, else
+// RD_ENOMEM; close returns it.
+//
+// Scheduling. Submitted requests wait in one FIFO. A request starts when its
+// stream has no request on the device and a slot is free: its samples go
+// host -> slot over the stream's CUDA stream, the chain runs after the copy,
+// and an event marks the end. Requests of different streams therefore
+// overlap on the device and are admitted the moment a slot frees, without
+// waiting for a batch to drain (continuous batching); requests of one stream
+// run in order, because each one continues the stream's state. Polling
+// collects finished requests, reads their outputs and starts whatever can
+// start next.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstring>
+#include <deque>
+#include <unordered_map>
+#include <vector>
+
+#include "rd_internal.h"
+
+namespace {
+
+#define SK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return rd::set_error(RD_EDEVICE, "%s failed: %s", #call, cudaGetErrorString(e_));   \
+  } while (0)
+
+struct Request {
+  uint64_t id = 0;
+  uint32_t stream = 0;
+  uint64_t n = 0;
+  int host_buf = -1;
+  int slot = -1;
+  double t_submit = 0, t_start = 0, t_done = 0;
+  rd_status status = RD_OK;
+  bool done = false;
+  std::vector<rd_event> events;
+  std::vector<uint32_t> flits;
+  std::vector<rd_cov_window> windows;
+  std::vector<int64_t> cov;
+  uint64_t n_events = 0, n_flits = 0;
+  uint32_t n_windows = 0, flit_words = 0;
+};
+
+struct StreamState {
+  rd_chain* ch = nullptr;
+  rd_config cfg{};
+  cudaStream_t cs = nullptr;
+  uint64_t footprint = 0;
+  uint32_t n_pairs = 0;
+  bool open = false;
+  bool busy = false;
+  uint32_t outstanding = 0;
+};
+
+struct Slot {
+  rd_cplx16* dev = nullptr;
+  cudaEvent_t done = nullptr;
+  uint64_t req = 0;
+  bool used = false;
+};
+
+}  // namespace
+
+struct rd_server {
+  rd_server_config cfg{};
+  uint64_t used = 0;
+  size_t slot_words = 0;
+  std::vector<StreamState> streams;
+  std::vector<Slot> slots;
+  std::vector<rd_cplx16*> host;   // pinned staging, queue_cap buffers
+  std::vector<int> free_host;
+  std::unordered_map<uint64_t, Request> reqs;
+  std::deque<uint64_t> waiting;   // submitted, not started (submission order)
+  std::vector<rd_completion> finished;
+  uint64_t next_id = 1;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  double now() const {
+    return std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - t0).count();
+  }
+};
+
+namespace {
+
+rd_status start_ready(rd_server* s) {
+  for (auto it = s->waiting.begin(); it != s->waiting.end();) {
+    Request& r = s->reqs[*it];
+    StreamState& st = s->streams[r.stream];
+    if (st.busy) {
+      ++it;
+      continue;
+    }
+    int slot = -1;
+    for (size_t k = 0; k < s->slots.size(); ++k)
+      if (!s->slots[k].used) {
+        slot = (int)k;
+        break;
+      }
+    if (slot < 0) break;
+    Slot& sl = s->slots[slot];
+    const size_t words = (size_t)st.cfg.n_chan * r.n;
+    SK(cudaMemcpyAsync(sl.dev, s->host[r.host_buf], words * 4, cudaMemcpyHostToDevice, st.cs));
+    rd_status rs = rd_chain_process_device(st.ch, sl.dev, r.n, r.n, st.cs);
+    if (rs != RD_OK) return rs;
+    SK(cudaEventRecord(sl.done, st.cs));
+    sl.used = true;
+    sl.req = r.id;
+    r.slot = slot;
+    r.t_start = s->now();
+    st.busy = true;
+    it = s->waiting.erase(it);
+  }
+  return RD_OK;
+}
+
+// Outputs of a finished request, read from its chain: with the default
+// capacities first, then once more at the exact sizes if they did not fit.
+rd_status collect(rd_server* s, Request& r) {
+  StreamState& st = s->streams[r.stream];
+  const rd_config& c = st.cfg;
+  const uint64_t frames = r.n / c.n_fft;
+  const uint32_t nfl = rd_detection_flits(c.packet_w), words = rd_flit_words(c.packet_w);
+  uint64_t cap = std::max<uint64_t>(frames * c.n_beams * (2ull + c.n_fft / 16u), 16);
+  const uint32_t wl = c.cov_window ? c.cov_window : 1u;
+  uint32_t cap_w = (uint32_t)(frames / wl + 2);
+  const size_t per = (size_t)c.n_fft * std::max(st.n_pairs, 1u) * 2;
+  for (int attempt = 0;; ++attempt) {
+    r.events.resize(cap);
+    r.flits.resize(cap * nfl * words);
+    r.windows.resize(cap_w);
+    r.cov.resize((size_t)cap_w * per);
+    rd_output o{};
+    o.events = r.events.data();
+    o.cap_events = cap;
+    o.flits = r.flits.data();
+    o.cap_flits = cap * nfl;
+    o.cov_windows = r.windows.data();
+    o.cov_acc = r.cov.data();
+    o.cap_cov_windows = cap_w;
+    const rd_status rs = rd_chain_fetch(st.ch, &o);
+    const bool grow = rs == RD_ETRUNC && attempt == 0 &&
+                      (o.n_events > cap || o.n_cov_windows > cap_w);
+    if (rs != RD_OK && rs != RD_ETRUNC) return rs;
+    if (grow) {
+      cap = std::max<uint64_t>(cap, o.n_events);
+      cap_w = std::max<uint32_t>(cap_w, o.n_cov_windows);
+      continue;
+    }
+    const uint64_t ne = std::min<uint64_t>(o.n_events, cap);
+    const uint32_t nw = std::min<uint32_t>(o.n_cov_windows, cap_w);
+    r.n_events = o.n_events;
+    r.n_flits = ne * nfl;
+    r.n_windows = nw;
+    r.flit_words = o.flit_words;
+    r.events.resize(ne);
+    r.flits.resize(ne * nfl * words);
+    r.windows.resize(nw);
+    r.cov.resize((size_t)nw * per);
+    return rs;  // RD_ETRUNC here: the chain's own event buffer overflowed
+  }
+}
+
+}  // namespace
+
+rd_status rd_server_create(const rd_server_config* cfg, rd_server** out) {
+  if (!cfg || !out || cfg->max_inflight == 0 || cfg->queue_cap < cfg->max_inflight ||
+      cfg->max_chan == 0 || cfg->max_request_samples == 0)
+    return rd::set_error(RD_EINVAL, "rd_server_create: bad configuration");
+  *out = nullptr;
+  if (!rd_device_ok()) return rd::set_error(RD_EDEVICE, "rd_server_create: no usable CUDA device");
+  rd_server* s = new rd_server();
+  s->cfg = *cfg;
+  s->slot_words = (size_t)cfg->max_chan * cfg->max_request_samples;
+  const uint64_t slot_bytes = (uint64_t)s->slot_words * 4;
+  if ((uint64_t)cfg->max_inflight * slot_bytes > cfg->hbm_budget) {
+    delete s;
+    return rd::set_error(RD_ENOMEM, "rd_server_create: %u request slots of %llu bytes exceed the "
+                         "budget", cfg->max_inflight, (unsigned long long)slot_bytes);
+  }
+  s->slots.resize(cfg->max_inflight);
+  for (Slot& sl : s->slots) {
+    if (cudaMalloc(&sl.dev, slot_bytes) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess) {
+      rd_server_destroy(s);
+      return rd::set_error(RD_ENOMEM, "rd_server_create: slot allocation failed");
+    }
+  }
+  s->used = (uint64_t)cfg->max_inflight * slot_bytes;
+  s->host.resize(cfg->queue_cap, nullptr);
+  for (uint32_t k = 0; k < cfg->queue_cap; ++k) {
+    if (cudaMallocHost(&s->host[k], slot_bytes) != cudaSuccess) {
+      rd_server_destroy(s);
+      return rd::set_error(RD_ENOMEM, "rd_server_create: pinned staging allocation failed");
+    }
+    s->free_host.push_back((int)k);
+  }
+  *out = s;
+  return RD_OK;
+}
+
+void rd_server_destroy(rd_server* s) {
+  if (!s) return;
+  for (StreamState& st : s->streams)
+    if (st.open) {
+      cudaStreamSynchronize(st.cs);
+      rd_chain_destroy(st.ch);
+      cudaStreamDestroy(st.cs);
+    }
+  for (Slot& sl : s->slots) {
+    if (sl.dev) cudaFree(sl.dev);
+    if (sl.done) cudaEventDestroy(sl.done);
+  }
+  for (rd_cplx16* h : s->host)
+    if (h) cudaFreeHost(h);
+  delete s;
+}
+
+rd_status rd_stream_open(rd_server* s, const rd_config* cfg, const rd_cplx16* coeff,
+                         const rd_cplx16* weights, uint32_t* stream_id) {
+  if (!s || !cfg || !coeff || !weights || !stream_id)
+    return rd::set_error(RD_EINVAL, "rd_stream_open: null argument");
+  rd_status st = rd_config_validate(cfg);
+  if (st != RD_OK) return st;
+  if (cfg->n_chan > s->cfg.max_chan)
+    return rd::set_error(RD_EINVAL, "rd_stream_open: %u channels, the server's slots hold %u",
+                         cfg->n_chan, s->cfg.max_chan);
+  const uint64_t frames = s->cfg.max_request_samples / cfg->n_fft;
+  const uint64_t fp = rd_chain_footprint(cfg, frames);
+  if (s->used + fp > s->cfg.hbm_budget)
+    return rd::set_error(RD_ENOMEM, "rd_stream_open: admission refused, the stream needs %llu "
+                         "bytes and %llu of the %llu-byte budget are free",
+                         (unsigned long long)fp, (unsigned long long)(s->cfg.hbm_budget - s->used),
+                         (unsigned long long)s->cfg.hbm_budget);
+  StreamState ss;
+  ss.cfg = *cfg;
+  ss.footprint = fp;
+  ss.n_pairs = rd_cov_pairs(cfg);
+  st = rd_chain_create(cfg, &ss.ch);
+  if (st == RD_OK) st = rd_chain_set_coeff(ss.ch, coeff);
+  if (st == RD_OK) st = rd_chain_set_weights(ss.ch, weights);
+  if (st == RD_OK && cudaStreamCreateWithFlags(&ss.cs, cudaStreamNonBlocking) != cudaSuccess)
+    st = rd::set_error(RD_EDEVICE, "rd_stream_open: stream creation failed");
+  if (st == RD_OK && frames) {
+    // size the chain's per-call buffers with one request of the largest
+    // size, so that requests never allocate (cudaMalloc would stall the
+    // device), then return the chain to its initial state
+    const uint64_t n = frames * cfg->n_fft;
+    rd_cplx16* z = s->slots[0].used ? nullptr : s->slots[0].dev;
+    rd_cplx16* tmp = nullptr;
+    if (!z && cudaMalloc(&tmp, (size_t)cfg->n_chan * n * 4) == cudaSuccess) z = tmp;
+    if (z && cudaMemsetAsync(z, 0, (size_t)cfg->n_chan * n * 4, ss.cs) == cudaSuccess) {
+      st = rd_chain_process_device(ss.ch, z, n, n, ss.cs);
+      if (st == RD_OK) st = rd_chain_reset(ss.ch, ss.cs);
+      if (cudaStreamSynchronize(ss.cs) != cudaSuccess)
+        st = rd::set_error(RD_EDEVICE, "rd_stream_open: warm-up failed");
+    }
+    if (tmp) cudaFree(tmp);
+  }
+  if (st != RD_OK) {
+    if (ss.cs) cudaStreamDestroy(ss.cs);
+    if (ss.ch) rd_chain_destroy(ss.ch);
+    return st;
+  }
+  ss.open = true;
+  s->used += fp;
+  uint32_t id = 0;
+  while (id < s->streams.size() && s->streams[id].open) ++id;
+  if (id == s->streams.size()) s->streams.push_back(ss);
+  else s->streams[id] = ss;
+  *stream_id = id;
+  return RD_OK;
+}
+
+rd_status rd_stream_close(rd_server* s, uint32_t id) {
+  if (!s || id >= s->streams.size() || !s->streams[id].open)
+    return rd::set_error(RD_EINVAL, "rd_stream_close: no such stream");
+  StreamState& st = s->streams[id];
+  if (st.outstanding) return rd::set_error(RD_EAGAIN, "rd_stream_close: requests outstanding");
+  cudaStreamSynchronize(st.cs);
+  rd_chain_destroy(st.ch);
+  cudaStreamDestroy(st.cs);
+  s->used -= st.footprint;
+  st = StreamState{};
+  return RD_OK;
+}
+
+rd_status rd_server_submit(rd_server* s, uint32_t id, const rd_cplx16* adc, uint64_t n,
+                           uint64_t ld, uint64_t* req_id) {
+  if (!s || !adc || !req_id || id >= s->streams.size() || !s->streams[id].open)
+    return rd::set_error(RD_EINVAL, "rd_server_submit: bad argument");
+  StreamState& st = s->streams[id];
+  if (n == 0 || n % st.cfg.n_fft || n > s->cfg.max_request_samples || ld < n)
+    return rd::set_error(RD_EINVAL, "rd_server_submit: %llu samples per channel (a multiple of "
+                         "%u, at most %llu)", (unsigned long long)n, st.cfg.n_fft,
+                         (unsigned long long)s->cfg.max_request_samples);
+  if (s->free_host.empty()) return rd::set_error(RD_EAGAIN, "rd_server_submit: queue full");
+  Request r;
+  r.id = s->next_id++;
+  r.stream = id;
+  r.n = n;
+  r.host_buf = s->free_host.back();
+  s->free_host.pop_back();
+  rd_cplx16* h = s->host[r.host_buf];
+  for (uint32_t c = 0; c < st.cfg.n_chan; ++c) std::memcpy(h + (size_t)c * n, adc + (size_t)c * ld, n * 4);
+  r.t_submit = s->now();
+  *req_id = r.id;
+  st.outstanding++;
+  s->waiting.push_back(r.id);
+  s->reqs.emplace(r.id, std::move(r));
+  return start_ready(s);
+}
+
+rd_status rd_server_poll(rd_server* s, rd_completion* out, uint32_t cap, uint32_t* n_out) {
+  if (!s) return rd::set_error(RD_EINVAL, "rd_server_poll: null server");
+  for (Slot& sl : s->slots) {
+    if (!sl.used) continue;
+    const cudaError_t q = cudaEventQuery(sl.done);
+    if (q == cudaErrorNotReady) continue;
+    Request& r = s->reqs[sl.req];
+    StreamState& st = s->streams[r.stream];
+    r.status = q == cudaSuccess ? collect(s, r)
+                                : rd::set_error(RD_EDEVICE, "request failed: %s", cudaGetErrorString(q));
+    r.t_done = s->now();
+    r.done = true;
+    sl.used = false;
+    s->free_host.push_back(r.host_buf);
+    r.host_buf = -1;
+    st.busy = false;
+    st.outstanding--;
+    rd_completion c{};
+    c.req_id = r.id;
+    c.stream_id = r.stream;
+    c.status = r.status;
+    c.n_events = r.n_events;
+    c.n_cov_windows = r.n_windows;
+    c.t_submit_us = r.t_submit;
+    c.t_start_us = r.t_start;
+    c.t_done_us = r.t_done;
+    s->finished.push_back(c);
+  }
+  rd_status st = start_ready(s);
+  uint32_t k = 0;
+  if (out) {
+    k = (uint32_t)std::min<size_t>(cap, s->finished.size());
+    std::memcpy(out, s->finished.data(), k * sizeof(rd_completion));
+    s->finished.erase(s->finished.begin(), s->finished.begin() + k);
+  }
+  if (n_out) *n_out = k;
+  return st;
+}
+
+rd_status rd_server_take(rd_server* s, uint64_t req_id, rd_output* out) {
+  if (!s || !out) return rd::set_error(RD_EINVAL, "rd_server_take: null argument");
+  auto it = s->reqs.find(req_id);
+  if (it == s->reqs.end() || !it->second.done)
+    return rd::set_error(RD_EINVAL, "rd_server_take: request %llu is not complete",
+                         (unsigned long long)req_id);
+  Request& r = it->second;
+  bool trunc = false;
+  out->n_events = r.n_events;
+  out->n_flits = r.n_flits;
+  out->flit_words = r.flit_words;
+  out->n_cov_windows = r.n_windows;
+  out->n_frames = r.n / s->streams[r.stream].cfg.n_fft;
+  if (out->events) {
+    const uint64_t k = std::min<uint64_t>(r.events.size(), out->cap_events);
+    trunc |= k < r.events.size();
+    std::memcpy(out->events, r.events.data(), k * sizeof(rd_event));
+  }
+  if (out->flits && r.flit_words) {
+    const uint64_t k = std::min<uint64_t>(r.n_flits, out->cap_flits);
+    trunc |= k < r.n_flits;
+    std::memcpy(out->flits, r.flits.data(), k * r.flit_words * 4);
+  }
+  if (r.n_windows) {
+    const uint32_t k = std::min<uint32_t>(r.n_windows, out->cap_cov_windows);
+    trunc |= k < r.n_windows;
+    if (out->cov_windows) std::memcpy(out->cov_windows, r.windows.data(), k * sizeof(rd_cov_window));
+    const size_t per = r.n_windows ? r.cov.size() / r.n_windows : 0;
+    if (out->cov_acc) std::memcpy(out->cov_acc, r.cov.data(), k * per * 8);
+  }
+  const rd_status st = r.status;
+  s->reqs.erase(it);
+  if (st != RD_OK) return st;
+  return trunc ? rd::set_error(RD_ETRUNC, "rd_server_take: output capacity exceeded") : RD_OK;
+}
+
+rd_status rd_server_info_get(rd_server* s, rd_server_info* info) {
+  if (!s || !info) return rd::set_error(RD_EINVAL, "rd_server_info_get: null argument");
+  info->hbm_budget = s->cfg.hbm_budget;
+  info->hbm_used = s->used;
+  info->streams = 0;
+  for (const StreamState& st : s->streams) info->streams += st.open ? 1u : 0u;
+  info->inflight = 0;
+  for (const Slot& sl : s->slots) info->inflight += sl.used ? 1u : 0u;
+  info->queued = (uint32_t)s->waiting.size();
+  return RD_OK;
+}
+
+rd_status rd_server_run_trace(rd_server* s, uint64_t n_req, const uint32_t* stream_ids,
+                              const double* arrival_us, const rd_cplx16* const* adc,
+                              const uint64_t* n, double* latency_us, double* makespan_us) {
+  if (!s || !stream_ids || !arrival_us || !adc || !n || !latency_us)
+    return rd::set_error(RD_EINVAL, "rd_server_run_trace: null argument");
+  std::unordered_map<uint64_t, uint64_t> idx;  // request id -> trace index
+  std::vector<rd_completion> comp(64);
+  const double t0 = s->now();
+  uint64_t next = 0, done = 0;
+  rd_status first_err = RD_OK;
+  while (done < n_req) {
+    const double t = s->now() - t0;
+    while (next < n_req && arrival_us[next] <= t) {
+      uint64_t id = 0;
+      const rd_status st = rd_server_submit(s, stream_ids[next], adc[next], n[next], n[next], &id);
+      if (st == RD_EAGAIN) break;  // queue full: the request waits on the host
+      if (st != RD_OK) return st;
+      idx[id] = next++;
+    }
+    uint32_t k = 0;
+    const rd_status ps = rd_server_poll(s, comp.data(), (uint32_t)comp.size(), &k);
+    if (ps != RD_OK) return ps;
+    for (uint32_t i = 0; i < k; ++i) {
+      const uint64_t j = idx[comp[i].req_id];
+      latency_us[j] = (comp[i].t_done_us - t0) - arrival_us[j];
+      if (comp[i].status != RD_OK && first_err == RD_OK) first_err = (rd_status)comp[i].status;
+      s->reqs.erase(comp[i].req_id);  // the outputs are not kept
+      ++done;
+    }
+  }
+  if (makespan_us) *makespan_us = s->now() - t0;
+  return first_err;
+}

@@ -120,6 +120,28 @@ def ptr(a) -> C.c_void_p | None:
 
 
 # C prototypes shared by the product library and the oracles' per-block calls.
+class RdBatchOptions(C.Structure):
+    _fields_ = [("n_streams", C.c_uint32), ("launch_frames", C.c_uint32), ("use_graph", C.c_int)]
+
+
+class RdServerConfig(C.Structure):
+    _fields_ = [("hbm_budget", C.c_uint64), ("max_inflight", C.c_uint32),
+                ("queue_cap", C.c_uint32), ("max_chan", C.c_uint32),
+                ("max_request_samples", C.c_uint64)]
+
+
+class RdCompletion(C.Structure):
+    _fields_ = [("req_id", C.c_uint64), ("stream_id", C.c_uint32), ("status", C.c_int32),
+                ("n_events", C.c_uint64), ("n_cov_windows", C.c_uint32),
+                ("t_submit_us", C.c_double), ("t_start_us", C.c_double),
+                ("t_done_us", C.c_double)]
+
+
+class RdServerInfo(C.Structure):
+    _fields_ = [("hbm_budget", C.c_uint64), ("hbm_used", C.c_uint64), ("streams", C.c_uint32),
+                ("inflight", C.c_uint32), ("queued", C.c_uint32)]
+
+
 def _proto(lib, name, res, args):
     f = getattr(lib, name)
     f.restype = res
@@ -152,6 +174,24 @@ def declare_rd(lib) -> None:
     _proto(lib, "rd_chain_kernel_times", I32, [VP, P(RdKernelTime), U32, P(U32)])
     _proto(lib, "rd_chain_stats", I32, [VP, P(RdStats)])
     _proto(lib, "rd_chain_read_history", I32, [VP, U32, U32, VP, P(U32), P(U32)])
+    _proto(lib, "rd_chain_reset", I32, [VP, VP])
+    _proto(lib, "rd_chain_set_launch_frames", I32, [VP, U32])
+    _proto(lib, "rd_chain_footprint", U64, [P(RdConfig), U64])
+    _proto(lib, "rd_batch_create", I32, [U32, P(RdConfig), VP, VP, P(RdBatchOptions), P(VP)])
+    _proto(lib, "rd_batch_destroy", None, [VP])
+    _proto(lib, "rd_batch_run", I32, [VP, VP, VP, VP])
+    _proto(lib, "rd_batch_run_sequential", I32, [VP, VP, VP, VP])
+    _proto(lib, "rd_batch_fetch", I32, [VP, U32, P(RdOutput)])
+    _proto(lib, "rd_batch_tune", I32, [VP, VP, VP, U32, P(RdBatchOptions), P(C.c_double)])
+    _proto(lib, "rd_server_create", I32, [P(RdServerConfig), P(VP)])
+    _proto(lib, "rd_server_destroy", None, [VP])
+    _proto(lib, "rd_stream_open", I32, [VP, P(RdConfig), VP, VP, P(U32)])
+    _proto(lib, "rd_stream_close", I32, [VP, U32])
+    _proto(lib, "rd_server_submit", I32, [VP, U32, VP, U64, U64, P(U64)])
+    _proto(lib, "rd_server_poll", I32, [VP, P(RdCompletion), U32, P(U32)])
+    _proto(lib, "rd_server_take", I32, [VP, U64, P(RdOutput)])
+    _proto(lib, "rd_server_info_get", I32, [VP, P(RdServerInfo)])
+    _proto(lib, "rd_server_run_trace", I32, [VP, U64, VP, VP, VP, VP, VP, P(C.c_double)])
     _proto(lib, "rd_pfb_run", I32, [U32, U32, VP, VP, VP, U32, VP, VP])
     _proto(lib, "rd_fft_run", I32, [U32, U32, U32, I32, VP, U32, VP, VP, VP])
     _proto(lib, "rd_bf_run", I32, [U32, U32, VP, VP, U64, VP, VP, VP, U32])
@@ -172,7 +212,12 @@ EXPORTED = [
     "rd_cov_pairs", "rd_chain_create", "rd_chain_destroy", "rd_chain_set_coeff",
     "rd_chain_set_weights", "rd_chain_set_pairs", "rd_chain_process",
     "rd_chain_process_device", "rd_chain_fetch", "rd_chain_last_launches",
-    "rd_chain_flush_cov", "rd_chain_set_profiling", "rd_chain_kernel_times", "rd_chain_stats", "rd_chain_read_history", "rd_pfb_run",
+    "rd_chain_flush_cov", "rd_chain_set_profiling", "rd_chain_kernel_times", "rd_chain_stats",
+    "rd_chain_reset", "rd_chain_set_launch_frames", "rd_chain_footprint",
+    "rd_batch_create", "rd_batch_destroy", "rd_batch_run", "rd_batch_run_sequential",
+    "rd_batch_fetch", "rd_batch_tune", "rd_server_create", "rd_server_destroy", "rd_stream_open",
+    "rd_stream_close", "rd_server_submit", "rd_server_poll", "rd_server_take",
+    "rd_server_info_get", "rd_server_run_trace", "rd_chain_read_history", "rd_pfb_run",
     "rd_fft_run", "rd_bf_run", "rd_power_run", "rd_cross_power_run", "rd_cfar_run", "rd_cfar_run_static",
     "rd_packetize", "rd_fxp_apply", "rd_last_error", "rd_device_ok", "rd_version",
 ]

@@ -1,0 +1,60 @@
+"""Many independent scenarios of uneven geometry in one CUDA graph: the
+ctypes wrapper of rd_batch_* (include/rd_chain.h)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .chain import Outputs
+
+
+class Batch:
+    def __init__(self, cfgs: list, coeffs: list, weights: list, n_streams: int = 16,
+                 launch_frames: int = 0, use_graph: bool = True):
+        self.L = abi.load()
+        n = len(cfgs)
+        self.cfgs = cfgs
+        arr = (abi.RdConfig * n)(*cfgs)
+        self._coeff = [np.ascontiguousarray(c, np.uint32) for c in coeffs]
+        self._w = [np.ascontiguousarray(w, np.uint32) for w in weights]
+        cp = (C.c_void_p * n)(*[c.ctypes.data for c in self._coeff])
+        wp = (C.c_void_p * n)(*[w.ctypes.data for w in self._w])
+        self.opt = abi.RdBatchOptions(n_streams, launch_frames, 1 if use_graph else 0)
+        self.h = C.c_void_p()
+        abi.check(self.L, self.L.rd_batch_create(n, arr, cp, wp, C.byref(self.opt),
+                                                 C.byref(self.h)), "rd_batch_create")
+
+    def _args(self, ptrs, ns):
+        n = len(self.cfgs)
+        return (C.c_void_p * n)(*ptrs), (C.c_uint64 * n)(*ns)
+
+    def run(self, ptrs, ns, stream: int = 0, sequential: bool = False) -> None:
+        p, q = self._args(ptrs, ns)
+        fn = self.L.rd_batch_run_sequential if sequential else self.L.rd_batch_run
+        abi.check(self.L, fn(self.h, p, q, C.c_void_p(stream)), "rd_batch_run")
+
+    def tune(self, ptrs, ns, reps: int = 3) -> tuple[dict, float]:
+        p, q = self._args(ptrs, ns)
+        o = abi.RdBatchOptions()
+        ms = C.c_double()
+        abi.check(self.L, self.L.rd_batch_tune(self.h, p, q, reps, C.byref(o), C.byref(ms)),
+                  "rd_batch_tune")
+        return {"n_streams": o.n_streams, "launch_frames": o.launch_frames}, ms.value
+
+    def fetch(self, i: int, frames: int, n_pairs: int) -> dict:
+        out = Outputs(self.cfgs[i], frames, n_pairs, False, None)
+        abi.check(self.L, self.L.rd_batch_fetch(self.h, i, C.byref(out.c)), "rd_batch_fetch")
+        return out.result()
+
+    def close(self) -> None:
+        if self.h:
+            self.L.rd_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -283,3 +283,31 @@ def adc(p: Preset, n: int, start: int = 0, seed: int | None = None,
         np.clip(im, -2047, 2047, out=im)
         out[row] = pack(re, im)
     return out
+
+
+# ---------------------------------------------------------------------------
+# The batching workload: independent scenarios of uneven geometry
+# ---------------------------------------------------------------------------
+
+def batch_scenarios(n: int, seed_index: int = 3, log2_min: int = 12,
+                    log2_max: int = 18) -> list[Preset]:
+    """`n` scenarios drawn from a seed: channels in {4, 16, 32, 64}, PFB/FFT
+    size in {16, 64, 256, 1024}, taps in {4, 8, 16}, CPI length log-uniform
+    in 2^log2_min .. 2^log2_max samples per channel (rounded to a multiple of
+    the FFT size), beams = channels, channel covariance over 256-frame
+    windows, CA-CFAR with reference/guard cells scaled to the frame, tones
+    plus noise."""
+    rng = np.random.default_rng(BASE_SEED + seed_index)
+    out = []
+    for i in range(n):
+        C = int(rng.choice([4, 16, 32, 64]))
+        N = int(rng.choice([16, 64, 256, 1024]))
+        T = int(rng.choice([4, 8, 16]))
+        cpi = int(round(2.0 ** rng.uniform(log2_min, log2_max)))
+        cpi = max(N, (cpi // N) * N)
+        ref = max(2, min(16, N // 8))
+        guard = max(1, min(4, N // 64))
+        out.append(Preset(f"batch{i}", C, N, T, 2, 8, C, (guard, guard), (ref, ref), guard, ref,
+                          0x0800, abi.RD_COV_CHANNEL, 256, 64, 128, cpi, 1, 3, False,
+                          1000 + i))
+    return out

@@ -226,11 +226,109 @@ rd_status rd_chain_flush_cov(rd_chain* ch, rd_output* out);
 
 rd_status rd_chain_stats(const rd_chain* ch, rd_stats* st);
 
+/* Returns the chain to its just-created state - delay lines, history,
+ * covariance windows, counters and packet sequence - keeping the
+ * coefficients, weights and pair table (no reference counterpart: the
+ * models are reset by constructing new ones). The device part is enqueued
+ * on `stream` (NULL: the legacy stream), so it can be captured in a graph. */
+rd_status rd_chain_reset(rd_chain* ch, void* stream);
+
+/* Frames per kernel launch, 1..max_frames (default max_frames). Results do
+ * not depend on it; the batch autotuner varies it. */
+rd_status rd_chain_set_launch_frames(rd_chain* ch, uint32_t frames);
+
+/* Device bytes a chain of this configuration holds, with the output
+ * buffers of calls of `frames_per_call` frames (admission by HBM budget). */
+uint64_t rd_chain_footprint(const rd_config* cfg, uint64_t frames_per_call);
+
 /* hist::Model::read (history_model.hpp:283-337): the antenna vector of
  * natural bin `bin`, `frame_off` frames back from the newest complete one. */
 rd_status rd_chain_read_history(rd_chain* ch, uint32_t bin, uint32_t frame_off,
                                 rd_cplx16* vec, uint32_t* frame_id,
                                 uint32_t* flags);
+
+/* ---- batching: many independent scenarios in one CUDA graph ------------
+ * No counterpart in the reference (its chain is one RTL instance). Each
+ * scenario is a chain; a run resets every chain and processes one input per
+ * scenario, the scenarios spread largest-first over `n_streams` concurrent
+ * streams, all of it captured once into a CUDA graph and replayed. */
+typedef struct rd_batch rd_batch;
+typedef struct {
+  uint32_t n_streams;          /* concurrent streams (0: autotune) */
+  uint32_t launch_frames;      /* frames per launch, capped per chain (0: autotune) */
+  int use_graph;               /* 1: capture once, replay; 0: launch eagerly */
+} rd_batch_options;
+rd_status rd_batch_create(uint32_t n, const rd_config* cfgs, const rd_cplx16* const* coeff,
+                          const rd_cplx16* const* weights, const rd_batch_options* opt,
+                          rd_batch** out);
+void rd_batch_destroy(rd_batch* b);
+/* adc_dev[i]: device samples of scenario i, [C][n_samples[i]]. Ordered after
+ * the work already on `stream` and before the work enqueued on it later. */
+rd_status rd_batch_run(rd_batch* b, const rd_cplx16* const* adc_dev, const uint64_t* n_samples,
+                       void* stream);
+/* The scenarios one after another on one stream, eagerly: the baseline the
+ * batched run is compared with. */
+rd_status rd_batch_run_sequential(rd_batch* b, const rd_cplx16* const* adc_dev,
+                                  const uint64_t* n_samples, void* stream);
+rd_status rd_batch_fetch(rd_batch* b, uint32_t i, rd_output* out);
+/* Autotuner: times every (n_streams, launch_frames) candidate on these
+ * inputs (graph replays, median of `reps`), keeps the fastest and reports
+ * it. */
+rd_status rd_batch_tune(rd_batch* b, const rd_cplx16* const* adc_dev, const uint64_t* n_samples,
+                        uint32_t reps, rd_batch_options* chosen, double* best_ms);
+
+/* ---- serving: a request loop over many resident streams -----------------
+ * (the submit / poll / stream_open shape of a streaming front end; no
+ * counterpart in the reference model). Each stream keeps its chain state -
+ * PFB delay lines, history, covariance windows, CFAR/packet counters - on
+ * the device between requests. A request is one block of samples of one
+ * stream; requests of a stream run in submission order, requests of
+ * different streams overlap on the device as request slots free up
+ * (continuous batching). Streams are admitted against a device-memory
+ * budget (RD_ENOMEM when a stream does not fit). */
+typedef struct rd_server rd_server;
+typedef struct {
+  uint64_t hbm_budget;          /* device bytes for streams + request slots */
+  uint32_t max_inflight;        /* requests on the device at once */
+  uint32_t queue_cap;           /* requests submitted but not finished */
+  uint32_t max_chan;            /* the largest n_chan a stream may have */
+  uint64_t max_request_samples; /* per channel */
+} rd_server_config;
+typedef struct {
+  uint64_t req_id;
+  uint32_t stream_id;
+  int32_t status;               /* rd_status of the request */
+  uint64_t n_events;
+  uint32_t n_cov_windows;
+  double t_submit_us, t_start_us, t_done_us;  /* server clock */
+} rd_completion;
+typedef struct {
+  uint64_t hbm_budget, hbm_used;
+  uint32_t streams, inflight, queued;
+} rd_server_info;
+rd_status rd_server_create(const rd_server_config* cfg, rd_server** out);
+void rd_server_destroy(rd_server* s);
+rd_status rd_stream_open(rd_server* s, const rd_config* cfg, const rd_cplx16* coeff,
+                         const rd_cplx16* weights, uint32_t* stream_id);
+rd_status rd_stream_close(rd_server* s, uint32_t stream_id);
+/* Copies the request's samples ([C][n], row stride ld) and queues it;
+ * RD_EAGAIN when queue_cap requests are outstanding. */
+rd_status rd_server_submit(rd_server* s, uint32_t stream_id, const rd_cplx16* adc, uint64_t n,
+                           uint64_t ld, uint64_t* req_id);
+/* Starts queued requests on free slots and collects finished ones (up to
+ * cap completions). */
+rd_status rd_server_poll(rd_server* s, rd_completion* out, uint32_t cap, uint32_t* n_out);
+/* The outputs of a completed request (events, flits, covariance windows),
+ * handed over once. */
+rd_status rd_server_take(rd_server* s, uint64_t req_id, rd_output* out);
+rd_status rd_server_info_get(rd_server* s, rd_server_info* info);
+/* A native request loop for measurement: request k (stream stream_ids[k],
+ * samples adc[k], n[k] per channel) arrives at arrival_us[k] after the
+ * start; each is submitted when it arrives (or as soon as the queue has
+ * room) and polled to completion. latency_us[k] = completion - arrival. */
+rd_status rd_server_run_trace(rd_server* s, uint64_t n_req, const uint32_t* stream_ids,
+                              const double* arrival_us, const rd_cplx16* const* adc,
+                              const uint64_t* n, double* latency_us, double* makespan_us);
 
 /* ---- per-block entry points (the model/cpp call surface, on the GPU) ---- */
 
