@@ -172,6 +172,7 @@ struct rd_chain {
   bool pairs_custom = false;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;  // ordering with the caller's stream
 
   DevBuf<uint32_t> coeff_t, weights, tail[2], ring, power, beams_bn, stage, tw_pos;
   DevBuf<int4> w_limbs;
@@ -390,6 +391,8 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
   };
   const uint32_t D = T > 1 ? T - 1 : 1;
   if (bad(cudaStreamCreateWithFlags(&ch->stream, cudaStreamNonBlocking)) ||
+      bad(cudaEventCreateWithFlags(&ch->ev_in, cudaEventDisableTiming)) ||
+      bad(cudaEventCreateWithFlags(&ch->ev_out, cudaEventDisableTiming)) ||
       bad(ch->coeff_t.ensure((size_t)T * N)) || bad(ch->weights.ensure((size_t)B * C)) ||
       bad(ch->w_limbs.ensure((size_t)B * C)) ||
       (c.form == RD_FORM_TENSOR && bad(ch->w_frag.ensure(beam_tc_fragment_words(C, B)))) ||
@@ -473,6 +476,8 @@ void rd_chain_destroy(rd_chain* ch) {
     cudaEventDestroy(p.b);
   }
   for (cudaEvent_t e : ch->pool) cudaEventDestroy(e);
+  if (ch->ev_in) cudaEventDestroy(ch->ev_in);
+  if (ch->ev_out) cudaEventDestroy(ch->ev_out);
   if (ch->own_stream && ch->stream) cudaStreamDestroy(ch->stream);
   delete ch;
 }
@@ -758,13 +763,10 @@ rd_status rd_chain_process_device(rd_chain* ch, const rd_cplx16* adc_dev, uint64
   // NULL means the legacy default stream; the chain's own stream does not
   // synchronise with it implicitly, so the order is made explicit both ways.
   cudaStream_t user = stream ? (cudaStream_t)stream : cudaStreamLegacy;
-  {  // order the chain after the caller's stream
-    cudaEvent_t ev_in;
-    CK(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
-    CK(cudaEventRecord(ev_in, user));
-    CK(cudaStreamWaitEvent(ch->stream, ev_in, 0));
-    cudaEventDestroy(ev_in);
-  }
+  // order the chain after the caller's stream (a wait uses the event's state
+  // at the call, so one event per direction serves every call)
+  CK(cudaEventRecord(ch->ev_in, user));
+  CK(cudaStreamWaitEvent(ch->stream, ch->ev_in, 0));
   const uint64_t frames = n / c.n_fft;
   rd_status st = begin_call(ch, frames, std::max<uint64_t>(ch->events.n, default_cap(c, frames)));
   if (st != RD_OK) return st;
@@ -775,13 +777,9 @@ rd_status rd_chain_process_device(rd_chain* ch, const rd_cplx16* adc_dev, uint64
   }
   st = end_call(ch);
   if (st != RD_OK) return st;
-  {  // and the caller's stream after the chain
-    cudaEvent_t ev_out;
-    CK(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming));
-    CK(cudaEventRecord(ev_out, ch->stream));
-    CK(cudaStreamWaitEvent(user, ev_out, 0));
-    cudaEventDestroy(ev_out);
-  }
+  // and the caller's stream after the chain
+  CK(cudaEventRecord(ch->ev_out, ch->stream));
+  CK(cudaStreamWaitEvent(user, ch->ev_out, 0));
   return RD_OK;
 }
 

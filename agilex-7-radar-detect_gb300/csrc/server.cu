@@ -20,6 +20,7 @@
 #include <chrono>
 #include <cstring>
 #include <deque>
+#include <utility>
 #include <unordered_map>
 #include <vector>
 
@@ -34,6 +35,28 @@ namespace {
       return rd::set_error(RD_EDEVICE, "%s failed: %s", #call, cudaGetErrorString(e_));   \
   } while (0)
 
+// A vector whose resize leaves new elements uninitialised (the outputs are
+// written by the device copy right after).
+template <typename T>
+struct NoInit {
+  using value_type = T;
+  NoInit() = default;
+  template <typename U>
+  NoInit(const NoInit<U>&) {}
+  T* allocate(size_t n) { return static_cast<T*>(::operator new(n * sizeof(T))); }
+  void deallocate(T* p, size_t) { ::operator delete(p); }
+  template <typename U, typename... A>
+  void construct(U* p, A&&... a) {
+    if constexpr (sizeof...(A) > 0) ::new ((void*)p) U(std::forward<A>(a)...);
+  }
+  template <typename U>
+  bool operator==(const NoInit<U>&) const { return true; }
+  template <typename U>
+  bool operator!=(const NoInit<U>&) const { return false; }
+};
+template <typename T>
+using RawVec = std::vector<T, NoInit<T>>;
+
 struct Request {
   uint64_t id = 0;
   uint32_t stream = 0;
@@ -43,10 +66,10 @@ struct Request {
   double t_submit = 0, t_start = 0, t_done = 0;
   rd_status status = RD_OK;
   bool done = false;
-  std::vector<rd_event> events;
-  std::vector<uint32_t> flits;
-  std::vector<rd_cov_window> windows;
-  std::vector<int64_t> cov;
+  RawVec<rd_event> events;
+  RawVec<uint32_t> flits;
+  RawVec<rd_cov_window> windows;
+  RawVec<int64_t> cov;
   uint64_t n_events = 0, n_flits = 0;
   uint32_t n_windows = 0, flit_words = 0;
 };
@@ -122,51 +145,34 @@ rd_status start_ready(rd_server* s) {
   return RD_OK;
 }
 
-// Outputs of a finished request, read from its chain: with the default
-// capacities first, then once more at the exact sizes if they did not fit.
+// Outputs of a finished request, read from its chain: the counts first
+// (no buffers), then the outputs into buffers of exactly that size.
 rd_status collect(rd_server* s, Request& r) {
   StreamState& st = s->streams[r.stream];
   const rd_config& c = st.cfg;
-  const uint64_t frames = r.n / c.n_fft;
   const uint32_t nfl = rd_detection_flits(c.packet_w), words = rd_flit_words(c.packet_w);
-  uint64_t cap = std::max<uint64_t>(frames * c.n_beams * (2ull + c.n_fft / 16u), 16);
-  const uint32_t wl = c.cov_window ? c.cov_window : 1u;
-  uint32_t cap_w = (uint32_t)(frames / wl + 2);
+  rd_output q{};
+  rd_status rs = rd_chain_fetch(st.ch, &q);
+  if (rs != RD_OK && rs != RD_ETRUNC) return rs;
   const size_t per = (size_t)c.n_fft * std::max(st.n_pairs, 1u) * 2;
-  for (int attempt = 0;; ++attempt) {
-    r.events.resize(cap);
-    r.flits.resize(cap * nfl * words);
-    r.windows.resize(cap_w);
-    r.cov.resize((size_t)cap_w * per);
-    rd_output o{};
-    o.events = r.events.data();
-    o.cap_events = cap;
-    o.flits = r.flits.data();
-    o.cap_flits = cap * nfl;
-    o.cov_windows = r.windows.data();
-    o.cov_acc = r.cov.data();
-    o.cap_cov_windows = cap_w;
-    const rd_status rs = rd_chain_fetch(st.ch, &o);
-    const bool grow = rs == RD_ETRUNC && attempt == 0 &&
-                      (o.n_events > cap || o.n_cov_windows > cap_w);
-    if (rs != RD_OK && rs != RD_ETRUNC) return rs;
-    if (grow) {
-      cap = std::max<uint64_t>(cap, o.n_events);
-      cap_w = std::max<uint32_t>(cap_w, o.n_cov_windows);
-      continue;
-    }
-    const uint64_t ne = std::min<uint64_t>(o.n_events, cap);
-    const uint32_t nw = std::min<uint32_t>(o.n_cov_windows, cap_w);
-    r.n_events = o.n_events;
-    r.n_flits = ne * nfl;
-    r.n_windows = nw;
-    r.flit_words = o.flit_words;
-    r.events.resize(ne);
-    r.flits.resize(ne * nfl * words);
-    r.windows.resize(nw);
-    r.cov.resize((size_t)nw * per);
-    return rs;  // RD_ETRUNC here: the chain's own event buffer overflowed
-  }
+  r.events.resize(q.n_events);
+  r.flits.resize(q.n_events * nfl * words);
+  r.windows.resize(q.n_cov_windows);
+  r.cov.resize((size_t)q.n_cov_windows * per);
+  rd_output o{};
+  o.events = r.events.data();
+  o.cap_events = q.n_events;
+  o.flits = r.flits.data();
+  o.cap_flits = q.n_events * nfl;
+  o.cov_windows = r.windows.data();
+  o.cov_acc = r.cov.data();
+  o.cap_cov_windows = q.n_cov_windows;
+  rs = rd_chain_fetch(st.ch, &o);
+  r.n_events = o.n_events;
+  r.n_flits = o.n_flits;
+  r.n_windows = o.n_cov_windows;
+  r.flit_words = o.flit_words;
+  return rs;  // RD_ETRUNC: the chain's own event buffer overflowed
 }
 
 }  // namespace

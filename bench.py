@@ -47,6 +47,8 @@ def args_():
     ap.add_argument("--form", choices=["cuda_core", "tensor"], default="cuda_core")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-patterns", action="store_true",
+                    help="skip the form comparison, batching and serving measurements")
     return ap.parse_args()
 
 
@@ -159,6 +161,199 @@ def cpu_baseline(p, cfg, coeff, w, pairs, x, cpis: int) -> dict:
             "sample": f"{cpis} CPIs x {p.n_chan} ch x {p.cpi_samples} samples of the same "
                       f"workload through oracle/orc_port.c with {threads} threads",
             "single_thread_value": round(p.n_chan * n1 / dt1 / 1e6, 3)}
+
+
+
+def tiled_adc(p, n: int, block: int = 65536):
+    """Seeded tones + noise for `n` samples per channel: one generated block
+    of `block` samples repeated (the generator is integer numpy and slow at
+    hundreds of millions of samples; the statistics are the same)."""
+    from rdgb import scenario as sc
+
+    b = sc.adc(p, min(n, block))
+    reps = -(-n // b.shape[1])
+    return np.ascontiguousarray(np.tile(b, (1, reps))[:, :n])
+
+
+def time_chain(torch, chain, dev, n: int, stream, steps: int, warmup: int):
+    """(ms per step, {kernel: avg us}) of process_device over `n` samples/ch."""
+    from rdgb import abi
+
+    sh = stream.cuda_stream
+    for _ in range(warmup):
+        chain.process_device(dev.data_ptr(), n, n, sh)
+    torch.cuda.synchronize()
+    chain.L.rd_chain_set_profiling(chain.h, 1)
+    kt = (abi.RdKernelTime * 16)()
+    nk = abi.C.c_uint32(0)
+    chain.L.rd_chain_kernel_times(chain.h, kt, 16, abi.C.byref(nk))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        chain.process_device(dev.data_ptr(), n, n, sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    chain.L.rd_chain_kernel_times(chain.h, kt, 16, abi.C.byref(nk))
+    chain.L.rd_chain_set_profiling(chain.h, 0)
+    ks = {kt[i].name.decode(): round(1e3 * kt[i].total_ms / max(kt[i].launches, 1), 2)
+          for i in range(nk.value)}
+    return e0.elapsed_time(e1) / steps, ks
+
+
+def run_forms(torch, a, stream) -> dict:
+    """The chain in the CUDA-core integer form and in the limb-split
+    tensor-core form, on the medium workload and on the full-scale one."""
+    from rdgb import abi, chain as gc, scenario as sc
+
+    out = {}
+    for wl, cpis in (("medium", 64), ("full", 2)):
+        p = sc.preset(wl)
+        n = cpis * p.cpi_samples
+        x = tiled_adc(p, n)
+        dev = torch.from_numpy(x.view(np.int32)).cuda()
+        coeff = sc.coefficients(p.n_fft, p.taps)
+        w = sc.steering_weights(p.n_chan, p.n_beams)
+        r = {"samples_per_step": p.n_chan * n}
+        for name, form in (("cuda_core", abi.RD_FORM_CUDA_CORE), ("tensor", abi.RD_FORM_TENSOR)):
+            ch = gc.Chain(sc.make_config(p, max_frames=1024, form=form), coeff, w,
+                          sc.pair_table(p))
+            ms, ks = time_chain(torch, ch, dev, n, stream, steps=3, warmup=3)
+            r[name] = {"value": round(p.n_chan * n / (ms / 1e3) / 1e6, 3), "unit": UNIT,
+                       "ms_per_step": round(ms, 3), "k_beam_us": ks.get("k_beam"),
+                       "k_cov_us": ks.get("k_cov")}
+            ch.close()
+        cc, tc = r["cuda_core"], r["tensor"]
+        r["chain_speedup"] = round(tc["value"] / cc["value"], 3)
+        r["beam_cov_speedup"] = round((cc["k_beam_us"] + cc["k_cov_us"]) /
+                                      (tc["k_beam_us"] + tc["k_cov_us"]), 3)
+        out[wl] = r
+        del dev
+    out["note"] = ("tensor form: int16 samples and weights split into 8-bit limbs held exactly "
+                   "in fp16, mma.sync with fp32 accumulation below 2^24, int64 recombine; "
+                   "per-launch stage times from CUDA events; inputs: one 65536-sample seeded "
+                   "block per channel repeated")
+    return out
+
+
+def run_batching(torch, n_scen: int = 256, runs: int = 5) -> dict:
+    """256 independent scenarios of seeded uneven geometry: one autotuned
+    graph replay against the scenarios one after another on one stream."""
+    from rdgb import abi, chain as gc, scenario as sc
+    from rdgb.batch import Batch
+
+    ps = sc.batch_scenarios(n_scen)
+    # the tensor form for every scenario (bit-identical to the CUDA-core one)
+    cfgs = [sc.make_config(p, max_frames=min(p.frames_per_cpi, 1024), form=abi.RD_FORM_TENSOR)
+            for p in ps]
+    coeffs = [sc.coefficients(p.n_fft, p.taps) for p in ps]
+    ws = [sc.steering_weights(p.n_chan, p.n_beams) for p in ps]
+    devs = [torch.from_numpy(tiled_adc(p, p.cpi_samples, 8192).view(np.int32)).cuda()
+            for p in ps]
+    ptrs = [d.data_ptr() for d in devs]
+    ns = [p.cpi_samples for p in ps]
+    samples = sum(p.n_chan * p.cpi_samples for p in ps)
+    b = Batch(cfgs, coeffs, ws, n_streams=16, use_graph=True)
+    st = torch.cuda.Stream()
+    b.run(ptrs, ns, st.cuda_stream)  # sizes every chain's buffers
+    t = time.perf_counter()
+    opt, tuned_ms = b.tune(ptrs, ns, reps=3)
+    tune_s = time.perf_counter() - t
+
+    def timed(sequential: bool) -> float:
+        for _ in range(2):
+            b.run(ptrs, ns, st.cuda_stream, sequential=sequential)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(runs):
+            b.run(ptrs, ns, st.cuda_stream, sequential=sequential)
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / runs
+
+    batched = timed(False)
+    seq = timed(True)
+    # the per-scenario API as a caller uses it: process, then read the results
+    chains = [gc.Chain(c, co, w) for c, co, w in zip(cfgs, coeffs, ws)]
+    for ch, d, n in zip(chains, devs, ns):  # warm
+        ch.process_device(d.data_ptr(), n, n, st.cuda_stream)
+        ch.fetch(n // ch.cfg.n_fft)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for ch, d, n in zip(chains, devs, ns):
+        ch.L.rd_chain_reset(ch.h, abi_ptr(st.cuda_stream))
+        ch.process_device(d.data_ptr(), n, n, st.cuda_stream)
+        ch.fetch(n // ch.cfg.n_fft)
+    seq_fetch = 1e3 * (time.perf_counter() - t)
+    for ch in chains:
+        ch.close()
+    b.close()
+    return {"scenarios": n_scen, "samples_per_run": samples,
+            "geometry": "channels {4,16,32,64}, PFB/FFT {16,64,256,1024}, taps {4,8,16}, "
+                        "CPI log-uniform 2^12..2^18 samples/ch, beams = channels",
+            "batched_ms": round(batched, 3), "sequential_ms": round(seq, 3),
+            "sequential_with_fetch_ms": round(seq_fetch, 3),
+            "speedup_vs_sequential": round(seq / batched, 3),
+            "speedup_vs_sequential_with_fetch": round(seq_fetch / batched, 3),
+            "batched_msamples_s": round(samples / (batched / 1e3) / 1e6, 1),
+            "autotuned": opt, "tune_s": round(tune_s, 2),
+            "note": "batched: one CUDA graph replay of every scenario's launches spread "
+                    "largest-first over the tuned number of streams; sequential: the same "
+                    "launches stream-ordered on one stream, no host waits; with_fetch: "
+                    "each scenario processed and its results read before the next"}
+
+
+def abi_ptr(v: int):
+    from rdgb import abi
+
+    return abi.C.c_void_p(v)
+
+
+def run_serving(torch, n_streams: int = 32, n_req: int = 400) -> dict:
+    """32 resident streams of mixed tiny / medium / full geometry; a request
+    is 4096 samples per channel; Poisson arrivals at 25/50/80/100 % of the
+    measured saturation rate; latency = completion - arrival."""
+    from rdgb import abi, scenario as sc
+    from rdgb.serve import Server
+
+    names = ["tiny", "medium", "full"]
+    srv = Server(hbm_budget=64 << 30, max_inflight=16, queue_cap=512, max_chan=64,
+                 max_request_samples=4096)
+    streams = []
+    for i in range(n_streams):
+        p = sc.preset(names[i % 3])
+        cfg = sc.make_config(p, max_frames=4096 // p.n_fft, form=abi.RD_FORM_TENSOR)
+        st, sid = srv.open(cfg, sc.coefficients(p.n_fft, p.taps),
+                           sc.steering_weights(p.n_chan, p.n_beams))
+        if st != 0:
+            raise RuntimeError(f"stream {i} not admitted: {st}")
+        blocks = [sc.adc(p, 4096, start=k * 4096, seed=p.seed + i) for k in range(4)]
+        streams.append((sid, p, blocks))
+    rng = np.random.default_rng(5)
+
+    def trace(n, rate_per_us):
+        idx = rng.integers(0, n_streams, n)
+        arrival = np.zeros(n) if rate_per_us is None else np.cumsum(rng.exponential(1.0 / rate_per_us, n))
+        adcs = [streams[s][2][k % 4] for k, s in enumerate(idx)]
+        lat, mk = srv.run_trace([streams[s][0] for s in idx], arrival, adcs)
+        samples = sum(streams[s][1].n_chan * 4096 for s in idx)
+        return lat, mk, samples
+
+    trace(64, None)  # warm
+    lat, mk, samples = trace(n_req, None)
+    sat = n_req / mk  # requests per microsecond
+    loads = []
+    for load in (0.25, 0.5, 0.8, 1.0):
+        lat, mk, samples = trace(n_req, sat * load)
+        loads.append({"load": load, "offered_req_per_s": round(sat * load * 1e6, 1),
+                      "p50_us": round(float(np.percentile(lat, 50)), 1),
+                      "p99_us": round(float(np.percentile(lat, 99)), 1),
+                      "throughput_msamples_s": round(samples / mk, 1)})
+    srv.close()
+    return {"streams": n_streams, "mix": "tiny / medium / full in turn, tensor form",
+            "request": "4096 samples per channel", "max_inflight": 16,
+            "saturation_req_per_s": round(sat * 1e6, 1), "loads": loads,
+            "p99_us_at_80pct": next(x["p99_us"] for x in loads if x["load"] == 0.8)}
 
 
 def run_reference(a, rank: int, world: int) -> None:
@@ -323,6 +518,13 @@ def run_gpu(a, rank: int, world: int, local: int) -> None:
     cpu = None
     if not a.no_cpu_baseline:
         cpu = cpu_baseline(p, cfg, coeff, w, pairs, x, cpis=min(16, cpis))
+    forms = batching = serving = None
+    if not a.no_patterns and world == 1:
+        del dev
+        chain.close()
+        forms = run_forms(torch, a, stream)
+        batching = run_batching(torch)
+        serving = run_serving(torch)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(t_max / a.steps, 4),
@@ -345,6 +547,9 @@ def run_gpu(a, rank: int, world: int, local: int) -> None:
                     for k, v in kernels.items()},
         "step_ms": [round(s, 4) for s in step_ms],
         "events_per_step": n_events,
+        "forms": forms,
+        "batching": batching,
+        "serving": serving,
     }
     print(json.dumps(line), flush=True)
     if dist:
