@@ -2,6 +2,8 @@
 // event packing and packet flits.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "fxp.cuh"
 #include "rd_internal.h"
 
@@ -327,19 +329,31 @@ __device__ __forceinline__ uint64_t cell_at(const CfarParams& p, uint64_t u, uns
 }
 
 // Inclusive prefix sums pre[1..n] of frame u (pre[0] = 0), warp-cooperative.
+// W >= ceil(n / 32) bounds the rows at compile time, so every row's cells are
+// loaded before the first scan step (the loads overlap instead of each row
+// waiting for its own).
+template <int W>
 __device__ __forceinline__ void warp_prefix(const CfarParams& p, uint64_t u, uint64_t* pre) {
   const unsigned lane = threadIdx.x & 31u;
-  uint64_t carry = 0;
+  uint64_t v[W];
+#pragma unroll
+  for (int r = 0; r < W; ++r) {
+    const unsigned i = (unsigned)r * 32u + lane;
+    v[r] = i < p.n ? cell_at(p, u, i) : 0ull;
+  }
   if (lane == 0) pre[0] = 0;
-  for (unsigned r = 0; r * 32u < p.n; ++r) {
-    const unsigned i = r * 32u + lane;
-    uint64_t v = i < p.n ? cell_at(p, u, i) : 0ull;
+  uint64_t carry = 0;
+#pragma unroll
+  for (int r = 0; r < W; ++r) {
+    uint64_t x = v[r];
+#pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const uint64_t t = __shfl_up_sync(0xffffffffu, v, o);
-      if ((int)lane >= o) v += t;
+      const uint64_t t = __shfl_up_sync(0xffffffffu, x, o);
+      if ((int)lane >= o) x += t;
     }
-    if (i < p.n) pre[i + 1] = carry + v;
-    carry += __shfl_sync(0xffffffffu, v, 31);
+    const unsigned i = (unsigned)r * 32u + lane;
+    if (i < p.n) pre[i + 1] = carry + x;
+    carry += __shfl_sync(0xffffffffu, x, 31);
   }
   __syncwarp();
 }
@@ -376,47 +390,60 @@ __device__ __forceinline__ CellDecision decide_cell(const CfarParams& p, const u
   return d;
 }
 
+// Pass 1. One warp per CFAR frame, 4 frames per CTA; the CTA's event total
+// goes to offsets[blockIdx.x] for the scan.
+template <int W>
 __global__ void __launch_bounds__(128) k_cfar_decide(CfarParams p) {
   extern __shared__ uint64_t s_pre[];
+  __shared__ unsigned s_cnt[4];
   const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   const uint64_t u = (uint64_t)blockIdx.x * 4u + warp;
   uint64_t* pre = s_pre + (size_t)warp * (p.n + 1u);
-  if (u >= p.frames) return;
-  warp_prefix(p, u, pre);
-  const unsigned words = (p.n + 31u) / 32u;
-  unsigned emitted = 0, det = 0, sup = 0;
-  for (unsigned r = 0; r < words; ++r) {
-    const unsigned i = r * 32u + lane;
-    bool em = false;
-    if (i < p.n) {
-      const CellDecision d = decide_cell(p, pre, i, pre[i + 1] - pre[i]);
-      em = d.emit;
-      det += d.detected;
-      sup += !d.evaluable;
+  unsigned count = 0;
+  if (u < p.frames) {
+    warp_prefix<W>(p, u, pre);
+    const unsigned words = (p.n + 31u) / 32u;
+    unsigned emitted = 0, det = 0, sup = 0;
+#pragma unroll
+    for (int r = 0; r < W; ++r) {
+      const unsigned i = (unsigned)r * 32u + lane;
+      bool em = false;
+      if (i < p.n) {
+        const CellDecision d = decide_cell(p, pre, i, pre[i + 1] - pre[i]);
+        em = d.emit;
+        det += d.detected;
+        sup += !d.evaluable;
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, em);
+      if (lane == 0 && (unsigned)r < words) p.mask[u * words + r] = m;
+      emitted += __popc(m);
     }
-    const unsigned m = __ballot_sync(0xffffffffu, em);
-    if (lane == 0) p.mask[u * words + r] = m;
-    emitted += __popc(m);
+    det = __reduce_add_sync(0xffffffffu, det);
+    sup = __reduce_add_sync(0xffffffffu, sup);
+    count = emitted + 1u;  // + SUMMARY
+    if (lane == 0) {
+      p.counts[u] = count;
+      p.detsup[2 * u] = det;
+      p.detsup[2 * u + 1] = sup;
+      if (det) atomicAdd(&p.stats->cfar_det, (unsigned long long)det);
+      if (sup) atomicAdd(&p.stats->cfar_sup, (unsigned long long)sup);
+    }
   }
-  det = __reduce_add_sync(0xffffffffu, det);
-  sup = __reduce_add_sync(0xffffffffu, sup);
-  if (lane == 0) {
-    p.counts[u] = emitted + 1u;  // + SUMMARY
-    p.detsup[2 * u] = det;
-    p.detsup[2 * u + 1] = sup;
-    atomicAdd(&p.stats->cfar_det, (unsigned long long)det);
-    atomicAdd(&p.stats->cfar_sup, (unsigned long long)sup);
-  }
+  if (lane == 0) s_cnt[warp] = count;
+  __syncthreads();
+  if (threadIdx.x == 0) p.offsets[blockIdx.x] = s_cnt[0] + s_cnt[1] + s_cnt[2] + s_cnt[3];
 }
 
-// Exclusive scan of counts -> offsets (+ the call's running event count).
+// Pass 2. Exclusive scan of the CTA totals (in place in offsets), plus the
+// call's running event count; one CTA, a few totals per thread.
 __global__ void __launch_bounds__(1024) k_cfar_scan(CfarParams p) {
   __shared__ unsigned long long s_part[1024];
   const unsigned tid = threadIdx.x;
-  const uint64_t per = (p.frames + 1023u) / 1024u;
-  const uint64_t lo = tid * per, hi = (lo + per) < p.frames ? (lo + per) : p.frames;
+  const uint64_t nb = ((uint64_t)p.frames + 3u) / 4u;
+  const uint64_t per = (nb + 1023u) / 1024u;
+  const uint64_t lo = tid * per, hi = (lo + per) < nb ? (lo + per) : nb;
   unsigned long long sum = 0;
-  for (uint64_t i = lo; i < hi; ++i) sum += p.counts[i];
+  for (uint64_t i = lo; i < hi; ++i) sum += p.offsets[i];
   s_part[tid] = sum;
   __syncthreads();
   for (unsigned o = 1; o < 1024u; o <<= 1) {
@@ -428,8 +455,9 @@ __global__ void __launch_bounds__(1024) k_cfar_scan(CfarParams p) {
   const unsigned long long base = p.stats->events_call;
   unsigned long long run = base + s_part[tid] - sum;
   for (uint64_t i = lo; i < hi; ++i) {
+    const unsigned long long c = p.offsets[i];
     p.offsets[i] = run;
-    run += p.counts[i];
+    run += c;
   }
   __syncthreads();
   if (tid == 1023u) p.stats->events_call = base + s_part[1023];
@@ -511,6 +539,64 @@ __device__ void write_packet(const rd_event* e, uint32_t* out, unsigned pw, unsi
   }
 }
 
+// The same packet as write_packet, built by the whole warp: item k of the
+// packet (flit k / words, word k % words) is lane k % 32's, in at most two
+// rounds (1 + ceil(176 / W) flits of ceil((W + 5) / 32) words is at most 34
+// items); each flit's odd-parity bit comes from an XOR reduction of its
+// words' popcounts. `w` is the event (the same on every lane).
+__device__ void warp_write_packet(const uint64_t* w, uint32_t* out, unsigned pw, unsigned words,
+                                  unsigned nfl, unsigned src, unsigned dest, unsigned vc,
+                                  unsigned seq) {
+  const unsigned lane = threadIdx.x & 31u;
+  const uint64_t hdr[3] = {(uint64_t)(dest & 0xFu) | ((uint64_t)(src & 0x1Fu) << 4) |
+                               ((uint64_t)(vc & 3u) << 9) | ((uint64_t)(nfl & 0x3Fu) << 14) |
+                               ((uint64_t)(seq & 0xFFFFu) << 20),
+                           0ull, 0ull};
+  const int top = 5 + (int)pw;
+  const unsigned items = nfl * words;
+  uint32_t val[2] = {0u, 0u};
+  unsigned fl[2] = {0u, 0u};
+  unsigned par = 0;  // bit f: parity of flit f so far
+#pragma unroll
+  for (int rnd = 0; rnd < 2; ++rnd) {
+    const unsigned k = (unsigned)rnd * 32u + lane;
+    uint32_t v = 0;
+    unsigned f = 0;
+    if (k < items) {
+      f = k / words;
+      const unsigned kk = k - f * words;
+      const uint64_t* data = f == 0 ? hdr : w;
+      const int off = f == 0 ? 0 : (int)((f - 1) * pw);
+      const int last = f == 0 ? 36 : (off + (int)pw < 176 ? off + (int)pw : 176);
+      const int lo = 32 * (int)kk;
+      v = ext32(data, off + lo - 5);
+      if (lo < 5) v &= ~0x1Fu;
+      const int lim = 5 + (last - off) < top ? 5 + (last - off) : top;
+      if (lo + 32 > lim) v &= (lim <= lo) ? 0u : ((1u << (lim - lo)) - 1u);
+      if (kk == 0)
+        v |= ((vc & 3u) << 1) | ((f == 0 ? 1u : 0u) << 3) | ((f + 1 == nfl ? 1u : 0u) << 4);
+    }
+    val[rnd] = v;
+    fl[rnd] = f;
+    const unsigned bit = k < items ? ((__popc(v) & 1u) << f) : 0u;
+    par ^= __reduce_xor_sync(0xffffffffu, bit);
+  }
+#pragma unroll
+  for (int rnd = 0; rnd < 2; ++rnd) {
+    const unsigned k = (unsigned)rnd * 32u + lane;
+    if (k < items) {
+      uint32_t v = val[rnd];
+      if (k % words == 0u && ((par >> fl[rnd]) & 1u) == 0u) v |= 1u;
+      out[k] = v;
+    }
+  }
+}
+
+// Pass 3. Each warp rebuilds its frame's sums only when the frame has
+// detections, and writes its events and packets at the frame's offset: words
+// with few events event by event with the whole warp packing each packet,
+// words with many events one event per lane; the SUMMARY last.
+template <int W>
 __global__ void __launch_bounds__(128) k_cfar_emit(CfarParams p) {
   extern __shared__ uint64_t s_pre[];
   const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
@@ -519,62 +605,93 @@ __global__ void __launch_bounds__(128) k_cfar_emit(CfarParams p) {
   if (u >= p.frames) return;
   const unsigned words = (p.n + 31u) / 32u;
   const uint32_t cnt = p.counts[u];
-  const uint64_t base = p.offsets[u];
+  uint64_t base = p.offsets[blockIdx.x];  // + the events of the CTA's earlier frames
+  for (unsigned k = 0; k < warp; ++k) base += p.counts[(uint64_t)blockIdx.x * 4u + k];
   const uint64_t frame = p.frame_ids ? p.frame_ids[u] : (p.g0 + u / p.beams);
   const unsigned fid = p.frame_ids ? p.frame_ids[u] : (unsigned)(frame & 0xFFFFu);
   const uint16_t beam = (uint16_t)(p.frame_ids ? u : (u % p.beams));
   const unsigned long long seq0 = p.stats->events_total;
+  const size_t pk = (size_t)p.nfl * p.flit_words;  // words per packet
   if (cnt > 1u) {
-    warp_prefix(p, u, pre);
+    warp_prefix<W>(p, u, pre);
     unsigned before = 0;
     for (unsigned r = 0; r < words; ++r) {
       const uint32_t m = p.mask[u * words + r];
-      const unsigned i = r * 32u + lane;
-      if ((m >> lane) & 1u) {
-        const uint64_t cut = pre[i + 1] - pre[i];
-        const CellDecision d = decide_cell(p, pre, i, cut);
-        const uint64_t idx = base + before + __popc(m & ((1u << lane) - 1u));
-        const unsigned kind = d.detected ? 0u : (!d.evaluable ? 2u : 1u);
-        if (idx < p.cap) {
-          rd_event ev;
-          make_event(&ev, kind, i, fid, d.evaluable ? d.n : 0u, p.alpha, 0, 0, cut,
-                     d.evaluable ? d.sum : 0ull, idx == base, false, (uint32_t)frame, beam);
-          p.events[idx] = ev;
-          if (p.flits)
-            write_packet(&ev, p.flits + idx * p.nfl * p.flit_words, p.packet_w, p.flit_words,
-                         p.nfl, p.src_id, p.dest, p.vc, (unsigned)((seq0 + idx) & 0xFFFFu));
+      if (__popc(m) > 4) {  // many events in this word: one per lane
+        const unsigned i = r * 32u + lane;
+        if ((m >> lane) & 1u) {
+          const uint64_t cut = pre[i + 1] - pre[i];
+          const CellDecision d = decide_cell(p, pre, i, cut);
+          const uint64_t idx = base + before + __popc(m & ((1u << lane) - 1u));
+          const unsigned kind = d.detected ? 0u : (!d.evaluable ? 2u : 1u);
+          if (idx < p.cap) {
+            rd_event ev;
+            make_event(&ev, kind, i, fid, d.evaluable ? d.n : 0u, p.alpha, 0, 0, cut,
+                       d.evaluable ? d.sum : 0ull, idx == base, false, (uint32_t)frame, beam);
+            p.events[idx] = ev;
+            if (p.flits)
+              write_packet(&ev, p.flits + idx * pk, p.packet_w, p.flit_words, p.nfl, p.src_id,
+                           p.dest, p.vc, (unsigned)((seq0 + idx) & 0xFFFFu));
+          }
+        }
+        __syncwarp();
+      } else {  // few events: the warp packs each packet together
+        uint32_t mm = m;
+        unsigned j = 0;
+        while (mm) {
+          const unsigned b = (unsigned)__ffs(mm) - 1u;
+          mm &= mm - 1u;
+          const unsigned i = r * 32u + b;
+          const uint64_t cut = pre[i + 1] - pre[i];
+          const CellDecision d = decide_cell(p, pre, i, cut);
+          const uint64_t idx = base + before + j++;
+          const unsigned kind = d.detected ? 0u : (!d.evaluable ? 2u : 1u);
+          if (idx < p.cap) {
+            rd_event ev;
+            make_event(&ev, kind, i, fid, d.evaluable ? d.n : 0u, p.alpha, 0, 0, cut,
+                       d.evaluable ? d.sum : 0ull, idx == base, false, (uint32_t)frame, beam);
+            if (lane == 0) p.events[idx] = ev;
+            if (p.flits)
+              warp_write_packet(ev.w, p.flits + idx * pk, p.packet_w, p.flit_words, p.nfl,
+                                p.src_id, p.dest, p.vc, (unsigned)((seq0 + idx) & 0xFFFFu));
+          }
         }
       }
       before += __popc(m);
     }
   }
-  if (lane == 0) {
-    const uint64_t idx = base + cnt - 1u;
-    if (idx < p.cap) {
-      rd_event ev;
-      make_event(&ev, 3u, p.n, fid, 0, p.alpha, p.detsup[2 * u], p.detsup[2 * u + 1], 0, 0,
-                 cnt == 1u, true, (uint32_t)frame, beam);
-      p.events[idx] = ev;
-      if (p.flits)
-        write_packet(&ev, p.flits + idx * p.nfl * p.flit_words, p.packet_w, p.flit_words, p.nfl,
-                     p.src_id, p.dest, p.vc, (unsigned)((seq0 + idx) & 0xFFFFu));
-    }
+  const uint64_t idx = base + cnt - 1u;  // the SUMMARY
+  if (idx < p.cap) {
+    rd_event ev;
+    make_event(&ev, 3u, p.n, fid, 0, p.alpha, p.detsup[2 * u], p.detsup[2 * u + 1], 0, 0,
+               cnt == 1u, true, (uint32_t)frame, beam);
+    if (lane == 0) p.events[idx] = ev;
+    if (p.flits)
+      warp_write_packet(ev.w, p.flits + idx * pk, p.packet_w, p.flit_words, p.nfl, p.src_id,
+                        p.dest, p.vc, (unsigned)((seq0 + idx) & 0xFFFFu));
   }
 }
 
 static size_t cfar_smem(const CfarParams& p) { return 4u * (p.n + 1u) * sizeof(uint64_t); }
-static bool g_cfar_attr_set = false;
-static void cfar_attrs() {
-  if (g_cfar_attr_set) return;
-  cudaFuncSetAttribute(k_cfar_decide, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  cudaFuncSetAttribute(k_cfar_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  g_cfar_attr_set = true;
-}
+
+// Instantiation by the row bound W of a frame of n cells (n <= 1024 = 32 x 32).
+// Shared memory: 4 frames x (n + 1) x 8 B <= 32.8 KB, under the default limit.
+#define RD_CFAR_DISPATCH(KERNEL, P, S)                                                      \
+  do {                                                                                      \
+    const unsigned w_ = ((P).n + 31u) / 32u;                                                \
+    const dim3 g_((unsigned)(((P).frames + 3u) / 4u));                                      \
+    const size_t sm_ = cfar_smem(P);                                                        \
+    if (w_ <= 1) KERNEL<1><<<g_, 128, sm_, S>>>(P);                                        \
+    else if (w_ <= 2) KERNEL<2><<<g_, 128, sm_, S>>>(P);                                   \
+    else if (w_ <= 4) KERNEL<4><<<g_, 128, sm_, S>>>(P);                                   \
+    else if (w_ <= 8) KERNEL<8><<<g_, 128, sm_, S>>>(P);                                   \
+    else if (w_ <= 16) KERNEL<16><<<g_, 128, sm_, S>>>(P);                                 \
+    else KERNEL<32><<<g_, 128, sm_, S>>>(P);                                               \
+  } while (0)
 
 void launch_cfar_decide(const CfarParams& p, cudaStream_t s) {
   if (!p.frames) return;
-  cfar_attrs();
-  k_cfar_decide<<<(unsigned)((p.frames + 3u) / 4u), 128, cfar_smem(p), s>>>(p);
+  RD_CFAR_DISPATCH(k_cfar_decide, p, s);
 }
 void launch_cfar_scan(const CfarParams& p, cudaStream_t s) {
   if (!p.frames) return;
@@ -582,8 +699,7 @@ void launch_cfar_scan(const CfarParams& p, cudaStream_t s) {
 }
 void launch_cfar_emit(const CfarParams& p, cudaStream_t s) {
   if (!p.frames) return;
-  cfar_attrs();
-  k_cfar_emit<<<(unsigned)((p.frames + 3u) / 4u), 128, cfar_smem(p), s>>>(p);
+  RD_CFAR_DISPATCH(k_cfar_emit, p, s);
 }
 
 // ---------------------------------------------------------------------------

@@ -151,7 +151,7 @@ struct CfarParams {
   uint32_t* counts;           // [frames] events per CFAR frame
   uint32_t* detsup;           // [frames][2]
   uint32_t* mask;             // [frames][ceil(n/32)] emitted-cell bitmask
-  unsigned long long* offsets;// [frames] exclusive offsets (from the scan)
+  unsigned long long* offsets;// [ceil(frames / 4)] per-CTA event totals, then their exclusive offsets
   rd_event* events;           // output, capacity cap
   uint64_t cap;
   uint32_t* flits;            // output flits or null
