@@ -55,14 +55,16 @@ enum { RD_EV_DETECT = 0, RD_EV_BIN = 1, RD_EV_SUPPRESSED = 2, RD_EV_SUMMARY = 3 
 enum { RD_COV_OFF = 0, RD_COV_CHANNEL = 1, RD_COV_BEAM = 2 };
 enum { RD_COV_BLOCK = 0, RD_COV_EXP = 1 };
 
-/* Form of the beamforming contraction. Both are bit-exact.
- * RD_FORM_CUDA_CORE: int32 limb multiply-accumulate on the CUDA cores.
- * RD_FORM_TENSOR: the int16 samples and weights split into 8-bit limbs held
- * exactly in fp16, multiplied on the tensor cores with fp32 accumulation
- * whose every partial sum is an integer below 2^24 (hence n_chan <=
- * RD_TC_MAX_CHAN), recombined in int64. Covariance always runs on the CUDA
- * cores. */
-enum { RD_FORM_CUDA_CORE = 0, RD_FORM_TENSOR = 1 };
+/* Form of the beamforming and covariance contractions. All are bit-exact.
+ * RD_FORM_CUDA_CORE: integer multiply-accumulate on the CUDA cores.
+ * RD_FORM_TENSOR: the int16 operands split into 8-bit limbs held exactly in
+ * fp16, multiplied on the tensor cores with fp32 accumulation whose every
+ * partial sum is an integer below 2^24 (hence n_chan <= RD_TC_MAX_CHAN),
+ * recombined in int64: the beamformer on tcgen05 (TMEM accumulators), the
+ * exact block-mode covariance on the warp-level mma path.
+ * RD_FORM_TENSOR_SYNC: the same limb split with the beamformer on the
+ * warp-level mma path too (for comparison). */
+enum { RD_FORM_CUDA_CORE = 0, RD_FORM_TENSOR = 1, RD_FORM_TENSOR_SYNC = 2 };
 #define RD_TC_MAX_CHAN 128u
 
 /* Stream geometry and block configuration. Zero-initialise, then fill;
@@ -350,7 +352,7 @@ rd_status rd_fft_run(uint32_t n_fft, uint32_t spc, uint32_t scale_sched,
  * n_vec antenna vectors x[n_vec][n_ant] -> y[n_vec][n_beams].
  * acc: [n_vec][n_beams][2] exact accumulators (may be NULL);
  * flags: [n_vec][n_beams] bytes (f_re << 2) | f_im (may be NULL).
- * form: RD_FORM_*; RD_FORM_TENSOR needs n_ant <= RD_TC_MAX_CHAN. */
+ * form: RD_FORM_*; the tensor forms need n_ant <= RD_TC_MAX_CHAN. */
 rd_status rd_bf_run(uint32_t n_ant, uint32_t n_beams, const rd_cplx16* w,
                     const rd_cplx16* x, uint64_t n_vec, rd_cplx16* y,
                     int64_t* acc, uint8_t* flags, uint32_t form);

@@ -19,20 +19,25 @@ def rnd(rng, n):
     return rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
 
 
+FORMS = [abi.RD_FORM_TENSOR, abi.RD_FORM_TENSOR_SYNC]
+
+
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("A,B", [(1, 1), (4, 2), (16, 16), (64, 64), (5, 3), (63, 17),
                                  (65, 16), (128, 7), (127, 33), (2, 100)])
-def test_bf_tensor_random_vs_oracle(gpulib, port, A, B):
+def test_bf_tensor_random_vs_oracle(gpulib, port, A, B, form):
     rng = np.random.default_rng(7 * A + B)
     w, x = rnd(rng, A * B), rnd(rng, 301 * A)
     want = port.bf(A, B, w, x)
-    for a, b in zip(gc.bf(A, B, w, x, form=TC), want):
+    for a, b in zip(gc.bf(A, B, w, x, form=form), want):
         assert np.array_equal(a, b)
-    for a, b in zip(gc.bf(A, B, w, x, form=TC), gc.bf(A, B, w, x)):
+    for a, b in zip(gc.bf(A, B, w, x, form=form), gc.bf(A, B, w, x)):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("A", [64, 128])
-def test_bf_tensor_extremes(gpulib, port, A):
+def test_bf_tensor_extremes(gpulib, port, A, form):
     # every limb at its extreme: -32768 (high limb -128, low 0), 32767
     # (127, 255), -1 (-1, 255), and mixed signs; at 128 channels the class
     # sums come within 0.4 % of 2^24, the most the fp32 accumulation holds
@@ -52,16 +57,17 @@ def test_bf_tensor_extremes(gpulib, port, A):
             wr[:], wi[:] = -32768 + 255, 32767
             xr[:], xi[:] = -32768 + 255, -32768 + 255
         w, x = sc.pack(wr, wi), sc.pack(xr, xi)
-        got, want = gc.bf(A, B, w, x, form=TC), port.bf(A, B, w, x)
+        got, want = gc.bf(A, B, w, x, form=form), port.bf(A, B, w, x)
         for a, b in zip(got, want):
             assert np.array_equal(a, b), trial
 
 
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("name", ["tiny", "ref_tiny", "medium_slice", "tiny_sat"])
-def test_chain_tensor_fixture(gpulib, name):
+def test_chain_tensor_fixture(gpulib, name, form):
     z = load_chain_fixture(name)
     cfg = cfg_from_fixture(z)
-    cfg.form = TC
+    cfg.form = form
     ch = gc.Chain(cfg, z["coeff"], z["weights"], (z["px"], z["py"]))
     n_fft, f0 = cfg.n_fft, 0
     for i, nf in enumerate(z["calls"]):
@@ -100,12 +106,13 @@ def test_chain_tensor_equals_cuda_core(gpulib, seed):
     w = rnd(rng, p.n_chan * p.n_beams) if seed else sc.steering_weights(p.n_chan, p.n_beams)
     x = sc.adc(p, p.cpi_samples // 4, start=seed * 1000 * p.n_fft)
     outs = []
-    for form in (abi.RD_FORM_CUDA_CORE, TC):
+    for form in (abi.RD_FORM_CUDA_CORE, TC, abi.RD_FORM_TENSOR_SYNC):
         cfg = sc.make_config(p, max_frames=int(rng.integers(20, 200)), form=form)
         ch = gc.Chain(cfg, coeff, w, (px, py))
         outs.append((ch.process(x, taps=True), ch.stats()))
-    assert diff(outs[0][0], outs[1][0], CHAIN_KEYS + TAP_KEYS) == []
-    assert diff_stats(outs[0][1], outs[1][1]) == []
+    for k in (1, 2):
+        assert diff(outs[0][0], outs[k][0], CHAIN_KEYS + TAP_KEYS) == [], k
+        assert diff_stats(outs[0][1], outs[k][1]) == [], k
 
 
 def _cov_chain_pair(p, cfg_over, pairs, x, coeff=None, w=None):
