@@ -168,6 +168,7 @@ struct rd_chain {
   rd_config cfg;
   uint32_t R = 0;            // ring frames
   uint32_t launch_frames = 0;  // frames per launch (<= max_frames)
+  uint32_t safe_in = 0;        // FFT inputs within this bound cannot saturate
   uint32_t S = 0, P = 0;     // covariance source length, pairs
   bool pairs_custom = false;
   cudaStream_t stream = nullptr;
@@ -384,6 +385,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
   const uint32_t N = c.n_fft, C = c.n_chan, B = c.n_beams, T = c.taps, F = c.max_frames;
   ch->R = F + c.hist_frames;
   ch->launch_frames = F;
+  ch->safe_in = front_safe_input(N, c.spc, c.scale_sched);
   auto bad = [&](cudaError_t e) {
     if (e == cudaSuccess) return false;
     fail(e == cudaErrorMemoryAllocation ? RD_ENOMEM : RD_EDEVICE, "allocation failed: %s",
@@ -568,6 +570,7 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   fp.T = c.taps;
   fp.spc = c.spc;
   fp.sched = c.scale_sched;
+  fp.safe_in = ch->safe_in;
   fp.stats = st;
   {
     KTimer t(ch, KT_FRONT);

@@ -8,10 +8,12 @@
 //    memory (one barrier per exchange, double-buffered);
 //  * stage constants fold at compile time; values stay as unpacked int32
 //    re/im between sub-stages;
-//  * saturation is detected with one LOP3 per value (r ^ clamp(r)); the exact
-//    per-sub-stage flags of fft_ref.hpp:230-234 are only recomputed, by the
-//    same code instantiated with flag tracking, for a pass in which some
-//    value saturated. Values never depend on the flag path.
+//  * saturation cannot happen in a pass whose PFB outputs are all within the
+//    bound `safe_in` the host derives from the scaling schedule and the
+//    twiddle table (front_safe_input): such a pass runs the sub-stages with
+//    plain rounding, no clamps and no flag tracking. Any other pass runs the
+//    same code instantiated with the exact saturation and per-sub-stage flags
+//    of fft_ref.hpp:230-234. Values never depend on which path ran.
 //
 // Thread t of an item owns lane q = t & 1 (spc 2) and quad index t >> 1, so a
 // warp's PFB loads read consecutive phases.
@@ -33,14 +35,14 @@ __device__ __forceinline__ uint32_t pk(C2 c) {
 }
 
 // round by sh in {0,1} (round_even, fxp.hpp:198-208), saturate to 16 bits
-// (fft_ref.hpp:315-319). FL: exact direction flags; else overflow indicator.
+// (fft_ref.hpp:315-319). FL: the exact path, saturation and direction flags;
+// else the bound-checked pass, where no value can leave 16 bits.
 template <bool FL>
 __device__ __forceinline__ int qsat(int v, unsigned sh, unsigned& ovf, unsigned& fl) {
   const int r = sh ? ((v >> 1) + ((v & (v >> 1)) & 1)) : v;
-  const int c = min(max(r, -32768), 32767);
-  if (FL) fl |= (r > 32767 ? 2u : 0u) | (r < -32768 ? 1u : 0u);
-  else ovf |= (unsigned)(r ^ c);
-  return c;
+  if (!FL) return r;
+  fl |= (r > 32767 ? 2u : 0u) | (r < -32768 ? 1u : 0u);
+  return min(max(r, -32768), 32767);
 }
 
 // round_sat(v, 15, 16) of an exact product sum |v| < 2^31 (fxp.hpp:221-231):
@@ -48,10 +50,9 @@ __device__ __forceinline__ int qsat(int v, unsigned sh, unsigned& ovf, unsigned&
 template <bool FL>
 __device__ __forceinline__ int q15(int v, unsigned& ovf, unsigned& fl) {
   const int r = (v + 0x3FFF + ((v >> 15) & 1)) >> 15;
-  const int c = min(max(r, -32768), 32767);
-  if (FL) fl |= (r > 32767 ? 2u : 0u) | (r < -32768 ? 1u : 0u);
-  else ovf |= (unsigned)(r ^ c);
-  return c;
+  if (!FL) return r;
+  fl |= (r > 32767 ? 2u : 0u) | (r < -32768 ? 1u : 0u);
+  return min(max(r, -32768), 32767);
 }
 
 // a, t <- (a + t', a - t'), t' = -j t when K1 (saturating negate of t.re)
@@ -60,10 +61,12 @@ __device__ __forceinline__ void bfly(C2& a, C2& t, unsigned sh, unsigned& ovf, u
   C2 u = t;
   if (K1) {
     const int n = -t.re;
-    const int c = min(n, 32767);
-    if (FL) fl |= n > 32767 ? 2u : 0u;
-    else ovf |= (unsigned)(n ^ c);
-    u = C2{t.im, c};
+    if (FL) {
+      fl |= n > 32767 ? 2u : 0u;
+      u = C2{t.im, min(n, 32767)};
+    } else {
+      u = C2{t.im, n};  // |t.re| <= 32767 in a bound-checked pass
+    }
   }
   const C2 lo{qsat<FL>(a.re + u.re, sh, ovf, fl), qsat<FL>(a.im + u.im, sh, ovf, fl)};
   const C2 hi{qsat<FL>(a.re - u.re, sh, ovf, fl), qsat<FL>(a.im - u.im, sh, ovf, fl)};
@@ -212,6 +215,14 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
     if (ok && p.tap_pfb)
       p.tap_pfb[((size_t)f * p.C + c) * G::N + ph0 + (j & 1) * dph1 + (j >> 1) * dph2] = pk(E[j]);
   }
+  // ---- the pass's bound check: every PFB output within safe_in means no
+  // sub-stage can saturate; otherwise the caller runs the exact path ----
+  if constexpr (!FL) {
+    int m = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) m = max(m, max(abs(E[j].re), abs(E[j].im)));
+    if (__syncthreads_or(ok && m > (int)p.safe_in)) return true;
+  }
   // ---- lane sub-stages (fft_ref.hpp:269-276) ----
   int cur = 0;
   lane_stages<NL, SPC, FL, 0>(E, q, tl, p.sched, twp, buf0, buf1, cur, ovf, sf);
@@ -245,7 +256,8 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
     }
   }
   if (FL && ok) sf_out |= sf;
-  return __syncthreads_or(ovf != 0u) != 0;
+  __syncthreads();  // the tile and the exchange buffers are reused next pass
+  return false;
 }
 
 // The exact-flags recomputation, kept out of line so it does not weigh on the
@@ -292,9 +304,9 @@ __global__ void __launch_bounds__(256) k_front_fast(FrontParams p, unsigned FB, 
     const unsigned f = f0 + fb, c = c0 + cc;
     const bool ok = it < n_items && f < p.F && c < p.C;
     uint32_t* tile_row = s_tile + (size_t)fb * N * cbp + cc;
-    const bool sat = front_pass_body<NL, SPC, TT, false>(p, T, q, tl, ok, f, c, s_tw, buf0, buf1,
+    const bool big = front_pass_body<NL, SPC, TT, false>(p, T, q, tl, ok, f, c, s_tw, buf0, buf1,
                                                          tile_row, cbp, pfl, psat, sf);
-    if (sat)  // recompute the pass with exact per-sub-stage flags
+    if (big)  // the exact path: saturation and per-sub-stage flags
       front_pass_flags<NL, SPC, TT>(p, T, q, tl, ok, f, c, s_tw, buf0, buf1, tile_row, cbp, &sf);
   }
   __syncthreads();

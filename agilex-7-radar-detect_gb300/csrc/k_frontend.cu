@@ -39,6 +39,55 @@ static unsigned host_bitrev(unsigned v, unsigned w) {
   return r;
 }
 
+uint32_t front_safe_input(uint32_t n, uint32_t spc, uint32_t sched) {
+  // |wr| + |wi| over the table bounds what a twiddle product can grow
+  uint64_t sw = 0;
+  for (int i = 0; i < 1024; ++i) {
+    const int wr = (int16_t)(uint16_t)(h_tw[i] & 0xFFFFu), wi = (int16_t)(uint16_t)(h_tw[i] >> 16);
+    const uint64_t s = (uint64_t)(wr < 0 ? -wr : wr) + (uint64_t)(wi < 0 ? -wi : wi);
+    if (s > sw) sw = s;
+  }
+  unsigned nl = 0;
+  while ((1u << nl) < n / spc) ++nl;
+  // the per-component bound after every sub-stage of the kernel's sequence:
+  // a butterfly output is RNE((a +- t) / 2^sh), at most M when it scales and
+  // 2M when it does not; a twiddle product rounded at 2^15 grows M by at most
+  // sw / 2^15 (plus one for the rounding)
+  auto fits = [&](uint64_t m) {
+    auto bf = [&](unsigned stage) {
+      m = ((sched >> stage) & 1u) ? m : 2 * m;
+      return m <= 32767u;
+    };
+    auto tw = [&]() {
+      m = (m * sw + 16384u) / 32768u + 1u;
+      return m <= 32767u;
+    };
+    for (unsigned st = 0; st < nl; st += 2) {
+      if (st + 1 < nl) {
+        if (!bf(st) || !bf(st + 1)) return false;
+        if (st + 2 < nl && !tw()) return false;
+      } else if (!bf(st)) {
+        return false;
+      }
+    }
+    if (spc == 2) {  // merge: twiddle on the odd lane, then a butterfly
+      const uint64_t e = m;
+      if (!tw()) return false;
+      m = m > e ? m : e;
+      if (!bf(nl)) return false;
+    }
+    return true;
+  };
+  uint32_t lo = 0, hi = 32767;  // largest fitting input bound
+  if (!fits(0)) return 0;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1u) / 2u;
+    if (fits(mid)) lo = mid;
+    else hi = mid - 1u;
+  }
+  return lo;
+}
+
 void twiddle_positions(uint32_t n, uint32_t spc, uint32_t* out, uint32_t* words) {
   const unsigned m = n / spc, nl = ilog2(m);
   const unsigned n_tw = (nl - 1u) / 2u;

@@ -41,9 +41,14 @@ struct FrontParams {
   const uint32_t* tw_pos;   // per-position twiddles, twiddle_positions()
   uint32_t* tap_pfb;        // [F][C][N] chunk-relative, or null
   uint32_t F, C, N, T, spc, sched;
+  uint32_t safe_in;         // PFB outputs within this bound cannot saturate the FFT
   DevStats* stats;
 };
 void launch_front(const FrontParams& p, cudaStream_t s);
+// The largest per-component magnitude of the FFT input for which no
+// sub-stage of an (n, spc) transform with this scaling schedule can
+// saturate (k_frontend.cu).
+uint32_t front_safe_input(uint32_t n, uint32_t spc, uint32_t sched);
 // The geometry-specialised kernel (k_front_fast.cu); false when the geometry
 // has no specialisation.
 bool launch_front_fast(const FrontParams& p, cudaStream_t s);
