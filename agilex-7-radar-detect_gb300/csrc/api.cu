@@ -177,6 +177,8 @@ struct rd_chain {
 
   DevBuf<uint32_t> coeff_t, weights, tail[2], ring, power, beams_bn, stage, tw_pos;
   DevBuf<int4> w_limbs;
+  DevBuf<int2> coeff2;      // [T][N] unpacked coefficients
+  uint32_t pfb32 = 0;       // 1: int32 PFB accumulation is exact for this bank
   DevBuf<uint32_t> w_frag;  // warp-MMA tensor form: mma fragments of the limb-split weights
   DevBuf<uint32_t> w_tc5;   // tcgen05 tensor form: the canonical-layout weight operand
   // tensor form of the exact covariance: plan, unit lists and pair map
@@ -396,7 +398,8 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
   if (bad(cudaStreamCreateWithFlags(&ch->stream, cudaStreamNonBlocking)) ||
       bad(cudaEventCreateWithFlags(&ch->ev_in, cudaEventDisableTiming)) ||
       bad(cudaEventCreateWithFlags(&ch->ev_out, cudaEventDisableTiming)) ||
-      bad(ch->coeff_t.ensure((size_t)T * N)) || bad(ch->weights.ensure((size_t)B * C)) ||
+      bad(ch->coeff_t.ensure((size_t)T * N)) || bad(ch->coeff2.ensure((size_t)T * N)) ||
+      bad(ch->weights.ensure((size_t)B * C)) ||
       bad(ch->w_limbs.ensure((size_t)B * C)) ||
       (c.form == RD_FORM_TENSOR_SYNC && bad(ch->w_frag.ensure(beam_tc_fragment_words(C, B)))) ||
       (c.form == RD_FORM_TENSOR && bad(ch->w_tc5.ensure(beam_tc5_operand_bytes(C, B) / 4))) ||
@@ -410,6 +413,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
   }
   ch->own_stream = true;
   cudaMemset(ch->coeff_t.p, 0, (size_t)T * N * 4);
+  cudaMemset(ch->coeff2.p, 0, (size_t)T * N * sizeof(int2));
   cudaMemset(ch->weights.p, 0, (size_t)B * C * 4);
   cudaMemset(ch->w_limbs.p, 0, (size_t)B * C * sizeof(int4));
   if (c.form == RD_FORM_TENSOR_SYNC)
@@ -469,7 +473,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
 void rd_chain_destroy(rd_chain* ch) {
   if (!ch) return;
   if (ch->stream) cudaStreamSynchronize(ch->stream);
-  ch->coeff_t.release(); ch->weights.release(); ch->w_limbs.release(); ch->w_frag.release(); ch->w_tc5.release(); ch->tail[0].release(); ch->tail[1].release();
+  ch->coeff_t.release(); ch->coeff2.release(); ch->weights.release(); ch->w_limbs.release(); ch->w_frag.release(); ch->w_tc5.release(); ch->tail[0].release(); ch->tail[1].release();
   ch->ring.release(); ch->power.release(); ch->beams_bn.release(); ch->stage.release();
   ch->tw_pos.release(); ch->ct_units.release(); ch->ct_pq.release();
   ch->px.release(); ch->py.release(); ch->acc_re.release(); ch->acc_im.release();
@@ -494,6 +498,23 @@ rd_status rd_chain_set_coeff(rd_chain* ch, const rd_cplx16* coeff) {
   for (uint32_t p = 0; p < N; ++p)
     for (uint32_t k = 0; k < T; ++k) t[(size_t)k * N + p] = coeff[(size_t)p * T + k];
   CK(cudaMemcpyAsync(ch->coeff_t.p, t.data(), t.size() * 4, cudaMemcpyHostToDevice, ch->stream));
+  // unpacked copy, and whether every phase's L1 norm sum_k |hr| + |hi| keeps
+  // the PFB sums of any int16 input inside int32 (|sum| <= 2^15 x norm)
+  std::vector<int2> t2(t.size());
+  uint64_t worst = 0;
+  for (uint32_t p = 0; p < N; ++p) {
+    uint64_t l1 = 0;
+    for (uint32_t k = 0; k < T; ++k) {
+      const uint32_t v = t[(size_t)k * N + p];
+      const int re = (int16_t)(uint16_t)(v & 0xFFFFu), im = (int16_t)(uint16_t)(v >> 16);
+      t2[(size_t)k * N + p] = make_int2(re, im);
+      l1 += (uint64_t)(re < 0 ? -re : re) + (uint64_t)(im < 0 ? -im : im);
+    }
+    worst = std::max(worst, l1);
+  }
+  ch->pfb32 = worst <= 65535u ? 1u : 0u;
+  CK(cudaMemcpyAsync(ch->coeff2.p, t2.data(), t2.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                     ch->stream));
   CK(cudaStreamSynchronize(ch->stream));
   return RD_OK;
 }
@@ -558,6 +579,8 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   fp.ld = ld;
   fp.tail = ch->tail[ch->tail_cur].p;
   fp.coeff_t = ch->coeff_t.p;
+  fp.coeff2 = ch->coeff2.p;
+  fp.pfb32 = ch->pfb32;
   fp.ring = ch->ring.p;
   fp.ring_frames = ch->R;
   fp.ring_base = ring_base;

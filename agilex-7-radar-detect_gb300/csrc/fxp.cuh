@@ -91,6 +91,13 @@ RD_HD int64_t rne15_64(int64_t v) {
   return q + ((rem > 0x4000) | ((rem == 0x4000) & (q & 1)));
 }
 // round_sat(v, 15, 16) of a 64-bit accumulator; flags into *fl.
+// round_sat(v, 15, 16) of an int32 sum whose |v| <= 2^31 - 2^15 (so the
+// rounding add cannot wrap), with the same flags as q15_out64
+RD_HD int32_t q15_out32(int32_t v, unsigned* fl) {
+  const int32_t r = (v + 0x3FFF + ((v >> 15) & 1)) >> 15;
+  *fl |= (r > 32767 ? 2u : 0u) | (r < -32768 ? 1u : 0u);
+  return r > 32767 ? 32767 : (r < -32768 ? -32768 : r);
+}
 RD_HD int32_t q15_out64(int64_t v, unsigned* fl) {
   const int64_t r = rne15_64(v);
   *fl |= (r > 32767 ? 2u : 0u) | (r < -32768 ? 1u : 0u);

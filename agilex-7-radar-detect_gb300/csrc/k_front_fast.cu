@@ -181,32 +181,7 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
   const int pos0 = tl;  // quad_base<NL-2>(tl) == tl
   const int ph0 = SPC * pos0 + q;
   constexpr int dph1 = SPC * d1, dph2 = SPC * d0;
-  long long ar[4] = {0, 0, 0, 0}, ai[4] = {0, 0, 0, 0};
-  if (ok) {
-    const uint32_t* xa = p.adc + (size_t)c * p.ld + ph0;
-    const uint32_t* xt = p.tail + (size_t)c * (T - 1) * G::N + ph0;
-    const uint32_t* hc = p.coeff_t + ph0;
-#pragma unroll
-    for (int k = 0; k < (TT ? TT : 16); ++k) {
-      if (!TT && k >= T) break;
-      const long long fr = (long long)f - k;
-      const uint32_t* xp = fr >= 0 ? xa + (size_t)fr * G::N : xt + (size_t)(-fr - 1) * G::N;
-      const uint32_t* hp = hc + (size_t)k * G::N;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int o = (j & 1) * dph1 + (j >> 1) * dph2;
-        const C2 x = unpk(__ldg(xp + o)), hk = unpk(__ldg(hp + o));
-        ar[j] += (long long)x.re * hk.re;
-        ar[j] -= (long long)x.im * hk.im;
-        ai[j] += (long long)x.re * hk.im;
-        ai[j] += (long long)x.im * hk.re;
-      }
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    unsigned fr = 0, fi = 0;
-    const int yr = q15_out64(ar[j], &fr), yi = q15_out64(ai[j], &fi);
+  auto finish = [&](int j, int yr, int yi, unsigned fr, unsigned fi) {
     if (fr | fi) {
       pfl |= fr | fi;
       ++psat;
@@ -214,6 +189,65 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
     E[j] = C2{yr, yi};
     if (ok && p.tap_pfb)
       p.tap_pfb[((size_t)f * p.C + c) * G::N + ph0 + (j & 1) * dph1 + (j >> 1) * dph2] = pk(E[j]);
+  };
+  if (p.pfb32) {
+    // every partial sum is bounded by 2^15 x the phase's L1 norm < 2^31
+    int ar[4] = {0, 0, 0, 0}, ai[4] = {0, 0, 0, 0};
+    if (ok) {
+      const uint32_t* xa = p.adc + (size_t)c * p.ld + ph0;
+      const uint32_t* xt = p.tail + (size_t)c * (T - 1) * G::N + ph0;
+      const int2* hc = p.coeff2 + ph0;
+#pragma unroll
+      for (int k = 0; k < (TT ? TT : 16); ++k) {
+        if (!TT && k >= T) break;
+        const long long fr = (long long)f - k;
+        const uint32_t* xp = fr >= 0 ? xa + (size_t)fr * G::N : xt + (size_t)(-fr - 1) * G::N;
+        const int2* hp = hc + (size_t)k * G::N;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int o = (j & 1) * dph1 + (j >> 1) * dph2;
+          const C2 x = unpk(__ldg(xp + o));
+          const int2 h = __ldg(hp + o);
+          ar[j] += x.re * h.x - x.im * h.y;
+          ai[j] += x.re * h.y + x.im * h.x;
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      unsigned fr = 0, fi = 0;
+      const int yr = q15_out32(ar[j], &fr), yi = q15_out32(ai[j], &fi);
+      finish(j, yr, yi, fr, fi);
+    }
+  } else {
+    long long ar[4] = {0, 0, 0, 0}, ai[4] = {0, 0, 0, 0};
+    if (ok) {
+      const uint32_t* xa = p.adc + (size_t)c * p.ld + ph0;
+      const uint32_t* xt = p.tail + (size_t)c * (T - 1) * G::N + ph0;
+      const uint32_t* hc = p.coeff_t + ph0;
+#pragma unroll
+      for (int k = 0; k < (TT ? TT : 16); ++k) {
+        if (!TT && k >= T) break;
+        const long long fr = (long long)f - k;
+        const uint32_t* xp = fr >= 0 ? xa + (size_t)fr * G::N : xt + (size_t)(-fr - 1) * G::N;
+        const uint32_t* hp = hc + (size_t)k * G::N;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int o = (j & 1) * dph1 + (j >> 1) * dph2;
+          const C2 x = unpk(__ldg(xp + o)), hk = unpk(__ldg(hp + o));
+          ar[j] += (long long)x.re * hk.re;
+          ar[j] -= (long long)x.im * hk.im;
+          ai[j] += (long long)x.re * hk.im;
+          ai[j] += (long long)x.im * hk.re;
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      unsigned fr = 0, fi = 0;
+      const int yr = q15_out64(ar[j], &fr), yi = q15_out64(ai[j], &fi);
+      finish(j, yr, yi, fr, fi);
+    }
   }
   // ---- the pass's bound check: every PFB output within safe_in means no
   // sub-stage can saturate; otherwise the caller runs the exact path ----

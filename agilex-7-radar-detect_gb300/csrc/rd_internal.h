@@ -34,6 +34,8 @@ struct FrontParams {
   uint64_t ld;
   const uint32_t* tail;     // [C][T-1][N]: tail[c][k][p] = frame -1-k
   const uint32_t* coeff_t;  // [T][N] (tap-major copy of the phase-major bank)
+  const int2* coeff2;       // [T][N] the same, unpacked {re, im}
+  uint32_t pfb32;           // 1: the bank's phase L1 norms keep every sum in int32
   uint32_t* ring;           // [R][N][C]
   uint32_t ring_frames;     // R
   uint32_t ring_base;       // ring slot of chunk frame 0 (g0 mod R)
