@@ -284,6 +284,95 @@ __global__ void __launch_bounds__(256) k_cov(CovParams p, unsigned BT, unsigned 
   }
 }
 
+// Exact block mode (MODE 0 of k_cov) with the source vectors staged once per
+// batch as unpacked {re, im} int32 pairs, so a (bin, pair) thread spends a
+// frame on two 64-bit shared loads and four multiply-adds. A CTA's frames are
+// one window segment (split as in k_cov), so the window closes at most once,
+// after the loop, and no frame needs a count check.
+__global__ void __launch_bounds__(256) k_cov_block(CovParams p, unsigned BT, unsigned QB,
+                                                   unsigned FB) {
+  extern __shared__ int2 s_xy[];  // [FB][BT][S]
+  const unsigned tid = threadIdx.x, nth = blockDim.x;
+  const unsigned S = p.S, row = BT * S, per_batch = FB * row;
+  const unsigned bin0 = blockIdx.x * BT;
+  const unsigned bl = tid / QB, q = blockIdx.y * QB + tid % QB;
+  const unsigned bin = bin0 + bl;
+  const bool live = bl < BT && bin < p.N && q < p.P;
+  const size_t k = (size_t)bin * p.P + q;
+  const unsigned z = blockIdx.z, nz = gridDim.z;
+  const unsigned first = p.wl - p.count0;  // frames until the open window closes
+  const unsigned lo = z == 0 ? 0u : first + (z - 1u) * p.wl;
+  const unsigned hi_ = z == 0 ? first : first + z * p.wl;
+  const unsigned hi = (nz == 1u || hi_ > p.F) ? p.F : hi_;
+  const unsigned xi = live ? bl * S + p.px[q] : 0u, yi = live ? bl * S + p.py[q] : 0u;
+  long long are = 0, aim = 0;
+  uint32_t pre[kCovPre];
+  auto load = [&](unsigned fbase) {
+#pragma unroll
+    for (unsigned j = 0; j < kCovPre; ++j) {
+      const unsigned w = tid + j * nth;
+      uint32_t v = 0;
+      if (w < per_batch) {
+        const unsigned fl = w / row, r = w % row;
+        const unsigned f = fbase + fl, b = bin0 + r / S, a = r % S;
+        if (f < hi && b < p.N) {
+          if (p.src_beam) {
+            v = __ldg(p.beams_bn + ((size_t)f * p.N + b) * S + a);
+          } else {
+            unsigned slot = p.ring_base + f;
+            if (slot >= p.ring_frames) slot -= p.ring_frames;
+            v = __ldg(p.ring + ((size_t)slot * p.N + b) * S + a);
+          }
+        }
+      }
+      pre[j] = v;
+    }
+  };
+  auto store = [&]() {
+#pragma unroll
+    for (unsigned j = 0; j < kCovPre; ++j) {
+      const unsigned w = tid + j * nth;
+      if (w < per_batch) s_xy[w] = make_int2((int)(int16_t)(uint16_t)(pre[j] & 0xFFFFu), (int)pre[j] >> 16);
+    }
+  };
+  if (lo < hi) load(lo);
+  for (unsigned fbase = lo; fbase < hi; fbase += FB) {
+    __syncthreads();
+    store();
+    __syncthreads();
+    if (fbase + FB < hi) load(fbase + FB);
+    const unsigned nf = (hi - fbase) < FB ? (hi - fbase) : FB;
+    if (live) {
+      const int2* xs = s_xy + xi;
+      const int2* ys = s_xy + yi;
+      // X * conj(Y) through the operand-swap wiring (covar_model.hpp:137-145)
+#pragma unroll 4
+      for (unsigned fl = 0; fl < nf; ++fl) {
+        const int2 x = xs[fl * row], y = ys[fl * row];
+        are += (long long)x.x * y.x;
+        are += (long long)x.y * y.y;
+        aim += (long long)x.y * y.x;
+        aim -= (long long)x.x * y.y;
+      }
+    }
+  }
+  if (!live) return;
+  if (z == 0u) {  // the open window carried in
+    are += p.acc_re[k];
+    aim += p.acc_im[k];
+  }
+  if (z < p.n_windows) {  // this segment closes window z of the launch
+    long long* o = p.out + (((size_t)z * p.N + bin) * p.P + q) * 2;
+    o[0] = are;
+    o[1] = aim;
+    are = aim = 0;
+  }
+  if (z + 1u == nz) {  // the window left open carried out
+    p.acc_re_out[k] = are;
+    p.acc_im_out[k] = aim;
+  }
+}
+
 void launch_cov(const CovParams& p, cudaStream_t s) {
   if (p.P == 0 || p.F == 0) return;
   unsigned QB, BT;
@@ -307,7 +396,7 @@ void launch_cov(const CovParams& p, cudaStream_t s) {
   }
   const dim3 grid((p.N + BT - 1u) / BT, (p.P + QB - 1u) / QB, nz);
   const size_t smem = (size_t)FB * BT * p.S * sizeof(uint32_t);
-  if (mode == 0) k_cov<0><<<grid, nth, smem, s>>>(p, BT, QB, FB);
+  if (mode == 0) k_cov_block<<<grid, nth, 2 * smem, s>>>(p, BT, QB, FB);
   else if (mode == 1) k_cov<1><<<grid, nth, smem, s>>>(p, BT, QB, FB);
   else k_cov<2><<<grid, nth, smem, s>>>(p, BT, QB, FB);
 }

@@ -369,11 +369,12 @@ __global__ void __launch_bounds__(256) k_beam_tc5(BeamParams p) {
       }
     }
     __syncthreads();
-    // lane 0 of each warp waits; the warp takes its verdict together
+    // every thread observes the MMAs' completion itself (an acquire of the
+    // accumulators for its own TMEM reads); __all_sync then reconverges the
+    // warp before the warp-collective loads and makes the verdict uniform
     bool ok = s_err == 0u;
-    if (ok && lane == 0u) ok = mbar_wait(&mb[1], g & 1u);
-    ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-    __syncwarp();
+    if (ok) ok = mbar_wait(&mb[1], g & 1u);
+    ok = __all_sync(0xffffffffu, ok);
     tc_fence_after();
     if (ok) {
       float v[48];

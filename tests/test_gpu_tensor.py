@@ -35,6 +35,20 @@ def test_bf_tensor_random_vs_oracle(gpulib, port, A, B, form):
         assert np.array_equal(a, b)
 
 
+def test_bf_tensor_repeated_calls(gpulib):
+    # many calls in a row, uneven sizes: any ordering gap between the tensor
+    # core's writes and the threads' reads would show as a mismatch
+    rng = np.random.default_rng(77)
+    for it in range(40):
+        A = int(rng.choice([4, 16, 33, 64, 128]))
+        B = int(rng.integers(1, 70))
+        n = int(rng.integers(1, 700))
+        w, x = rnd(rng, A * B), rnd(rng, n * A)
+        want = gc.bf(A, B, w, x)
+        for a, b in zip(gc.bf(A, B, w, x, form=TC), want):
+            assert np.array_equal(a, b), (it, A, B, n)
+
+
 @pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("A", [64, 128])
 def test_bf_tensor_extremes(gpulib, port, A, form):
