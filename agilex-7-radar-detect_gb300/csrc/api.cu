@@ -178,9 +178,9 @@ struct rd_chain {
   DevBuf<uint32_t> coeff_t, weights, tail[2], ring, power, beams_bn, stage, tw_pos;
   DevBuf<int4> w_limbs;
   DevBuf<int2> coeff2;      // [T][N] unpacked coefficients
+  uint32_t x_safe = 0;      // beamformer: |x| bound for exact int32 sums
   uint32_t pfb32 = 0;       // 1: int32 PFB accumulation is exact for this bank
-  DevBuf<uint32_t> w_frag;  // warp-MMA tensor form: mma fragments of the limb-split weights
-  DevBuf<uint32_t> w_tc5;   // tcgen05 tensor form: the canonical-layout weight operand
+  DevBuf<uint32_t> w_frag;  // tensor form: mma fragments of the limb-split weights
   // tensor form of the exact covariance: plan, unit lists and pair map
   CovTcHost cov_tc{};
   bool cov_tc_ok = false;
@@ -337,7 +337,7 @@ rd_status rd_config_validate(const rd_config* c) {
     if (c->cov_window > 65535) return fail(RD_EINVAL, "cov_window must fit 16 bits");
   }
   if (c->max_frames < 1 || c->max_frames > 65536) return fail(RD_EINVAL, "max_frames 1..65536");
-  if (c->form > RD_FORM_TENSOR_SYNC) return fail(RD_EINVAL, "bad form");
+  if (c->form > RD_FORM_TENSOR) return fail(RD_EINVAL, "bad form");
   if (c->form != RD_FORM_CUDA_CORE && c->n_chan > RD_TC_MAX_CHAN)
     return fail(RD_EINVAL, "the tensor form takes at most %u channels", RD_TC_MAX_CHAN);
   if (c->vc > 3 || c->src_id > 31 || c->dest > 15) return fail(RD_EINVAL, "packet header field out of range");
@@ -401,8 +401,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
       bad(ch->coeff_t.ensure((size_t)T * N)) || bad(ch->coeff2.ensure((size_t)T * N)) ||
       bad(ch->weights.ensure((size_t)B * C)) ||
       bad(ch->w_limbs.ensure((size_t)B * C)) ||
-      (c.form == RD_FORM_TENSOR_SYNC && bad(ch->w_frag.ensure(beam_tc_fragment_words(C, B)))) ||
-      (c.form == RD_FORM_TENSOR && bad(ch->w_tc5.ensure(beam_tc5_operand_bytes(C, B) / 4))) ||
+      (c.form == RD_FORM_TENSOR && bad(ch->w_frag.ensure(beam_tc_fragment_words(C, B)))) ||
       bad(ch->tail[0].ensure((size_t)C * D * N)) || bad(ch->tail[1].ensure((size_t)C * D * N)) ||
       bad(ch->ring.ensure((size_t)ch->R * N * C)) || bad(ch->power.ensure((size_t)F * B * N)) ||
       bad(ch->counts.ensure((size_t)F * B)) || bad(ch->detsup.ensure((size_t)F * B * 2)) ||
@@ -416,9 +415,8 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
   cudaMemset(ch->coeff2.p, 0, (size_t)T * N * sizeof(int2));
   cudaMemset(ch->weights.p, 0, (size_t)B * C * 4);
   cudaMemset(ch->w_limbs.p, 0, (size_t)B * C * sizeof(int4));
-  if (c.form == RD_FORM_TENSOR_SYNC)
+  if (c.form == RD_FORM_TENSOR)
     cudaMemset(ch->w_frag.p, 0, (size_t)beam_tc_fragment_words(C, B) * 4);
-  if (c.form == RD_FORM_TENSOR) cudaMemset(ch->w_tc5.p, 0, beam_tc5_operand_bytes(C, B));
   cudaMemset(ch->tail[0].p, 0, (size_t)C * D * N * 4);
   cudaMemset(ch->tail[1].p, 0, (size_t)C * D * N * 4);
   cudaMemset(ch->ring.p, 0, (size_t)ch->R * N * C * 4);
@@ -473,7 +471,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
 void rd_chain_destroy(rd_chain* ch) {
   if (!ch) return;
   if (ch->stream) cudaStreamSynchronize(ch->stream);
-  ch->coeff_t.release(); ch->coeff2.release(); ch->weights.release(); ch->w_limbs.release(); ch->w_frag.release(); ch->w_tc5.release(); ch->tail[0].release(); ch->tail[1].release();
+  ch->coeff_t.release(); ch->coeff2.release(); ch->weights.release(); ch->w_limbs.release(); ch->w_frag.release(); ch->tail[0].release(); ch->tail[1].release();
   ch->ring.release(); ch->power.release(); ch->beams_bn.release(); ch->stage.release();
   ch->tw_pos.release(); ch->ct_units.release(); ch->ct_pq.release();
   ch->px.release(); ch->py.release(); ch->acc_re.release(); ch->acc_im.release();
@@ -523,22 +521,28 @@ rd_status rd_chain_set_weights(rd_chain* ch, const rd_cplx16* w) {
   if (!ch || !w) return fail(RD_EINVAL, "null argument");
   const size_t n = (size_t)ch->cfg.n_beams * ch->cfg.n_chan;
   std::vector<int4> limbs(n);
+  uint64_t l1max = 0;
   for (size_t i = 0; i < n; ++i) {  // w = 256 * wh + wl, wl in [0, 255]
     const int re = (int16_t)(uint16_t)(w[i] & 0xFFFFu), im = (int16_t)(uint16_t)(w[i] >> 16);
     limbs[i] = make_int4(re >> 8, im >> 8, re & 255, im & 255);
   }
+  // |sum_a x_a w_ba| <= max|x| x sum_a (|wr| + |wi|): below 2^31 the plain
+  // int32 sum is exact
+  for (uint32_t b = 0; b < ch->cfg.n_beams; ++b) {
+    uint64_t l1 = 0;
+    for (uint32_t a = 0; a < ch->cfg.n_chan; ++a) {
+      const uint32_t v = w[(size_t)b * ch->cfg.n_chan + a];
+      const int re = (int16_t)(uint16_t)(v & 0xFFFFu), im = (int16_t)(uint16_t)(v >> 16);
+      l1 += (uint64_t)(re < 0 ? -re : re) + (uint64_t)(im < 0 ? -im : im);
+    }
+    l1max = std::max(l1max, l1);
+  }
+  ch->x_safe = l1max ? (uint32_t)std::min<uint64_t>(0x7FFFFFFFull / l1max, 32768u) : 32768u;
   CK(cudaMemcpyAsync(ch->weights.p, w, n * 4, cudaMemcpyHostToDevice, ch->stream));
   CK(cudaMemcpyAsync(ch->w_limbs.p, limbs.data(), n * sizeof(int4), cudaMemcpyHostToDevice,
                      ch->stream));
   std::vector<uint32_t> frag;
-  std::vector<uint16_t> op5;
   if (ch->cfg.form == RD_FORM_TENSOR) {
-    op5.resize(beam_tc5_operand_bytes(ch->cfg.n_chan, ch->cfg.n_beams) / 2);
-    beam_tc5_operand(w, ch->cfg.n_chan, ch->cfg.n_beams, op5.data());
-    CK(cudaMemcpyAsync(ch->w_tc5.p, op5.data(), op5.size() * 2, cudaMemcpyHostToDevice,
-                       ch->stream));
-  }
-  if (ch->cfg.form == RD_FORM_TENSOR_SYNC) {
     frag.resize(beam_tc_fragment_words(ch->cfg.n_chan, ch->cfg.n_beams));
     beam_tc_fragments(w, ch->cfg.n_chan, ch->cfg.n_beams, frag.data());
     CK(cudaMemcpyAsync(ch->w_frag.p, frag.data(), frag.size() * 4, cudaMemcpyHostToDevice,
@@ -614,8 +618,8 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   bp.g0 = ch->frame;
   bp.weights = ch->weights.p;
   bp.w_limbs = ch->w_limbs.p;
+  bp.x_safe = ch->x_safe;
   bp.w_frag = ch->w_frag.p;
-  bp.w_tc5 = ch->w_tc5.p;
   bp.power = ch->power.p;
   bp.beams_bn = ch->beams_bn.p;
   bp.F = F;
@@ -626,8 +630,6 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   {
     KTimer t(ch, KT_BEAM);
     if (c.form == RD_FORM_TENSOR)
-      launch_beam_tc5(bp, s);
-    else if (c.form == RD_FORM_TENSOR_SYNC)
       launch_beam_tc(bp, s);
     else
       launch_beam(bp, s);
@@ -830,7 +832,6 @@ rd_status rd_chain_fetch(rd_chain* ch, rd_output* out) {
   CK(cudaStreamSynchronize(ch->stream));
   DevStats ds;
   CK(cudaMemcpy(&ds, ch->stats.p, sizeof(ds), cudaMemcpyDeviceToHost));
-  if (ds.tc_timeout) return fail(RD_ETIMEOUT, "a bounded tensor-core wait gave up");
   const uint64_t n_ev = ds.scan_scratch[0];
   const uint32_t nfl = rd_detection_flits(c.packet_w), words = rd_flit_words(c.packet_w);
   bool trunc = n_ev > ch->call_cap_events;
@@ -1203,7 +1204,7 @@ rd_status rd_fft_run(uint32_t n_fft, uint32_t spc, uint32_t sched, int reorder,
 
 rd_status rd_bf_run(uint32_t n_ant, uint32_t n_beams, const rd_cplx16* w, const rd_cplx16* x,
                     uint64_t n_vec, rd_cplx16* y, int64_t* acc, uint8_t* flags, uint32_t form) {
-  if (!w || !x || !y || n_ant == 0 || n_beams == 0 || form > RD_FORM_TENSOR_SYNC)
+  if (!w || !x || !y || n_ant == 0 || n_beams == 0 || form > RD_FORM_TENSOR)
     return fail(RD_EINVAL, "bad argument");
   if (form != RD_FORM_CUDA_CORE && n_ant > RD_TC_MAX_CHAN)
     return fail(RD_EINVAL, "the tensor form takes at most %u antennas", RD_TC_MAX_CHAN);
@@ -1221,20 +1222,11 @@ rd_status rd_bf_run(uint32_t n_ant, uint32_t n_beams, const rd_cplx16* w, const 
   CK(cudaMemcpy(dx, x, n_vec * n_ant * 4, cudaMemcpyHostToDevice));
   if (form != RD_FORM_CUDA_CORE) {
     // the vectors as a one-bin "ring" of n_vec frames, in launches of < 2^31 rows
-    std::vector<uint32_t> frag;
-    if (form == RD_FORM_TENSOR) {
-      frag.resize(beam_tc5_operand_bytes(n_ant, n_beams) / 4);
-      beam_tc5_operand(w, n_ant, n_beams, reinterpret_cast<uint16_t*>(frag.data()));
-    } else {
-      frag.resize(beam_tc_fragment_words(n_ant, n_beams));
-      beam_tc_fragments(w, n_ant, n_beams, frag.data());
-    }
+    std::vector<uint32_t> frag(beam_tc_fragment_words(n_ant, n_beams));
+    beam_tc_fragments(w, n_ant, n_beams, frag.data());
     uint32_t* dfrag;
     CK(sc.alloc(&dfrag, frag.size()));
     CK(cudaMemcpy(dfrag, frag.data(), frag.size() * 4, cudaMemcpyHostToDevice));
-    DevStats* dst;
-    CK(sc.alloc(&dst, 1));
-    CK(cudaMemset(dst, 0, sizeof(DevStats)));
     const uint64_t step = 1ull << 30;
     for (uint64_t v0 = 0; v0 < n_vec; v0 += step) {
       const uint32_t F = (uint32_t)(n_vec - v0 < step ? n_vec - v0 : step);
@@ -1242,8 +1234,6 @@ rd_status rd_bf_run(uint32_t n_ant, uint32_t n_beams, const rd_cplx16* w, const 
       bp.ring = dx + v0 * n_ant;
       bp.ring_frames = F;
       bp.w_frag = dfrag;
-      bp.w_tc5 = dfrag;
-      bp.stats = dst;
       bp.y_rows = dy + v0 * n_beams;
       bp.acc_rows = dacc ? dacc + v0 * n_beams * 2 : nullptr;
       bp.flag_rows = df ? df + v0 * n_beams : nullptr;
@@ -1251,14 +1241,8 @@ rd_status rd_bf_run(uint32_t n_ant, uint32_t n_beams, const rd_cplx16* w, const 
       bp.C = n_ant;
       bp.N = 1;
       bp.B = n_beams;
-      if (form == RD_FORM_TENSOR)
-        launch_beam_tc5(bp, 0);
-      else
-        launch_beam_tc(bp, 0);
+      launch_beam_tc(bp, 0);
     }
-    DevStats hs;
-    CK(cudaMemcpy(&hs, dst, sizeof(hs), cudaMemcpyDeviceToHost));
-    if (hs.tc_timeout) return fail(RD_ETIMEOUT, "a bounded tensor-core wait gave up");
   } else {
     launch_bf_block(n_ant, n_beams, dw, dx, n_vec, dy, dacc, df, 0);
   }

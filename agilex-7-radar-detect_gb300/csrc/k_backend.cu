@@ -31,23 +31,58 @@ __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
   const unsigned C = p.C, B = p.B, N = p.N;
   const unsigned xs = C + 1;  // padded row
   int4* s_w = reinterpret_cast<int4*>(sm);          // [B][C] limbs
-  uint32_t* s_x = sm + 4u * B * C;
+  int2* s_w2 = reinterpret_cast<int2*>(sm + 4u * B * C);  // [B][C] {re, im}
+  uint32_t* s_x = sm + 6u * B * C;
   const unsigned tid = threadIdx.x;
   const unsigned bin0 = blockIdx.x * 64u;
   const uint64_t f = blockIdx.y;
   unsigned slot = p.ring_base + (unsigned)f;
   if (slot >= p.ring_frames) slot -= p.ring_frames;
-  for (unsigned k = tid; k < B * C; k += 256u) s_w[k] = p.w_limbs[k];
+  for (unsigned k = tid; k < B * C; k += 256u) {
+    s_w[k] = p.w_limbs[k];
+    const uint32_t w = p.weights[k];
+    s_w2[k] = make_int2((int)(int16_t)(uint16_t)(w & 0xFFFFu), (int)w >> 16);
+  }
   const uint32_t* xsrc = p.ring + ((size_t)slot * N + bin0) * C;
   const unsigned nb = (N - bin0) < 64u ? (N - bin0) : 64u;
-  for (unsigned k = tid; k < nb * C; k += 256u) s_x[(k / C) * xs + (k % C)] = xsrc[k];
-  __syncthreads();
+  int xmax = 0;
+  for (unsigned k = tid; k < nb * C; k += 256u) {
+    const uint32_t v = xsrc[k];
+    s_x[(k / C) * xs + (k % C)] = v;
+    xmax = max(xmax, max(abs((int)(int16_t)(uint16_t)(v & 0xFFFFu)), abs((int)v >> 16)));
+  }
+  // every sum is at most max|x| x the largest beam L1 norm of the weights:
+  // within x_safe the plain int32 sum is exact
+  const bool wide = __syncthreads_or(xmax > (int)p.x_safe) != 0;
   const unsigned bl = tid & 63u, bg = tid >> 6;
   const unsigned bin = bin0 + bl;
   long long ar[BPT], ai[BPT];
 #pragma unroll
   for (int j = 0; j < BPT; ++j) ar[j] = ai[j] = 0;
-  if (bl < nb) {
+  if (bl < nb && !wide) {
+    const uint32_t* xr = s_x + bl * xs;
+    int sr[BPT], si[BPT];
+#pragma unroll
+    for (int j = 0; j < BPT; ++j) sr[j] = si[j] = 0;
+    for (unsigned a = 0; a < C; ++a) {
+      const uint32_t xv = xr[a];
+      const int x_re = (int)(int16_t)(uint16_t)(xv & 0xFFFFu), x_im = (int)xv >> 16;
+#pragma unroll
+      for (int j = 0; j < BPT; ++j) {
+        const unsigned b = bg + 4u * j;
+        if (BPT == 1 || b < B) {
+          const int2 w = s_w2[b * C + a];
+          sr[j] += x_re * w.x - x_im * w.y;
+          si[j] += x_re * w.y + x_im * w.x;
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < BPT; ++j) {
+      ar[j] = sr[j];
+      ai[j] = si[j];
+    }
+  } else if (bl < nb) {
     const uint32_t* xr = s_x + bl * xs;
     for (unsigned a0 = 0; a0 < C; a0 += 64u) {
       const unsigned a1 = (a0 + 64u) < C ? (a0 + 64u) : C;
@@ -108,7 +143,7 @@ static bool g_beam_attr_set = false;
 void launch_beam(const BeamParams& p, cudaStream_t s) {
   const unsigned bpt = (p.B + 3u) / 4u;
   const dim3 grid((p.N + 63u) / 64u, p.F);
-  const size_t smem = ((size_t)4u * p.B * p.C + 64u * (p.C + 1u)) * sizeof(uint32_t);
+  const size_t smem = ((size_t)6u * p.B * p.C + 64u * (p.C + 1u)) * sizeof(uint32_t);
   if (!g_beam_attr_set) {
     cudaFuncSetAttribute(k_beam<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     cudaFuncSetAttribute(k_beam<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
@@ -328,21 +363,41 @@ __global__ void __launch_bounds__(256) k_cov_block(CovParams p, unsigned BT, uns
       pre[j] = v;
     }
   };
+  int smax = 0;
   auto store = [&]() {
+    smax = 0;
 #pragma unroll
     for (unsigned j = 0; j < kCovPre; ++j) {
       const unsigned w = tid + j * nth;
-      if (w < per_batch) s_xy[w] = make_int2((int)(int16_t)(uint16_t)(pre[j] & 0xFFFFu), (int)pre[j] >> 16);
+      if (w < per_batch) {
+        const int re = (int)(int16_t)(uint16_t)(pre[j] & 0xFFFFu), im = (int)pre[j] >> 16;
+        s_xy[w] = make_int2(re, im);
+        smax = max(smax, max(abs(re), abs(im)));
+      }
     }
   };
   if (lo < hi) load(lo);
   for (unsigned fbase = lo; fbase < hi; fbase += FB) {
     __syncthreads();
     store();
-    __syncthreads();
+    // a batch of at most 32 frames whose values are all <= 5792 in magnitude
+    // sums at most 32 x 2 x 5792^2 < 2^31 per pair: exact in int32
+    const bool wide = __syncthreads_or(smax > 5792) != 0;
     if (fbase + FB < hi) load(fbase + FB);
     const unsigned nf = (hi - fbase) < FB ? (hi - fbase) : FB;
-    if (live) {
+    if (live && !wide) {
+      const int2* xs = s_xy + xi;
+      const int2* ys = s_xy + yi;
+      int sr = 0, si = 0;
+#pragma unroll 4
+      for (unsigned fl = 0; fl < nf; ++fl) {
+        const int2 x = xs[fl * row], y = ys[fl * row];
+        sr += x.x * y.x + x.y * y.y;
+        si += x.y * y.x - x.x * y.y;
+      }
+      are += sr;
+      aim += si;
+    } else if (live) {
       const int2* xs = s_xy + xi;
       const int2* ys = s_xy + yi;
       // X * conj(Y) through the operand-swap wiring (covar_model.hpp:137-145)
@@ -385,7 +440,7 @@ void launch_cov(const CovParams& p, cudaStream_t s) {
   }
   const unsigned nth = ((BT * QB + 31u) / 32u) * 32u;
   unsigned FB = (kCovPre * nth) / (BT * p.S);
-  if (FB > 32u) FB = 32u;
+  if (FB > 32u) FB = 32u;  // (k_cov_block's int32 batch bound assumes <= 32)
   if (FB < 1u) FB = 1u;
   const int mode = !p.exact ? 2 : (p.exp_mode ? 1 : 0);
   // segments: the open window, every whole window, the trailing partial one

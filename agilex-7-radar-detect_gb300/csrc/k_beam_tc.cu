@@ -245,210 +245,6 @@ __global__ void __launch_bounds__(256, 2) k_beam_tc(BeamParams p) {
   }
 }
 
-// ---- tcgen05 form ----------------------------------------------------------
-// The same limb-split GEMM on the 5th-generation tensor cores. A CTA owns 128
-// ring rows (M = 128, one TMEM lane per row) and loops over groups of 16
-// beams (N = 96 class columns, column 6 b + class). The rows are converted
-// once into fp16 limb words in shared memory in the canonical K-major layout
-// (8-row x 16-byte core matrices: row r, k-chunk j at (r / 8) sbo + 128 j +
-// 16 (r % 8)); each group's weight operand, stored in that layout by the
-// host, arrives by a TMA bulk copy; one thread issues the Kp / 16 MMAs
-// (fp32 accumulators in TMEM) and commits them to an mbarrier; then the 256
-// threads read the accumulators back (warp w: TMEM lanes 32 (w % 4) .. + 31,
-// columns 48 (w / 4) .. + 47 = 8 beams) and finish the outputs. Every wait is
-// bounded; a wait that gives up sets DevStats::tc_timeout.
-constexpr unsigned k5Rows = 128u, k5Cols = 96u;
-
-uint32_t beam_tc5_operand_bytes(uint32_t C, uint32_t B) {
-  const uint32_t Kp = 4u * ((C + 3u) & ~3u), G = (B + 15u) / 16u;
-  return G * k5Cols * Kp * 2u;
-}
-
-void beam_tc5_operand(const uint32_t* w, uint32_t C, uint32_t B, uint16_t* out) {
-  const uint32_t Kp = 4u * ((C + 3u) & ~3u), G = (B + 15u) / 16u;
-  const size_t sbo = 16u * Kp / 2u;  // elements per 8-row group
-  for (uint32_t g = 0; g < G; ++g) {
-    uint16_t* o = out + (size_t)g * k5Cols * Kp;
-    for (uint32_t n = 0; n < k5Cols; ++n)
-      for (uint32_t k = 0; k < Kp; ++k) {
-        const uint32_t b = g * 16u + n / 6u;
-        o[(n / 8u) * sbo + (k / 8u) * 64u + (n % 8u) * 8u + (k % 8u)] =
-            host_f16(wprime(w, C, B, b, k, (int)(n % 6u)));
-      }
-  }
-}
-
-size_t beam_tc5_smem(uint32_t C) {
-  const size_t Kp = 4u * ((C + 3u) & ~3u);
-  const size_t need = (k5Rows + k5Cols) * Kp * 2u + 64u;
-  // at least a quarter of an SM's shared memory, so that at most four CTAs
-  // (4 x 128 TMEM columns = all 512) share an SM and an allocation never waits
-  return need > 58u * 1024u ? need : 58u * 1024u;
-}
-
-__global__ void __launch_bounds__(256) k_beam_tc5(BeamParams p) {
-  extern __shared__ __align__(128) uint8_t sm5[];
-  __shared__ unsigned s_err;
-  const unsigned C = p.C, B = p.B, N = p.N;
-  const unsigned Cp = (C + 3u) & ~3u, Kp = 4u * Cp;
-  const uint32_t sbo = 16u * Kp;                   // bytes per 8-row group
-  uint8_t* sA = sm5;                               // 128 rows
-  uint8_t* sB = sA + (size_t)k5Rows * Kp * 2u;     // 96 rows
-  uint64_t* mb = reinterpret_cast<uint64_t*>(sB + (size_t)k5Cols * Kp * 2u);  // [2]
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(mb + 2);
-  const unsigned tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
-  const uint64_t rows = (uint64_t)p.F * N;
-  const uint64_t r0 = (uint64_t)blockIdx.x * k5Rows;
-  // row r of the chunk is (frame r >> lgN, bin r & (N - 1)): N is a power of two
-  const unsigned lgN = 31u - (unsigned)__clz(N);
-  if (tid == 0) {
-    mbar_init(&mb[0], 1);
-    mbar_init(&mb[1], 1);
-    s_err = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  // tcgen05.alloc / ld / dealloc are warp-collective (.sync.aligned): every
-  // one is preceded by an explicit reconvergence of the warp
-  __syncwarp();
-  if (warp == 0) tmem_alloc(tslot, 128);
-  // A operand: 16-byte chunk (row, channel pair j) at its canonical place;
-  // eight consecutive threads fill one 128-byte core matrix
-  const unsigned pairs = Cp / 2u;
-  const bool even = (C & 1u) == 0u;
-  for (unsigned it = tid; it < k5Rows * pairs; it += 256u) {
-    const unsigned rg = it / (8u * pairs), rem = it - rg * 8u * pairs;
-    const unsigned j = rem >> 3, rr = rem & 7u, row = rg * 8u + rr;
-    const uint64_t r = r0 + row;
-    uint32_t v0 = 0, v1 = 0;
-    const unsigned a = 2u * j;
-    if (r < rows && a < C) {
-      unsigned slot = p.ring_base + (unsigned)(r >> lgN);
-      if (slot >= p.ring_frames) slot -= p.ring_frames;
-      const uint32_t* src = p.ring + (((size_t)slot << lgN) + (r & (N - 1u))) * C + a;
-      if (even) {
-        const uint2 t = *reinterpret_cast<const uint2*>(src);
-        v0 = t.x, v1 = t.y;
-      } else {
-        v0 = src[0];
-        if (a + 1u < C) v1 = src[1];
-      }
-    }
-    uint4 w;
-    limb_words(v0, w.x, w.y);
-    limb_words(v1, w.z, w.w);
-    *reinterpret_cast<uint4*>(sA + (size_t)rg * sbo + 128u * j + 16u * rr) = w;
-  }
-  fence_async_smem();
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = *tslot;
-  const unsigned G = (B + 15u) / 16u;
-  const uint32_t idesc = umma_idesc_f16(k5Rows, k5Cols);
-  const uint32_t gbytes = k5Cols * Kp * 2u;
-  const unsigned quad = warp & 3u, half = warp >> 2;
-  const unsigned row = quad * 32u + lane;
-  const uint64_t r = r0 + row;
-  const bool live = r < rows;
-  const uint64_t f = r >> lgN, bin = r & (N - 1u);
-  unsigned fl_any = 0;
-  unsigned long long nsat = 0;
-  for (unsigned g = 0; g < G; ++g) {
-    if (tid == 0) {
-      bulk_g2s(sB, reinterpret_cast<const uint8_t*>(p.w_tc5) + (size_t)g * gbytes, gbytes, &mb[0]);
-      if (!mbar_wait(&mb[0], g & 1u)) {
-        s_err = 1;
-      } else {
-        tc_fence_after();
-        // one K = 16 step is two core matrices (256 bytes, 16 in the
-        // descriptor's address field) further along K in both operands
-        uint64_t da = umma_desc(smem_u32(sA), 128u, sbo), db = umma_desc(smem_u32(sB), 128u, sbo);
-        for (unsigned kk = 0; kk < Kp / 16u; ++kk, da += 16u, db += 16u)
-          umma_f16(tmem, da, db, idesc, kk > 0u);
-        umma_commit(&mb[1]);
-      }
-    }
-    __syncthreads();
-    // every thread observes the MMAs' completion itself (an acquire of the
-    // accumulators for its own TMEM reads); __all_sync then reconverges the
-    // warp before the warp-collective loads and makes the verdict uniform
-    bool ok = s_err == 0u;
-    if (ok) ok = mbar_wait(&mb[1], g & 1u);
-    ok = __all_sync(0xffffffffu, ok);
-    tc_fence_after();
-    if (ok) {
-      float v[48];
-      const uint32_t ta = tmem + ((quad * 32u) << 16) + 48u * half;
-      tmem_ld16(ta, *reinterpret_cast<float(*)[16]>(v));
-      tmem_ld16(ta + 16u, *reinterpret_cast<float(*)[16]>(v + 16));
-      tmem_ld16(ta + 32u, *reinterpret_cast<float(*)[16]>(v + 32));
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const unsigned b = g * 16u + half * 8u + (unsigned)i;
-        if (!live || b >= B) continue;
-        const long long re_v = fold3(v[6 * i], v[6 * i + 1], v[6 * i + 2]);
-        const long long im_v = fold3(v[6 * i + 3], v[6 * i + 4], v[6 * i + 5]);
-        unsigned fr = 0, fi = 0;
-        const int32_t yr = q15_out64(re_v, &fr), yi = q15_out64(im_v, &fi);
-        if (fr | fi) {
-          fl_any |= fr | fi;
-          ++nsat;
-        }
-        cplx y;
-        y.re = (int16_t)yr;
-        y.im = (int16_t)yi;
-        if (p.power) p.power[(f * B + b) * N + bin] = power_u32(y);
-        if (p.beams_bn) p.beams_bn[(f * N + bin) * B + b] = pack(y);
-        if (p.y_rows) p.y_rows[r * B + b] = pack(y);
-        if (p.acc_rows) {
-          p.acc_rows[(r * B + b) * 2] = re_v;
-          p.acc_rows[(r * B + b) * 2 + 1] = im_v;
-        }
-        if (p.flag_rows) p.flag_rows[r * B + b] = (uint8_t)((fr << 2) | fi);
-      }
-    } else if (tid == 0 && p.stats) {
-      atomicOr(&p.stats->tc_timeout, 1u);
-    }
-    tc_fence_before();
-    __syncthreads();  // TMEM and the B buffer are free for the next group
-    tc_fence_after();
-    if (s_err || !ok) {
-      // a wait gave up: wait once more (bounded) for this CTA's own copy and
-      // MMAs in flight before the shared memory and TMEM are given back
-      if (tid == 0) {
-        mbar_wait(&mb[0], g & 1u);
-        if (!s_err) mbar_wait(&mb[1], g & 1u);
-      }
-      __syncthreads();
-      break;
-    }
-  }
-  const unsigned a = __reduce_or_sync(0xffffffffu, fl_any);
-  for (int o = 16; o > 0; o >>= 1) nsat += __shfl_xor_sync(0xffffffffu, nsat, o);
-  if (lane == 0u && p.stats) {
-    if (a) atomicOr(&p.stats->bf_flags, a);
-    if (nsat) atomicAdd(&p.stats->bf_sat, nsat);
-  }
-  __syncwarp();
-  if (warp == 0) tmem_dealloc(tmem, 128);
-}
-
-static std::atomic<bool> g_tc5_attr[64];
-
-void launch_beam_tc5(const BeamParams& p, cudaStream_t s) {
-  const uint64_t rows = (uint64_t)p.F * p.N;
-  if (!rows) return;
-  const size_t smem = beam_tc5_smem(p.C);
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64 || !g_tc5_attr[dev].load()) {
-    cudaFuncSetAttribute(k_beam_tc5, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)beam_tc5_smem(RD_TC_MAX_CHAN));
-    if (dev >= 0 && dev < 64) g_tc5_attr[dev].store(true);
-  }
-  k_beam_tc5<<<(unsigned)((rows + k5Rows - 1u) / k5Rows), 256, smem, s>>>(p);
-}
-
 size_t beam_tc_smem(uint32_t C) {
   const size_t S = 8u * ((C + 3u) / 4u) + 4u;
   return (kTcRows * S + 4u * kTcRows) * sizeof(uint32_t);

@@ -25,7 +25,6 @@ struct DevStats {
   unsigned long long events_total;   // events emitted so far (packet seq base)
   unsigned long long events_call;    // events of the current call
   unsigned long long scan_scratch[4];
-  unsigned tc_timeout;               // a bounded tensor-core wait gave up
 };
 
 // ---- front end: PFB + FFT + corner turn into the spectrum ring ------------
@@ -84,25 +83,20 @@ struct BeamParams {
   uint64_t g0;
   const uint32_t* weights;  // [B][C]
   const int4* w_limbs;      // [B][C] {wh.re, wh.im, wl.re, wl.im}, w = 256 wh + wl
-  const uint32_t* w_frag;   // warp-MMA tensor form: beam_tc_fragments() of the weights
-  const uint32_t* w_tc5;    // tcgen05 tensor form: beam_tc5_operand() of the weights
+  const uint32_t* w_frag;   // tensor form: beam_tc_fragments() of the weights
   uint32_t* power;          // [F][B][N] (or null)
   uint32_t* beams_bn;       // [F][N][B] beam samples (null unless needed)
   uint32_t* y_rows;         // per-block entry: [rows][B] y, acc, flags (or null)
   long long* acc_rows;
   uint8_t* flag_rows;
   uint32_t F, C, N, B;
+  uint32_t x_safe;          // spectrum tiles within this magnitude sum exactly in int32
   DevStats* stats;          // may be null
 };
 void launch_beam(const BeamParams& p, cudaStream_t s);
 // Tensor-core form (k_beam_tc.cu): mma fragments of the limb-split weights.
 void launch_beam_tc(const BeamParams& p, cudaStream_t s);
 uint32_t beam_tc_fragment_words(uint32_t C, uint32_t B);
-// tcgen05 form (k_beam_tc.cu): the weight operand in the canonical layout
-void launch_beam_tc5(const BeamParams& p, cudaStream_t s);
-uint32_t beam_tc5_operand_bytes(uint32_t C, uint32_t B);
-void beam_tc5_operand(const uint32_t* w, uint32_t C, uint32_t B, uint16_t* out);
-size_t beam_tc5_smem(uint32_t C);
 size_t beam_tc_smem(uint32_t C);
 void beam_tc_fragments(const uint32_t* w, uint32_t C, uint32_t B, uint32_t* out);
 

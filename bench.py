@@ -44,7 +44,7 @@ def args_():
     ap.add_argument("--workload", default="medium")
     ap.add_argument("--cpis", type=int, default=None, help="CPIs per step (default: the workload's)")
     ap.add_argument("--max-frames", type=int, default=1024)
-    ap.add_argument("--form", choices=["cuda_core", "tensor", "tensor_sync"], default="cuda_core")
+    ap.add_argument("--form", choices=["cuda_core", "tensor"], default="cuda_core")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-patterns", action="store_true",
@@ -214,8 +214,7 @@ def run_forms(torch, a, stream) -> dict:
         coeff = sc.coefficients(p.n_fft, p.taps)
         w = sc.steering_weights(p.n_chan, p.n_beams)
         r = {"samples_per_step": p.n_chan * n}
-        for name, form in (("cuda_core", abi.RD_FORM_CUDA_CORE), ("tensor", abi.RD_FORM_TENSOR),
-                           ("tensor_sync", abi.RD_FORM_TENSOR_SYNC)):
+        for name, form in (("cuda_core", abi.RD_FORM_CUDA_CORE), ("tensor", abi.RD_FORM_TENSOR)):
             ch = gc.Chain(sc.make_config(p, max_frames=1024, form=form), coeff, w,
                           sc.pair_table(p))
             ms, ks = time_chain(torch, ch, dev, n, stream, steps=3, warmup=3)
@@ -229,11 +228,8 @@ def run_forms(torch, a, stream) -> dict:
                                       (tc["k_beam_us"] + tc["k_cov_us"]), 3)
         out[wl] = r
         del dev
-    out["note"] = ("tensor forms: int16 samples and weights split into 8-bit limbs held exactly "
-                   "in fp16, fp32 accumulation below 2^24, int64 recombine; 'tensor' runs the "
-                   "beamformer on tcgen05 (TMEM accumulators, TMA bulk weight loads), "
-                   "'tensor_sync' on warp-level mma.sync; the exact covariance runs on "
-                   "mma.sync in both; "
+    out["note"] = ("tensor form: int16 samples and weights split into 8-bit limbs held exactly "
+                   "in fp16, mma.sync with fp32 accumulation below 2^24, int64 recombine; "
                    "per-launch stage times from CUDA events; inputs: one 65536-sample seeded "
                    "block per channel repeated")
     return out
@@ -421,8 +417,7 @@ def run_gpu(a, rank: int, world: int, local: int) -> None:
     p = sc.preset(a.workload)
     cpis = a.cpis or p.n_cpi
     n = cpis * p.cpi_samples
-    form = {"tensor": abi.RD_FORM_TENSOR, "tensor_sync": abi.RD_FORM_TENSOR_SYNC}.get(
-        a.form, abi.RD_FORM_CUDA_CORE)
+    form = abi.RD_FORM_TENSOR if a.form == "tensor" else abi.RD_FORM_CUDA_CORE
     cfg = sc.make_config(p, max_frames=a.max_frames, form=form)
     pairs = sc.pair_table(p)
     coeff = sc.coefficients(p.n_fft, p.taps)
