@@ -1119,6 +1119,39 @@ rd_status rd_chain_stats(const rd_chain* ch, rd_stats* st) {
   return RD_OK;
 }
 
+rd_status rd_chain_doppler(rd_chain* ch, uint32_t n_frames, uint32_t scale_sched,
+                           rd_cplx16* out, uint8_t* stage_flags) {
+  if (!ch || !out) return fail(RD_EINVAL, "null argument");
+  const rd_config& c = ch->cfg;
+  if (!is_pow2(n_frames) || n_frames < 8 || n_frames > 1024)
+    return fail(RD_EINVAL, "n_frames %u must be a power of two in 8..1024", n_frames);
+  if (n_frames > ch->frame || n_frames > ch->R)
+    return fail(RD_EINVAL, "%u frames requested, %llu processed, %u held in the ring", n_frames,
+                (unsigned long long)ch->frame, ch->R);
+  const uint32_t N = c.n_fft, C = c.n_chan;
+  const size_t n = (size_t)C * N * n_frames;
+  const unsigned stages = clog2(n_frames);
+  Scratch sc;
+  uint32_t *dv, *dbins, *dtw;
+  uint8_t* dsf = nullptr;
+  CK(sc.alloc(&dv, n));
+  CK(sc.alloc(&dbins, n));
+  if (stage_flags) CK(sc.alloc(&dsf, (size_t)C * N * stages));
+  std::vector<uint32_t> tp(5u * n_frames);
+  uint32_t words = 0;
+  twiddle_positions(n_frames, 1, tp.data(), &words);
+  CK(sc.alloc(&dtw, words ? words : 1));
+  if (words) CK(cudaMemcpy(dtw, tp.data(), words * 4, cudaMemcpyHostToDevice));
+  CK(cudaStreamSynchronize(ch->stream));
+  launch_doppler_gather(ch->ring.p, ch->R, ch->frame - n_frames, N, C, n_frames, dv, ch->stream);
+  launch_fft_block(n_frames, 1, scale_sched, 1, dtw, dv, C * N, nullptr, dbins, dsf, ch->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ch->stream));
+  CK(cudaMemcpy(out, dbins, n * 4, cudaMemcpyDeviceToHost));
+  if (stage_flags) CK(cudaMemcpy(stage_flags, dsf, (size_t)C * N * stages, cudaMemcpyDeviceToHost));
+  return RD_OK;
+}
+
 rd_status rd_chain_read_history(rd_chain* ch, uint32_t bin, uint32_t frame_off, rd_cplx16* vec,
                                 uint32_t* frame_id, uint32_t* flags) {
   if (!ch || !vec || !frame_id || !flags) return fail(RD_EINVAL, "null argument");

@@ -450,4 +450,24 @@ void launch_fft_block(uint32_t n, uint32_t spc, uint32_t sched, int reorder,
                                       stage_flags);
 }
 
+// Slow-time vectors for the Doppler transform: out[(c * N + bin) * H + k] is
+// channel c, bin `bin` of stream frame g_first + k, read from the ring.
+__global__ void k_doppler_gather(const uint32_t* ring, uint32_t R, uint64_t g_first, uint32_t N,
+                                 uint32_t C, uint32_t H, uint32_t* out) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t total = (uint64_t)C * N * H;
+  if (i >= total) return;
+  const uint64_t v = i / H;
+  const uint32_t k = (uint32_t)(i - v * H);
+  const uint32_t c = (uint32_t)(v / N), bin = (uint32_t)(v - (uint64_t)c * N);
+  const uint64_t slot = (g_first + k) % R;
+  out[i] = ring[(slot * N + bin) * C + c];
+}
+
+void launch_doppler_gather(const uint32_t* ring, uint32_t R, uint64_t g_first, uint32_t N,
+                           uint32_t C, uint32_t H, uint32_t* out, cudaStream_t s) {
+  const uint64_t total = (uint64_t)C * N * H;
+  if (total) k_doppler_gather<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(ring, R, g_first, N, C, H, out);
+}
+
 }  // namespace rd

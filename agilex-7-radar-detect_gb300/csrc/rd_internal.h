@@ -185,6 +185,11 @@ void launch_fxp(const uint32_t* op, const int64_t* a, const int64_t* b, const ui
 // Records a formatted message for rd_last_error() and returns st (api.cu).
 rd_status set_error(rd_status st, const char* fmt, ...);
 
+// Slow-time vectors [C][N][H] of the last H ring frames from stream frame
+// g_first on (k_frontend.cu)
+void launch_doppler_gather(const uint32_t* ring, uint32_t R, uint64_t g_first, uint32_t N,
+                           uint32_t C, uint32_t H, uint32_t* out, cudaStream_t s);
+
 // Q1.15 twiddle table in device global memory (k_frontend.cu)
 const uint32_t* twiddles_device();
 

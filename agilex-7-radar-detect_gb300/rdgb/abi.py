@@ -175,6 +175,7 @@ def declare_rd(lib) -> None:
     _proto(lib, "rd_chain_stats", I32, [VP, P(RdStats)])
     _proto(lib, "rd_chain_read_history", I32, [VP, U32, U32, VP, P(U32), P(U32)])
     _proto(lib, "rd_chain_reset", I32, [VP, VP])
+    _proto(lib, "rd_chain_doppler", I32, [VP, U32, U32, VP, VP])
     _proto(lib, "rd_chain_set_launch_frames", I32, [VP, U32])
     _proto(lib, "rd_chain_footprint", U64, [P(RdConfig), U64])
     _proto(lib, "rd_batch_create", I32, [U32, P(RdConfig), VP, VP, P(RdBatchOptions), P(VP)])
@@ -213,7 +214,7 @@ EXPORTED = [
     "rd_chain_set_weights", "rd_chain_set_pairs", "rd_chain_process",
     "rd_chain_process_device", "rd_chain_fetch", "rd_chain_last_launches",
     "rd_chain_flush_cov", "rd_chain_set_profiling", "rd_chain_kernel_times", "rd_chain_stats",
-    "rd_chain_reset", "rd_chain_set_launch_frames", "rd_chain_footprint",
+    "rd_chain_reset", "rd_chain_set_launch_frames", "rd_chain_footprint", "rd_chain_doppler",
     "rd_batch_create", "rd_batch_destroy", "rd_batch_run", "rd_batch_run_sequential",
     "rd_batch_fetch", "rd_batch_tune", "rd_server_create", "rd_server_destroy", "rd_stream_open",
     "rd_stream_close", "rd_server_submit", "rd_server_poll", "rd_server_take",

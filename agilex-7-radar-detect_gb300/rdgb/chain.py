@@ -137,6 +137,18 @@ class Chain:
         abi.check(self.L, self.L.rd_chain_stats(self.h, C.byref(s)), "rd_chain_stats")
         return s.as_dict()
 
+    def doppler(self, n_frames: int, scale_sched: int = 0xFFFFFFFF):
+        """(map, stage_flags): map [n_chan][n_fft][n_frames] packed Q1.15, the
+        slow-time transform of every (channel, bin) over the newest n_frames
+        frames (rd_chain_doppler)."""
+        C, N = self.cfg.n_chan, self.cfg.n_fft
+        out = np.zeros((C, N, n_frames), np.uint32)
+        st = int(np.log2(n_frames))
+        fl = np.zeros((C * N, st), np.uint8)
+        abi.check(self.L, self.L.rd_chain_doppler(self.h, n_frames, scale_sched, ptr(out),
+                                                  ptr(fl)), "rd_chain_doppler")
+        return out, fl
+
     def read_history(self, bin_: int, frame_off: int):
         vec = np.zeros(self.cfg.n_chan, np.uint32)
         fid, fl = C.c_uint32(0), C.c_uint32(0)

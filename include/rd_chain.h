@@ -241,6 +241,19 @@ rd_status rd_chain_set_launch_frames(rd_chain* ch, uint32_t frames);
  * buffers of calls of `frames_per_call` frames (admission by HBM budget). */
 uint64_t rd_chain_footprint(const rd_config* cfg, uint64_t frames_per_call);
 
+/* Range-Doppler map: for every (channel, bin), the slow-time transform of
+ * that bin over the newest n_frames frames of the history ring (the map
+ * model/python/range_doppler.py:254-266 computes in floating point; here the
+ * chain's own fixed-point R2^2 transform, fft::transform of
+ * fft_ref.hpp:409-412 with spc 1, natural output order and the given scaling
+ * schedule). out: [n_chan][n_fft][n_frames], Doppler bin k of channel c, range
+ * bin r at (c * n_fft + r) * n_frames + k (no fftshift); stage_flags:
+ * [n_chan * n_fft][log2 n_frames] or NULL. n_frames: a power of two in 8..1024,
+ * at most the frames processed and the frames the ring holds
+ * (max_frames + hist_frames). No counterpart in the C++ model. */
+rd_status rd_chain_doppler(rd_chain* ch, uint32_t n_frames, uint32_t scale_sched,
+                           rd_cplx16* out, uint8_t* stage_flags);
+
 /* hist::Model::read (history_model.hpp:283-337): the antenna vector of
  * natural bin `bin`, `frame_off` frames back from the newest complete one. */
 rd_status rd_chain_read_history(rd_chain* ch, uint32_t bin, uint32_t frame_off,
