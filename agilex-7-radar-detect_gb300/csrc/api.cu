@@ -1421,3 +1421,15 @@ rd_status rd_fxp_apply(const uint32_t* op, const int64_t* a, const int64_t* b, c
 }
 
 }  // extern "C"
+
+rd_egress_source rd::chain_egress_source(const rd_chain* ch) {
+  rd_egress_source e{};
+  e.flits = ch->flits.p;
+  e.count_dev = (const uint64_t*)&ch->stats.p->scan_scratch[0];  // set by k_call_end
+  e.n_packets = ch->flits.p ? ch->call_cap_events : 0;
+  e.dest = ch->cfg.dest;
+  return e;
+}
+
+uint32_t rd::chain_packet_w(const rd_chain* ch) { return ch->cfg.packet_w; }
+

@@ -281,3 +281,19 @@ rd_status rd_batch_tune(rd_batch* b, const rd_cplx16* const* adc_dev, const uint
   if (best_ms) *best_ms = best_t;
   return RD_OK;
 }
+
+rd_status rd_batch_egress(rd_batch* b, uint32_t n_ports, uint32_t* ring_dev, uint64_t cap_per_port,
+                          uint32_t* src_of_dev, uint64_t* port_count_dev, void* stream) {
+  if (!b) return rd::set_error(RD_EINVAL, "rd_batch_egress: bad argument");
+  if (!b->last) return rd::set_error(RD_EINVAL, "rd_batch_egress: the batch has not run");
+  const uint32_t n = (uint32_t)b->chains.size();
+  std::vector<rd_egress_source> src(n);
+  const uint32_t pw = rd::chain_packet_w(b->chains[0]);
+  for (uint32_t i = 0; i < n; ++i) {
+    if (rd::chain_packet_w(b->chains[i]) != pw)
+      return rd::set_error(RD_EINVAL, "rd_batch_egress: scenario %u has another packet width", i);
+    src[i] = rd::chain_egress_source(b->chains[i]);
+  }
+  return rd::egress_merge(src.data(), n, pw, n_ports, ring_dev, cap_per_port, src_of_dev,
+                          port_count_dev, stream ? (cudaStream_t)stream : cudaStreamLegacy);
+}

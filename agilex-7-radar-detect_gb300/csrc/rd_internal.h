@@ -190,6 +190,17 @@ rd_status set_error(rd_status st, const char* fmt, ...);
 void launch_doppler_gather(const uint32_t* ring, uint32_t R, uint64_t g_first, uint32_t N,
                            uint32_t C, uint32_t H, uint32_t* out, cudaStream_t s);
 
+// The packets of the chain's last call as an egress source: its flit
+// buffer, the device count of the call's events (capped at the buffer) and
+// its configured destination port (api.cu)
+rd_egress_source chain_egress_source(const rd_chain* ch);
+uint32_t chain_packet_w(const rd_chain* ch);
+
+// rd_egress_merge on a stream (fabric.cu)
+rd_status egress_merge(const rd_egress_source* src, uint32_t n_src, uint32_t packet_w,
+                       uint32_t n_ports, uint32_t* ring_dev, uint64_t cap_per_port,
+                       uint32_t* src_of_dev, uint64_t* port_count_dev, cudaStream_t st);
+
 // Q1.15 twiddle table in device global memory (k_frontend.cu)
 const uint32_t* twiddles_device();
 

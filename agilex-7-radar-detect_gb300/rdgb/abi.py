@@ -142,6 +142,14 @@ class RdServerInfo(C.Structure):
                 ("inflight", C.c_uint32), ("queued", C.c_uint32)]
 
 
+class RdEgressSource(C.Structure):
+    _fields_ = [("flits", C.c_void_p), ("count_dev", C.c_void_p), ("n_packets", C.c_uint64),
+                ("dest", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+RD_EGRESS_MAX_SRC = 512
+
+
 def _proto(lib, name, res, args):
     f = getattr(lib, name)
     f.restype = res
@@ -175,6 +183,9 @@ def declare_rd(lib) -> None:
     _proto(lib, "rd_chain_stats", I32, [VP, P(RdStats)])
     _proto(lib, "rd_chain_read_history", I32, [VP, U32, U32, VP, P(U32), P(U32)])
     _proto(lib, "rd_chain_reset", I32, [VP, VP])
+    _proto(lib, "rd_egress_merge", I32, [P(RdEgressSource), U32, U32, U32, VP, U64, VP, VP, VP])
+    _proto(lib, "rd_batch_egress", I32, [VP, U32, VP, U64, VP, VP, VP])
+    _proto(lib, "rd_route_path", I32, [U32, U32, U32, U32, VP])
     _proto(lib, "rd_chain_doppler", I32, [VP, U32, U32, VP, VP])
     _proto(lib, "rd_chain_set_launch_frames", I32, [VP, U32])
     _proto(lib, "rd_chain_footprint", U64, [P(RdConfig), U64])
@@ -215,8 +226,10 @@ EXPORTED = [
     "rd_chain_process_device", "rd_chain_fetch", "rd_chain_last_launches",
     "rd_chain_flush_cov", "rd_chain_set_profiling", "rd_chain_kernel_times", "rd_chain_stats",
     "rd_chain_reset", "rd_chain_set_launch_frames", "rd_chain_footprint", "rd_chain_doppler",
+    "rd_egress_merge", "rd_route_path",
     "rd_batch_create", "rd_batch_destroy", "rd_batch_run", "rd_batch_run_sequential",
-    "rd_batch_fetch", "rd_batch_tune", "rd_server_create", "rd_server_destroy", "rd_stream_open",
+    "rd_batch_fetch", "rd_batch_tune", "rd_batch_egress", "rd_server_create",
+    "rd_server_destroy", "rd_stream_open",
     "rd_stream_close", "rd_server_submit", "rd_server_poll", "rd_server_take",
     "rd_server_info_get", "rd_server_run_trace", "rd_chain_read_history", "rd_pfb_run",
     "rd_fft_run", "rd_bf_run", "rd_power_run", "rd_cross_power_run", "rd_cfar_run", "rd_cfar_run_static",

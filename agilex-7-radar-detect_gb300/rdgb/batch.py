@@ -48,6 +48,15 @@ class Batch:
         abi.check(self.L, self.L.rd_batch_fetch(self.h, i, C.byref(out.c)), "rd_batch_fetch")
         return out.result()
 
+    def egress(self, n_ports: int, ring: int, cap_per_port: int, port_count: int,
+               src_of: int = 0, stream: int = 0) -> None:
+        """rd_batch_egress: the last run's packets, scenario i a source of
+        port cfgs[i].dest, merged into device rings on `stream`."""
+        abi.check(self.L, self.L.rd_batch_egress(self.h, n_ports, C.c_void_p(ring), cap_per_port,
+                                                 C.c_void_p(src_of or None),
+                                                 C.c_void_p(port_count), C.c_void_p(stream)),
+                  "rd_batch_egress")
+
     def close(self) -> None:
         if self.h:
             self.L.rd_batch_destroy(self.h)

@@ -289,6 +289,12 @@ rd_status rd_batch_fetch(rd_batch* b, uint32_t i, rd_output* out);
  * it. */
 rd_status rd_batch_tune(rd_batch* b, const rd_cplx16* const* adc_dev, const uint64_t* n_samples,
                         uint32_t reps, rd_batch_options* chosen, double* best_ms);
+/* The detection packets of the last run, every scenario a source (index i,
+ * port cfgs[i].dest), merged by rd_egress_merge on `stream` - the stream the
+ * run was given, or one ordered after it. Counts are read on the device, so
+ * nothing waits for the run. */
+rd_status rd_batch_egress(rd_batch* b, uint32_t n_ports, uint32_t* ring_dev, uint64_t cap_per_port,
+                          uint32_t* src_of_dev, uint64_t* port_count_dev, void* stream);
 
 /* ---- serving: a request loop over many resident streams -----------------
  * (the submit / poll / stream_open shape of a streaming front end; no
@@ -342,6 +348,39 @@ rd_status rd_server_info_get(rd_server* s, rd_server_info* info);
 rd_status rd_server_run_trace(rd_server* s, uint64_t n_req, const uint32_t* stream_ids,
                               const double* arrival_us, const rd_cplx16* const* adc,
                               const uint64_t* n, double* latency_us, double* makespan_us);
+
+/* ---- packet fabric egress --------------------------------------------------
+ * Many streams' detection packets merged into per-port DMA rings. Each port
+ * is fed by one round-robin arbiter over the sources that target it, the
+ * fabric's arbiter (rtl/packet/pkt_rr_arb.sv: the lowest requesting index at
+ * or after the pointer, the pointer one past the grant): with every source's
+ * packets queued that is cyclic source order, skipping sources that have run
+ * dry, and each source's packets keep their order - the per-(src, VC, dest)
+ * ordering the fabric's scoreboard checks (packet_model.hpp:475-500). No
+ * counterpart in the C++ model, which checks a fabric rather than being one. */
+#define RD_EGRESS_MAX_SRC 512u
+typedef struct rd_egress_source {
+  const uint32_t* flits;      /* device: packets of rd_detection_flits(packet_w)
+                                 flits of rd_flit_words(packet_w) words each */
+  const uint64_t* count_dev;  /* device: packet count, read when the merge runs; or NULL */
+  uint64_t n_packets;         /* the packet count (count_dev NULL), else its upper bound */
+  uint32_t dest;              /* egress port, < n_ports */
+  uint32_t reserved;
+} rd_egress_source;
+
+/* Asynchronous on `stream`: ring_dev [n_ports][cap_per_port] packets,
+ * src_of_dev [n_ports][cap_per_port] source indices (or NULL), and
+ * port_count_dev [n_ports] the packets each port was given - more than
+ * cap_per_port means that port's ring dropped the rest. */
+rd_status rd_egress_merge(const rd_egress_source* src, uint32_t n_src, uint32_t packet_w,
+                          uint32_t n_ports, uint32_t* ring_dev, uint64_t cap_per_port,
+                          uint32_t* src_of_dev, uint64_t* port_count_dev, void* stream);
+
+/* packet_model::route_path (packet_model.hpp:283-309): the wires a packet
+ * from src to dest occupies in a stages-stage radix-radix butterfly, path[0]
+ * = src, stages + 1 entries; the last equals dest (route determinism). */
+rd_status rd_route_path(uint32_t src, uint32_t dest, uint32_t radix, uint32_t stages,
+                        uint32_t* path);
 
 /* ---- per-block entry points (the model/cpp call surface, on the GPU) ---- */
 

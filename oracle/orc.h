@@ -67,6 +67,13 @@ int orc_fxp_apply(const uint32_t* op, const int64_t* a, const int64_t* b,
                   const uint32_t* sh, const uint32_t* w, uint64_t n, int64_t* y,
                   uint8_t* flags);
 /* The 1024-entry Q1.15 twiddle table (fft_twiddle_table.hpp:43). */
+/* liborc_ref.so only: the reference's packet_model::Scoreboard (see
+ * ref_chain.cpp) */
+int orc_ref_scoreboard(uint32_t packet_w, uint32_t radix, uint32_t stages,
+                       const uint32_t* inj, uint64_t n_inj_flits, const uint32_t* obs_port,
+                       const uint32_t* obs, uint64_t n_obs, uint64_t* counts, char* log,
+                       uint64_t log_cap);
+
 void orc_twiddles(uint32_t* out1024);
 const char* orc_name(void);
 

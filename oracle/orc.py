@@ -70,6 +70,9 @@ class Oracle:
         ]:
             f = getattr(L, name)
             f.restype, f.argtypes = res, args
+        if hasattr(L, "orc_ref_scoreboard"):  # the reference leg only
+            L.orc_ref_scoreboard.restype = I32
+            L.orc_ref_scoreboard.argtypes = [U32, U32, U32, VP, U64, VP, VP, U64, VP, VP, U64]
 
     # ---- per block --------------------------------------------------------
     def twiddles(self) -> np.ndarray:
@@ -142,6 +145,24 @@ class Oracle:
         assert self.lib.orc_packetize(abi.ptr(ev), len(ev), packet_w, src, dest, vc, seq0,
                                       abi.ptr(fl)) == 0
         return fl.reshape(len(ev) * nfl, words)
+
+    def scoreboard(self, packet_w, radix, stages, injected, ports, observed):
+        """The reference's packet_model::Scoreboard (liborc_ref.so only):
+        whole packets injected as flit rows, then (port, flit row) observed;
+        returns the counts and the delivery log."""
+        from scoreboard import COUNT_KEYS
+        inj = np.ascontiguousarray(injected, np.uint32)
+        obs = np.ascontiguousarray(observed, np.uint32)
+        words = (packet_w + 5 + 31) // 32
+        pt = np.ascontiguousarray(ports, np.uint32)
+        counts = np.zeros(9, np.uint64)
+        cap = 64 + 32 * (obs.size // words + 1)
+        log = C.create_string_buffer(cap)
+        r = self.lib.orc_ref_scoreboard(packet_w, radix, stages, abi.ptr(inj), inj.size // words,
+                                        abi.ptr(pt), abi.ptr(obs), obs.size // words,
+                                        abi.ptr(counts), log, cap)
+        assert r == 0, r
+        return dict(zip(COUNT_KEYS, map(int, counts))), log.value.decode().split()
 
     def fxp(self, op, a, b, sh, w):
         n = len(op)

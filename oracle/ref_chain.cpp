@@ -20,6 +20,7 @@
 //     run_frame order (the RTL merges beams with pkt_rr_arb, :1600-1611);
 //   * one packet per event on the DMA tap (:1716-1960): dest 0, type
 //     DETECTION, vc 0, src 0, len = detection_flits, per-VC seq counter.
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <string>
@@ -632,6 +633,54 @@ int orc_fxp_apply(const uint32_t* op, const int64_t* a, const int64_t* b,
     flags[i] = static_cast<uint8_t>(r.flags.packed());
   }
   return RD_OK;
+}
+
+// The reference's packet_model::Scoreboard over whole packets injected as
+// flit rows and flits observed at egress ports (ref leg only; it pins the
+// Python restatement of the scoreboard). counts: delivered, lost, duplicated,
+// misrouted, corrupted, reordered, framing, parity, unexpected; log: the
+// delivery log, one entry per line.
+int orc_ref_scoreboard(uint32_t packet_w, uint32_t radix, uint32_t stages,
+                       const uint32_t* inj, uint64_t n_inj_flits, const uint32_t* obs_port,
+                       const uint32_t* obs, uint64_t n_obs, uint64_t* counts, char* log,
+                       uint64_t log_cap) {
+  if (packet_w < 64 || packet_w > 512 || packet_w % 32) return RD_EINVAL;
+  packet_model::Scoreboard sb(packet_w, radix, stages);
+  const unsigned words = rd_flit_words(packet_w);
+  auto flit_at = [&](const uint32_t* rows, uint64_t i) {
+    packet_model::Flit f;
+    f.resize_for(packet_w);
+    for (unsigned k = 0; k < words; ++k) f.w[k] = rows[i * words + k];
+    return f;
+  };
+  for (uint64_t i = 0; i < n_inj_flits;) {
+    packet_model::Packet p;
+    p.hdr = flit_at(inj, i).header();
+    const uint64_t n = p.hdr.length ? p.hdr.length : 1;
+    if (i + n > n_inj_flits) return RD_EINVAL;
+    for (uint64_t k = 1; k < n; ++k) {
+      const packet_model::Flit f = flit_at(inj, i + k);
+      std::vector<std::uint64_t> d;
+      for (unsigned q = 0; q * 64 < packet_w; ++q) d.push_back(f.data64(q));
+      p.payload.push_back(d);
+    }
+    sb.inject(p);
+    i += n;
+  }
+  for (uint64_t i = 0; i < n_obs; ++i) sb.observe(obs_port[i], flit_at(obs, i));
+  sb.finish();
+  const packet_model::Counts& c = sb.counts();
+  const std::size_t v[9] = {c.delivered, c.lost, c.duplicated, c.misrouted, c.corrupted,
+                            c.reordered, c.framing, c.parity, c.unexpected};
+  for (int k = 0; k < 9; ++k) counts[k] = v[k];
+  std::string all;
+  for (const std::string& e : sb.log()) all += e + "\n";
+  if (log && log_cap) {
+    const std::size_t k = std::min<std::size_t>(all.size(), log_cap - 1);
+    std::memcpy(log, all.data(), k);
+    log[k] = 0;
+  }
+  return all.size() < log_cap ? RD_OK : RD_ETRUNC;
 }
 
 // Shared geometry helpers (also exported by the product library).
