@@ -194,8 +194,7 @@ struct rd_chain {
   DevBuf<long long> acc_re, acc_im, cov_out;
   uint32_t acc_cur = 0;
   DevBuf<unsigned> sticky, satcnt, win_flags;
-  DevBuf<uint32_t> counts, detsup, mask;
-  DevBuf<unsigned long long> offsets;
+  DevBuf<unsigned long long> tile_state;  // CFAR look-back, zero between launches
   DevBuf<rd_event> events;
   DevBuf<uint32_t> flits;
   DevBuf<uint32_t> tap_pfb;
@@ -236,8 +235,8 @@ struct rd_chain {
 };
 
 static const char* kKernelNames[8] = {"k_front", "k_tail", "k_beam", "k_cov",
-                                      "k_cfar_decide", "k_cfar_scan", "k_cfar_emit", "k_call"};
-enum { KT_FRONT = 0, KT_TAIL, KT_BEAM, KT_COV, KT_DECIDE, KT_SCAN, KT_EMIT, KT_CALL };
+                                      "k_cfar",  "",       "",       "k_call"};
+enum { KT_FRONT = 0, KT_TAIL, KT_BEAM, KT_COV, KT_CFAR, KT_CALL = 7 };
 
 // Brackets one kernel launch with events on the chain's stream when stage
 // timing is on.
@@ -404,9 +403,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
       (c.form == RD_FORM_TENSOR && bad(ch->w_frag.ensure(beam_tc_fragment_words(C, B)))) ||
       bad(ch->tail[0].ensure((size_t)C * D * N)) || bad(ch->tail[1].ensure((size_t)C * D * N)) ||
       bad(ch->ring.ensure((size_t)ch->R * N * C)) || bad(ch->power.ensure((size_t)F * B * N)) ||
-      bad(ch->counts.ensure((size_t)F * B)) || bad(ch->detsup.ensure((size_t)F * B * 2)) ||
-      bad(ch->mask.ensure((size_t)F * B * ((N + 31) / 32))) ||
-      bad(ch->offsets.ensure((size_t)F * B)) || bad(ch->stats.ensure(1))) {
+      bad(ch->tile_state.ensure(cfar_tiles(F * B))) || bad(ch->stats.ensure(1))) {
     rd_chain_destroy(ch);
     return RD_ENOMEM;
   }
@@ -421,6 +418,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
   cudaMemset(ch->tail[1].p, 0, (size_t)C * D * N * 4);
   cudaMemset(ch->ring.p, 0, (size_t)ch->R * N * C * 4);
   cudaMemset(ch->stats.p, 0, sizeof(DevStats));
+  cudaMemset(ch->tile_state.p, 0, ch->tile_state.n * sizeof(unsigned long long));
   if (c.cov_source != RD_COV_OFF) {
     ch->S = c.cov_source == RD_COV_CHANNEL ? C : B;
     const uint32_t np = rd_cov_pairs(&c);
@@ -476,7 +474,7 @@ void rd_chain_destroy(rd_chain* ch) {
   ch->tw_pos.release(); ch->ct_units.release(); ch->ct_pq.release();
   ch->px.release(); ch->py.release(); ch->acc_re.release(); ch->acc_im.release();
   ch->cov_out.release(); ch->sticky.release(); ch->satcnt.release(); ch->win_flags.release();
-  ch->counts.release(); ch->detsup.release(); ch->mask.release(); ch->offsets.release();
+  ch->tile_state.release();
   ch->events.release(); ch->flits.release(); ch->tap_pfb.release(); ch->stats.release();
   for (const rd_chain::Pending& p : ch->pending) {
     cudaEventDestroy(p.a);
@@ -715,10 +713,9 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   fp2.rl = std::min(c.ref_lead, c.max_ref);
   fp2.rg = std::min(c.ref_lag, c.max_ref);
   fp2.alpha = c.alpha;
-  fp2.counts = ch->counts.p;
-  fp2.detsup = ch->detsup.p;
-  fp2.mask = ch->mask.p;
-  fp2.offsets = ch->offsets.p;
+  fp2.tile_state = ch->tile_state.p;
+  fp2.vec = (N % 4u) == 0;  // cudaMalloc'd power cells: 256-byte aligned
+  fp2.ev16 = 1;
   fp2.events = ch->events.p;
   fp2.cap = ch->call_cap_events;
   fp2.flits = ch->flits.p;
@@ -730,18 +727,10 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   fp2.nfl = rd_detection_flits(c.packet_w);
   fp2.stats = st;
   {
-    KTimer t(ch, KT_DECIDE);
-    launch_cfar_decide(fp2, s);
+    KTimer t(ch, KT_CFAR);
+    launch_cfar(fp2, s);
   }
-  {
-    KTimer t(ch, KT_SCAN);
-    launch_cfar_scan(fp2, s);
-  }
-  {
-    KTimer t(ch, KT_EMIT);
-    launch_cfar_emit(fp2, s);
-  }
-  ch->launches += 3;
+  ch->launches += 1;
 
   // host bookkeeping of the history and align counters, frame by frame
   for (uint32_t f = 0; f < F; ++f) {
@@ -832,6 +821,7 @@ rd_status rd_chain_fetch(rd_chain* ch, rd_output* out) {
   CK(cudaStreamSynchronize(ch->stream));
   DevStats ds;
   CK(cudaMemcpy(&ds, ch->stats.p, sizeof(ds), cudaMemcpyDeviceToHost));
+  if (ds.cfar_fault) return fail(RD_EDEVICE, "CFAR offset look-back timed out");
   const uint64_t n_ev = ds.scan_scratch[0];
   const uint32_t nfl = rd_detection_flits(c.packet_w), words = rd_flit_words(c.packet_w);
   bool trunc = n_ev > ch->call_cap_events;
@@ -1321,27 +1311,24 @@ rd_status rd_cross_power_run(const rd_cplx16* x, const rd_cplx16* y, uint64_t n,
 rd_status rd_cfar_run(const int64_t* cells, uint32_t n, uint32_t frames, const rd_config* cfg,
                       const uint32_t* frame_ids, rd_event* events, uint64_t cap,
                       uint64_t* n_events) {
-  if (!cells || !cfg || !frame_ids || !n_events || n == 0 || n > 4096)
-    return fail(RD_EINVAL, "bad argument (frames of 1..4096 cells)");
+  if (!cells || !cfg || !frame_ids || !n_events || n == 0 || n > 1024)
+    return fail(RD_EINVAL, "bad argument (frames of 1..1024 cells)");
   if (!rd_device_ok()) return fail(RD_EDEVICE, "no usable CUDA device");
   Scratch sc;
   long long* dc;
-  uint32_t *dfid, *dcnt, *dds, *dmask;
-  unsigned long long* doff;
+  uint32_t* dfid;
+  unsigned long long* dtile;
   rd_event* dev = nullptr;
   DevStats* dst;
-  const size_t words = (n + 31) / 32;
   CK(sc.alloc(&dc, (size_t)frames * n));
   CK(sc.alloc(&dfid, frames));
-  CK(sc.alloc(&dcnt, frames));
-  CK(sc.alloc(&dds, (size_t)frames * 2));
-  CK(sc.alloc(&dmask, (size_t)frames * words));
-  CK(sc.alloc(&doff, frames));
+  CK(sc.alloc(&dtile, cfar_tiles(frames)));
   CK(sc.alloc(&dst, 1));
   CK(sc.alloc(&dev, std::max<uint64_t>(cap, 1)));
   CK(cudaMemcpy(dc, cells, (size_t)frames * n * 8, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(dfid, frame_ids, (size_t)frames * 4, cudaMemcpyHostToDevice));
   CK(cudaMemset(dst, 0, sizeof(DevStats)));
+  CK(cudaMemset(dtile, 0, cfar_tiles(frames) * sizeof(unsigned long long)));
   CfarParams p{};
   p.cells_i64 = (const int64_t*)dc;
   p.frames = frames;
@@ -1356,19 +1343,17 @@ rd_status rd_cfar_run(const int64_t* cells, uint32_t n, uint32_t frames, const r
   p.rl = std::min(cfg->ref_lead, cfg->max_ref);
   p.rg = std::min(cfg->ref_lag, cfg->max_ref);
   p.alpha = cfg->alpha;
-  p.counts = dcnt;
-  p.detsup = dds;
-  p.mask = dmask;
-  p.offsets = doff;
+  p.tile_state = dtile;
+  p.vec = (n % 4u) == 0;  // cudaMalloc'd cells: 256-byte aligned
+  p.ev16 = 1;
   p.events = dev;
   p.cap = cap;
   p.stats = dst;
-  launch_cfar_decide(p, 0);
-  launch_cfar_scan(p, 0);
-  launch_cfar_emit(p, 0);
+  launch_cfar(p, 0);
   CK(cudaGetLastError());
   DevStats hs;
   CK(cudaMemcpy(&hs, dst, sizeof(hs), cudaMemcpyDeviceToHost));
+  if (hs.cfar_fault) return fail(RD_EDEVICE, "CFAR offset look-back timed out");
   *n_events = hs.events_call;
   const uint64_t k = std::min<uint64_t>(hs.events_call, cap);
   if (k && events) CK(cudaMemcpy(events, dev, k * sizeof(rd_event), cudaMemcpyDeviceToHost));

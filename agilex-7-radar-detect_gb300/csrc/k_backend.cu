@@ -457,46 +457,92 @@ void launch_cov(const CovParams& p, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------------
-// CFAR (cfar_model.hpp:243-340). One warp per CFAR frame (frame x beam).
-// Pass 1 (decide): prefix sums of the frame's cells in shared memory, the
-// lead/lag reference sums of every cell as prefix differences (the same
-// integers the model's per-cell loops add), the CA or GO decision, and a
-// ballot bitmask of the cells that emit an event. Pass 2 (scan): exclusive
-// offsets of every frame's event count. Pass 3 (emit): each warp rebuilds its
-// frame's sums only when it has events, packs the 176-bit events in bin order
-// followed by the SUMMARY, and writes the packet flits next to them.
+// CFAR (cfar_model.hpp:243-340) in one launch. A CTA takes 8 CFAR frames
+// (frame x beam), one warp each, in the order of a ticket it draws from a
+// device counter (so every lower tile's CTA has already started). A warp
+// loads its frame with 16-byte loads (4 cells a lane), builds the prefix sums
+// in shared memory, decides every cell (the lead/lag reference sums as prefix
+// differences - the same integers the model's loops add) and ballots the
+// cells that emit. The CTA publishes its event total, finds the events of all
+// earlier tiles by decoupled look-back over the tiles' published totals, and
+// then writes its events and packets at that offset: each lane its own cells
+// in bin order, the SUMMARY last. The last CTA to finish records the call's
+// event count and clears the tile states and counters for the next launch.
 // ---------------------------------------------------------------------------
+constexpr unsigned kCfarWarps = 8;
+constexpr unsigned long long kTileAgg = 1ull << 62, kTileIncl = 2ull << 62;
+constexpr unsigned long long kTileVal = (1ull << 62) - 1ull;
+constexpr unsigned kLookbackSpins = 1u << 22;  // ~0.3 s with the back-off below
+
+__device__ __forceinline__ void st_release(unsigned long long* a, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(a), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* a) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(a) : "memory");
+  return v;
+}
+
 __device__ __forceinline__ uint64_t cell_at(const CfarParams& p, uint64_t u, unsigned i) {
   if (p.power_u32) return p.power_u32[u * p.n + i];
   const long long v = p.cells_i64[u * p.n + i];
   return v < 0 ? 0ull : (uint64_t)v;  // clamp_cell (cfar_model.hpp:238-240)
 }
 
-// Inclusive prefix sums pre[1..n] of frame u (pre[0] = 0), warp-cooperative.
-// W >= ceil(n / 32) bounds the rows at compile time, so every row's cells are
-// loaded before the first scan step (the loads overlap instead of each row
-// waiting for its own).
-template <int W>
-__device__ __forceinline__ void warp_prefix(const CfarParams& p, uint64_t u, uint64_t* pre) {
-  const unsigned lane = threadIdx.x & 31u;
-  uint64_t v[W];
-#pragma unroll
-  for (int r = 0; r < W; ++r) {
-    const unsigned i = (unsigned)r * 32u + lane;
-    v[r] = i < p.n ? cell_at(p, u, i) : 0ull;
+// Cells 4 at a time: lane l of row r holds cells 128 r + 4 l .. + 3.
+__device__ __forceinline__ void cells4(const CfarParams& p, uint64_t u, unsigned i0, bool vec,
+                                       uint64_t* c) {
+  if (vec && i0 < p.n) {  // n % 4 == 0: the whole quad is in the frame
+    if (p.power_u32) {
+      const uint4 v = __ldcs(reinterpret_cast<const uint4*>(p.power_u32 + u * p.n + i0));
+      c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
+    } else {
+      const longlong2* q = reinterpret_cast<const longlong2*>(p.cells_i64 + u * p.n + i0);
+      const longlong2 a = __ldcs(q), b = __ldcs(q + 1);
+      c[0] = a.x < 0 ? 0ull : (uint64_t)a.x;
+      c[1] = a.y < 0 ? 0ull : (uint64_t)a.y;
+      c[2] = b.x < 0 ? 0ull : (uint64_t)b.x;
+      c[3] = b.y < 0 ? 0ull : (uint64_t)b.y;
+    }
+    return;
   }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) c[k] = i0 + k < p.n ? cell_at(p, u, i0 + k) : 0ull;
+}
+
+// Inclusive prefix sums pre[1..n] of frame u (pre[0] = 0), warp-cooperative.
+// pre sits one word past a 16-byte boundary, so lane l's pre[4l + 1 .. 4l + 4]
+// are two aligned 16-byte stores. R >= ceil(n / 128) bounds the rows at
+// compile time; every row's cells are loaded before the first scan step.
+template <int R>
+__device__ __forceinline__ void warp_prefix(const CfarParams& p, uint64_t u, uint64_t* pre,
+                                            bool vec) {
+  const unsigned lane = threadIdx.x & 31u;
+  uint64_t c[R][4];
+#pragma unroll
+  for (int r = 0; r < R; ++r) cells4(p, u, (unsigned)r * 128u + lane * 4u, vec, c[r]);
   if (lane == 0) pre[0] = 0;
   uint64_t carry = 0;
 #pragma unroll
-  for (int r = 0; r < W; ++r) {
-    uint64_t x = v[r];
+  for (int r = 0; r < R; ++r) {
+    const uint64_t t0 = c[r][0], t1 = t0 + c[r][1], t2 = t1 + c[r][2], t3 = t2 + c[r][3];
+    uint64_t x = t3;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const uint64_t t = __shfl_up_sync(0xffffffffu, x, o);
       if ((int)lane >= o) x += t;
     }
-    const unsigned i = (unsigned)r * 32u + lane;
-    if (i < p.n) pre[i + 1] = carry + x;
+    const uint64_t b = carry + x - t3;
+    const unsigned i0 = (unsigned)r * 128u + lane * 4u;
+    if (vec && i0 < p.n) {
+      reinterpret_cast<ulonglong2*>(pre + i0 + 1)[0] = make_ulonglong2(b + t0, b + t1);
+      reinterpret_cast<ulonglong2*>(pre + i0 + 3)[0] = make_ulonglong2(b + t2, b + t3);
+    } else {
+      if (i0 < p.n) pre[i0 + 1] = b + t0;
+      if (i0 + 1 < p.n) pre[i0 + 2] = b + t1;
+      if (i0 + 2 < p.n) pre[i0 + 3] = b + t2;
+      if (i0 + 3 < p.n) pre[i0 + 4] = b + t3;
+    }
     carry += __shfl_sync(0xffffffffu, x, 31);
   }
   __syncwarp();
@@ -534,79 +580,6 @@ __device__ __forceinline__ CellDecision decide_cell(const CfarParams& p, const u
   return d;
 }
 
-// Pass 1. One warp per CFAR frame, 4 frames per CTA; the CTA's event total
-// goes to offsets[blockIdx.x] for the scan.
-template <int W>
-__global__ void __launch_bounds__(128) k_cfar_decide(CfarParams p) {
-  extern __shared__ uint64_t s_pre[];
-  __shared__ unsigned s_cnt[4];
-  const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  const uint64_t u = (uint64_t)blockIdx.x * 4u + warp;
-  uint64_t* pre = s_pre + (size_t)warp * (p.n + 1u);
-  unsigned count = 0;
-  if (u < p.frames) {
-    warp_prefix<W>(p, u, pre);
-    const unsigned words = (p.n + 31u) / 32u;
-    unsigned emitted = 0, det = 0, sup = 0;
-#pragma unroll
-    for (int r = 0; r < W; ++r) {
-      const unsigned i = (unsigned)r * 32u + lane;
-      bool em = false;
-      if (i < p.n) {
-        const CellDecision d = decide_cell(p, pre, i, pre[i + 1] - pre[i]);
-        em = d.emit;
-        det += d.detected;
-        sup += !d.evaluable;
-      }
-      const unsigned m = __ballot_sync(0xffffffffu, em);
-      if (lane == 0 && (unsigned)r < words) p.mask[u * words + r] = m;
-      emitted += __popc(m);
-    }
-    det = __reduce_add_sync(0xffffffffu, det);
-    sup = __reduce_add_sync(0xffffffffu, sup);
-    count = emitted + 1u;  // + SUMMARY
-    if (lane == 0) {
-      p.counts[u] = count;
-      p.detsup[2 * u] = det;
-      p.detsup[2 * u + 1] = sup;
-      if (det) atomicAdd(&p.stats->cfar_det, (unsigned long long)det);
-      if (sup) atomicAdd(&p.stats->cfar_sup, (unsigned long long)sup);
-    }
-  }
-  if (lane == 0) s_cnt[warp] = count;
-  __syncthreads();
-  if (threadIdx.x == 0) p.offsets[blockIdx.x] = s_cnt[0] + s_cnt[1] + s_cnt[2] + s_cnt[3];
-}
-
-// Pass 2. Exclusive scan of the CTA totals (in place in offsets), plus the
-// call's running event count; one CTA, a few totals per thread.
-__global__ void __launch_bounds__(1024) k_cfar_scan(CfarParams p) {
-  __shared__ unsigned long long s_part[1024];
-  const unsigned tid = threadIdx.x;
-  const uint64_t nb = ((uint64_t)p.frames + 3u) / 4u;
-  const uint64_t per = (nb + 1023u) / 1024u;
-  const uint64_t lo = tid * per, hi = (lo + per) < nb ? (lo + per) : nb;
-  unsigned long long sum = 0;
-  for (uint64_t i = lo; i < hi; ++i) sum += p.offsets[i];
-  s_part[tid] = sum;
-  __syncthreads();
-  for (unsigned o = 1; o < 1024u; o <<= 1) {
-    const unsigned long long t = tid >= o ? s_part[tid - o] : 0ull;
-    __syncthreads();
-    s_part[tid] += t;
-    __syncthreads();
-  }
-  const unsigned long long base = p.stats->events_call;
-  unsigned long long run = base + s_part[tid] - sum;
-  for (uint64_t i = lo; i < hi; ++i) {
-    const unsigned long long c = p.offsets[i];
-    p.offsets[i] = run;
-    run += c;
-  }
-  __syncthreads();
-  if (tid == 1023u) p.stats->events_call = base + s_part[1023];
-}
-
 __device__ __forceinline__ void set_field(uint64_t* w, unsigned lsb, unsigned n, uint64_t v) {
   v &= (n >= 64) ? ~0ull : ((1ull << n) - 1ull);
   const unsigned wi = lsb >> 6, sh = lsb & 63u;
@@ -639,13 +612,32 @@ __device__ __forceinline__ void make_event(rd_event* e, unsigned kind, unsigned 
   e->framing = (uint8_t)((sof ? 1u : 0u) | (eof ? 2u : 0u));
 }
 
-// 32 bits of the zero-padded 192-bit string w[0..2] starting at signed bit s.
-__device__ __forceinline__ uint32_t ext32(const uint64_t* w, int s) {
+// An event as two 16-byte stores when the buffer allows it (the layout of
+// rd_event: w[3], frame, beam, kind, framing).
+__device__ __forceinline__ void store_event(rd_event* d, const rd_event& e, bool v16) {
+  if (v16) {
+    const unsigned long long tail = (unsigned long long)e.frame |
+                                    ((unsigned long long)e.beam << 32) |
+                                    ((unsigned long long)e.kind << 48) |
+                                    ((unsigned long long)e.framing << 56);
+    ulonglong2* q = reinterpret_cast<ulonglong2*>(d);
+    q[0] = make_ulonglong2(e.w[0], e.w[1]);
+    q[1] = make_ulonglong2(e.w[2], tail);
+  } else {
+    *d = e;
+  }
+}
+
+// 32 bits of the zero-padded 192-bit string {w0, w1, w2} starting at signed
+// bit s (the words picked by selects, so nothing goes to local memory).
+__device__ __forceinline__ uint32_t ext32(uint64_t w0, uint64_t w1, uint64_t w2, int s) {
   if (s >= 192 || s <= -32) return 0u;
-  if (s < 0) return (uint32_t)(w[0] << (-s));
+  if (s < 0) return (uint32_t)(w0 << (-s));
   const int lo = s >> 6, sh = s & 63;
-  uint64_t v = w[lo] >> sh;
-  if (sh && lo < 2) v |= w[lo + 1] << (64 - sh);
+  const uint64_t a = lo == 0 ? w0 : (lo == 1 ? w1 : w2);
+  const uint64_t b = lo == 0 ? w1 : (lo == 1 ? w2 : 0ull);
+  uint64_t v = a >> sh;
+  if (sh) v |= b << (64 - sh);
   return (uint32_t)v;
 }
 
@@ -653,26 +645,26 @@ __device__ __forceinline__ uint32_t ext32(const uint64_t* w, int s) {
 // payload flits carrying the event LS word first (benchmark_sim_top.sv:
 // 1818-1936); flit = data << 5 | eof << 4 | sof << 3 | vc << 1 | odd parity.
 // Each 32-bit flit word is cut from the payload bit string with two shifts.
-__device__ void write_packet(const rd_event* e, uint32_t* out, unsigned pw, unsigned words,
+__device__ void write_packet(const rd_event& e, uint32_t* out, unsigned pw, unsigned words,
                              unsigned nfl, unsigned src, unsigned dest, unsigned vc,
                              unsigned seq) {
-  const uint64_t hdr[3] = {(uint64_t)(dest & 0xFu) | ((uint64_t)(src & 0x1Fu) << 4) |
-                               ((uint64_t)(vc & 3u) << 9) | ((uint64_t)0u << 11) |
-                               ((uint64_t)(nfl & 0x3Fu) << 14) | ((uint64_t)(seq & 0xFFFFu) << 20),
-                           0ull, 0ull};
+  const uint64_t hdr = (uint64_t)(dest & 0xFu) | ((uint64_t)(src & 0x1Fu) << 4) |
+                       ((uint64_t)(vc & 3u) << 9) | ((uint64_t)0u << 11) |
+                       ((uint64_t)(nfl & 0x3Fu) << 14) | ((uint64_t)(seq & 0xFFFFu) << 20);
   const int top = 5 + (int)pw;  // first flit bit past the data
   for (unsigned f = 0; f < nfl; ++f) {
     uint32_t* o = out + (size_t)f * words;
-    const uint64_t* data = f == 0 ? hdr : e->w;
+    const uint64_t w0 = f == 0 ? hdr : e.w[0], w1 = f == 0 ? 0ull : e.w[1],
+                   w2 = f == 0 ? 0ull : e.w[2];
     const int off = f == 0 ? 0 : (int)((f - 1) * pw);
     // payload bits past this flit's slice belong to the next flit
     const int last = f == 0 ? 36 : (off + (int)pw < 176 ? off + (int)pw : 176);
+    const int lim = 5 + (last - off) < top ? 5 + (last - off) : top;  // flit bits in use
     unsigned pop = 0;
     for (unsigned k = 0; k < words; ++k) {
       const int lo = 32 * (int)k;
-      uint32_t v = ext32(data, off + lo - 5);
+      uint32_t v = ext32(w0, w1, w2, off + lo - 5);
       if (lo < 5) v &= ~0x1Fu;
-      const int lim = 5 + (last - off) < top ? 5 + (last - off) : top;  // flit bits in use
       if (lo + 32 > lim) v &= (lim <= lo) ? 0u : ((1u << (lim - lo)) - 1u);
       if (k == 0)
         v |= ((vc & 3u) << 1) | ((f == 0 ? 1u : 0u) << 3) | ((f + 1 == nfl ? 1u : 0u) << 4);
@@ -683,167 +675,180 @@ __device__ void write_packet(const rd_event* e, uint32_t* out, unsigned pw, unsi
   }
 }
 
-// The same packet as write_packet, built by the whole warp: item k of the
-// packet (flit k / words, word k % words) is lane k % 32's, in at most two
-// rounds (1 + ceil(176 / W) flits of ceil((W + 5) / 32) words is at most 34
-// items); each flit's odd-parity bit comes from an XOR reduction of its
-// words' popcounts. `w` is the event (the same on every lane).
-__device__ void warp_write_packet(const uint64_t* w, uint32_t* out, unsigned pw, unsigned words,
-                                  unsigned nfl, unsigned src, unsigned dest, unsigned vc,
-                                  unsigned seq) {
-  const unsigned lane = threadIdx.x & 31u;
-  const uint64_t hdr[3] = {(uint64_t)(dest & 0xFu) | ((uint64_t)(src & 0x1Fu) << 4) |
-                               ((uint64_t)(vc & 3u) << 9) | ((uint64_t)(nfl & 0x3Fu) << 14) |
-                               ((uint64_t)(seq & 0xFFFFu) << 20),
-                           0ull, 0ull};
-  const int top = 5 + (int)pw;
-  const unsigned items = nfl * words;
-  uint32_t val[2] = {0u, 0u};
-  unsigned fl[2] = {0u, 0u};
-  unsigned par = 0;  // bit f: parity of flit f so far
-#pragma unroll
-  for (int rnd = 0; rnd < 2; ++rnd) {
-    const unsigned k = (unsigned)rnd * 32u + lane;
-    uint32_t v = 0;
-    unsigned f = 0;
-    if (k < items) {
-      f = k / words;
-      const unsigned kk = k - f * words;
-      const uint64_t* data = f == 0 ? hdr : w;
-      const int off = f == 0 ? 0 : (int)((f - 1) * pw);
-      const int last = f == 0 ? 36 : (off + (int)pw < 176 ? off + (int)pw : 176);
-      const int lo = 32 * (int)kk;
-      v = ext32(data, off + lo - 5);
-      if (lo < 5) v &= ~0x1Fu;
-      const int lim = 5 + (last - off) < top ? 5 + (last - off) : top;
-      if (lo + 32 > lim) v &= (lim <= lo) ? 0u : ((1u << (lim - lo)) - 1u);
-      if (kk == 0)
-        v |= ((vc & 3u) << 1) | ((f == 0 ? 1u : 0u) << 3) | ((f + 1 == nfl ? 1u : 0u) << 4);
-    }
-    val[rnd] = v;
-    fl[rnd] = f;
-    const unsigned bit = k < items ? ((__popc(v) & 1u) << f) : 0u;
-    par ^= __reduce_xor_sync(0xffffffffu, bit);
+// Events before this CTA's tile, by decoupled look-back: publish the tile's
+// total, then walk back over earlier tiles, adding totals until a tile that
+// already holds its inclusive prefix. A tile that has not published yet
+// belongs to a CTA that started earlier and publishes without waiting on
+// anyone, so the wait ends; it is still bounded, and a wait that runs out
+// sets the fault flag (the host reports it) instead of spinning on.
+__device__ unsigned long long tile_lookback(const CfarParams& p, unsigned tile,
+                                            unsigned long long agg) {
+  unsigned long long* st = p.tile_state;
+  if (tile == 0) {
+    st_release(st, kTileIncl | agg);
+    return 0;
   }
-#pragma unroll
-  for (int rnd = 0; rnd < 2; ++rnd) {
-    const unsigned k = (unsigned)rnd * 32u + lane;
-    if (k < items) {
-      uint32_t v = val[rnd];
-      if (k % words == 0u && ((par >> fl[rnd]) & 1u) == 0u) v |= 1u;
-      out[k] = v;
+  st_release(st + tile, kTileAgg | agg);
+  unsigned long long excl = 0;
+  unsigned spins = 0;
+  for (int t = (int)tile - 1; t >= 0;) {
+    const unsigned long long v = ld_acquire(st + t);
+    if (v & kTileIncl) {
+      excl += v & kTileVal;
+      break;
     }
+    if (v & kTileAgg) {
+      excl += v & kTileVal;
+      --t;
+      continue;
+    }
+    if (++spins > kLookbackSpins) {
+      atomicOr(&p.stats->cfar_fault, 1u);
+      break;
+    }
+    __nanosleep(64);
   }
+  st_release(st + tile, kTileIncl | (excl + agg));
+  return excl;
 }
 
-// Pass 3. Each warp rebuilds its frame's sums only when the frame has
-// detections, and writes its events and packets at the frame's offset: words
-// with few events event by event with the whole warp packing each packet,
-// words with many events one event per lane; the SUMMARY last.
-template <int W>
-__global__ void __launch_bounds__(128) k_cfar_emit(CfarParams p) {
-  extern __shared__ uint64_t s_pre[];
+template <int R>
+__global__ void __launch_bounds__(kCfarWarps * 32) k_cfar(CfarParams p) {
+  extern __shared__ __align__(16) uint64_t s_pre[];
+  __shared__ uint32_t s_mask[kCfarWarps][32];
+  __shared__ unsigned s_cnt[kCfarWarps];
+  __shared__ unsigned long long s_excl, s_base0, s_ds[2];
+  __shared__ unsigned s_tile, s_last;
   const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  const uint64_t u = (uint64_t)blockIdx.x * 4u + warp;
-  uint64_t* pre = s_pre + (size_t)warp * (p.n + 1u);
-  if (u >= p.frames) return;
+  if (threadIdx.x == 0) {
+    s_tile = atomicAdd(&p.stats->cfar_ticket, 1u);
+    s_base0 = *(volatile unsigned long long*)&p.stats->events_call;
+    s_ds[0] = s_ds[1] = 0;
+  }
+  __syncthreads();
+  const unsigned tile = s_tile;
+  const uint64_t u = (uint64_t)tile * kCfarWarps + warp;
+  // pre[0] one word past a 16-byte boundary (n + 2 words a warp, n even)
+  uint64_t* pre = s_pre + (size_t)warp * (p.n + 2u) + 1u;
   const unsigned words = (p.n + 31u) / 32u;
-  const uint32_t cnt = p.counts[u];
-  uint64_t base = p.offsets[blockIdx.x];  // + the events of the CTA's earlier frames
-  for (unsigned k = 0; k < warp; ++k) base += p.counts[(uint64_t)blockIdx.x * 4u + k];
-  const uint64_t frame = p.frame_ids ? p.frame_ids[u] : (p.g0 + u / p.beams);
-  const unsigned fid = p.frame_ids ? p.frame_ids[u] : (unsigned)(frame & 0xFFFFu);
-  const uint16_t beam = (uint16_t)(p.frame_ids ? u : (u % p.beams));
-  const unsigned long long seq0 = p.stats->events_total;
-  const size_t pk = (size_t)p.nfl * p.flit_words;  // words per packet
-  if (cnt > 1u) {
-    warp_prefix<W>(p, u, pre);
+  unsigned count = 0, det = 0, sup = 0;
+  if (u < p.frames) {
+    warp_prefix<R>(p, u, pre, p.vec);
+    unsigned emitted = 0;
+    for (unsigned r = 0; r < words; ++r) {
+      const unsigned i = r * 32u + lane;
+      bool em = false, dt = false, sp = false;
+      if (i < p.n) {
+        const CellDecision d = decide_cell(p, pre, i, pre[i + 1] - pre[i]);
+        em = d.emit;
+        dt = d.detected;
+        sp = !d.evaluable;
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, em);
+      det += __popc(__ballot_sync(0xffffffffu, dt));
+      sup += __popc(__ballot_sync(0xffffffffu, sp));
+      if (lane == 0) s_mask[warp][r] = m;
+      emitted += __popc(m);
+    }
+    count = emitted + 1u;  // + SUMMARY
+  }
+  if (lane == 0) {
+    s_cnt[warp] = count;
+    if (det) atomicAdd(&s_ds[0], (unsigned long long)det);
+    if (sup) atomicAdd(&s_ds[1], (unsigned long long)sup);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long agg = 0;
+    for (unsigned k = 0; k < kCfarWarps; ++k) agg += s_cnt[k];
+    s_excl = tile_lookback(p, tile, agg);
+    if (s_ds[0]) atomicAdd(&p.stats->cfar_det, s_ds[0]);
+    if (s_ds[1]) atomicAdd(&p.stats->cfar_sup, s_ds[1]);
+  }
+  __syncthreads();
+  if (u < p.frames) {
+    uint64_t base = s_base0 + s_excl;
+    for (unsigned k = 0; k < warp; ++k) base += s_cnt[k];
+    const uint64_t frame = p.frame_ids ? p.frame_ids[u] : (p.g0 + u / p.beams);
+    const unsigned fid = p.frame_ids ? p.frame_ids[u] : (unsigned)(frame & 0xFFFFu);
+    const uint16_t beam = (uint16_t)(p.frame_ids ? u : (u % p.beams));
+    const unsigned long long seq0 = p.stats->events_total;
+    const size_t pk = (size_t)p.nfl * p.flit_words;  // words per packet
     unsigned before = 0;
     for (unsigned r = 0; r < words; ++r) {
-      const uint32_t m = p.mask[u * words + r];
-      if (__popc(m) > 4) {  // many events in this word: one per lane
+      const uint32_t m = s_mask[warp][r];
+      if ((m >> lane) & 1u) {
         const unsigned i = r * 32u + lane;
-        if ((m >> lane) & 1u) {
-          const uint64_t cut = pre[i + 1] - pre[i];
-          const CellDecision d = decide_cell(p, pre, i, cut);
-          const uint64_t idx = base + before + __popc(m & ((1u << lane) - 1u));
+        const uint64_t cut = pre[i + 1] - pre[i];
+        const CellDecision d = decide_cell(p, pre, i, cut);
+        const uint64_t idx = base + before + __popc(m & ((1u << lane) - 1u));
+        if (idx < p.cap) {
           const unsigned kind = d.detected ? 0u : (!d.evaluable ? 2u : 1u);
-          if (idx < p.cap) {
-            rd_event ev;
-            make_event(&ev, kind, i, fid, d.evaluable ? d.n : 0u, p.alpha, 0, 0, cut,
-                       d.evaluable ? d.sum : 0ull, idx == base, false, (uint32_t)frame, beam);
-            p.events[idx] = ev;
-            if (p.flits)
-              write_packet(&ev, p.flits + idx * pk, p.packet_w, p.flit_words, p.nfl, p.src_id,
-                           p.dest, p.vc, (unsigned)((seq0 + idx) & 0xFFFFu));
-          }
-        }
-        __syncwarp();
-      } else {  // few events: the warp packs each packet together
-        uint32_t mm = m;
-        unsigned j = 0;
-        while (mm) {
-          const unsigned b = (unsigned)__ffs(mm) - 1u;
-          mm &= mm - 1u;
-          const unsigned i = r * 32u + b;
-          const uint64_t cut = pre[i + 1] - pre[i];
-          const CellDecision d = decide_cell(p, pre, i, cut);
-          const uint64_t idx = base + before + j++;
-          const unsigned kind = d.detected ? 0u : (!d.evaluable ? 2u : 1u);
-          if (idx < p.cap) {
-            rd_event ev;
-            make_event(&ev, kind, i, fid, d.evaluable ? d.n : 0u, p.alpha, 0, 0, cut,
-                       d.evaluable ? d.sum : 0ull, idx == base, false, (uint32_t)frame, beam);
-            if (lane == 0) p.events[idx] = ev;
-            if (p.flits)
-              warp_write_packet(ev.w, p.flits + idx * pk, p.packet_w, p.flit_words, p.nfl,
-                                p.src_id, p.dest, p.vc, (unsigned)((seq0 + idx) & 0xFFFFu));
-          }
+          rd_event ev;
+          make_event(&ev, kind, i, fid, d.evaluable ? d.n : 0u, p.alpha, 0, 0, cut,
+                     d.evaluable ? d.sum : 0ull, idx == base, false, (uint32_t)frame, beam);
+          store_event(p.events + idx, ev, p.ev16);
+          if (p.flits)
+            write_packet(ev, p.flits + idx * pk, p.packet_w, p.flit_words, p.nfl, p.src_id,
+                         p.dest, p.vc, (unsigned)((seq0 + idx) & 0xFFFFu));
         }
       }
       before += __popc(m);
     }
+    const uint64_t idx = base + count - 1u;  // the SUMMARY
+    if (lane == 0 && idx < p.cap) {
+      rd_event ev;
+      make_event(&ev, 3u, p.n, fid, 0, p.alpha, det, sup, 0, 0, count == 1u, true,
+                 (uint32_t)frame, beam);
+      store_event(p.events + idx, ev, p.ev16);
+      if (p.flits)
+        write_packet(ev, p.flits + idx * pk, p.packet_w, p.flit_words, p.nfl, p.src_id,
+                     p.dest, p.vc, (unsigned)((seq0 + idx) & 0xFFFFu));
+    }
   }
-  const uint64_t idx = base + cnt - 1u;  // the SUMMARY
-  if (idx < p.cap) {
-    rd_event ev;
-    make_event(&ev, 3u, p.n, fid, 0, p.alpha, p.detsup[2 * u], p.detsup[2 * u + 1], 0, 0,
-               cnt == 1u, true, (uint32_t)frame, beam);
-    if (lane == 0) p.events[idx] = ev;
-    if (p.flits)
-      warp_write_packet(ev.w, p.flits + idx * pk, p.packet_w, p.flit_words, p.nfl, p.src_id,
-                        p.dest, p.vc, (unsigned)((seq0 + idx) & 0xFFFFu));
+  // the last CTA out: the call's event count, then a clean slate
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(&p.stats->cfar_done, 1u) == gridDim.x - 1u;
+  }
+  __syncthreads();
+  if (s_last) {
+    __threadfence();
+    const unsigned n_tiles = gridDim.x;
+    if (threadIdx.x == 0) {
+      p.stats->events_call = s_base0 + (ld_acquire(p.tile_state + n_tiles - 1) & kTileVal);
+      p.stats->cfar_ticket = 0;
+      p.stats->cfar_done = 0;
+    }
+    for (unsigned t = threadIdx.x; t < n_tiles; t += blockDim.x) p.tile_state[t] = 0;
   }
 }
 
-static size_t cfar_smem(const CfarParams& p) { return 4u * (p.n + 1u) * sizeof(uint64_t); }
-
-// Instantiation by the row bound W of a frame of n cells (n <= 1024 = 32 x 32).
-// Shared memory: 4 frames x (n + 1) x 8 B <= 32.8 KB, under the default limit.
-#define RD_CFAR_DISPATCH(KERNEL, P, S)                                                      \
-  do {                                                                                      \
-    const unsigned w_ = ((P).n + 31u) / 32u;                                                \
-    const dim3 g_((unsigned)(((P).frames + 3u) / 4u));                                      \
-    const size_t sm_ = cfar_smem(P);                                                        \
-    if (w_ <= 1) KERNEL<1><<<g_, 128, sm_, S>>>(P);                                        \
-    else if (w_ <= 2) KERNEL<2><<<g_, 128, sm_, S>>>(P);                                   \
-    else if (w_ <= 4) KERNEL<4><<<g_, 128, sm_, S>>>(P);                                   \
-    else if (w_ <= 8) KERNEL<8><<<g_, 128, sm_, S>>>(P);                                   \
-    else if (w_ <= 16) KERNEL<16><<<g_, 128, sm_, S>>>(P);                                 \
-    else KERNEL<32><<<g_, 128, sm_, S>>>(P);                                               \
-  } while (0)
-
-void launch_cfar_decide(const CfarParams& p, cudaStream_t s) {
-  if (!p.frames) return;
-  RD_CFAR_DISPATCH(k_cfar_decide, p, s);
+// Shared memory: 8 frames x (n + 2) words; n <= 1024 needs the opt-in above
+// 48 KB, set once per instantiation.
+template <int R>
+static void launch_cfar_r(const CfarParams& p, cudaStream_t s) {
+  static bool attr = false;
+  const size_t sm = (size_t)kCfarWarps * (p.n + 2u) * sizeof(uint64_t);
+  if (!attr) {
+    cudaFuncSetAttribute(k_cfar<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)((size_t)kCfarWarps * (128u * R + 2u) * sizeof(uint64_t)));
+    attr = true;
+  }
+  const unsigned tiles = (unsigned)((p.frames + kCfarWarps - 1u) / kCfarWarps);
+  k_cfar<R><<<tiles, kCfarWarps * 32, sm, s>>>(p);
 }
-void launch_cfar_scan(const CfarParams& p, cudaStream_t s) {
+
+unsigned cfar_tiles(uint32_t frames) { return (frames + kCfarWarps - 1u) / kCfarWarps; }
+
+void launch_cfar(const CfarParams& p, cudaStream_t s) {
   if (!p.frames) return;
-  k_cfar_scan<<<1, 1024, 0, s>>>(p);
-}
-void launch_cfar_emit(const CfarParams& p, cudaStream_t s) {
-  if (!p.frames) return;
-  RD_CFAR_DISPATCH(k_cfar_emit, p, s);
+  const unsigned rows = (p.n + 127u) / 128u;
+  if (rows <= 1) launch_cfar_r<1>(p, s);
+  else if (rows <= 2) launch_cfar_r<2>(p, s);
+  else if (rows <= 4) launch_cfar_r<4>(p, s);
+  else launch_cfar_r<8>(p, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -904,7 +909,7 @@ __global__ void k_packetize(const rd_event* ev, uint64_t n, uint32_t pw, uint32_
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const rd_event e = ev[i];
-  write_packet(&e, flits + i * nfl * words, pw, words, nfl, src, dest, vc,
+  write_packet(e, flits + i * nfl * words, pw, words, nfl, src, dest, vc,
                (unsigned)((seq0 + i) & 0xFFFFu));
 }
 void launch_packetize(const rd_event* ev, uint64_t n, uint32_t packet_w, uint32_t src,

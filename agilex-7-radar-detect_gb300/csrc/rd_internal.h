@@ -25,6 +25,10 @@ struct DevStats {
   unsigned long long events_total;   // events emitted so far (packet seq base)
   unsigned long long events_call;    // events of the current call
   unsigned long long scan_scratch[4];
+  unsigned cfar_ticket;              // CFAR tiles drawn in the running launch
+  unsigned cfar_done;                // CFAR tiles finished in the running launch
+  unsigned cfar_fault;               // a CFAR offset look-back ran out of time
+  unsigned pad_;
 };
 
 // ---- front end: PFB + FFT + corner turn into the spectrum ring ------------
@@ -156,19 +160,20 @@ struct CfarParams {
   const uint32_t* frame_ids;  // per CFAR frame (per-block entry) or null
   int enable, go, dense;
   uint32_t gl, gg, rl, rg, alpha;  // clamped geometry
-  uint32_t* counts;           // [frames] events per CFAR frame
-  uint32_t* detsup;           // [frames][2]
-  uint32_t* mask;             // [frames][ceil(n/32)] emitted-cell bitmask
-  unsigned long long* offsets;// [ceil(frames / 4)] per-CTA event totals, then their exclusive offsets
+  unsigned long long* tile_state;  // [ceil(frames / 8)] look-back states, zero between launches
+  int vec;                    // n % 4 == 0 and the cells 16-byte aligned: 16-byte loads
+  int ev16;                   // events 16-byte aligned: 16-byte stores
   rd_event* events;           // output, capacity cap
   uint64_t cap;
   uint32_t* flits;            // output flits or null
   uint32_t packet_w, src_id, dest, vc, flit_words, nfl;
   DevStats* stats;
 };
-void launch_cfar_decide(const CfarParams& p, cudaStream_t s);
-void launch_cfar_scan(const CfarParams& p, cudaStream_t s);
-void launch_cfar_emit(const CfarParams& p, cudaStream_t s);
+// One launch: decide, offsets, events and packets (k_backend.cu). Needs
+// stats->cfar_ticket/cfar_done zero and tile_state[0 .. cfar_tiles) zero on
+// entry, and leaves them so.
+void launch_cfar(const CfarParams& p, cudaStream_t s);
+unsigned cfar_tiles(uint32_t frames);
 
 void launch_bf_block(uint32_t n_ant, uint32_t n_beams, const uint32_t* w,
                      const uint32_t* x, uint64_t n_vec, uint32_t* y, long long* acc,

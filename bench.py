@@ -119,7 +119,7 @@ def kernel_bytes(cfg, name: str, frames: int) -> float:
         return frames * N * (C + B) * 4.0
     if name == "k_cov":        # spectrum read (windows amortise to ~0)
         return frames * N * C * 4.0
-    if name == "k_cfar_decide":  # power cells read
+    if name == "k_cfar":       # power cells read (events and packets come on top)
         return frames * N * B * 4.0
     return 0.0
 
