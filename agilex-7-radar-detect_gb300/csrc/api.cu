@@ -194,7 +194,9 @@ struct rd_chain {
   DevBuf<long long> acc_re, acc_im, cov_out;
   uint32_t acc_cur = 0;
   DevBuf<unsigned> sticky, satcnt, win_flags;
-  DevBuf<unsigned long long> tile_state;  // CFAR look-back, zero between launches
+  DevBuf<uint32_t> counts, detsup, mask;   // CFAR per-frame decisions
+  DevBuf<unsigned long long> totals;       // CFAR events per decide CTA
+  DevBuf<uint4> slots;                     // CFAR detections per frame
   DevBuf<rd_event> events;
   DevBuf<uint32_t> flits;
   DevBuf<uint32_t> tap_pfb;
@@ -403,7 +405,10 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
       (c.form == RD_FORM_TENSOR && bad(ch->w_frag.ensure(beam_tc_fragment_words(C, B)))) ||
       bad(ch->tail[0].ensure((size_t)C * D * N)) || bad(ch->tail[1].ensure((size_t)C * D * N)) ||
       bad(ch->ring.ensure((size_t)ch->R * N * C)) || bad(ch->power.ensure((size_t)F * B * N)) ||
-      bad(ch->tile_state.ensure(cfar_tiles(F * B))) || bad(ch->stats.ensure(1))) {
+      bad(ch->counts.ensure((size_t)F * B)) || bad(ch->detsup.ensure((size_t)F * B)) ||
+      bad(ch->mask.ensure((size_t)F * B * ((N + 31) / 32))) ||
+      bad(ch->totals.ensure(cfar_tiles(F * B))) ||
+      bad(ch->slots.ensure((size_t)F * B * kCfarSlots)) || bad(ch->stats.ensure(1))) {
     rd_chain_destroy(ch);
     return RD_ENOMEM;
   }
@@ -418,7 +423,6 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
   cudaMemset(ch->tail[1].p, 0, (size_t)C * D * N * 4);
   cudaMemset(ch->ring.p, 0, (size_t)ch->R * N * C * 4);
   cudaMemset(ch->stats.p, 0, sizeof(DevStats));
-  cudaMemset(ch->tile_state.p, 0, ch->tile_state.n * sizeof(unsigned long long));
   if (c.cov_source != RD_COV_OFF) {
     ch->S = c.cov_source == RD_COV_CHANNEL ? C : B;
     const uint32_t np = rd_cov_pairs(&c);
@@ -474,7 +478,8 @@ void rd_chain_destroy(rd_chain* ch) {
   ch->tw_pos.release(); ch->ct_units.release(); ch->ct_pq.release();
   ch->px.release(); ch->py.release(); ch->acc_re.release(); ch->acc_im.release();
   ch->cov_out.release(); ch->sticky.release(); ch->satcnt.release(); ch->win_flags.release();
-  ch->tile_state.release();
+  ch->counts.release(); ch->detsup.release(); ch->mask.release(); ch->totals.release();
+  ch->slots.release();
   ch->events.release(); ch->flits.release(); ch->tap_pfb.release(); ch->stats.release();
   for (const rd_chain::Pending& p : ch->pending) {
     cudaEventDestroy(p.a);
@@ -713,7 +718,11 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   fp2.rl = std::min(c.ref_lead, c.max_ref);
   fp2.rg = std::min(c.ref_lag, c.max_ref);
   fp2.alpha = c.alpha;
-  fp2.tile_state = ch->tile_state.p;
+  fp2.counts = ch->counts.p;
+  fp2.detsup = ch->detsup.p;
+  fp2.mask = ch->mask.p;
+  fp2.totals = ch->totals.p;
+  fp2.slots = ch->slots.p;
   fp2.vec = (N % 4u) == 0;  // cudaMalloc'd power cells: 256-byte aligned
   fp2.ev16 = 1;
   fp2.events = ch->events.p;
@@ -821,7 +830,6 @@ rd_status rd_chain_fetch(rd_chain* ch, rd_output* out) {
   CK(cudaStreamSynchronize(ch->stream));
   DevStats ds;
   CK(cudaMemcpy(&ds, ch->stats.p, sizeof(ds), cudaMemcpyDeviceToHost));
-  if (ds.cfar_fault) return fail(RD_EDEVICE, "CFAR offset look-back timed out");
   const uint64_t n_ev = ds.scan_scratch[0];
   const uint32_t nfl = rd_detection_flits(c.packet_w), words = rd_flit_words(c.packet_w);
   bool trunc = n_ev > ch->call_cap_events;
@@ -1316,19 +1324,23 @@ rd_status rd_cfar_run(const int64_t* cells, uint32_t n, uint32_t frames, const r
   if (!rd_device_ok()) return fail(RD_EDEVICE, "no usable CUDA device");
   Scratch sc;
   long long* dc;
-  uint32_t* dfid;
-  unsigned long long* dtile;
+  uint32_t *dfid, *dcnt, *dds, *dmask;
+  unsigned long long* dtot;
+  uint4* dslot;
   rd_event* dev = nullptr;
   DevStats* dst;
   CK(sc.alloc(&dc, (size_t)frames * n));
   CK(sc.alloc(&dfid, frames));
-  CK(sc.alloc(&dtile, cfar_tiles(frames)));
+  CK(sc.alloc(&dcnt, frames));
+  CK(sc.alloc(&dds, frames));
+  CK(sc.alloc(&dmask, (size_t)frames * ((n + 31) / 32)));
+  CK(sc.alloc(&dtot, cfar_tiles(frames)));
+  CK(sc.alloc(&dslot, (size_t)frames * kCfarSlots));
   CK(sc.alloc(&dst, 1));
   CK(sc.alloc(&dev, std::max<uint64_t>(cap, 1)));
   CK(cudaMemcpy(dc, cells, (size_t)frames * n * 8, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(dfid, frame_ids, (size_t)frames * 4, cudaMemcpyHostToDevice));
   CK(cudaMemset(dst, 0, sizeof(DevStats)));
-  CK(cudaMemset(dtile, 0, cfar_tiles(frames) * sizeof(unsigned long long)));
   CfarParams p{};
   p.cells_i64 = (const int64_t*)dc;
   p.frames = frames;
@@ -1343,7 +1355,11 @@ rd_status rd_cfar_run(const int64_t* cells, uint32_t n, uint32_t frames, const r
   p.rl = std::min(cfg->ref_lead, cfg->max_ref);
   p.rg = std::min(cfg->ref_lag, cfg->max_ref);
   p.alpha = cfg->alpha;
-  p.tile_state = dtile;
+  p.counts = dcnt;
+  p.detsup = dds;
+  p.mask = dmask;
+  p.totals = dtot;
+  p.slots = dslot;
   p.vec = (n % 4u) == 0;  // cudaMalloc'd cells: 256-byte aligned
   p.ev16 = 1;
   p.events = dev;
@@ -1353,7 +1369,6 @@ rd_status rd_cfar_run(const int64_t* cells, uint32_t n, uint32_t frames, const r
   CK(cudaGetLastError());
   DevStats hs;
   CK(cudaMemcpy(&hs, dst, sizeof(hs), cudaMemcpyDeviceToHost));
-  if (hs.cfar_fault) return fail(RD_EDEVICE, "CFAR offset look-back timed out");
   *n_events = hs.events_call;
   const uint64_t k = std::min<uint64_t>(hs.events_call, cap);
   if (k && events) CK(cudaMemcpy(events, dev, k * sizeof(rd_event), cudaMemcpyDeviceToHost));

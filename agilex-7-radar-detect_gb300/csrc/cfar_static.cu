@@ -10,7 +10,7 @@
 // calls no cudaMalloc, cudaFree or allocating library routine.
 //
 // Limits and sharing: the scratch holds at most RD_STATIC_CFAR_MAX_FRAMES
-// frames of at most RD_STATIC_CFAR_MAX_CELLS cells (about 33 KB, held by
+// frames of at most RD_STATIC_CFAR_MAX_CELLS cells (about 1.6 MB, held by
 // every GPU that loads the library until the process exits). Every call on a
 // device uses the same array and leaves its contents behind; the per-call
 // counters are cleared at the start of each call. Two calls whose work
@@ -34,7 +34,11 @@ namespace {
 
 struct StaticCfarScratch {
   rd::DevStats stats;
-  unsigned long long tile_state[RD_STATIC_CFAR_MAX_FRAMES];
+  unsigned long long totals[RD_STATIC_CFAR_MAX_FRAMES];
+  uint32_t counts[RD_STATIC_CFAR_MAX_FRAMES];
+  uint32_t detsup[RD_STATIC_CFAR_MAX_FRAMES];
+  uint32_t mask[RD_STATIC_CFAR_MAX_FRAMES * (RD_STATIC_CFAR_MAX_CELLS / 32)];
+  uint4 slots[RD_STATIC_CFAR_MAX_FRAMES * rd::kCfarSlots];
 };
 
 std::mutex g_mu;
@@ -48,8 +52,7 @@ static __device__ __align__(256) unsigned char g_cfar_scratch[sizeof(StaticCfarS
 namespace {
 
 __global__ void k_static_count_out(const rd::DevStats* st, unsigned long long* n_events) {
-  // all ones: the offset look-back timed out and the events are not valid
-  *n_events = st->cfar_fault ? ~0ull : st->events_call;
+  *n_events = st->events_call;
 }
 
 // Device address of the scratch on the current device (looked up once).
@@ -89,10 +92,8 @@ extern "C" rd_status rd_cfar_run_static(const int64_t* cells, uint32_t n, uint32
     return rd::set_error(RD_EDEVICE, "rd_cfar_run_static: cudaGetSymbolAddress failed: %s",
                          cudaGetErrorString(e));
   cudaStream_t s = (cudaStream_t)stream;
-  // the counters and look-back states start at zero each call
+  // the counters the kernels accumulate start at zero each call
   e = cudaMemsetAsync(&sc->stats, 0, sizeof(rd::DevStats), s);
-  if (e == cudaSuccess)
-    e = cudaMemsetAsync(sc->tile_state, 0, rd::cfar_tiles(frames) * sizeof(unsigned long long), s);
   if (e != cudaSuccess)
     return rd::set_error(RD_EDEVICE, "rd_cfar_run_static: %s", cudaGetErrorString(e));
   rd::CfarParams p{};
@@ -109,7 +110,11 @@ extern "C" rd_status rd_cfar_run_static(const int64_t* cells, uint32_t n, uint32
   p.rl = cfg->ref_lead < cfg->max_ref ? cfg->ref_lead : cfg->max_ref;
   p.rg = cfg->ref_lag < cfg->max_ref ? cfg->ref_lag : cfg->max_ref;
   p.alpha = cfg->alpha;
-  p.tile_state = sc->tile_state;
+  p.counts = sc->counts;
+  p.detsup = sc->detsup;
+  p.mask = sc->mask;
+  p.totals = sc->totals;
+  p.slots = sc->slots;
   p.vec = (n % 4u) == 0 && reinterpret_cast<uintptr_t>(cells) % 16u == 0;
   p.ev16 = reinterpret_cast<uintptr_t>(events) % 16u == 0;
   p.events = events;

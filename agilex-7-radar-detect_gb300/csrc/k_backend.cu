@@ -457,31 +457,22 @@ void launch_cov(const CovParams& p, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------------
-// CFAR (cfar_model.hpp:243-340) in one launch. A CTA takes 8 CFAR frames
-// (frame x beam), one warp each, in the order of a ticket it draws from a
-// device counter (so every lower tile's CTA has already started). A warp
+// CFAR (cfar_model.hpp:243-340) in two launches.
+// Decide: one warp per CFAR frame (frame x beam), 8 frames per CTA. The warp
 // loads its frame with 16-byte loads (4 cells a lane), builds the prefix sums
 // in shared memory, decides every cell (the lead/lag reference sums as prefix
-// differences - the same integers the model's loops add) and ballots the
-// cells that emit. The CTA publishes its event total, finds the events of all
-// earlier tiles by decoupled look-back over the tiles' published totals, and
-// then writes its events and packets at that offset: each lane its own cells
-// in bin order, the SUMMARY last. The last CTA to finish records the call's
-// event count and clears the tile states and counters for the next launch.
+// differences - the same integers the model's loops add) and keeps a ballot
+// mask of the cells that emit, the frame's event count and its detected /
+// suppressed counts; the CTA writes its event total.
+// Emit: a CTA takes 64 frames. Its first event's offset is the sum of the
+// totals of all earlier decide CTAs (read in parallel, no scan pass); a scan
+// of its frames' counts gives each frame's offset. Every frame's SUMMARY is
+// written by one thread (64 frames at once); frames with detections are
+// re-read (from L2) by a warp, which writes each detection from the lane that
+// owns its cell, in bin order.
 // ---------------------------------------------------------------------------
-constexpr unsigned kCfarWarps = 8;
-constexpr unsigned long long kTileAgg = 1ull << 62, kTileIncl = 2ull << 62;
-constexpr unsigned long long kTileVal = (1ull << 62) - 1ull;
-constexpr unsigned kLookbackSpins = 1u << 22;  // ~0.3 s with the back-off below
-
-__device__ __forceinline__ void st_release(unsigned long long* a, unsigned long long v) {
-  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(a), "l"(v) : "memory");
-}
-__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* a) {
-  unsigned long long v;
-  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(a) : "memory");
-  return v;
-}
+constexpr unsigned kCfarWarps = 8;        // decide: frames per CTA
+constexpr unsigned kEmitFrames = 32;      // emit: frames per CTA (4 decide CTAs)
 
 __device__ __forceinline__ uint64_t cell_at(const CfarParams& p, uint64_t u, unsigned i) {
   if (p.power_u32) return p.power_u32[u * p.n + i];
@@ -675,59 +666,29 @@ __device__ void write_packet(const rd_event& e, uint32_t* out, unsigned pw, unsi
   }
 }
 
-// Events before this CTA's tile, by decoupled look-back: publish the tile's
-// total, then walk back over earlier tiles, adding totals until a tile that
-// already holds its inclusive prefix. A tile that has not published yet
-// belongs to a CTA that started earlier and publishes without waiting on
-// anyone, so the wait ends; it is still bounded, and a wait that runs out
-// sets the fault flag (the host reports it) instead of spinning on.
-__device__ unsigned long long tile_lookback(const CfarParams& p, unsigned tile,
-                                            unsigned long long agg) {
-  unsigned long long* st = p.tile_state;
-  if (tile == 0) {
-    st_release(st, kTileIncl | agg);
-    return 0;
-  }
-  st_release(st + tile, kTileAgg | agg);
-  unsigned long long excl = 0;
-  unsigned spins = 0;
-  for (int t = (int)tile - 1; t >= 0;) {
-    const unsigned long long v = ld_acquire(st + t);
-    if (v & kTileIncl) {
-      excl += v & kTileVal;
-      break;
-    }
-    if (v & kTileAgg) {
-      excl += v & kTileVal;
-      --t;
-      continue;
-    }
-    if (++spins > kLookbackSpins) {
-      atomicOr(&p.stats->cfar_fault, 1u);
-      break;
-    }
-    __nanosleep(64);
-  }
-  st_release(st + tile, kTileIncl | (excl + agg));
-  return excl;
+__device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// A detection as the emit pass needs it, 16 bytes: cut (40 bits), bin,
+// kind, the window sum (47 bits) and the reference count - the fields of the
+// 176-bit event that the decision sets (cfar_model.hpp:75-84 widths).
+__device__ __forceinline__ uint4 pack_detection(uint64_t cut, unsigned bin, unsigned kind,
+                                                uint64_t sum, unsigned refc) {
+  cut &= (1ull << 40) - 1ull;
+  sum &= (1ull << 47) - 1ull;
+  return make_uint4((uint32_t)cut, (uint32_t)(cut >> 32) | ((bin & 0xFFFFu) << 8) | (kind << 24),
+                    (uint32_t)sum, (uint32_t)(sum >> 32) | ((refc & 0x7Fu) << 15));
 }
 
 template <int R>
-__global__ void __launch_bounds__(kCfarWarps * 32) k_cfar(CfarParams p) {
+__global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_decide(CfarParams p) {
   extern __shared__ __align__(16) uint64_t s_pre[];
-  __shared__ uint32_t s_mask[kCfarWarps][32];
-  __shared__ unsigned s_cnt[kCfarWarps];
-  __shared__ unsigned long long s_excl, s_base0, s_ds[2];
-  __shared__ unsigned s_tile, s_last;
+  __shared__ unsigned s_cnt[kCfarWarps], s_det[kCfarWarps], s_sup[kCfarWarps];
   const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  if (threadIdx.x == 0) {
-    s_tile = atomicAdd(&p.stats->cfar_ticket, 1u);
-    s_base0 = *(volatile unsigned long long*)&p.stats->events_call;
-    s_ds[0] = s_ds[1] = 0;
-  }
-  __syncthreads();
-  const unsigned tile = s_tile;
-  const uint64_t u = (uint64_t)tile * kCfarWarps + warp;
+  const uint64_t u = (uint64_t)blockIdx.x * kCfarWarps + warp;
   // pre[0] one word past a 16-byte boundary (n + 2 words a warp, n even)
   uint64_t* pre = s_pre + (size_t)warp * (p.n + 2u) + 1u;
   const unsigned words = (p.n + 31u) / 32u;
@@ -738,8 +699,11 @@ __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar(CfarParams p) {
     for (unsigned r = 0; r < words; ++r) {
       const unsigned i = r * 32u + lane;
       bool em = false, dt = false, sp = false;
+      CellDecision d{};
+      uint64_t cut = 0;
       if (i < p.n) {
-        const CellDecision d = decide_cell(p, pre, i, pre[i + 1] - pre[i]);
+        cut = pre[i + 1] - pre[i];
+        d = decide_cell(p, pre, i, cut);
         em = d.emit;
         dt = d.detected;
         sp = !d.evaluable;
@@ -747,97 +711,167 @@ __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar(CfarParams p) {
       const unsigned m = __ballot_sync(0xffffffffu, em);
       det += __popc(__ballot_sync(0xffffffffu, dt));
       sup += __popc(__ballot_sync(0xffffffffu, sp));
-      if (lane == 0) s_mask[warp][r] = m;
+      if (lane == 0) p.mask[u * words + r] = m;
+      if (em) {  // the frame's k-th event, while it fits the frame's slots
+        const unsigned k = emitted + __popc(m & ((1u << lane) - 1u));
+        if (k < kCfarSlots)
+          p.slots[u * kCfarSlots + k] =
+              pack_detection(cut, i, d.detected ? 0u : (!d.evaluable ? 2u : 1u),
+                             d.evaluable ? d.sum : 0ull, d.evaluable ? d.n : 0u);
+      }
       emitted += __popc(m);
     }
     count = emitted + 1u;  // + SUMMARY
+    if (lane == 0) {
+      p.counts[u] = count;
+      p.detsup[u] = det | (sup << 16);  // n <= 1024: both fit 16 bits
+    }
   }
   if (lane == 0) {
     s_cnt[warp] = count;
-    if (det) atomicAdd(&s_ds[0], (unsigned long long)det);
-    if (sup) atomicAdd(&s_ds[1], (unsigned long long)sup);
+    s_det[warp] = det;
+    s_sup[warp] = sup;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    unsigned long long agg = 0;
-    for (unsigned k = 0; k < kCfarWarps; ++k) agg += s_cnt[k];
-    s_excl = tile_lookback(p, tile, agg);
-    if (s_ds[0]) atomicAdd(&p.stats->cfar_det, s_ds[0]);
-    if (s_ds[1]) atomicAdd(&p.stats->cfar_sup, s_ds[1]);
-  }
-  __syncthreads();
-  if (u < p.frames) {
-    uint64_t base = s_base0 + s_excl;
-    for (unsigned k = 0; k < warp; ++k) base += s_cnt[k];
-    const uint64_t frame = p.frame_ids ? p.frame_ids[u] : (p.g0 + u / p.beams);
-    const unsigned fid = p.frame_ids ? p.frame_ids[u] : (unsigned)(frame & 0xFFFFu);
-    const uint16_t beam = (uint16_t)(p.frame_ids ? u : (u % p.beams));
-    const unsigned long long seq0 = p.stats->events_total;
-    const size_t pk = (size_t)p.nfl * p.flit_words;  // words per packet
-    unsigned before = 0;
-    for (unsigned r = 0; r < words; ++r) {
-      const uint32_t m = s_mask[warp][r];
-      if ((m >> lane) & 1u) {
-        const unsigned i = r * 32u + lane;
-        const uint64_t cut = pre[i + 1] - pre[i];
-        const CellDecision d = decide_cell(p, pre, i, cut);
-        const uint64_t idx = base + before + __popc(m & ((1u << lane) - 1u));
-        if (idx < p.cap) {
-          const unsigned kind = d.detected ? 0u : (!d.evaluable ? 2u : 1u);
-          rd_event ev;
-          make_event(&ev, kind, i, fid, d.evaluable ? d.n : 0u, p.alpha, 0, 0, cut,
-                     d.evaluable ? d.sum : 0ull, idx == base, false, (uint32_t)frame, beam);
-          store_event(p.events + idx, ev, p.ev16);
-          if (p.flits)
-            write_packet(ev, p.flits + idx * pk, p.packet_w, p.flit_words, p.nfl, p.src_id,
-                         p.dest, p.vc, (unsigned)((seq0 + idx) & 0xFFFFu));
-        }
-      }
-      before += __popc(m);
+    unsigned long long tot = 0, d = 0, q = 0;
+    for (unsigned k = 0; k < kCfarWarps; ++k) {
+      tot += s_cnt[k];
+      d += s_det[k];
+      q += s_sup[k];
     }
-    const uint64_t idx = base + count - 1u;  // the SUMMARY
-    if (lane == 0 && idx < p.cap) {
-      rd_event ev;
-      make_event(&ev, 3u, p.n, fid, 0, p.alpha, det, sup, 0, 0, count == 1u, true,
-                 (uint32_t)frame, beam);
-      store_event(p.events + idx, ev, p.ev16);
-      if (p.flits)
-        write_packet(ev, p.flits + idx * pk, p.packet_w, p.flit_words, p.nfl, p.src_id,
-                     p.dest, p.vc, (unsigned)((seq0 + idx) & 0xFFFFu));
-    }
-  }
-  // the last CTA out: the call's event count, then a clean slate
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    s_last = atomicAdd(&p.stats->cfar_done, 1u) == gridDim.x - 1u;
-  }
-  __syncthreads();
-  if (s_last) {
-    __threadfence();
-    const unsigned n_tiles = gridDim.x;
-    if (threadIdx.x == 0) {
-      p.stats->events_call = s_base0 + (ld_acquire(p.tile_state + n_tiles - 1) & kTileVal);
-      p.stats->cfar_ticket = 0;
-      p.stats->cfar_done = 0;
-    }
-    for (unsigned t = threadIdx.x; t < n_tiles; t += blockDim.x) p.tile_state[t] = 0;
+    p.totals[blockIdx.x] = tot;
+    if (d) atomicAdd(&p.stats->cfar_det, d);
+    if (q) atomicAdd(&p.stats->cfar_sup, q);
+    // the emit pass counts from the events before this launch
+    if (blockIdx.x == 0) p.stats->scan_scratch[1] = p.stats->events_call;
   }
 }
 
-// Shared memory: 8 frames x (n + 2) words; n <= 1024 needs the opt-in above
-// 48 KB, set once per instantiation.
+// The k-th emitted cell of frame u re-decided from the cells themselves (the
+// window sums added up directly: the same integers as the prefix
+// differences), for frames with more events than their slots.
+__device__ uint4 redecide(const CfarParams& p, uint64_t u, unsigned k) {
+  const unsigned words = (p.n + 31u) / 32u;
+  unsigned i = 0;
+  for (unsigned r = 0; r < words; ++r) {
+    uint32_t m = p.mask[u * words + r];
+    const unsigned c = __popc(m);
+    if (k < c) {
+      for (unsigned t = 0; t < k; ++t) m &= m - 1u;  // drop the k lower set bits
+      i = r * 32u + (unsigned)(__ffs(m) - 1);
+      break;
+    }
+    k -= c;
+  }
+  const uint64_t cut = cell_at(p, u, i);
+  const long long hi = (long long)i + p.gl + p.rl;
+  const long long lo = (long long)i - (long long)p.gg - (long long)p.rg;
+  const bool ok = hi < (long long)p.n && lo >= 0;
+  uint64_t sl = 0, sg = 0;
+  if (ok) {
+    for (unsigned j = 0; j < p.rl; ++j) sl += cell_at(p, u, i + p.gl + 1u + j);
+    for (unsigned j = 0; j < p.rg; ++j) sg += cell_at(p, u, i - p.gg - p.rg + j);
+  }
+  // decide_cell on these sums (cfar_model.hpp:295-340)
+  uint64_t sum;
+  unsigned nref;
+  if (p.go) {
+    const bool lead = (sl * p.rg) >= (sg * p.rl);
+    sum = lead ? sl : sg;
+    nref = lead ? p.rl : p.rg;
+  } else {
+    sum = sl + sg;
+    nref = p.rl + p.rg;
+  }
+  const bool usable = p.go ? (p.rl != 0u && p.rg != 0u) : (p.rl + p.rg) != 0u;
+  const bool evaluable = ok && p.enable && usable;
+  const bool detected = evaluable && ((cut * nref) << 8) > ((uint64_t)p.alpha * sum);
+  return pack_detection(cut, i, detected ? 0u : (!evaluable ? 2u : 1u), evaluable ? sum : 0ull,
+                        evaluable ? nref : 0u);
+}
+
+__global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_emit(CfarParams p) {
+  __shared__ unsigned long long s_red[kCfarWarps], s_fbase[kEmitFrames + 1];
+  __shared__ unsigned s_c[kEmitFrames];
+  const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, tid = threadIdx.x;
+  const uint64_t f0 = (uint64_t)blockIdx.x * kEmitFrames;
+  // events before this CTA: the launch's base plus every earlier decide CTA's total
+  const uint64_t t_end = f0 / kCfarWarps;
+  unsigned long long part = 0;
+  for (uint64_t t = tid; t < t_end; t += blockDim.x) part += p.totals[t];
+  part = warp_sum64(part);
+  if (lane == 0) s_red[warp] = part;
+  // this CTA's frames: counts and their exclusive scan (warp 0)
+  if (warp == 0) {
+    const unsigned c = f0 + lane < p.frames ? p.counts[f0 + lane] : 0u;
+    s_c[lane] = c;
+    unsigned long long x = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long t = __shfl_up_sync(0xffffffffu, x, o);
+      if ((int)lane >= o) x += t;
+    }
+    s_fbase[lane] = x - c;
+    if (lane == 31) s_fbase[kEmitFrames] = x;
+  }
+  __syncthreads();
+  unsigned long long base = p.stats->scan_scratch[1];
+  for (unsigned k = 0; k < kCfarWarps; ++k) base += s_red[k];
+  const unsigned long long total = s_fbase[kEmitFrames];
+  if (blockIdx.x == gridDim.x - 1 && tid == 0)  // the launch's last frame is here
+    p.stats->events_call = base + total;
+  const unsigned long long seq0 = p.stats->events_total;
+  const size_t pk = (size_t)p.nfl * p.flit_words;  // words per packet
+  // one event a thread, in output order
+  for (unsigned long long j = tid; j < total; j += blockDim.x) {
+    unsigned f = 0;  // the frame holding event j: s_fbase[f] <= j < s_fbase[f + 1]
+#pragma unroll
+    for (unsigned step = kEmitFrames / 2; step > 0; step >>= 1)
+      if (s_fbase[f + step] <= j) f += step;
+    const unsigned k = (unsigned)(j - s_fbase[f]), c = s_c[f];
+    const uint64_t u = f0 + f;
+    const unsigned u32 = (unsigned)u;  // u < frames < 2^32: 32-bit division
+    const unsigned fq = u32 / p.beams;
+    const uint64_t frame = p.frame_ids ? p.frame_ids[u] : (p.g0 + fq);
+    const unsigned fid = p.frame_ids ? p.frame_ids[u] : (unsigned)(frame & 0xFFFFu);
+    const uint16_t beam = (uint16_t)(p.frame_ids ? u32 : (u32 - fq * p.beams));
+    const uint64_t idx = base + j;
+    if (idx >= p.cap) continue;
+    rd_event ev;
+    if (k + 1u == c) {  // the SUMMARY
+      const uint32_t ds = p.detsup[u];
+      make_event(&ev, 3u, p.n, fid, 0, p.alpha, ds & 0xFFFFu, ds >> 16, 0, 0, c == 1u, true,
+                 (uint32_t)frame, beam);
+    } else {
+      const uint4 e = c - 1u <= kCfarSlots ? p.slots[u * kCfarSlots + k] : redecide(p, u, k);
+      const uint64_t cut = (uint64_t)e.x | ((uint64_t)(e.y & 0xFFu) << 32);
+      const uint64_t sum = (uint64_t)e.z | ((uint64_t)(e.w & 0x7FFFu) << 32);
+      make_event(&ev, e.y >> 24, (e.y >> 8) & 0xFFFFu, fid, (e.w >> 15) & 0x7Fu, p.alpha, 0, 0,
+                 cut, sum, k == 0u, false, (uint32_t)frame, beam);
+    }
+    store_event(p.events + idx, ev, p.ev16);
+    if (p.flits)
+      write_packet(ev, p.flits + idx * pk, p.packet_w, p.flit_words, p.nfl, p.src_id, p.dest,
+                   p.vc, (unsigned)((seq0 + idx) & 0xFFFFu));
+  }
+}
+
+// Decide: 8 frames x (n + 2) words of shared memory; n <= 1024 needs the
+// opt-in above 48 KB, set once per instantiation.
 template <int R>
 static void launch_cfar_r(const CfarParams& p, cudaStream_t s) {
   static bool attr = false;
   const size_t sm = (size_t)kCfarWarps * (p.n + 2u) * sizeof(uint64_t);
   if (!attr) {
-    cudaFuncSetAttribute(k_cfar<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)((size_t)kCfarWarps * (128u * R + 2u) * sizeof(uint64_t)));
+    const int most = (int)((size_t)kCfarWarps * (128u * R + 2u) * sizeof(uint64_t));
+    cudaFuncSetAttribute(k_cfar_decide<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
     attr = true;
   }
-  const unsigned tiles = (unsigned)((p.frames + kCfarWarps - 1u) / kCfarWarps);
-  k_cfar<R><<<tiles, kCfarWarps * 32, sm, s>>>(p);
+  const unsigned tiles = cfar_tiles(p.frames);
+  const unsigned emits = (unsigned)((p.frames + kEmitFrames - 1u) / kEmitFrames);
+  k_cfar_decide<R><<<tiles, kCfarWarps * 32, sm, s>>>(p);
+  k_cfar_emit<<<emits, kCfarWarps * 32, 0, s>>>(p);
 }
 
 unsigned cfar_tiles(uint32_t frames) { return (frames + kCfarWarps - 1u) / kCfarWarps; }

@@ -25,10 +25,6 @@ struct DevStats {
   unsigned long long events_total;   // events emitted so far (packet seq base)
   unsigned long long events_call;    // events of the current call
   unsigned long long scan_scratch[4];
-  unsigned cfar_ticket;              // CFAR tiles drawn in the running launch
-  unsigned cfar_done;                // CFAR tiles finished in the running launch
-  unsigned cfar_fault;               // a CFAR offset look-back ran out of time
-  unsigned pad_;
 };
 
 // ---- front end: PFB + FFT + corner turn into the spectrum ring ------------
@@ -151,6 +147,10 @@ bool cov_tc_plan(uint32_t S, const uint32_t* px, const uint32_t* py, uint32_t P,
 size_t cov_tc_smem(const CovTcPlan& t);
 void launch_cov_tc(const CovParams& p, const CovTcPlan& t, cudaStream_t s);
 
+// Detections a CFAR frame keeps from its decision for the emit pass; a frame
+// with more (DENSE output, clutter) re-decides its events there.
+constexpr unsigned kCfarSlots = 16;
+
 struct CfarParams {
   const uint32_t* power_u32;  // [frames][n] (chain) ...
   const int64_t* cells_i64;   // ... or raw signed cells (per-block entry)
@@ -160,7 +160,11 @@ struct CfarParams {
   const uint32_t* frame_ids;  // per CFAR frame (per-block entry) or null
   int enable, go, dense;
   uint32_t gl, gg, rl, rg, alpha;  // clamped geometry
-  unsigned long long* tile_state;  // [ceil(frames / 8)] look-back states, zero between launches
+  uint32_t* counts;           // [frames] events per CFAR frame (SUMMARY included)
+  uint32_t* detsup;           // [frames] detected | suppressed << 16
+  uint32_t* mask;             // [frames][ceil(n / 32)] emitted-cell bitmask
+  unsigned long long* totals; // [cfar_tiles(frames)] events per decide CTA
+  uint4* slots;               // [frames][kCfarSlots] the frame's first detections
   int vec;                    // n % 4 == 0 and the cells 16-byte aligned: 16-byte loads
   int ev16;                   // events 16-byte aligned: 16-byte stores
   rd_event* events;           // output, capacity cap
@@ -169,9 +173,7 @@ struct CfarParams {
   uint32_t packet_w, src_id, dest, vc, flit_words, nfl;
   DevStats* stats;
 };
-// One launch: decide, offsets, events and packets (k_backend.cu). Needs
-// stats->cfar_ticket/cfar_done zero and tile_state[0 .. cfar_tiles) zero on
-// entry, and leaves them so.
+// Decide, then events and packets at their offsets: two launches (k_backend.cu)
 void launch_cfar(const CfarParams& p, cudaStream_t s);
 unsigned cfar_tiles(uint32_t frames);
 

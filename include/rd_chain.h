@@ -431,9 +431,7 @@ rd_status rd_cfar_run(const int64_t* cells, uint32_t n, uint32_t frames,
  * work overlaps on the GPU race on it. The first call on each device looks up
  * the scratch address and should come before any stream capture. cells,
  * frame_ids, events and n_events (one uint64) are device pointers; the call
- * is asynchronous on `stream` (a cudaStream_t, NULL = legacy stream).
- * *n_events all ones means the events are not valid (the detector's bounded
- * wait for its offsets ran out; it does not happen in a correct launch). */
+ * is asynchronous on `stream` (a cudaStream_t, NULL = legacy stream). */
 #define RD_STATIC_CFAR_MAX_FRAMES 4096u
 #define RD_STATIC_CFAR_MAX_CELLS 1024u
 rd_status rd_cfar_run_static(const int64_t* cells, uint32_t n, uint32_t frames,
