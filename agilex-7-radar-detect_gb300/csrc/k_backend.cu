@@ -686,51 +686,75 @@ __device__ __forceinline__ uint4 pack_detection(uint64_t cut, unsigned bin, unsi
 template <int R>
 __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_decide(CfarParams p) {
   extern __shared__ __align__(16) uint64_t s_pre[];
-  __shared__ unsigned s_cnt[kCfarWarps], s_det[kCfarWarps], s_sup[kCfarWarps];
+  __shared__ unsigned s_cnt[kCfarWarps], s_det[kCfarWarps];
   const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   const uint64_t u = (uint64_t)blockIdx.x * kCfarWarps + warp;
   // pre[0] one word past a 16-byte boundary (n + 2 words a warp, n even)
   uint64_t* pre = s_pre + (size_t)warp * (p.n + 2u) + 1u;
   const unsigned words = (p.n + 31u) / 32u;
-  unsigned count = 0, det = 0, sup = 0;
+  // cells whose window fits the frame: lo_b <= i < hi_b; only they are
+  // evaluable, so the suppressed count is the same for every frame
+  const int lo_b = (int)(p.gg + p.rg), hi_b = (int)p.n - (int)(p.gl + p.rl);
+  const bool usable = p.go ? (p.rl != 0u && p.rg != 0u) : (p.rl + p.rg) != 0u;
+  const bool live = p.enable && usable;
+  const unsigned n_ok = live && hi_b > lo_b ? (unsigned)(hi_b - lo_b) : 0u;
+  const unsigned ca_n8 = (p.rl + p.rg) << 8;
+  unsigned count = 0, det = 0, mword = 0;
   if (u < p.frames) {
     warp_prefix<R>(p, u, pre, p.vec);
     unsigned emitted = 0;
     for (unsigned r = 0; r < words; ++r) {
       const unsigned i = r * 32u + lane;
-      bool em = false, dt = false, sp = false;
-      CellDecision d{};
-      uint64_t cut = 0;
-      if (i < p.n) {
+      bool dt = false;
+      uint64_t cut = 0, sum = 0;
+      unsigned nref = 0;
+      const bool ok = live && (int)i >= lo_b && (int)i < hi_b;  // i < n follows
+      if (ok) {
         cut = pre[i + 1] - pre[i];
-        d = decide_cell(p, pre, i, cut);
-        em = d.emit;
-        dt = d.detected;
-        sp = !d.evaluable;
+        const uint64_t sl = pre[i + p.gl + p.rl + 1] - pre[i + p.gl + 1];
+        const uint64_t sg = pre[i - p.gg] - pre[i - p.gg - p.rg];
+        uint64_t lhs;
+        if (p.go) {
+          const bool lead = (sl * p.rg) >= (sg * p.rl);
+          sum = lead ? sl : sg;
+          nref = lead ? p.rl : p.rg;
+          lhs = (cut * nref) << 8;
+        } else {
+          sum = sl + sg;
+          nref = p.rl + p.rg;
+          lhs = cut * ca_n8;
+        }
+        dt = lhs > (uint64_t)p.alpha * sum;
       }
-      const unsigned m = __ballot_sync(0xffffffffu, em);
-      det += __popc(__ballot_sync(0xffffffffu, dt));
-      sup += __popc(__ballot_sync(0xffffffffu, sp));
-      if (lane == 0) p.mask[u * words + r] = m;
+      bool em = dt;
+      unsigned m = __ballot_sync(0xffffffffu, dt);
+      if (p.dense) {  // every cell emits; the detected ones still count
+        det += __popc(m);
+        em = i < p.n;
+        m = __ballot_sync(0xffffffffu, em);
+        if (em && !ok) cut = pre[i + 1] - pre[i];
+      } else {
+        det += __popc(m);
+      }
+      if (lane == (r & 31u)) mword = m;
       if (em) {  // the frame's k-th event, while it fits the frame's slots
         const unsigned k = emitted + __popc(m & ((1u << lane) - 1u));
         if (k < kCfarSlots)
           p.slots[u * kCfarSlots + k] =
-              pack_detection(cut, i, d.detected ? 0u : (!d.evaluable ? 2u : 1u),
-                             d.evaluable ? d.sum : 0ull, d.evaluable ? d.n : 0u);
+              pack_detection(cut, i, dt ? 0u : (!ok ? 2u : 1u), ok ? sum : 0ull, ok ? nref : 0u);
       }
       emitted += __popc(m);
     }
+    if (lane < words) p.mask[u * words + lane] = mword;  // words <= 32
     count = emitted + 1u;  // + SUMMARY
     if (lane == 0) {
       p.counts[u] = count;
-      p.detsup[u] = det | (sup << 16);  // n <= 1024: both fit 16 bits
+      p.detsup[u] = det | ((p.n - n_ok) << 16);  // n <= 1024: both fit 16 bits
     }
   }
   if (lane == 0) {
     s_cnt[warp] = count;
     s_det[warp] = det;
-    s_sup[warp] = sup;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -738,7 +762,7 @@ __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_decide(CfarParams p) {
     for (unsigned k = 0; k < kCfarWarps; ++k) {
       tot += s_cnt[k];
       d += s_det[k];
-      q += s_sup[k];
+      if (s_cnt[k]) q += p.n - n_ok;
     }
     p.totals[blockIdx.x] = tot;
     if (d) atomicAdd(&p.stats->cfar_det, d);
