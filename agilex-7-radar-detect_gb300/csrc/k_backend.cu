@@ -815,6 +815,44 @@ __device__ uint4 redecide(const CfarParams& p, uint64_t u, unsigned k) {
                         evaluable ? nref : 0u);
 }
 
+// Event j of an emit CTA (frame f of the CTA, its k-th event): the SUMMARY
+// from the frame's counts, a detection from the frame's slot (or
+// re-decided); the event goes straight out, its packet to `pkt`.
+__device__ __forceinline__ void emit_one(const CfarParams& p, unsigned long long j,
+                                         unsigned long long base, unsigned long long seq0,
+                                         size_t pk, uint64_t f0, const unsigned long long* s_fbase,
+                                         const unsigned* s_c, uint32_t* pkt) {
+  unsigned f = 0;  // the frame holding event j: s_fbase[f] <= j < s_fbase[f + 1]
+#pragma unroll
+  for (unsigned step = kEmitFrames / 2; step > 0; step >>= 1)
+    if (s_fbase[f + step] <= j) f += step;
+  const unsigned k = (unsigned)(j - s_fbase[f]), c = s_c[f];
+  const uint64_t u = f0 + f;
+  const unsigned u32 = (unsigned)u;  // u < frames < 2^32: 32-bit division
+  const unsigned fq = u32 / p.beams;
+  const uint64_t frame = p.frame_ids ? p.frame_ids[u] : (p.g0 + fq);
+  const unsigned fid = p.frame_ids ? p.frame_ids[u] : (unsigned)(frame & 0xFFFFu);
+  const uint16_t beam = (uint16_t)(p.frame_ids ? u32 : (u32 - fq * p.beams));
+  const uint64_t idx = base + j;
+  if (idx >= p.cap) return;
+  rd_event ev;
+  if (k + 1u == c) {  // the SUMMARY
+    const uint32_t ds = p.detsup[u];
+    make_event(&ev, 3u, p.n, fid, 0, p.alpha, ds & 0xFFFFu, ds >> 16, 0, 0, c == 1u, true,
+               (uint32_t)frame, beam);
+  } else {
+    const uint4 e = c - 1u <= kCfarSlots ? p.slots[u * kCfarSlots + k] : redecide(p, u, k);
+    const uint64_t cut = (uint64_t)e.x | ((uint64_t)(e.y & 0xFFu) << 32);
+    const uint64_t sum = (uint64_t)e.z | ((uint64_t)(e.w & 0x7FFFu) << 32);
+    make_event(&ev, e.y >> 24, (e.y >> 8) & 0xFFFFu, fid, (e.w >> 15) & 0x7Fu, p.alpha, 0, 0,
+               cut, sum, k == 0u, false, (uint32_t)frame, beam);
+  }
+  store_event(p.events + idx, ev, p.ev16);
+  if (p.flits)
+    write_packet(ev, pkt, p.packet_w, p.flit_words, p.nfl, p.src_id, p.dest, p.vc,
+                 (unsigned)((seq0 + idx) & 0xFFFFu));
+}
+
 __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_emit(CfarParams p) {
   __shared__ unsigned long long s_red[kCfarWarps], s_fbase[kEmitFrames + 1];
   __shared__ unsigned s_c[kEmitFrames];
@@ -823,7 +861,16 @@ __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_emit(CfarParams p) {
   // events before this CTA: the launch's base plus every earlier decide CTA's total
   const uint64_t t_end = f0 / kCfarWarps;
   unsigned long long part = 0;
-  for (uint64_t t = tid; t < t_end; t += blockDim.x) part += p.totals[t];
+  for (uint64_t t0 = 0; t0 < t_end; t0 += 8ull * blockDim.x) {
+    unsigned long long v[8];  // eight independent loads in flight
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const uint64_t t = t0 + (uint64_t)q * blockDim.x + tid;
+      v[q] = t < t_end ? p.totals[t] : 0ull;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) part += v[q];
+  }
   part = warp_sum64(part);
   if (lane == 0) s_red[warp] = part;
   // this CTA's frames: counts and their exclusive scan (warp 0)
@@ -847,37 +894,21 @@ __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_emit(CfarParams p) {
     p.stats->events_call = base + total;
   const unsigned long long seq0 = p.stats->events_total;
   const size_t pk = (size_t)p.nfl * p.flit_words;  // words per packet
-  // one event a thread, in output order
-  for (unsigned long long j = tid; j < total; j += blockDim.x) {
-    unsigned f = 0;  // the frame holding event j: s_fbase[f] <= j < s_fbase[f + 1]
-#pragma unroll
-    for (unsigned step = kEmitFrames / 2; step > 0; step >>= 1)
-      if (s_fbase[f + step] <= j) f += step;
-    const unsigned k = (unsigned)(j - s_fbase[f]), c = s_c[f];
-    const uint64_t u = f0 + f;
-    const unsigned u32 = (unsigned)u;  // u < frames < 2^32: 32-bit division
-    const unsigned fq = u32 / p.beams;
-    const uint64_t frame = p.frame_ids ? p.frame_ids[u] : (p.g0 + fq);
-    const unsigned fid = p.frame_ids ? p.frame_ids[u] : (unsigned)(frame & 0xFFFFu);
-    const uint16_t beam = (uint16_t)(p.frame_ids ? u32 : (u32 - fq * p.beams));
-    const uint64_t idx = base + j;
-    if (idx >= p.cap) continue;
-    rd_event ev;
-    if (k + 1u == c) {  // the SUMMARY
-      const uint32_t ds = p.detsup[u];
-      make_event(&ev, 3u, p.n, fid, 0, p.alpha, ds & 0xFFFFu, ds >> 16, 0, 0, c == 1u, true,
-                 (uint32_t)frame, beam);
-    } else {
-      const uint4 e = c - 1u <= kCfarSlots ? p.slots[u * kCfarSlots + k] : redecide(p, u, k);
-      const uint64_t cut = (uint64_t)e.x | ((uint64_t)(e.y & 0xFFu) << 32);
-      const uint64_t sum = (uint64_t)e.z | ((uint64_t)(e.w & 0x7FFFu) << 32);
-      make_event(&ev, e.y >> 24, (e.y >> 8) & 0xFFFFu, fid, (e.w >> 15) & 0x7Fu, p.alpha, 0, 0,
-                 cut, sum, k == 0u, false, (uint32_t)frame, beam);
+  // one event a thread, in output order; the round's packets are built in
+  // shared memory and leave as one contiguous, coalesced run
+  extern __shared__ uint32_t s_pk[];
+  for (unsigned long long j0 = 0; j0 < total; j0 += blockDim.x) {
+    const unsigned long long j = j0 + tid;
+    const unsigned long long end = base + (total < j0 + blockDim.x ? total : j0 + blockDim.x);
+    const unsigned long long stop = end < p.cap ? end : p.cap;  // events of the round kept
+    if (j < total) emit_one(p, j, base, seq0, pk, f0, s_fbase, s_c, s_pk + (size_t)tid * pk);
+    __syncthreads();
+    if (p.flits && stop > base + j0) {
+      const size_t nw = (size_t)(stop - (base + j0)) * pk;
+      uint32_t* dst = p.flits + (size_t)(base + j0) * pk;
+      for (size_t w = tid; w < nw; w += blockDim.x) dst[w] = s_pk[w];
     }
-    store_event(p.events + idx, ev, p.ev16);
-    if (p.flits)
-      write_packet(ev, p.flits + idx * pk, p.packet_w, p.flit_words, p.nfl, p.src_id, p.dest,
-                   p.vc, (unsigned)((seq0 + idx) & 0xFFFFu));
+    __syncthreads();
   }
 }
 
@@ -895,7 +926,7 @@ static void launch_cfar_r(const CfarParams& p, cudaStream_t s) {
   const unsigned tiles = cfar_tiles(p.frames);
   const unsigned emits = (unsigned)((p.frames + kEmitFrames - 1u) / kEmitFrames);
   k_cfar_decide<R><<<tiles, kCfarWarps * 32, sm, s>>>(p);
-  k_cfar_emit<<<emits, kCfarWarps * 32, 0, s>>>(p);
+  k_cfar_emit<<<emits, kCfarWarps * 32, (size_t)kCfarWarps * 32 * p.nfl * p.flit_words * 4, s>>>(p);
 }
 
 unsigned cfar_tiles(uint32_t frames) { return (frames + kCfarWarps - 1u) / kCfarWarps; }
