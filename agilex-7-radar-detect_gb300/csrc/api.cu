@@ -540,7 +540,8 @@ rd_status rd_chain_set_weights(rd_chain* ch, const rd_cplx16* w) {
     }
     l1max = std::max(l1max, l1);
   }
-  ch->x_safe = l1max ? (uint32_t)std::min<uint64_t>(0x7FFFFFFFull / l1max, 32768u) : 32768u;
+  // sums within 2^31 - 2^15 also round in int32 without wrapping
+  ch->x_safe = l1max ? (uint32_t)std::min<uint64_t>(0x7FFF7FFFull / l1max, 32768u) : 32768u;
   CK(cudaMemcpyAsync(ch->weights.p, w, n * 4, cudaMemcpyHostToDevice, ch->stream));
   CK(cudaMemcpyAsync(ch->w_limbs.p, limbs.data(), n * sizeof(int4), cudaMemcpyHostToDevice,
                      ch->stream));
@@ -622,6 +623,7 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   bp.weights = ch->weights.p;
   bp.w_limbs = ch->w_limbs.p;
   bp.x_safe = ch->x_safe;
+  bp.cshift = (C & (C - 1u)) == 0u ? __builtin_ctz(C) : -1;
   bp.w_frag = ch->w_frag.p;
   bp.power = ch->power.p;
   bp.beams_bn = ch->beams_bn.p;

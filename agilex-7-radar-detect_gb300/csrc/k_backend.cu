@@ -46,19 +46,53 @@ __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
   const uint32_t* xsrc = p.ring + ((size_t)slot * N + bin0) * C;
   const unsigned nb = (N - bin0) < 64u ? (N - bin0) : 64u;
   int xmax = 0;
-  for (unsigned k = tid; k < nb * C; k += 256u) {
-    const uint32_t v = xsrc[k];
-    s_x[(k / C) * xs + (k % C)] = v;
+  auto absmax = [&](uint32_t v) {
     xmax = max(xmax, max(abs((int)(int16_t)(uint16_t)(v & 0xFFFFu)), abs((int)v >> 16)));
+  };
+  if (p.cshift >= 0 && (C & 3u) == 0u) {
+    // the tile's nb x C words are contiguous (16-byte aligned): quad loads,
+    // row and column by shift
+    const uint4* src4 = reinterpret_cast<const uint4*>(xsrc);
+    const unsigned nq = nb * C / 4u, cm = C - 1u;
+    for (unsigned q = tid; q < nq; q += 256u) {
+      const uint4 v = src4[q];
+      const unsigned k = 4u * q;
+      uint32_t* d = s_x + (k >> p.cshift) * xs + (k & cm);
+      d[0] = v.x;
+      d[1] = v.y;
+      d[2] = v.z;
+      d[3] = v.w;
+      absmax(v.x);
+      absmax(v.y);
+      absmax(v.z);
+      absmax(v.w);
+    }
+  } else {
+    for (unsigned k = tid; k < nb * C; k += 256u) {
+      const uint32_t v = xsrc[k];
+      s_x[(k / C) * xs + (k % C)] = v;
+      absmax(v);
+    }
   }
   // every sum is at most max|x| x the largest beam L1 norm of the weights:
   // within x_safe the plain int32 sum is exact
   const bool wide = __syncthreads_or(xmax > (int)p.x_safe) != 0;
   const unsigned bl = tid & 63u, bg = tid >> 6;
   const unsigned bin = bin0 + bl;
-  long long ar[BPT], ai[BPT];
-#pragma unroll
-  for (int j = 0; j < BPT; ++j) ar[j] = ai[j] = 0;
+  unsigned fl_any = 0;
+  unsigned long long nsat = 0;
+  // beam b's rounded output y (round_sat(., 15, 16)) to the power cells
+  auto out = [&](unsigned b, int32_t yr, int32_t yi, unsigned fr, unsigned fi) {
+    if (fr | fi) {
+      fl_any |= fr | fi;
+      ++nsat;
+    }
+    cplx y;
+    y.re = (int16_t)yr;
+    y.im = (int16_t)yi;
+    p.power[(f * B + b) * N + bin] = power_u32(y);
+    if (p.beams_bn) p.beams_bn[(f * N + bin) * B + b] = pack(y);
+  };
   if (bl < nb && !wide) {
     const uint32_t* xr = s_x + bl * xs;
     int sr[BPT], si[BPT];
@@ -77,12 +111,20 @@ __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
         }
       }
     }
+    // |sum| <= x_safe x L1 < 2^31 - 2^15: the int32 rounding cannot wrap
 #pragma unroll
     for (int j = 0; j < BPT; ++j) {
-      ar[j] = sr[j];
-      ai[j] = si[j];
+      const unsigned b = bg + 4u * j;
+      if (b < B) {
+        unsigned fr = 0, fi = 0;
+        const int32_t yr = q15_out32(sr[j], &fr), yi = q15_out32(si[j], &fi);
+        out(b, yr, yi, fr, fi);
+      }
     }
   } else if (bl < nb) {
+    long long ar[BPT], ai[BPT];
+#pragma unroll
+    for (int j = 0; j < BPT; ++j) ar[j] = ai[j] = 0;
     const uint32_t* xr = s_x + bl * xs;
     for (unsigned a0 = 0; a0 < C; a0 += 64u) {
       const unsigned a1 = (a0 + 64u) < C ? (a0 + 64u) : C;
@@ -110,24 +152,14 @@ __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
         ai[j] += (long long)hi[j] * 256 + li[j];
       }
     }
-  }
-  unsigned fl_any = 0;
-  unsigned long long nsat = 0;
 #pragma unroll
-  for (int j = 0; j < BPT; ++j) {
-    const unsigned b = bg + 4u * j;
-    if (b < B && bl < nb) {
-      unsigned fr = 0, fi = 0;
-      const int32_t yr = q15_out64(ar[j], &fr), yi = q15_out64(ai[j], &fi);
-      if (fr | fi) {
-        fl_any |= fr | fi;
-        ++nsat;
+    for (int j = 0; j < BPT; ++j) {
+      const unsigned b = bg + 4u * j;
+      if (b < B) {
+        unsigned fr = 0, fi = 0;
+        const int32_t yr = q15_out64(ar[j], &fr), yi = q15_out64(ai[j], &fi);
+        out(b, yr, yi, fr, fi);
       }
-      cplx y;
-      y.re = (int16_t)yr;
-      y.im = (int16_t)yi;
-      p.power[(f * B + b) * N + bin] = power_u32(y);
-      if (p.beams_bn) p.beams_bn[(f * N + bin) * B + b] = pack(y);
     }
   }
   const unsigned a = __reduce_or_sync(0xffffffffu, fl_any);

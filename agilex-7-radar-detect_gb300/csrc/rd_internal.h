@@ -91,6 +91,7 @@ struct BeamParams {
   uint8_t* flag_rows;
   uint32_t F, C, N, B;
   uint32_t x_safe;          // spectrum tiles within this magnitude sum exactly in int32
+  int cshift;               // log2 C when C is a power of two, else -1
   DevStats* stats;          // may be null
 };
 void launch_beam(const BeamParams& p, cudaStream_t s);
