@@ -31,8 +31,8 @@ __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
   const unsigned C = p.C, B = p.B, N = p.N;
   const unsigned xs = C + 1;  // padded row
   int4* s_w = reinterpret_cast<int4*>(sm);          // [B][C] limbs
-  int2* s_w2 = reinterpret_cast<int2*>(sm + 4u * B * C);  // [B][C] {re, im}
-  uint32_t* s_x = sm + 6u * B * C;
+  int4* s_w3 = reinterpret_cast<int4*>(sm + 4u * B * C);  // [B][C] {re, im, re + im, 0}
+  uint32_t* s_x = sm + 8u * B * C;
   const unsigned tid = threadIdx.x;
   const unsigned bin0 = blockIdx.x * 64u;
   const uint64_t f = blockIdx.y;
@@ -41,7 +41,8 @@ __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
   for (unsigned k = tid; k < B * C; k += 256u) {
     s_w[k] = p.w_limbs[k];
     const uint32_t w = p.weights[k];
-    s_w2[k] = make_int2((int)(int16_t)(uint16_t)(w & 0xFFFFu), (int)w >> 16);
+    const int wr = (int)(int16_t)(uint16_t)(w & 0xFFFFu), wi = (int)w >> 16;
+    s_w3[k] = make_int4(wr, wi, wr + wi, 0);
   }
   const uint32_t* xsrc = p.ring + ((size_t)slot * N + bin0) * C;
   const unsigned nb = (N - bin0) < 64u ? (N - bin0) : 64u;
@@ -94,30 +95,36 @@ __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
     if (p.beams_bn) p.beams_bn[(f * N + bin) * B + b] = pack(y);
   };
   if (bl < nb && !wide) {
+    // three products a complex term (Gauss): re = sum xr wr - sum xi wi,
+    // im = sum (xr + xi)(wr + wi) - sum xr wr - sum xi wi. The sums run
+    // modulo 2^32; the true re and im are below 2^31 - 2^15 in magnitude
+    // (x_safe), so the wrapped results are the exact integers.
     const uint32_t* xr = s_x + bl * xs;
-    int sr[BPT], si[BPT];
+    uint32_t sac[BPT], sbd[BPT], sk[BPT];
 #pragma unroll
-    for (int j = 0; j < BPT; ++j) sr[j] = si[j] = 0;
+    for (int j = 0; j < BPT; ++j) sac[j] = sbd[j] = sk[j] = 0u;
     for (unsigned a = 0; a < C; ++a) {
       const uint32_t xv = xr[a];
       const int x_re = (int)(int16_t)(uint16_t)(xv & 0xFFFFu), x_im = (int)xv >> 16;
+      const uint32_t x_s = (uint32_t)(x_re + x_im);
 #pragma unroll
       for (int j = 0; j < BPT; ++j) {
         const unsigned b = bg + 4u * j;
         if (BPT == 1 || b < B) {
-          const int2 w = s_w2[b * C + a];
-          sr[j] += x_re * w.x - x_im * w.y;
-          si[j] += x_re * w.y + x_im * w.x;
+          const int4 w = s_w3[b * C + a];
+          sac[j] += (uint32_t)(x_re * w.x);
+          sbd[j] += (uint32_t)(x_im * w.y);
+          sk[j] += x_s * (uint32_t)w.z;
         }
       }
     }
-    // |sum| <= x_safe x L1 < 2^31 - 2^15: the int32 rounding cannot wrap
 #pragma unroll
     for (int j = 0; j < BPT; ++j) {
       const unsigned b = bg + 4u * j;
       if (b < B) {
         unsigned fr = 0, fi = 0;
-        const int32_t yr = q15_out32(sr[j], &fr), yi = q15_out32(si[j], &fi);
+        const int32_t yr = q15_out32((int32_t)(sac[j] - sbd[j]), &fr);
+        const int32_t yi = q15_out32((int32_t)(sk[j] - sac[j] - sbd[j]), &fi);
         out(b, yr, yi, fr, fi);
       }
     }
@@ -175,7 +182,7 @@ static bool g_beam_attr_set = false;
 void launch_beam(const BeamParams& p, cudaStream_t s) {
   const unsigned bpt = (p.B + 3u) / 4u;
   const dim3 grid((p.N + 63u) / 64u, p.F);
-  const size_t smem = ((size_t)6u * p.B * p.C + 64u * (p.C + 1u)) * sizeof(uint32_t);
+  const size_t smem = ((size_t)8u * p.B * p.C + 64u * (p.C + 1u)) * sizeof(uint32_t);
   if (!g_beam_attr_set) {
     cudaFuncSetAttribute(k_beam<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     cudaFuncSetAttribute(k_beam<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
