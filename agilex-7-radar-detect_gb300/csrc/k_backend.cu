@@ -419,23 +419,27 @@ __global__ void __launch_bounds__(256) k_cov_block(CovParams p, unsigned BT, uns
   for (unsigned fbase = lo; fbase < hi; fbase += FB) {
     __syncthreads();
     store();
-    // a batch of at most 32 frames whose values are all <= 5792 in magnitude
-    // sums at most 32 x 2 x 5792^2 < 2^31 per pair: exact in int32
+    // with every value of the batch <= 5792 in magnitude, 32 frames sum at
+    // most 32 x 2 x 5792^2 < 2^31 per pair: exact in int32, folded into the
+    // int64 sums every 32 frames
     const bool wide = __syncthreads_or(smax > 5792) != 0;
     if (fbase + FB < hi) load(fbase + FB);
     const unsigned nf = (hi - fbase) < FB ? (hi - fbase) : FB;
     if (live && !wide) {
       const int2* xs = s_xy + xi;
       const int2* ys = s_xy + yi;
-      int sr = 0, si = 0;
+      for (unsigned s0 = 0; s0 < nf; s0 += 32u) {
+        const unsigned s1 = (nf - s0) < 32u ? nf : s0 + 32u;
+        int sr = 0, si = 0;
 #pragma unroll 4
-      for (unsigned fl = 0; fl < nf; ++fl) {
-        const int2 x = xs[fl * row], y = ys[fl * row];
-        sr += x.x * y.x + x.y * y.y;
-        si += x.y * y.x - x.x * y.y;
+        for (unsigned fl = s0; fl < s1; ++fl) {
+          const int2 x = xs[fl * row], y = ys[fl * row];
+          sr += x.x * y.x + x.y * y.y;
+          si += x.y * y.x - x.x * y.y;
+        }
+        are += sr;
+        aim += si;
       }
-      are += sr;
-      aim += si;
     } else if (live) {
       const int2* xs = s_xy + xi;
       const int2* ys = s_xy + yi;
@@ -478,10 +482,13 @@ void launch_cov(const CovParams& p, cudaStream_t s) {
     BT = 256u / p.P;
   }
   const unsigned nth = ((BT * QB + 31u) / 32u) * 32u;
-  unsigned FB = (kCovPre * nth) / (BT * p.S);
-  if (FB > 32u) FB = 32u;  // (k_cov_block's int32 batch bound assumes <= 32)
-  if (FB < 1u) FB = 1u;
   const int mode = !p.exact ? 2 : (p.exp_mode ? 1 : 0);
+  // frames staged per barrier: as many as the prefetch registers hold (the
+  // block kernel folds its int32 sums every 32 frames; the sequential
+  // integrators stage at most 32)
+  unsigned FB = (kCovPre * nth) / (BT * p.S);
+  if (FB > (mode == 0 ? 128u : 32u)) FB = mode == 0 ? 128u : 32u;
+  if (FB < 1u) FB = 1u;
   // segments: the open window, every whole window, the trailing partial one
   unsigned nz = 1;
   if (mode == 0) {
