@@ -309,7 +309,7 @@ __device__ __noinline__ void front_pass_flags(const FrontParams& p, int T, int q
 }
 
 template <int NL, int SPC, int TT>
-__global__ void __launch_bounds__(256) k_front_fast(FrontParams p, unsigned FB, unsigned CB) {
+__global__ void __launch_bounds__(256, 3) k_front_fast(FrontParams p, unsigned FB, unsigned CB) {
   using G = Geo<NL, SPC>;
   constexpr int N = G::N, M = G::M, TPI = G::TPI;
   constexpr int IPP = 256 / TPI;  // items per pass
