@@ -586,6 +586,7 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   fp.adc = adc;
   fp.ld = ld;
   fp.tail = ch->tail[ch->tail_cur].p;
+  fp.tail_out = c.taps > 1 ? ch->tail[ch->tail_cur ^ 1].p : nullptr;
   fp.coeff_t = ch->coeff_t.p;
   fp.coeff2 = ch->coeff2.p;
   fp.pfb32 = ch->pfb32;
@@ -605,15 +606,9 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   fp.stats = st;
   {
     KTimer t(ch, KT_FRONT);
-    launch_front(fp, s);
-  }
-  if (c.taps > 1) {
-    KTimer t(ch, KT_TAIL);
-    launch_tail_update(adc, ld, ch->tail[ch->tail_cur].p, ch->tail[ch->tail_cur ^ 1].p, F, C,
-                       N, c.taps, s);
+    ch->launches += launch_front(fp, s);
   }
   ch->tail_cur ^= (c.taps > 1) ? 1 : 0;
-  ch->launches += (c.taps > 1) ? 2 : 1;
 
   BeamParams bp{};
   bp.ring = ch->ring.p;

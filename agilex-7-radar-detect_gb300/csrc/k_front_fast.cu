@@ -181,6 +181,11 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
   const int pos0 = tl;  // quad_base<NL-2>(tl) == tl
   const int ph0 = SPC * pos0 + q;
   constexpr int dph1 = SPC * d1, dph2 = SPC * d0;
+  // the chunk's last T - 1 frames become the next chunk's delay line
+  // (pfb_model.hpp:170-175): this frame's samples go there as they are read
+  uint32_t* tail_row = nullptr;
+  if (!FL && ok && p.tail_out && f + (unsigned)T > p.F)
+    tail_row = p.tail_out + ((size_t)c * (T - 1) + (p.F - 1u - f)) * G::N + ph0;
   auto finish = [&](int j, int yr, int yi, unsigned fr, unsigned fi) {
     if (fr | fi) {
       pfl |= fr | fi;
@@ -206,7 +211,9 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int o = (j & 1) * dph1 + (j >> 1) * dph2;
-          const C2 x = unpk(__ldg(xp + o));
+          const uint32_t xw = __ldg(xp + o);
+          if (k == 0 && tail_row) tail_row[o] = xw;
+          const C2 x = unpk(xw);
           const int2 h = __ldg(hp + o);
           ar[j] += x.re * h.x - x.im * h.y;
           ai[j] += x.re * h.y + x.im * h.x;
@@ -234,7 +241,9 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int o = (j & 1) * dph1 + (j >> 1) * dph2;
-          const C2 x = unpk(__ldg(xp + o)), hk = unpk(__ldg(hp + o));
+          const uint32_t xw = __ldg(xp + o);
+          if (k == 0 && tail_row) tail_row[o] = xw;
+          const C2 x = unpk(xw), hk = unpk(__ldg(hp + o));
           ar[j] += (long long)x.re * hk.re;
           ar[j] -= (long long)x.im * hk.im;
           ai[j] += (long long)x.re * hk.im;
@@ -331,6 +340,15 @@ __global__ void __launch_bounds__(256, 3) k_front_fast(FrontParams p, unsigned F
   const unsigned n_items = FB * CB;
   unsigned pfl = 0, sf = 0;
   unsigned long long psat = 0;
+  if (p.tail_out && blockIdx.x == 0 && blockIdx.y == 0 && p.F + 1u < (unsigned)T) {
+    // a chunk shorter than the delay line keeps the old line's first frames
+    const unsigned D = (unsigned)T - 1u, keep = D - p.F;
+    for (unsigned i = tid; i < p.C * keep * N; i += 256u) {
+      const unsigned c = i / (keep * N), r = i % (keep * N);
+      const unsigned k = p.F + r / N, ph = r % N;
+      p.tail_out[((size_t)c * D + k) * N + ph] = p.tail[((size_t)c * D + (k - p.F)) * N + ph];
+    }
+  }
   __syncthreads();
   for (unsigned base = 0; base < n_items; base += IPP) {
     const unsigned it = base + item;

@@ -299,8 +299,8 @@ __global__ void __launch_bounds__(MAXT) k_front(FrontParams p, unsigned FB, unsi
 
 static bool g_front_attr = false;
 
-void launch_front(const FrontParams& p, cudaStream_t s) {
-  if (launch_front_fast(p, s)) return;
+unsigned launch_front(const FrontParams& p, cudaStream_t s) {
+  if (launch_front_fast(p, s)) return 1;  // it writes tail_out too
   const unsigned nth = p.N > 256u ? p.N : 256u;
   const unsigned ipp = nth / p.N;
   unsigned CB = 8192u / p.N;
@@ -340,6 +340,9 @@ void launch_front(const FrontParams& p, cudaStream_t s) {
       default: k_front<0, 1024><<<grid, nth, smem, s>>>(p, FB, CB, twn); break;
     }
   }
+  if (!p.tail_out || p.T <= 1) return 1;
+  launch_tail_update(p.adc, p.ld, p.tail, p.tail_out, p.F, p.C, p.N, p.T, s);
+  return 2;
 }
 
 // New delay line after a chunk of F frames: tail'[c][k] = frame F-1-k of the

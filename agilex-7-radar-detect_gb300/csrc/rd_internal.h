@@ -32,6 +32,7 @@ struct FrontParams {
   const uint32_t* adc;      // chunk frame 0 of channel 0; channel c at +c*ld
   uint64_t ld;
   const uint32_t* tail;     // [C][T-1][N]: tail[c][k][p] = frame -1-k
+  uint32_t* tail_out;       // the delay line after this chunk (the other buffer), or null
   const uint32_t* coeff_t;  // [T][N] (tap-major copy of the phase-major bank)
   const int2* coeff2;       // [T][N] the same, unpacked {re, im}
   uint32_t pfb32;           // 1: the bank's phase L1 norms keep every sum in int32
@@ -45,7 +46,9 @@ struct FrontParams {
   uint32_t safe_in;         // PFB outputs within this bound cannot saturate the FFT
   DevStats* stats;
 };
-void launch_front(const FrontParams& p, cudaStream_t s);
+// Returns the launches made: the front end writes tail_out itself where it can,
+// else a second launch does (pfb_model.hpp:170-175).
+unsigned launch_front(const FrontParams& p, cudaStream_t s);
 // The largest per-component magnitude of the FFT input for which no
 // sub-stage of an (n, spc) transform with this scaling schedule can
 // saturate (k_frontend.cu).

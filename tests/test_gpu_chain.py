@@ -86,6 +86,27 @@ def test_chain_random_vs_oracle(gpulib, port, seed):
     assert diff(fg, fo, ("cov_windows", "cov_acc")) == []
 
 
+@pytest.mark.parametrize("name,max_frames,calls", [("medium", 3, (1, 2, 5, 9, 1)),
+                                                    ("full", 4, (1, 3, 6, 2))])
+def test_chain_short_chunks_delay_line(gpulib, port, name, max_frames, calls):
+    # launches shorter than the PFB delay line (taps - 1 frames): the next
+    # delay line keeps part of the old one, the rest comes from the chunk
+    p = sc.preset(name, cov_window=8)
+    cfg = sc.make_config(p, max_frames=max_frames)
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    g = gc.Chain(cfg, coeff, w, (px, py))
+    o = port.chain(cfg, coeff, w, px, py)
+    start = 0
+    for nf in calls:
+        x = sc.adc(p, nf * p.n_fft, start=start * p.n_fft)
+        rg = g.process(x, taps=True)
+        ro = o.process(x, taps=True, threads=8)
+        assert diff(rg, ro, CHAIN_KEYS + TAP_KEYS) == [], (name, nf)
+        start += nf
+    assert diff_stats(g.stats(), o.stats()) == []
+
+
 def test_chain_medium_cpi_vs_oracle(gpulib, port):
     p = sc.preset("medium")
     cfg = sc.make_config(p, max_frames=100)
