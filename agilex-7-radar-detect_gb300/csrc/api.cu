@@ -176,6 +176,9 @@ struct rd_chain {
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;  // ordering with the caller's stream
 
   DevBuf<uint32_t> coeff_t, weights, tail[2], ring, power, beams_bn, stage, tw_pos;
+  DevBuf<uint32_t> stage2;                 // host-input staging: two buffers, so the
+  cudaStream_t copy_stream = nullptr;      // next chunk's copy overlaps this chunk
+  cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   DevBuf<int4> w_limbs;
   DevBuf<int2> coeff2;      // [T][N] unpacked coefficients
   uint32_t x_safe = 0;      // beamformer: |x| bound for exact int32 sums
@@ -475,6 +478,13 @@ void rd_chain_destroy(rd_chain* ch) {
   if (ch->stream) cudaStreamSynchronize(ch->stream);
   ch->coeff_t.release(); ch->coeff2.release(); ch->weights.release(); ch->w_limbs.release(); ch->w_frag.release(); ch->tail[0].release(); ch->tail[1].release();
   ch->ring.release(); ch->power.release(); ch->beams_bn.release(); ch->stage.release();
+  ch->stage2.release();
+  if (ch->copy_stream) cudaStreamSynchronize(ch->copy_stream);
+  for (int b = 0; b < 2; ++b) {
+    if (ch->ev_ready[b]) cudaEventDestroy(ch->ev_ready[b]);
+    if (ch->ev_free[b]) cudaEventDestroy(ch->ev_free[b]);
+  }
+  if (ch->copy_stream) cudaStreamDestroy(ch->copy_stream);
   ch->tw_pos.release(); ch->ct_units.release(); ch->ct_pq.release();
   ch->px.release(); ch->py.release(); ch->acc_re.release(); ch->acc_im.release();
   ch->cov_out.release(); ch->sticky.release(); ch->satcnt.release(); ch->win_flags.release();
@@ -874,6 +884,14 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
   const uint64_t frames = n / N;
   const uint64_t sld = (uint64_t)c.max_frames * N;
   CK(ch->stage.ensure((size_t)C * sld));
+  CK(ch->stage2.ensure((size_t)C * sld));
+  if (!ch->copy_stream) {
+    CK(cudaStreamCreateWithFlags(&ch->copy_stream, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; ++b) {
+      CK(cudaEventCreateWithFlags(&ch->ev_ready[b], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&ch->ev_free[b], cudaEventDisableTiming));
+    }
+  }
   const bool taps = out->tap_pfb || out->tap_spectrum || out->tap_beams || out->tap_power;
   if (taps) {
     CK(ch->tap_pfb.ensure((size_t)c.max_frames * C * N));
@@ -882,14 +900,24 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
   const uint64_t cap = out->events ? out->cap_events : default_cap(c, frames);
   rd_status st = begin_call(ch, frames, std::max<uint64_t>(cap, 1));
   if (st != RD_OK) return st;
+  // chunk i is copied into staging buffer i % 2 on the copy stream once the
+  // chain has finished with that buffer's previous chunk, so the copy of chunk
+  // i + 1 runs while chunk i computes
+  for (int b = 0; b < 2; ++b) CK(cudaEventRecord(ch->ev_free[b], ch->stream));
   std::vector<uint32_t> hb;
-  for (uint64_t f = 0; f < frames; f += ch->launch_frames) {
+  unsigned bi = 0;
+  for (uint64_t f = 0; f < frames; f += ch->launch_frames, bi ^= 1u) {
     const uint32_t F = (uint32_t)std::min<uint64_t>(ch->launch_frames, frames - f);
-    CK(cudaMemcpy2DAsync(ch->stage.p, sld * 4, adc + f * N, ld * 4, (size_t)F * N * 4, C,
-                         cudaMemcpyHostToDevice, ch->stream));
+    uint32_t* stg = bi ? ch->stage2.p : ch->stage.p;
+    CK(cudaStreamWaitEvent(ch->copy_stream, ch->ev_free[bi], 0));
+    CK(cudaMemcpy2DAsync(stg, sld * 4, adc + f * N, ld * 4, (size_t)F * N * 4, C,
+                         cudaMemcpyHostToDevice, ch->copy_stream));
+    CK(cudaEventRecord(ch->ev_ready[bi], ch->copy_stream));
+    CK(cudaStreamWaitEvent(ch->stream, ch->ev_ready[bi], 0));
     const uint64_t g0 = ch->frame;
-    st = run_chunk(ch, ch->stage.p, sld, F, taps ? ch->tap_pfb.p : nullptr);
+    st = run_chunk(ch, stg, sld, F, taps ? ch->tap_pfb.p : nullptr);
     if (st != RD_OK) return st;
+    CK(cudaEventRecord(ch->ev_free[bi], ch->stream));
     if (taps) {  // debug taps: copied out chunk by chunk
       CK(cudaStreamSynchronize(ch->stream));
       const size_t fcn = (size_t)F * C * N, fbn = (size_t)F * B * N;

@@ -28,7 +28,9 @@ class Outputs:
     """Host result buffers for one process call (layout of rd_output)."""
 
     def __init__(self, cfg: abi.RdConfig, frames: int, n_pairs: int, taps: bool = False,
-                 cap_events: int | None = None):
+                 cap_events: int | None = None, alloc=np.zeros):
+        """`alloc(shape, dtype)` makes the result arrays (np.zeros; a caller
+        may pass pinned host memory so the device writes them by DMA)."""
         N, Cn, B = cfg.n_fft, cfg.n_chan, cfg.n_beams
         if cap_events is None:
             cap_events = frames * B * (2 + N // 16)
@@ -36,10 +38,10 @@ class Outputs:
         nfl = 1 + (176 + cfg.packet_w - 1) // cfg.packet_w
         wl = max(cfg.cov_window, 1)
         cap_w = frames // wl + 2 if cfg.cov_source else 0
-        self.events = np.zeros(max(cap_events, 1), abi.EVENT_DTYPE)
-        self.flits = np.zeros((max(cap_events, 1) * nfl, words), np.uint32)
-        self.cov_windows = np.zeros(max(cap_w, 1), abi.COVWIN_DTYPE)
-        self.cov_acc = np.zeros((max(cap_w, 1), N, max(n_pairs, 1), 2), np.int64)
+        self.events = alloc(max(cap_events, 1), abi.EVENT_DTYPE)
+        self.flits = alloc((max(cap_events, 1) * nfl, words), np.uint32)
+        self.cov_windows = alloc(max(cap_w, 1), abi.COVWIN_DTYPE)
+        self.cov_acc = alloc((max(cap_w, 1), N, max(n_pairs, 1), 2), np.int64)
         self.taps = taps
         o = self.c = abi.RdOutput()
         o.events, o.cap_events = ptr(self.events), cap_events

@@ -488,7 +488,13 @@ def run_gpu(a, rank: int, world: int, local: int) -> None:
     e2e = None
     if not a.no_e2e:
         cap = max(4 * n_events, 1024)
-        out = gc.Outputs(cfg, n // p.n_fft, chain.n_pairs, False, cap)
+
+        def pinned(shape, dtype):  # page-locked result buffers: the D2H runs as DMA
+            dt = np.dtype(dtype)
+            k = int(np.prod(shape)) * dt.itemsize
+            return torch.empty(k, dtype=torch.uint8, pin_memory=True).numpy().view(dt).reshape(shape)
+
+        out = gc.Outputs(cfg, n // p.n_fft, chain.n_pairs, False, cap, alloc=pinned)
         adc_ptr = abi.C.c_void_p(host.data_ptr())
         times = []
         for i in range(max(2, a.warmup) + a.steps):
