@@ -179,6 +179,13 @@ struct rd_chain {
   DevBuf<uint32_t> stage2;                 // host-input staging: two buffers, so the
   cudaStream_t copy_stream = nullptr;      // next chunk's copy overlaps this chunk
   cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
+  // results drained into page-locked host buffers chunk by chunk
+  cudaStream_t out_stream = nullptr;
+  unsigned long long* h_snaps = nullptr;   // page-locked: events of the call after each chunk
+  size_t h_snaps_n = 0;
+  cudaEvent_t ev_snap[2] = {nullptr, nullptr};
+  bool drained_events = false, drained_flits = false;
+  uint32_t drained_windows = 0;
   DevBuf<int4> w_limbs;
   DevBuf<int2> coeff2;      // [T][N] unpacked coefficients
   uint32_t x_safe = 0;      // beamformer: |x| bound for exact int32 sums
@@ -485,6 +492,13 @@ void rd_chain_destroy(rd_chain* ch) {
     if (ch->ev_free[b]) cudaEventDestroy(ch->ev_free[b]);
   }
   if (ch->copy_stream) cudaStreamDestroy(ch->copy_stream);
+  if (ch->out_stream) {
+    cudaStreamSynchronize(ch->out_stream);
+    cudaStreamDestroy(ch->out_stream);
+  }
+  if (ch->h_snaps) cudaFreeHost(ch->h_snaps);
+  for (int b = 0; b < 2; ++b)
+    if (ch->ev_snap[b]) cudaEventDestroy(ch->ev_snap[b]);
   ch->tw_pos.release(); ch->ct_units.release(); ch->ct_pq.release();
   ch->px.release(); ch->py.release(); ch->acc_re.release(); ch->acc_im.release();
   ch->cov_out.release(); ch->sticky.release(); ch->satcnt.release(); ch->win_flags.release();
@@ -577,6 +591,7 @@ rd_status rd_chain_set_pairs(rd_chain* ch, const uint32_t* x, const uint32_t* y,
 }
 
 __global__ void k_call_begin(DevStats* s) { s->events_call = 0; }
+
 __global__ void k_call_end(DevStats* s) {
   s->scan_scratch[0] = s->events_call;  // events of the call just finished
   s->events_total += s->events_call;
@@ -764,6 +779,8 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
 static rd_status begin_call(rd_chain* ch, uint64_t frames, uint64_t cap_events) {
   const rd_config& c = ch->cfg;
   ch->call_frames = frames;
+  ch->drained_events = ch->drained_flits = false;
+  ch->drained_windows = 0;
   ch->call_windows.clear();
   ch->launches = 0;
   const uint64_t worst = frames * c.n_beams * (c.n_fft + 1ull);
@@ -835,6 +852,7 @@ rd_status rd_chain_fetch(rd_chain* ch, rd_output* out) {
   if (!ch || !out) return fail(RD_EINVAL, "null argument");
   const rd_config& c = ch->cfg;
   CK(cudaStreamSynchronize(ch->stream));
+  if (ch->out_stream) CK(cudaStreamSynchronize(ch->out_stream));
   DevStats ds;
   CK(cudaMemcpy(&ds, ch->stats.p, sizeof(ds), cudaMemcpyDeviceToHost));
   const uint64_t n_ev = ds.scan_scratch[0];
@@ -848,12 +866,14 @@ rd_status rd_chain_fetch(rd_chain* ch, rd_output* out) {
   if (out->events) {
     const uint64_t k = std::min<uint64_t>(avail, out->cap_events);
     if (k < n_ev) trunc = true;
-    if (k) CK(cudaMemcpy(out->events, ch->events.p, k * sizeof(rd_event), cudaMemcpyDeviceToHost));
+    if (k && !ch->drained_events)
+      CK(cudaMemcpy(out->events, ch->events.p, k * sizeof(rd_event), cudaMemcpyDeviceToHost));
   }
   if (out->flits) {
     const uint64_t k = std::min<uint64_t>(avail, out->cap_flits / nfl);
     if (k < n_ev) trunc = true;
-    if (k) CK(cudaMemcpy(out->flits, ch->flits.p, k * nfl * words * 4, cudaMemcpyDeviceToHost));
+    if (k && !ch->drained_flits)
+      CK(cudaMemcpy(out->flits, ch->flits.p, k * nfl * words * 4, cudaMemcpyDeviceToHost));
   }
   const uint32_t nw = (uint32_t)ch->call_windows.size();
   out->n_cov_windows = nw;
@@ -867,9 +887,12 @@ rd_status rd_chain_fetch(rd_chain* ch, rd_output* out) {
         out->cov_windows[w] = ch->call_windows[w];
         out->cov_windows[w].sat_flags = (uint8_t)wf[w];
       }
-    if (out->cov_acc && k)
-      CK(cudaMemcpy(out->cov_acc, ch->cov_out.p, (size_t)k * c.n_fft * ch->P * 2 * 8,
+    const uint32_t d = std::min(ch->drained_windows, k);  // already there
+    if (out->cov_acc && k > d) {
+      const size_t per = (size_t)c.n_fft * ch->P * 2;
+      CK(cudaMemcpy(out->cov_acc + d * per, ch->cov_out.p + d * per, (size_t)(k - d) * per * 8,
                     cudaMemcpyDeviceToHost));
+    }
   }
   return trunc ? fail(RD_ETRUNC, "output capacity exceeded") : RD_OK;
 }
@@ -905,8 +928,64 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
   // i + 1 runs while chunk i computes
   for (int b = 0; b < 2; ++b) CK(cudaEventRecord(ch->ev_free[b], ch->stream));
   std::vector<uint32_t> hb;
-  unsigned bi = 0;
-  for (uint64_t f = 0; f < frames; f += ch->launch_frames, bi ^= 1u) {
+  // results into page-locked host buffers are copied chunk by chunk on a third
+  // stream while later chunks compute: once chunk i - 1 has finished, the
+  // host reads its event count (a page-locked snapshot) and queues the copy of
+  // exactly its events, packets and closed windows. Other host buffers are
+  // filled at the end.
+  auto pinned = [](const void* p) {
+    cudaPointerAttributes a{};
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+  };
+  const bool dev_ev = !taps && pinned(out->events), dev_fl = !taps && pinned(out->flits);
+  const bool dev_cov = !taps && pinned(out->cov_acc);
+  const bool drain = dev_ev || dev_fl || dev_cov;
+  const uint64_t n_chunks = (frames + ch->launch_frames - 1) / ch->launch_frames;
+  const uint32_t nfl = rd_detection_flits(c.packet_w);
+  const size_t pk = (size_t)nfl * rd_flit_words(c.packet_w);
+  if (drain) {
+    if (!ch->out_stream) {
+      CK(cudaStreamCreateWithFlags(&ch->out_stream, cudaStreamNonBlocking));
+      for (int b = 0; b < 2; ++b) CK(cudaEventCreateWithFlags(&ch->ev_snap[b], cudaEventDisableTiming));
+    }
+    if (ch->h_snaps_n < n_chunks) {
+      if (ch->h_snaps) CK(cudaFreeHost(ch->h_snaps));
+      ch->h_snaps = nullptr;
+      ch->h_snaps_n = 0;
+      CK(cudaHostAlloc((void**)&ch->h_snaps, n_chunks * sizeof(unsigned long long),
+                       cudaHostAllocDefault));
+      ch->h_snaps_n = n_chunks;
+    }
+  }
+  const uint64_t cap_ev = std::min<uint64_t>(ch->call_cap_events, out->cap_events);
+  const uint64_t cap_fl = std::min<uint64_t>(ch->call_cap_events, out->cap_flits / nfl);
+  const size_t cov_per = (size_t)N * ch->P * 2;
+  std::vector<uint32_t> win_end(n_chunks, 0);  // windows closed by the end of each chunk
+  // queue the copies of chunk k's results (its snapshot has landed)
+  auto drain_chunk = [&](uint64_t k) -> rd_status {
+    CK(cudaEventSynchronize(ch->ev_snap[k & 1]));  // chunk k is done: its results are final
+    const uint64_t lo = k ? ch->h_snaps[k - 1] : 0, hi = ch->h_snaps[k];
+    const uint64_t e1 = std::min(hi, cap_ev), f1 = std::min(hi, cap_fl);
+    if (dev_ev && e1 > lo)
+      CK(cudaMemcpyAsync(out->events + lo, ch->events.p + lo, (e1 - lo) * sizeof(rd_event),
+                         cudaMemcpyDeviceToHost, ch->out_stream));
+    if (dev_fl && f1 > lo)
+      CK(cudaMemcpyAsync(out->flits + lo * pk, ch->flits.p + lo * pk, (f1 - lo) * pk * 4,
+                         cudaMemcpyDeviceToHost, ch->out_stream));
+    const uint32_t w0 = k ? win_end[k - 1] : 0u;
+    const uint32_t w1 = std::min<uint32_t>(win_end[k], out->cap_cov_windows);
+    if (dev_cov && w1 > w0)
+      CK(cudaMemcpyAsync(out->cov_acc + w0 * cov_per, ch->cov_out.p + w0 * cov_per,
+                         (size_t)(w1 - w0) * cov_per * 8, cudaMemcpyDeviceToHost, ch->out_stream));
+    if (dev_cov) ch->drained_windows = std::max(ch->drained_windows, w1);
+    return RD_OK;
+  };
+  unsigned bi = 0, chunk = 0;
+  for (uint64_t f = 0; f < frames; f += ch->launch_frames, bi ^= 1u, ++chunk) {
     const uint32_t F = (uint32_t)std::min<uint64_t>(ch->launch_frames, frames - f);
     uint32_t* stg = bi ? ch->stage2.p : ch->stage.p;
     CK(cudaStreamWaitEvent(ch->copy_stream, ch->ev_free[bi], 0));
@@ -918,6 +997,18 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
     st = run_chunk(ch, stg, sld, F, taps ? ch->tap_pfb.p : nullptr);
     if (st != RD_OK) return st;
     CK(cudaEventRecord(ch->ev_free[bi], ch->stream));
+    if (drain) {
+      // the chunk's event count (its CFAR's events_call) into the snapshot
+      win_end[chunk] = (uint32_t)ch->call_windows.size();
+      CK(cudaMemcpyAsync(ch->h_snaps + chunk, &ch->stats.p->events_call,
+                         sizeof(unsigned long long), cudaMemcpyDeviceToHost, ch->stream));
+      CK(cudaEventRecord(ch->ev_snap[chunk & 1], ch->stream));
+      // chunk + 1 is queued behind this one; the previous chunk's results go now
+      if (chunk) {
+        st = drain_chunk(chunk - 1);
+        if (st != RD_OK) return st;
+      }
+    }
     if (taps) {  // debug taps: copied out chunk by chunk
       CK(cudaStreamSynchronize(ch->stream));
       const size_t fcn = (size_t)F * C * N, fbn = (size_t)F * B * N;
@@ -942,8 +1033,14 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
       }
     }
   }
+  if (drain && chunk) {
+    st = drain_chunk(chunk - 1);
+    if (st != RD_OK) return st;
+  }
   st = end_call(ch);
   if (st != RD_OK) return st;
+  ch->drained_events = dev_ev;
+  ch->drained_flits = dev_fl;
   return rd_chain_fetch(ch, out);
 }
 

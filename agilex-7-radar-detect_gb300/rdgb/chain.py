@@ -105,12 +105,15 @@ class Chain:
         c = _u32(w)
         abi.check(self.L, self.L.rd_chain_set_weights(self.h, ptr(c)), "rd_chain_set_weights")
 
-    def process(self, adc: np.ndarray, taps: bool = False, cap_events: int | None = None) -> dict:
-        """Runs n samples per channel of host ADC data [n_chan][n]."""
+    def process(self, adc: np.ndarray, taps: bool = False, cap_events: int | None = None,
+                alloc=np.zeros) -> dict:
+        """Runs n samples per channel of host ADC data [n_chan][n]; `alloc`
+        makes the result buffers (page-locked ones fill while later chunks
+        compute)."""
         adc = _u32(adc)
         n = adc.shape[1]
         frames = n // self.cfg.n_fft
-        out = Outputs(self.cfg, frames, self.n_pairs, taps, cap_events)
+        out = Outputs(self.cfg, frames, self.n_pairs, taps, cap_events, alloc=alloc)
         abi.check(self.L, self.L.rd_chain_process(self.h, ptr(adc), n, n, C.byref(out.c)),
                   "rd_chain_process")
         return out.result()

@@ -107,6 +107,58 @@ def test_chain_short_chunks_delay_line(gpulib, port, name, max_frames, calls):
     assert diff_stats(g.stats(), o.stats()) == []
 
 
+def _pinned_alloc(torch):
+    def alloc(shape, dtype):
+        dt = np.dtype(dtype)
+        k = int(np.prod(shape)) * dt.itemsize
+        a = torch.empty(max(k, 1), dtype=torch.uint8, pin_memory=True).numpy()[:k]
+        a[:] = 0xA5  # anything not written by the call shows
+        return a.view(dt).reshape(shape)
+    return alloc
+
+
+@pytest.mark.parametrize("window", [16, 100])
+def test_process_into_pinned_buffers(gpulib, window):
+    # page-locked result buffers fill chunk by chunk while later chunks
+    # compute; the results equal the ones read at the end into pageable ones
+    torch = pytest.importorskip("torch")
+    p = sc.preset("medium", cov_window=window)
+    cfg = sc.make_config(p, max_frames=64)
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    x = sc.adc(p, 700 * p.n_fft)
+    a, b = gc.Chain(cfg, coeff, w, (px, py)), gc.Chain(cfg, coeff, w, (px, py))
+    for lo, hi in ((0, 400), (400, 700)):  # the second call reuses the drain state
+        xs = x[:, lo * p.n_fft:hi * p.n_fft]
+        want = a.process(xs)
+        got = b.process(xs, alloc=_pinned_alloc(torch))
+        assert diff(got, want) == [], (lo, hi)
+        assert len(want["events"]) > 1000 and len(want["cov_windows"]) >= 2
+
+
+def test_process_into_pinned_buffers_truncated(gpulib):
+    # an event capacity below the call's events: both buffers keep the first
+    # cap events and packets, and the call reports the truncation
+    torch = pytest.importorskip("torch")
+    p = sc.preset("medium")
+    cfg = sc.make_config(p, max_frames=64)
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    x = gc._u32(sc.adc(p, 300 * p.n_fft))
+    outs = []
+    for alloc in (np.zeros, _pinned_alloc(torch)):
+        ch = gc.Chain(cfg, coeff, w, (px, py))
+        o = gc.Outputs(cfg, 300, ch.n_pairs, False, 777, alloc=alloc)
+        st = ch.L.rd_chain_process(ch.h, gc.ptr(x), x.shape[1], x.shape[1], gc.C.byref(o.c))
+        assert st == abi.RD_ETRUNC
+        outs.append(o)
+    a, b = outs
+    assert a.c.n_events == b.c.n_events > 777
+    assert np.array_equal(a.events[:777], b.events[:777])
+    nfl = len(a.flits) // 777
+    assert np.array_equal(a.flits[:777 * nfl], b.flits[:777 * nfl])
+
+
 def test_chain_medium_cpi_vs_oracle(gpulib, port):
     p = sc.preset("medium")
     cfg = sc.make_config(p, max_frames=100)
