@@ -193,7 +193,11 @@ rd_status rd_chain_set_pairs(rd_chain* ch, const uint32_t* x, const uint32_t* y,
                              uint32_t n_pairs);
 
 /* Process n samples per channel (a multiple of n_fft) from HOST memory laid
- * out [n_chan][ld]. Copies in, runs, copies the results out. Synchronous. */
+ * out [n_chan][ld]. Copies in, runs, copies the results out. Synchronous.
+ * The copies overlap the kernels chunk by chunk: each chunk's input is copied
+ * while the previous chunk computes, and results into page-locked host
+ * buffers (cudaHostAlloc, cudaHostRegister) are copied as each chunk
+ * finishes; into pageable buffers they are copied at the end. */
 rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n,
                            uint64_t ld, rd_output* out);
 
