@@ -188,6 +188,8 @@ struct rd_chain {
   uint32_t drained_windows = 0;
   DevBuf<int4> w_limbs;
   DevBuf<int2> coeff2;      // [T][N] unpacked coefficients
+  DevBuf<uint2> coeff_dp;   // [T][N] byte limbs for the two-way dot products
+  uint32_t pfb_dp = 0;
   uint32_t x_safe = 0;      // beamformer: |x| bound for exact int32 sums
   uint32_t pfb32 = 0;       // 1: int32 PFB accumulation is exact for this bank
   DevBuf<uint32_t> w_frag;  // tensor form: mma fragments of the limb-split weights
@@ -410,6 +412,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
       bad(cudaEventCreateWithFlags(&ch->ev_in, cudaEventDisableTiming)) ||
       bad(cudaEventCreateWithFlags(&ch->ev_out, cudaEventDisableTiming)) ||
       bad(ch->coeff_t.ensure((size_t)T * N)) || bad(ch->coeff2.ensure((size_t)T * N)) ||
+      bad(ch->coeff_dp.ensure((size_t)T * N)) ||
       bad(ch->weights.ensure((size_t)B * C)) ||
       bad(ch->w_limbs.ensure((size_t)B * C)) ||
       (c.form == RD_FORM_TENSOR && bad(ch->w_frag.ensure(beam_tc_fragment_words(C, B)))) ||
@@ -425,6 +428,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
   ch->own_stream = true;
   cudaMemset(ch->coeff_t.p, 0, (size_t)T * N * 4);
   cudaMemset(ch->coeff2.p, 0, (size_t)T * N * sizeof(int2));
+  cudaMemset(ch->coeff_dp.p, 0, (size_t)T * N * sizeof(uint2));
   cudaMemset(ch->weights.p, 0, (size_t)B * C * 4);
   cudaMemset(ch->w_limbs.p, 0, (size_t)B * C * sizeof(int4));
   if (c.form == RD_FORM_TENSOR)
@@ -483,7 +487,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
 void rd_chain_destroy(rd_chain* ch) {
   if (!ch) return;
   if (ch->stream) cudaStreamSynchronize(ch->stream);
-  ch->coeff_t.release(); ch->coeff2.release(); ch->weights.release(); ch->w_limbs.release(); ch->w_frag.release(); ch->tail[0].release(); ch->tail[1].release();
+  ch->coeff_t.release(); ch->coeff2.release(); ch->coeff_dp.release(); ch->weights.release(); ch->w_limbs.release(); ch->w_frag.release(); ch->tail[0].release(); ch->tail[1].release();
   ch->ring.release(); ch->power.release(); ch->beams_bn.release(); ch->stage.release();
   ch->stage2.release();
   if (ch->copy_stream) cudaStreamSynchronize(ch->copy_stream);
@@ -526,6 +530,12 @@ rd_status rd_chain_set_coeff(rd_chain* ch, const rd_cplx16* coeff) {
   // unpacked copy, and whether every phase's L1 norm sum_k |hr| + |hi| keeps
   // the PFB sums of any int16 input inside int32 (|sum| <= 2^15 x norm)
   std::vector<int2> t2(t.size());
+  // byte limbs for dp2a: h = 256 hh + hl, hl in [0, 255]; the real part uses
+  // -hi, so a bank holding hi = -32768 (whose negation has no int8 high
+  // limb) keeps the plain multiplies
+  std::vector<uint2> tdp(t.size());
+  bool neg_ok = true;
+  auto lim = [](int v, int sh) { return (uint32_t)((sh ? (v >> 8) : (v & 0xFF)) & 0xFF); };
   uint64_t worst = 0;
   for (uint32_t p = 0; p < N; ++p) {
     uint64_t l1 = 0;
@@ -534,12 +544,21 @@ rd_status rd_chain_set_coeff(rd_chain* ch, const rd_cplx16* coeff) {
       const int re = (int16_t)(uint16_t)(v & 0xFFFFu), im = (int16_t)(uint16_t)(v >> 16);
       t2[(size_t)k * N + p] = make_int2(re, im);
       l1 += (uint64_t)(re < 0 ? -re : re) + (uint64_t)(im < 0 ? -im : im);
+      if (im == -32768) neg_ok = false;
+      const int ni = -im;
+      // high limbs {re, -im, im, re}, low limbs likewise (bytes 0..3)
+      tdp[(size_t)k * N + p] = make_uint2(
+          lim(re, 1) | lim(ni, 1) << 8 | lim(im, 1) << 16 | lim(re, 1) << 24,
+          lim(re, 0) | lim(ni, 0) << 8 | lim(im, 0) << 16 | lim(re, 0) << 24);
     }
     worst = std::max(worst, l1);
   }
   ch->pfb32 = worst <= 65535u ? 1u : 0u;
+  ch->pfb_dp = ch->pfb32 && neg_ok ? 1u : 0u;
   CK(cudaMemcpyAsync(ch->coeff2.p, t2.data(), t2.size() * sizeof(int2), cudaMemcpyHostToDevice,
                      ch->stream));
+  CK(cudaMemcpyAsync(ch->coeff_dp.p, tdp.data(), tdp.size() * sizeof(uint2),
+                     cudaMemcpyHostToDevice, ch->stream));
   CK(cudaStreamSynchronize(ch->stream));
   return RD_OK;
 }
@@ -614,6 +633,8 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   fp.tail_out = c.taps > 1 ? ch->tail[ch->tail_cur ^ 1].p : nullptr;
   fp.coeff_t = ch->coeff_t.p;
   fp.coeff2 = ch->coeff2.p;
+  fp.coeff_dp = ch->coeff_dp.p;
+  fp.pfb_dp = ch->pfb_dp;
   fp.pfb32 = ch->pfb32;
   fp.ring = ch->ring.p;
   fp.ring_frames = ch->R;

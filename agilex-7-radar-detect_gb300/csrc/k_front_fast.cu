@@ -81,6 +81,30 @@ __device__ __forceinline__ C2 twm(C2 a, uint32_t wp, unsigned& ovf, unsigned& fl
   return C2{q15<FL>(a.re * wr - a.im * wi, ovf, fl), q15<FL>(a.re * wi + a.im * wr, ovf, fl)};
 }
 
+// Two-way dot products of the packed sample {re, im} (signed 16-bit halves)
+// with two bytes of b (dp2a: .lo bytes 0-1, .hi bytes 2-3; signed or
+// unsigned bytes), accumulated into c
+__device__ __forceinline__ int dp2a_lo_ss(uint32_t a, uint32_t b, int c) {
+  int d;
+  asm("dp2a.lo.s32.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+__device__ __forceinline__ int dp2a_hi_ss(uint32_t a, uint32_t b, int c) {
+  int d;
+  asm("dp2a.hi.s32.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+__device__ __forceinline__ int dp2a_lo_su(uint32_t a, uint32_t b, int c) {
+  int d;
+  asm("dp2a.lo.s32.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+__device__ __forceinline__ int dp2a_hi_su(uint32_t a, uint32_t b, int c) {
+  int d;
+  asm("dp2a.hi.s32.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+
 // positions of the quad of quad-index tl for a stage pair whose inner
 // distance is 2^P (outer 2^(P+1)): base + {0, d1, d0, d0 + d1}
 template <int P>
@@ -195,7 +219,43 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
     if (ok && p.tap_pfb)
       p.tap_pfb[((size_t)f * p.C + c) * G::N + ph0 + (j & 1) * dph1 + (j >> 1) * dph2] = pk(E[j]);
   };
-  if (p.pfb32) {
+  if (p.pfb_dp) {
+    // x h = 256 x hh + x hl with byte limbs: re = x.re hr + x.im (-hi),
+    // im = x.re hi + x.im hr, two dp2a per limb on the packed sample. The
+    // limb sums stay below 2^28; the true sums are below 2^31 (pfb32), so
+    // recombining modulo 2^32 gives them exactly
+    int hr[4] = {0, 0, 0, 0}, hi[4] = {0, 0, 0, 0}, lr[4] = {0, 0, 0, 0}, li[4] = {0, 0, 0, 0};
+    if (ok) {
+      const uint32_t* xa = p.adc + (size_t)c * p.ld + ph0;
+      const uint32_t* xt = p.tail + (size_t)c * (T - 1) * G::N + ph0;
+      const uint2* hc = p.coeff_dp + ph0;
+#pragma unroll
+      for (int k = 0; k < (TT ? TT : 16); ++k) {
+        if (!TT && k >= T) break;
+        const long long fr = (long long)f - k;
+        const uint32_t* xp = fr >= 0 ? xa + (size_t)fr * G::N : xt + (size_t)(-fr - 1) * G::N;
+        const uint2* hp = hc + (size_t)k * G::N;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int o = (j & 1) * dph1 + (j >> 1) * dph2;
+          const uint32_t xw = __ldg(xp + o);
+          if (k == 0 && tail_row) tail_row[o] = xw;
+          const uint2 h = __ldg(hp + o);
+          hr[j] = dp2a_lo_ss(xw, h.x, hr[j]);
+          hi[j] = dp2a_hi_ss(xw, h.x, hi[j]);
+          lr[j] = dp2a_lo_su(xw, h.y, lr[j]);
+          li[j] = dp2a_hi_su(xw, h.y, li[j]);
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      unsigned fr = 0, fi = 0;
+      const int yr = q15_out32((int)((uint32_t)hr[j] * 256u + (uint32_t)lr[j]), &fr);
+      const int yi = q15_out32((int)((uint32_t)hi[j] * 256u + (uint32_t)li[j]), &fi);
+      finish(j, yr, yi, fr, fi);
+    }
+  } else if (p.pfb32) {
     // every partial sum is bounded by 2^15 x the phase's L1 norm < 2^31
     int ar[4] = {0, 0, 0, 0}, ai[4] = {0, 0, 0, 0};
     if (ok) {

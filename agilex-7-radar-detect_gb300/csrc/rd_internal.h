@@ -36,6 +36,8 @@ struct FrontParams {
   const uint32_t* coeff_t;  // [T][N] (tap-major copy of the phase-major bank)
   const int2* coeff2;       // [T][N] the same, unpacked {re, im}
   uint32_t pfb32;           // 1: the bank's phase L1 norms keep every sum in int32
+  const uint2* coeff_dp;    // [T][N] byte limbs {hh: re, -im, im, re}, {hl: ...} for dp2a
+  uint32_t pfb_dp;          // 1: pfb32 and the limbs hold (no im = -32768): dp2a path
   uint32_t* ring;           // [R][N][C]
   uint32_t ring_frames;     // R
   uint32_t ring_base;       // ring slot of chunk frame 0 (g0 mod R)

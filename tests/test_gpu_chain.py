@@ -159,6 +159,30 @@ def test_process_into_pinned_buffers_truncated(gpulib):
     assert np.array_equal(a.flits[:777 * nfl], b.flits[:777 * nfl])
 
 
+@pytest.mark.parametrize("extreme", [False, True])
+def test_pfb_small_bank_paths(gpulib, port, extreme):
+    # a bank whose phase norms keep the PFB sums in int32 runs the byte-limb
+    # dot products; one holding an imaginary -32768 (its negation has no int8
+    # high limb) runs the plain int32 multiplies - both bit-exact
+    rng = np.random.default_rng(31 + extreme)
+    p = sc.preset("medium")
+    re = rng.integers(-800, 800, p.n_fft * p.taps)
+    im = rng.integers(-800, 800, p.n_fft * p.taps)
+    re[::p.taps] = 16000
+    im[1::p.taps] = -32768 if extreme else -32767
+    re[2::p.taps], im[2::p.taps] = 0, 0
+    l1 = (np.abs(re) + np.abs(im)).reshape(p.n_fft, p.taps).sum(1).max()
+    assert l1 <= 65535  # the int32 PFB sums hold
+    coeff = sc.pack(re, im)
+    cfg = sc.make_config(p, max_frames=40)
+    px, py = sc.pair_table(p)
+    w = sc.steering_weights(p.n_chan, p.n_beams)
+    x = sc.adc(p, 90 * p.n_fft)
+    rg = gc.Chain(cfg, coeff, w, (px, py)).process(x, taps=True)
+    ro = port.chain(cfg, coeff, w, px, py).process(x, taps=True, threads=8)
+    assert diff(rg, ro, CHAIN_KEYS + TAP_KEYS) == []
+
+
 def test_chain_medium_cpi_vs_oracle(gpulib, port):
     p = sc.preset("medium")
     cfg = sc.make_config(p, max_frames=100)
