@@ -74,11 +74,11 @@ __device__ __forceinline__ void bfly(C2& a, C2& t, unsigned sh, unsigned& ovf, u
   t = hi;
 }
 
-// a * w rounded once (cmul_q15, fxp.hpp:314-318) for a twiddle w
+// a * w rounded once (cmul_q15, fxp.hpp:314-318) for a twiddle w {re, im}
+// (kept unpacked in shared memory)
 template <bool FL>
-__device__ __forceinline__ C2 twm(C2 a, uint32_t wp, unsigned& ovf, unsigned& fl) {
-  const int wr = sext16(wp), wi = (int)wp >> 16;
-  return C2{q15<FL>(a.re * wr - a.im * wi, ovf, fl), q15<FL>(a.re * wi + a.im * wr, ovf, fl)};
+__device__ __forceinline__ C2 twm(C2 a, int2 w, unsigned& ovf, unsigned& fl) {
+  return C2{q15<FL>(a.re * w.x - a.im * w.y, ovf, fl), q15<FL>(a.re * w.y + a.im * w.x, ovf, fl)};
 }
 
 // Two-way dot products of the packed sample {re, im} (signed 16-bit halves)
@@ -131,7 +131,7 @@ __device__ __forceinline__ int sidx(int q, int pos) {
 // the lane values are in buf[cur] (smem, phase order), cur updated.
 template <int NL, int SPC, bool FL, int S>
 __device__ __forceinline__ void lane_stages(C2 (&E)[4], int q, int tl, unsigned sched,
-                                            const uint32_t* twp, uint32_t* buf0, uint32_t* buf1,
+                                            const int2* twp, uint32_t* buf0, uint32_t* buf1,
                                             int& cur, unsigned& ovf, unsigned& sf) {
   constexpr int M = 1 << NL;
   if constexpr (S + 1 < NL) {
@@ -146,7 +146,7 @@ __device__ __forceinline__ void lane_stages(C2 (&E)[4], int q, int tl, unsigned 
     bfly<FL, false>(E[0], E[1], sh1, ovf, f1);  // BF2II, distance d1
     bfly<FL, true>(E[2], E[3], sh1, ovf, f1);   // odd block: -j on the lower half
     if constexpr (S + 2 < NL) {                 // group-closing twiddle
-      const uint32_t* tw = twp + (S / 2) * M;
+      const int2* tw = twp + (S / 2) * M;
       E[0] = twm<FL>(E[0], tw[base], ovf, f1);
       E[1] = twm<FL>(E[1], tw[base + d1], ovf, f1);
       E[2] = twm<FL>(E[2], tw[base + d0], ovf, f1);
@@ -192,7 +192,7 @@ __device__ __forceinline__ void lane_stages(C2 (&E)[4], int q, int tl, unsigned 
 // of the pass saturated (block-uniform).
 template <int NL, int SPC, int TT, bool FL>
 __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int q, int tl, bool ok,
-                                                unsigned f, unsigned c, const uint32_t* twp,
+                                                unsigned f, unsigned c, const int2* twp,
                                                 uint32_t* buf0, uint32_t* buf1,
                                                 uint32_t* tile_row, unsigned cbp, unsigned& pfl,
                                                 unsigned long long& psat, unsigned& sf_out) {
@@ -336,7 +336,7 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
     const int t = 2 * tl + q;
     const unsigned shm = (p.sched >> NL) & 1u;
     unsigned fm = 0;
-    const uint32_t* tw = twp + G::NTW * M;
+    const int2* tw = twp + G::NTW * M;
 #pragma unroll
     for (int h2 = 0; h2 < 2; ++h2) {
       const int j = t + h2 * (M / 2);
@@ -367,7 +367,7 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
 // register allocation of the common path.
 template <int NL, int SPC, int TT>
 __device__ __noinline__ void front_pass_flags(const FrontParams& p, int T, int q, int tl, bool ok,
-                                              unsigned f, unsigned c, const uint32_t* twp,
+                                              unsigned f, unsigned c, const int2* twp,
                                               uint32_t* buf0, uint32_t* buf1, uint32_t* tile_row,
                                               unsigned cbp, unsigned* sf_out) {
   unsigned pfl = 0, sf = 0;
@@ -384,12 +384,15 @@ __global__ void __launch_bounds__(256, 3) k_front_fast(FrontParams p, unsigned F
   constexpr int IPP = 256 / TPI;  // items per pass
   extern __shared__ uint32_t sm[];
   const unsigned twn = G::NTW * M + (SPC == 2 ? M : 0);
-  uint32_t* s_tw = sm;
-  uint32_t* s_buf = sm + twn;             // [2][IPP][N]
+  int2* s_tw = reinterpret_cast<int2*>(sm);  // [twn] {re, im}
+  uint32_t* s_buf = sm + 2 * twn;         // [2][IPP][N]
   uint32_t* s_tile = s_buf + 2 * IPP * N; // [FB][N][CB+1]
   const unsigned cbp = CB + 1u;
   const int tid = threadIdx.x;
-  for (unsigned k = tid; k < twn; k += 256u) s_tw[k] = p.tw_pos[k];
+  for (unsigned k = tid; k < twn; k += 256u) {
+    const uint32_t w = p.tw_pos[k];
+    s_tw[k] = make_int2(sext16(w), (int)w >> 16);
+  }
   const int item = tid / TPI, t = tid % TPI;
   const int q = SPC == 2 ? (t & 1) : 0;
   const int tl = SPC == 2 ? (t >> 1) : t;
@@ -454,7 +457,7 @@ static void launch_fast(const FrontParams& p, cudaStream_t s) {
   while (FB * CB * N > 8192u && FB > 1u) FB /= 2;
   while (FB * CB * N > 8192u && CB > 1u) CB /= 2;
   const unsigned twn = G::NTW * G::M + (SPC == 2 ? G::M : 0);
-  const size_t smem = (twn + 2u * IPP * N + (size_t)FB * N * (CB + 1u)) * sizeof(uint32_t);
+  const size_t smem = (2u * twn + 2u * IPP * N + (size_t)FB * N * (CB + 1u)) * sizeof(uint32_t);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_front_fast<NL, SPC, TT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
