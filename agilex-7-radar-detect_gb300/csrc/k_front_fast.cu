@@ -403,10 +403,14 @@ __global__ void __launch_bounds__(256, 3) k_front_fast(FrontParams p, unsigned F
   const unsigned n_items = FB * CB;
   unsigned pfl = 0, sf = 0;
   unsigned long long psat = 0;
-  if (p.tail_out && blockIdx.x == 0 && blockIdx.y == 0 && p.F + 1u < (unsigned)T) {
+  if (p.tail_out && p.F + 1u < (unsigned)T) {
     // a chunk shorter than the delay line keeps the old line's first frames
+    // (spread over the whole grid: at full scale that is 11 x 1024 words a
+    // channel)
     const unsigned D = (unsigned)T - 1u, keep = D - p.F;
-    for (unsigned i = tid; i < p.C * keep * N; i += 256u) {
+    const unsigned nthr = gridDim.x * gridDim.y * 256u;
+    const unsigned g = (blockIdx.y * gridDim.x + blockIdx.x) * 256u + tid;
+    for (unsigned i = g; i < p.C * keep * N; i += nthr) {
       const unsigned c = i / (keep * N), r = i % (keep * N);
       const unsigned k = p.F + r / N, ph = r % N;
       p.tail_out[((size_t)c * D + k) * N + ph] = p.tail[((size_t)c * D + (k - p.F)) * N + ph];
