@@ -1062,7 +1062,12 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
   if (st != RD_OK) return st;
   ch->drained_events = dev_ev;
   ch->drained_flits = dev_fl;
-  return rd_chain_fetch(ch, out);
+  st = rd_chain_fetch(ch, out);
+  // what was copied chunk by chunk went to this call's buffers only: a later
+  // rd_chain_fetch into other buffers copies everything again
+  ch->drained_events = ch->drained_flits = false;
+  ch->drained_windows = 0;
+  return st;
 }
 
 __global__ void k_cov_flush(long long* acc_re, long long* acc_im, unsigned* sticky,

@@ -136,6 +136,21 @@ def test_process_into_pinned_buffers(gpulib, window):
         assert len(want["events"]) > 1000 and len(want["cov_windows"]) >= 2
 
 
+def test_fetch_after_pinned_process(gpulib):
+    # results copied chunk by chunk into one call's page-locked buffers are
+    # read again in full by a later fetch into other buffers
+    torch = pytest.importorskip("torch")
+    p = sc.preset("medium", cov_window=32)
+    cfg = sc.make_config(p, max_frames=64)
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    x = sc.adc(p, 300 * p.n_fft)
+    ch = gc.Chain(cfg, coeff, w, (px, py))
+    first = ch.process(x, alloc=_pinned_alloc(torch))
+    again = ch.fetch(300)
+    assert diff(again, first) == []
+
+
 def test_process_into_pinned_buffers_truncated(gpulib):
     # an event capacity below the call's events: both buffers keep the first
     # cap events and packets, and the call reports the truncation
