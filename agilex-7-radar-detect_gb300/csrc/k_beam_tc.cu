@@ -146,17 +146,45 @@ __global__ void __launch_bounds__(256, 2) k_beam_tc(BeamParams p) {
   }
   __syncthreads();
   // stage: 4 channels per item (channels >= C and rows >= rows read as 0,
-  // whose limbs are 0)
+  // whose limbs are 0). With C a multiple of 4, every thread issues eight
+  // quad loads, then converts them, so the loads overlap instead of each
+  // waiting on the last
   const bool vec = (C & 3u) == 0u;
-  for (unsigned k = tid; k < kTcRows * ks; k += 256u) {
+  constexpr unsigned kBatch = 8u;  // quads in flight per thread
+  for (unsigned k0 = 0; vec && k0 < kTcRows * ks; k0 += kBatch * 256u) {
+    uint4 t[kBatch];
+#pragma unroll
+    for (unsigned q = 0; q < kBatch; ++q) {
+      const unsigned k = k0 + tid + q * 256u;
+      t[q] = make_uint4(0u, 0u, 0u, 0u);
+      if (k < kTcRows * ks) {
+        const unsigned rr = k / ks, j = k - rr * ks;
+        const unsigned long long off = s_off[rr];
+        if (off != ~0ull) t[q] = __ldg(reinterpret_cast<const uint4*>(p.ring + off) + j);
+      }
+    }
+#pragma unroll
+    for (unsigned q = 0; q < kBatch; ++q) {
+      const unsigned k = k0 + tid + q * 256u;
+      if (k < kTcRows * ks) {
+        const unsigned rr = k / ks, j = k - rr * ks;
+        uint4 w0, w1;
+        limb_words(t[q].x, w0.x, w0.y);
+        limb_words(t[q].y, w0.z, w0.w);
+        limb_words(t[q].z, w1.x, w1.y);
+        limb_words(t[q].w, w1.z, w1.w);
+        uint4* dst = reinterpret_cast<uint4*>(s_x + rr * S + 8u * j);
+        dst[0] = w0;
+        dst[1] = w1;
+      }
+    }
+  }
+  for (unsigned k = tid; !vec && k < kTcRows * ks; k += 256u) {
     const unsigned rr = k / ks, j = k - rr * ks;
     const unsigned long long off = s_off[rr];
     uint32_t v0 = 0, v1 = 0, v2 = 0, v3 = 0;
     if (off != ~0ull) {
-      if (vec) {
-        const uint4 t = __ldg(reinterpret_cast<const uint4*>(p.ring + off) + j);
-        v0 = t.x, v1 = t.y, v2 = t.z, v3 = t.w;
-      } else {
+      {
         const unsigned a = 4u * j;
         v0 = p.ring[off + a];
         if (a + 1u < C) v1 = p.ring[off + a + 1u];
