@@ -248,9 +248,9 @@ struct rd_chain {
   }
 };
 
-static const char* kKernelNames[8] = {"k_front", "k_tail", "k_beam", "k_cov",
-                                      "k_cfar",  "",       "",       "k_call"};
-enum { KT_FRONT = 0, KT_TAIL, KT_BEAM, KT_COV, KT_CFAR, KT_CALL = 7 };
+static const char* kKernelNames[8] = {"k_front", "k_beam", "k_cov", "k_cfar",
+                                      "",        "",       "",      "k_call"};
+enum { KT_FRONT = 0, KT_BEAM, KT_COV, KT_CFAR, KT_CALL = 7 };
 
 // Brackets one kernel launch with events on the chain's stream when stage
 // timing is on.
