@@ -712,6 +712,49 @@ __device__ void write_packet(const rd_event& e, uint32_t* out, unsigned pw, unsi
   }
 }
 
+// write_packet for a packet width fixed at compile time: every word's bit
+// offset is a constant, so each word is one funnel shift of the event words
+// and a mask. PW = 0 falls back to the general form.
+template <unsigned PW>
+__device__ __forceinline__ void write_packet_w(const rd_event& e, uint32_t* out, unsigned pw,
+                                               unsigned words, unsigned nfl, unsigned src,
+                                               unsigned dest, unsigned vc, unsigned seq) {
+  if constexpr (PW == 0) {
+    write_packet(e, out, pw, words, nfl, src, dest, vc, seq);
+  } else {
+    constexpr unsigned W = (PW + 5u + 31u) / 32u, NF = 1u + (176u + PW - 1u) / PW;
+    constexpr int top = 5 + (int)PW;
+    const uint64_t hdr = (uint64_t)(dest & 0xFu) | ((uint64_t)(src & 0x1Fu) << 4) |
+                         ((uint64_t)(vc & 3u) << 9) | ((uint64_t)(NF & 0x3Fu) << 14) |
+                         ((uint64_t)(seq & 0xFFFFu) << 20);
+#pragma unroll
+    for (unsigned f = 0; f < NF; ++f) {
+      const uint64_t w0 = f == 0 ? hdr : e.w[0], w1 = f == 0 ? 0ull : e.w[1],
+                     w2 = f == 0 ? 0ull : e.w[2];
+      const int off = f == 0 ? 0 : (int)((f - 1) * PW);
+      const int last = f == 0 ? 36 : (off + (int)PW < 176 ? off + (int)PW : 176);
+      const int lim = 5 + (last - off) < top ? 5 + (last - off) : top;
+      unsigned pop = 0;
+      uint32_t first = 0;
+#pragma unroll
+      for (unsigned k = 0; k < W; ++k) {
+        const int lo = 32 * (int)k;
+        uint32_t v = ext32(w0, w1, w2, off + lo - 5);
+        if (lo < 5) v &= ~0x1Fu;
+        if (lo + 32 > lim) v &= (lim <= lo) ? 0u : ((1u << (lim - lo)) - 1u);
+        if (k == 0) {
+          v |= ((vc & 3u) << 1) | ((f == 0 ? 1u : 0u) << 3) | ((f + 1 == NF ? 1u : 0u) << 4);
+          first = v;
+        } else {
+          out[f * W + k] = v;
+        }
+        pop += __popc(v);
+      }
+      out[f * W] = first | ((pop & 1u) ? 0u : 1u);  // odd parity
+    }
+  }
+}
+
 __device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -864,6 +907,7 @@ __device__ uint4 redecide(const CfarParams& p, uint64_t u, unsigned k) {
 // Event j of an emit CTA (frame f of the CTA, its k-th event): the SUMMARY
 // from the frame's counts, a detection from the frame's slot (or
 // re-decided); the event goes straight out, its packet to `pkt`.
+template <unsigned PW>
 __device__ __forceinline__ void emit_one(const CfarParams& p, unsigned long long j,
                                          unsigned long long base, unsigned long long seq0,
                                          size_t pk, uint64_t f0, const unsigned long long* s_fbase,
@@ -895,10 +939,11 @@ __device__ __forceinline__ void emit_one(const CfarParams& p, unsigned long long
   }
   store_event(p.events + idx, ev, p.ev16);
   if (p.flits)
-    write_packet(ev, pkt, p.packet_w, p.flit_words, p.nfl, p.src_id, p.dest, p.vc,
+    write_packet_w<PW>(ev, pkt, p.packet_w, p.flit_words, p.nfl, p.src_id, p.dest, p.vc,
                  (unsigned)((seq0 + idx) & 0xFFFFu));
 }
 
+template <unsigned PW>
 __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_emit(CfarParams p) {
   __shared__ unsigned long long s_red[kCfarWarps], s_fbase[kEmitFrames + 1];
   __shared__ unsigned s_c[kEmitFrames];
@@ -947,7 +992,7 @@ __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_emit(CfarParams p) {
     const unsigned long long j = j0 + tid;
     const unsigned long long end = base + (total < j0 + blockDim.x ? total : j0 + blockDim.x);
     const unsigned long long stop = end < p.cap ? end : p.cap;  // events of the round kept
-    if (j < total) emit_one(p, j, base, seq0, pk, f0, s_fbase, s_c, s_pk + (size_t)tid * pk);
+    if (j < total) emit_one<PW>(p, j, base, seq0, pk, f0, s_fbase, s_c, s_pk + (size_t)tid * pk);
     __syncthreads();
     if (p.flits && stop > base + j0) {
       const size_t nw = (size_t)(stop - (base + j0)) * pk;
@@ -972,7 +1017,14 @@ static void launch_cfar_r(const CfarParams& p, cudaStream_t s) {
   const unsigned tiles = cfar_tiles(p.frames);
   const unsigned emits = (unsigned)((p.frames + kEmitFrames - 1u) / kEmitFrames);
   k_cfar_decide<R><<<tiles, kCfarWarps * 32, sm, s>>>(p);
-  k_cfar_emit<<<emits, kCfarWarps * 32, (size_t)kCfarWarps * 32 * p.nfl * p.flit_words * 4, s>>>(p);
+  const size_t esm = (size_t)kCfarWarps * 32 * p.nfl * p.flit_words * 4;
+  switch (p.packet_w) {  // the common widths with their word layout fixed
+    case 64: k_cfar_emit<64><<<emits, kCfarWarps * 32, esm, s>>>(p); break;
+    case 128: k_cfar_emit<128><<<emits, kCfarWarps * 32, esm, s>>>(p); break;
+    case 256: k_cfar_emit<256><<<emits, kCfarWarps * 32, esm, s>>>(p); break;
+    case 512: k_cfar_emit<512><<<emits, kCfarWarps * 32, esm, s>>>(p); break;
+    default: k_cfar_emit<0><<<emits, kCfarWarps * 32, esm, s>>>(p); break;
+  }
 }
 
 unsigned cfar_tiles(uint32_t frames) { return (frames + kCfarWarps - 1u) / kCfarWarps; }
