@@ -381,14 +381,30 @@ __global__ void __launch_bounds__(256) k_cov_block(CovParams p, unsigned BT, uns
   const unsigned xi = live ? bl * S + p.px[q] : 0u, yi = live ? bl * S + p.py[q] : 0u;
   long long are = 0, aim = 0;
   uint32_t pre[kCovPre];
+  // row and S powers of two (the usual geometries): the staged word's frame,
+  // bin and channel by shifts
+  const int rsh = (row & (row - 1u)) == 0u ? __ffs(row) - 1 : -1;
+  const int ssh = (S & (S - 1u)) == 0u ? __ffs(S) - 1 : -1;
+  const bool pow2 = rsh >= 0 && ssh >= 0;
   auto load = [&](unsigned fbase) {
 #pragma unroll
     for (unsigned j = 0; j < kCovPre; ++j) {
       const unsigned w = tid + j * nth;
       uint32_t v = 0;
       if (w < per_batch) {
-        const unsigned fl = w / row, r = w % row;
-        const unsigned f = fbase + fl, b = bin0 + r / S, a = r % S;
+        unsigned fl, r, bq, a;
+        if (pow2) {
+          fl = w >> rsh;
+          r = w & (row - 1u);
+          bq = r >> ssh;
+          a = r & (S - 1u);
+        } else {
+          fl = w / row;
+          r = w % row;
+          bq = r / S;
+          a = r % S;
+        }
+        const unsigned f = fbase + fl, b = bin0 + bq;
         if (f < hi && b < p.N) {
           if (p.src_beam) {
             v = __ldg(p.beams_bn + ((size_t)f * p.N + b) * S + a);
