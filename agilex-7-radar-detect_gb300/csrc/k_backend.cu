@@ -226,7 +226,7 @@ __device__ __forceinline__ void integ_step(long long& acc, long long x, unsigned
   if (fl && satcnt != 0xFFFFFFFFu) ++satcnt;
 }
 
-constexpr unsigned kCovPre = 8;  // prefetch registers per thread
+constexpr unsigned kCovPre = 4;  // prefetch registers per thread
 
 // MODE: 0 = exact block mode, 1 = exact exponential mode, 2 = saturating
 // (either mode, sequential). In exact block mode the chunk's frames are split
