@@ -16,8 +16,6 @@
 // together so that its loads and stores run over whole packets.
 #include <cuda_runtime.h>
 
-#include <vector>
-
 #include "rd_internal.h"
 
 namespace {
@@ -138,8 +136,8 @@ rd_status egress_merge(const rd_egress_source* src, uint32_t n_src, uint32_t pac
                      RD_EGRESS_MAX_SRC);
   if (packet_w < 64 || packet_w > 512 || packet_w % 32)
     return set_error(RD_EINVAL, "rd_egress_merge: packet_w %u", packet_w);
-  // a port ring, its source table and the scan all index in 64 bits; the
-  // ring's word offsets must fit as well
+  // ring word offsets (port x cap + position) x words must stay far inside
+  // 64 bits
   const uint32_t words = rd_detection_flits(packet_w) * rd_flit_words(packet_w);
   if (cap_per_port > (~0ull >> 8) / n_ports / words)
     return set_error(RD_EINVAL, "rd_egress_merge: ring too large");
