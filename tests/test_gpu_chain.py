@@ -198,6 +198,23 @@ def test_pfb_small_bank_paths(gpulib, port, extreme):
     assert diff(rg, ro, CHAIN_KEYS + TAP_KEYS) == []
 
 
+@pytest.mark.parametrize("packet_w", [64, 96, 128, 160, 256, 480, 512])
+def test_chain_packet_widths(gpulib, port, packet_w):
+    # the CFAR emit's packet layouts: fixed at compile time for 64/128/256/512,
+    # computed at run time for the other widths - the same flits as the model
+    p = sc.preset("tiny")
+    cfg = sc.make_config(p, max_frames=16)
+    cfg.packet_w = packet_w
+    cfg.src_id, cfg.dest, cfg.vc = 5, 9, 2
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    x = sc.adc(p, 60 * p.n_fft)
+    rg = gc.Chain(cfg, coeff, w, (px, py)).process(x)
+    ro = port.chain(cfg, coeff, w, px, py).process(x, taps=False, threads=4)
+    assert diff(rg, ro) == []
+    assert len(rg["flits"]) == len(rg["events"]) * (1 + -(-176 // packet_w))
+
+
 def test_chain_medium_cpi_vs_oracle(gpulib, port):
     p = sc.preset("medium")
     cfg = sc.make_config(p, max_frames=100)
