@@ -25,10 +25,12 @@ namespace rd {
 // product term is exact in int32: |x * wh| <= 2^22, |x * wl| < 2^23, and a
 // 64-channel block of complex terms stays below 2^31. Blocks are combined in
 // int64 as acc = 256 * acc_h + acc_l - the same integer bf::dot sums.
-template <int BPT>
+// CC > 0 fixes the channel count at compile time (every shared-memory offset
+// of the channel loop a constant); CC = 0 takes it from the parameters.
+template <int BPT, int CC>
 __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
   extern __shared__ uint32_t sm[];
-  const unsigned C = p.C, B = p.B, N = p.N;
+  const unsigned C = CC ? (unsigned)CC : p.C, B = p.B, N = p.N;
   const unsigned xs = C + 1;  // padded row
   int4* s_w = reinterpret_cast<int4*>(sm);          // [B][C] limbs
   int4* s_w3 = reinterpret_cast<int4*>(sm + 4u * B * C);  // [B][C] {re, im, re + im, 0}
@@ -100,9 +102,11 @@ __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
     // modulo 2^32; the true re and im are below 2^31 - 2^15 in magnitude
     // (x_safe), so the wrapped results are the exact integers.
     const uint32_t* xr = s_x + bl * xs;
+    const int4* w3 = s_w3 + bg * C;  // beam bg + 4 j at w3 + 4 j C
     uint32_t sac[BPT], sbd[BPT], sk[BPT];
 #pragma unroll
     for (int j = 0; j < BPT; ++j) sac[j] = sbd[j] = sk[j] = 0u;
+#pragma unroll(CC ? 16 : 4)
     for (unsigned a = 0; a < C; ++a) {
       const uint32_t xv = xr[a];
       const int x_re = (int)(int16_t)(uint16_t)(xv & 0xFFFFu), x_im = (int)xv >> 16;
@@ -111,7 +115,7 @@ __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
       for (int j = 0; j < BPT; ++j) {
         const unsigned b = bg + 4u * j;
         if (BPT == 1 || b < B) {
-          const int4 w = s_w3[b * C + a];
+          const int4 w = w3[4u * j * C + a];
           sac[j] += (uint32_t)(x_re * w.x);
           sbd[j] += (uint32_t)(x_im * w.y);
           sk[j] += x_s * (uint32_t)w.z;
@@ -177,27 +181,42 @@ __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
   }
 }
 
-static bool g_beam_attr_set = false;
+template <int BPT, int CC>
+static void launch_beam_k(const BeamParams& p, dim3 grid, size_t smem, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_beam<BPT, CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr = true;
+  }
+  k_beam<BPT, CC><<<grid, 256, smem, s>>>(p);
+}
+
+// The channel counts of the workloads (16, 32, 64) at compile time (up to 64
+// beams)
+template <int BPT>
+static void launch_beam_b(const BeamParams& p, dim3 grid, size_t smem, cudaStream_t s) {
+  if constexpr (BPT > 16) {
+    launch_beam_k<BPT, 0>(p, grid, smem, s);
+  } else {
+    switch (p.C) {
+      case 16: launch_beam_k<BPT, 16>(p, grid, smem, s); break;
+      case 32: launch_beam_k<BPT, 32>(p, grid, smem, s); break;
+      case 64: launch_beam_k<BPT, 64>(p, grid, smem, s); break;
+      default: launch_beam_k<BPT, 0>(p, grid, smem, s); break;
+    }
+  }
+}
 
 void launch_beam(const BeamParams& p, cudaStream_t s) {
   const unsigned bpt = (p.B + 3u) / 4u;
   const dim3 grid((p.N + 63u) / 64u, p.F);
   const size_t smem = ((size_t)8u * p.B * p.C + 64u * (p.C + 1u)) * sizeof(uint32_t);
-  if (!g_beam_attr_set) {
-    cudaFuncSetAttribute(k_beam<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(k_beam<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(k_beam<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(k_beam<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(k_beam<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(k_beam<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    g_beam_attr_set = true;
-  }
-  if (bpt <= 1) k_beam<1><<<grid, 256, smem, s>>>(p);
-  else if (bpt <= 2) k_beam<2><<<grid, 256, smem, s>>>(p);
-  else if (bpt <= 4) k_beam<4><<<grid, 256, smem, s>>>(p);
-  else if (bpt <= 8) k_beam<8><<<grid, 256, smem, s>>>(p);
-  else if (bpt <= 16) k_beam<16><<<grid, 256, smem, s>>>(p);
-  else k_beam<32><<<grid, 256, smem, s>>>(p);
+  if (bpt <= 1) launch_beam_b<1>(p, grid, smem, s);
+  else if (bpt <= 2) launch_beam_b<2>(p, grid, smem, s);
+  else if (bpt <= 4) launch_beam_b<4>(p, grid, smem, s);
+  else if (bpt <= 8) launch_beam_b<8>(p, grid, smem, s);
+  else if (bpt <= 16) launch_beam_b<16>(p, grid, smem, s);
+  else launch_beam_b<32>(p, grid, smem, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -362,16 +381,20 @@ __global__ void __launch_bounds__(256) k_cov(CovParams p, unsigned BT, unsigned 
 // batch as unpacked {re, im} int32 pairs, so a (bin, pair) thread spends a
 // frame on two 64-bit shared loads and four multiply-adds. A CTA's frames are
 // one window segment (split as in k_cov), so the window closes at most once,
-// after the loop, and no frame needs a count check.
+// after the loop, and no frame needs a count check. SS > 0 fixes the source
+// width at compile time for launches of one bin a CTA (BT = 1), so a frame's
+// staged row is a constant stride.
+template <int SS>
 __global__ void __launch_bounds__(256) k_cov_block(CovParams p, unsigned BT, unsigned QB,
                                                    unsigned FB) {
   extern __shared__ int2 s_xy[];  // [FB][BT][S]
   const unsigned tid = threadIdx.x, nth = blockDim.x;
-  const unsigned S = p.S, row = BT * S, per_batch = FB * row;
+  const unsigned S = SS ? (unsigned)SS : p.S, row = SS ? (unsigned)SS : BT * S;
+  const unsigned per_batch = FB * row;
   const unsigned bin0 = blockIdx.x * BT;
-  const unsigned bl = tid / QB, q = blockIdx.y * QB + tid % QB;
+  const unsigned bl = SS ? 0u : tid / QB, q = blockIdx.y * QB + (SS ? tid : tid % QB);
   const unsigned bin = bin0 + bl;
-  const bool live = bl < BT && bin < p.N && q < p.P;
+  const bool live = (SS ? tid < QB : bl < BT) && bin < p.N && q < p.P;
   const size_t k = (size_t)bin * p.P + q;
   const unsigned z = blockIdx.z, nz = gridDim.z;
   const unsigned first = p.wl - p.count0;  // frames until the open window closes
@@ -447,7 +470,7 @@ __global__ void __launch_bounds__(256) k_cov_block(CovParams p, unsigned BT, uns
       for (unsigned s0 = 0; s0 < nf; s0 += 32u) {
         const unsigned s1 = (nf - s0) < 32u ? nf : s0 + 32u;
         int sr = 0, si = 0;
-#pragma unroll 4
+#pragma unroll(SS ? 8 : 4)
         for (unsigned fl = s0; fl < s1; ++fl) {
           const int2 x = xs[fl * row], y = ys[fl * row];
           sr += x.x * y.x + x.y * y.y;
@@ -513,7 +536,15 @@ void launch_cov(const CovParams& p, cudaStream_t s) {
   }
   const dim3 grid((p.N + BT - 1u) / BT, (p.P + QB - 1u) / QB, nz);
   const size_t smem = (size_t)FB * BT * p.S * sizeof(uint32_t);
-  if (mode == 0) k_cov_block<<<grid, nth, 2 * smem, s>>>(p, BT, QB, FB);
+  if (mode == 0) {
+    if (BT == 1u && (p.S == 16u || p.S == 32u || p.S == 64u)) {
+      if (p.S == 16u) k_cov_block<16><<<grid, nth, 2 * smem, s>>>(p, BT, QB, FB);
+      else if (p.S == 32u) k_cov_block<32><<<grid, nth, 2 * smem, s>>>(p, BT, QB, FB);
+      else k_cov_block<64><<<grid, nth, 2 * smem, s>>>(p, BT, QB, FB);
+    } else {
+      k_cov_block<0><<<grid, nth, 2 * smem, s>>>(p, BT, QB, FB);
+    }
+  }
   else if (mode == 1) k_cov<1><<<grid, nth, smem, s>>>(p, BT, QB, FB);
   else k_cov<2><<<grid, nth, smem, s>>>(p, BT, QB, FB);
 }
@@ -563,33 +594,52 @@ __device__ __forceinline__ void cells4(const CfarParams& p, uint64_t u, unsigned
   for (int k = 0; k < 4; ++k) c[k] = i0 + k < p.n ? cell_at(p, u, i0 + k) : 0ull;
 }
 
-// Inclusive prefix sums pre[1..n] of frame u (pre[0] = 0), warp-cooperative.
-// pre sits one word past a 16-byte boundary, so lane l's pre[4l + 1 .. 4l + 4]
-// are two aligned 16-byte stores. R >= ceil(n / 128) bounds the rows at
-// compile time; every row's cells are loaded before the first scan step.
+// The frame's cells, 4 a lane per row: lane l of row r holds cells
+// 128 r + 4 l .. + 3 (zero past the frame). R >= ceil(n / 128) bounds the
+// rows at compile time; every row is loaded before the first scan step.
 template <int R>
-__device__ __forceinline__ void warp_prefix(const CfarParams& p, uint64_t u, uint64_t* pre,
-                                            bool vec) {
+__device__ __forceinline__ void load_cells(const CfarParams& p, uint64_t u, bool vec,
+                                           uint64_t (&c)[R][4]) {
   const unsigned lane = threadIdx.x & 31u;
-  uint64_t c[R][4];
 #pragma unroll
   for (int r = 0; r < R; ++r) cells4(p, u, (unsigned)r * 128u + lane * 4u, vec, c[r]);
+}
+
+__device__ __forceinline__ void store4(uint64_t* d, uint64_t a, uint64_t b, uint64_t c,
+                                       uint64_t e) {
+  reinterpret_cast<ulonglong2*>(d)[0] = make_ulonglong2(a, b);
+  reinterpret_cast<ulonglong2*>(d)[1] = make_ulonglong2(c, e);
+}
+__device__ __forceinline__ void store4(uint32_t* d, uint32_t a, uint32_t b, uint32_t c,
+                                       uint32_t e) {
+  reinterpret_cast<uint4*>(d)[0] = make_uint4(a, b, c, e);
+}
+
+// Inclusive prefix sums pre[1..n] of the loaded cells (pre[0] = 0),
+// warp-cooperative, in Tp: uint64_t, or uint32_t modulo 2^32 when every
+// window sum the decisions take is below 2^32 (a difference of two wrapped
+// prefixes is then the exact sum). pre + 1 sits on a 16-byte boundary, so
+// lane l's pre[4l + 1 .. 4l + 4] are aligned 16-byte stores.
+template <int R, class Tp>
+__device__ __forceinline__ void warp_prefix(const CfarParams& p, const uint64_t (&c)[R][4], Tp* pre,
+                                            bool vec) {
+  const unsigned lane = threadIdx.x & 31u;
   if (lane == 0) pre[0] = 0;
-  uint64_t carry = 0;
+  Tp carry = 0;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    const uint64_t t0 = c[r][0], t1 = t0 + c[r][1], t2 = t1 + c[r][2], t3 = t2 + c[r][3];
-    uint64_t x = t3;
+    const Tp t0 = (Tp)c[r][0], t1 = t0 + (Tp)c[r][1], t2 = t1 + (Tp)c[r][2],
+             t3 = t2 + (Tp)c[r][3];
+    Tp x = t3;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const uint64_t t = __shfl_up_sync(0xffffffffu, x, o);
+      const Tp t = __shfl_up_sync(0xffffffffu, x, o);
       if ((int)lane >= o) x += t;
     }
-    const uint64_t b = carry + x - t3;
+    const Tp b = carry + x - t3;
     const unsigned i0 = (unsigned)r * 128u + lane * 4u;
     if (vec && i0 < p.n) {
-      reinterpret_cast<ulonglong2*>(pre + i0 + 1)[0] = make_ulonglong2(b + t0, b + t1);
-      reinterpret_cast<ulonglong2*>(pre + i0 + 3)[0] = make_ulonglong2(b + t2, b + t3);
+      store4(pre + i0 + 1, b + t0, b + t1, b + t2, b + t3);
     } else {
       if (i0 < p.n) pre[i0 + 1] = b + t0;
       if (i0 + 1 < p.n) pre[i0 + 2] = b + t1;
@@ -599,38 +649,6 @@ __device__ __forceinline__ void warp_prefix(const CfarParams& p, uint64_t u, uin
     carry += __shfl_sync(0xffffffffu, x, 31);
   }
   __syncwarp();
-}
-
-struct CellDecision {
-  bool emit, detected, evaluable;
-  uint64_t sum;
-  unsigned n;
-};
-
-__device__ __forceinline__ CellDecision decide_cell(const CfarParams& p, const uint64_t* pre,
-                                                    unsigned i, uint64_t cut) {
-  CellDecision d;
-  const long long hi = (long long)i + p.gl + p.rl;
-  const long long lo = (long long)i - (long long)p.gg - (long long)p.rg;
-  const bool ok = hi < (long long)p.n && lo >= 0;
-  uint64_t sl = 0, sg = 0;
-  if (ok) {
-    sl = pre[i + p.gl + p.rl + 1] - pre[i + p.gl + 1];
-    sg = pre[i - p.gg] - pre[i - p.gg - p.rg];
-  }
-  if (p.go) {
-    const bool lead = (sl * p.rg) >= (sg * p.rl);
-    d.sum = lead ? sl : sg;
-    d.n = lead ? p.rl : p.rg;
-  } else {
-    d.sum = sl + sg;
-    d.n = p.rl + p.rg;
-  }
-  const bool usable = p.go ? (p.rl != 0u && p.rg != 0u) : (p.rl + p.rg) != 0u;
-  d.evaluable = ok && p.enable && usable;
-  d.detected = d.evaluable && ((cut * d.n) << 8) > ((uint64_t)p.alpha * d.sum);
-  d.emit = d.detected || p.dense;
-  return d;
 }
 
 __device__ __forceinline__ void set_field(uint64_t* w, unsigned lsb, unsigned n, uint64_t v) {
@@ -788,73 +806,104 @@ __device__ __forceinline__ uint4 pack_detection(uint64_t cut, unsigned bin, unsi
                     (uint32_t)sum, (uint32_t)(sum >> 32) | ((refc & 0x7Fu) << 15));
 }
 
+// Decides every cell of frame u from its prefix sums (Tp as in warp_prefix;
+// the products and comparisons in 64 bits either way): the ballot mask of the
+// emitting cells, the detection slots, the frame's counts. Returns the
+// frame's event count (detections + SUMMARY) and adds its detections to det.
+template <class Tp>
+__device__ __forceinline__ unsigned decide_frame(const CfarParams& p, uint64_t u, const Tp* pre,
+                                                 bool live, int lo_b, int hi_b, unsigned n_ok,
+                                                 unsigned& det) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned words = (p.n + 31u) / 32u;
+  const unsigned ca_n8 = (p.rl + p.rg) << 8;
+  unsigned emitted = 0, mword = 0;
+  for (unsigned r = 0; r < words; ++r) {
+    const unsigned i = r * 32u + lane;
+    bool dt = false;
+    uint64_t cut = 0, sum = 0;
+    unsigned nref = 0;
+    const bool ok = live && (int)i >= lo_b && (int)i < hi_b;  // i < n follows
+    if (ok) {
+      cut = (Tp)(pre[i + 1] - pre[i]);
+      const uint64_t sl = (Tp)(pre[i + p.gl + p.rl + 1] - pre[i + p.gl + 1]);
+      const uint64_t sg = (Tp)(pre[i - p.gg] - pre[i - p.gg - p.rg]);
+      uint64_t lhs;
+      if (p.go) {
+        const bool lead = (sl * p.rg) >= (sg * p.rl);
+        sum = lead ? sl : sg;
+        nref = lead ? p.rl : p.rg;
+        lhs = (cut * nref) << 8;
+      } else {
+        sum = sl + sg;
+        nref = p.rl + p.rg;
+        lhs = cut * ca_n8;
+      }
+      dt = lhs > (uint64_t)p.alpha * sum;
+    }
+    bool em = dt;
+    unsigned m = __ballot_sync(0xffffffffu, dt);
+    det += __popc(m);
+    if (p.dense) {  // every cell emits; the detected ones still count
+      em = i < p.n;
+      m = __ballot_sync(0xffffffffu, em);
+      if (em && !ok) cut = (Tp)(pre[i + 1] - pre[i]);
+    }
+    if (lane == (r & 31u)) mword = m;
+    if (em) {  // the frame's k-th event, while it fits the frame's slots
+      const unsigned k = emitted + __popc(m & ((1u << lane) - 1u));
+      if (k < kCfarSlots)
+        p.slots[u * kCfarSlots + k] =
+            pack_detection(cut, i, dt ? 0u : (!ok ? 2u : 1u), ok ? sum : 0ull, ok ? nref : 0u);
+    }
+    emitted += __popc(m);
+  }
+  if (lane < words) p.mask[u * words + lane] = mword;  // words <= 32
+  if (lane == 0) {
+    p.counts[u] = emitted + 1u;
+    p.detsup[u] = det | ((p.n - n_ok) << 16);  // n <= 1024: both fit 16 bits
+  }
+  return emitted + 1u;  // + SUMMARY
+}
+
 template <int R>
 __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_decide(CfarParams p) {
   extern __shared__ __align__(16) uint64_t s_pre[];
   __shared__ unsigned s_cnt[kCfarWarps], s_det[kCfarWarps];
   const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   const uint64_t u = (uint64_t)blockIdx.x * kCfarWarps + warp;
-  // pre[0] one word past a 16-byte boundary (n + 2 words a warp, n even)
-  uint64_t* pre = s_pre + (size_t)warp * (p.n + 2u) + 1u;
-  const unsigned words = (p.n + 31u) / 32u;
+  // the warp's n + 2 words (on a 16-byte boundary when n is even, as the
+  // 16-byte stores need)
+  uint64_t* wbase = s_pre + (size_t)warp * (p.n + 2u);
   // cells whose window fits the frame: lo_b <= i < hi_b; only they are
   // evaluable, so the suppressed count is the same for every frame
   const int lo_b = (int)(p.gg + p.rg), hi_b = (int)p.n - (int)(p.gl + p.rl);
   const bool usable = p.go ? (p.rl != 0u && p.rg != 0u) : (p.rl + p.rg) != 0u;
   const bool live = p.enable && usable;
   const unsigned n_ok = live && hi_b > lo_b ? (unsigned)(hi_b - lo_b) : 0u;
-  const unsigned ca_n8 = (p.rl + p.rg) << 8;
-  unsigned count = 0, det = 0, mword = 0;
+  unsigned count = 0, det = 0;
   if (u < p.frames) {
-    warp_prefix<R>(p, u, pre, p.vec);
-    unsigned emitted = 0;
-    for (unsigned r = 0; r < words; ++r) {
-      const unsigned i = r * 32u + lane;
-      bool dt = false;
-      uint64_t cut = 0, sum = 0;
-      unsigned nref = 0;
-      const bool ok = live && (int)i >= lo_b && (int)i < hi_b;  // i < n follows
-      if (ok) {
-        cut = pre[i + 1] - pre[i];
-        const uint64_t sl = pre[i + p.gl + p.rl + 1] - pre[i + p.gl + 1];
-        const uint64_t sg = pre[i - p.gg] - pre[i - p.gg - p.rg];
-        uint64_t lhs;
-        if (p.go) {
-          const bool lead = (sl * p.rg) >= (sg * p.rl);
-          sum = lead ? sl : sg;
-          nref = lead ? p.rl : p.rg;
-          lhs = (cut * nref) << 8;
-        } else {
-          sum = sl + sg;
-          nref = p.rl + p.rg;
-          lhs = cut * ca_n8;
-        }
-        dt = lhs > (uint64_t)p.alpha * sum;
-      }
-      bool em = dt;
-      unsigned m = __ballot_sync(0xffffffffu, dt);
-      if (p.dense) {  // every cell emits; the detected ones still count
-        det += __popc(m);
-        em = i < p.n;
-        m = __ballot_sync(0xffffffffu, em);
-        if (em && !ok) cut = pre[i + 1] - pre[i];
-      } else {
-        det += __popc(m);
-      }
-      if (lane == (r & 31u)) mword = m;
-      if (em) {  // the frame's k-th event, while it fits the frame's slots
-        const unsigned k = emitted + __popc(m & ((1u << lane) - 1u));
-        if (k < kCfarSlots)
-          p.slots[u * kCfarSlots + k] =
-              pack_detection(cut, i, dt ? 0u : (!ok ? 2u : 1u), ok ? sum : 0ull, ok ? nref : 0u);
-      }
-      emitted += __popc(m);
-    }
-    if (lane < words) p.mask[u * words + lane] = mword;  // words <= 32
-    count = emitted + 1u;  // + SUMMARY
-    if (lane == 0) {
-      p.counts[u] = count;
-      p.detsup[u] = det | ((p.n - n_ok) << 16);  // n <= 1024: both fit 16 bits
+    uint64_t c[R][4];
+    load_cells<R>(p, u, p.vec, c);
+    // every window sum (and the cell) below 2^32 when the largest cell times
+    // the reference cells plus one is: the scan then runs in 32 bits
+    uint64_t mx = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) mx = c[r][k] > mx ? c[r][k] : mx;
+    bool narrow = !__any_sync(0xffffffffu, (mx >> 32) != 0ull);
+    if (narrow)
+      narrow = (uint64_t)__reduce_max_sync(0xffffffffu, (unsigned)mx) * (p.rl + p.rg + 1u) <=
+               0xFFFFFFFFull;
+    if (narrow) {  // pre[0] three words past the boundary: pre + 1 on it
+      uint32_t* pre = reinterpret_cast<uint32_t*>(wbase) + 3;
+      warp_prefix<R>(p, c, pre, p.vec);
+      count = decide_frame(p, u, pre, live, lo_b, hi_b, n_ok, det);
+    } else {  // pre[0] one word past the boundary
+      uint64_t* pre = wbase + 1;
+      warp_prefix<R>(p, c, pre, p.vec);
+      count = decide_frame(p, u, pre, live, lo_b, hi_b, n_ok, det);
     }
   }
   if (lane == 0) {
@@ -902,7 +951,7 @@ __device__ uint4 redecide(const CfarParams& p, uint64_t u, unsigned k) {
     for (unsigned j = 0; j < p.rl; ++j) sl += cell_at(p, u, i + p.gl + 1u + j);
     for (unsigned j = 0; j < p.rg; ++j) sg += cell_at(p, u, i - p.gg - p.rg + j);
   }
-  // decide_cell on these sums (cfar_model.hpp:295-340)
+  // the decision on these sums (cfar_model.hpp:295-340)
   uint64_t sum;
   unsigned nref;
   if (p.go) {

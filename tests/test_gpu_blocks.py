@@ -194,6 +194,28 @@ def test_cfar_random_vs_oracle(gpulib, port, mode, out):
             assert np.array_equal(g, o), (n, geo)
 
 
+@pytest.mark.parametrize("mode", [abi.RD_CFAR_CA, abi.RD_CFAR_GO])
+def test_cfar_large_cells_vs_oracle(gpulib, port, mode):
+    # cells near 2^26: a frame's total passes 2^32 while every window sum
+    # stays below it (the 32-bit scan, wrapping), and frames with a cell
+    # whose windows may pass 2^32 (the 64-bit scan) in the same launch
+    rng = np.random.default_rng(11 + mode)
+    n, frames = 1024, 12
+    cells = rng.integers(2**25, 2**26, frames * n).astype(np.int64)
+    cells[rng.integers(0, cells.size, 40)] = 2**26 - 1
+    cells[3 * n + 500] = 2**27          # 33 x 2^27 > 2^32: that frame scans in 64 bits
+    cells[7 * n + 9] = 2**32 + 5        # a cell above 32 bits
+    cells[9 * n:10 * n] = 2**31 - 1     # every cell at the 31-bit power limit
+    fid = np.arange(frames, dtype=np.uint32)
+    for out in (abi.RD_CFAR_EVENTS, abi.RD_CFAR_DENSE):
+        for geo, alpha in (((4, 4, 16, 16), 333), ((2, 2, 8, 8), 320), ((0, 3, 5, 0), 256)):
+            cfg = cfar_cfg(mode, out, *geo, alpha)
+            g, o = gc.cfar(cells, n, cfg, fid), port.cfar(cells, n, cfg, fid)
+            assert np.array_equal(g, o), (out, geo)
+            if out == abi.RD_CFAR_EVENTS and geo[2] == 16:
+                assert (event_fields(g)["kind"] == 0).any()
+
+
 def test_cfar_directed(gpulib, port):
     n = 128
     cells = np.full(n, 100, np.int64)
