@@ -210,6 +210,11 @@ __global__ void __launch_bounds__(256, 2) k_beam_tc(BeamParams p) {
   const unsigned f0 = s_f[rr0], f1 = s_f[rr0 + 8u];
   const unsigned bin0 = s_bin[rr0], bin1 = s_bin[rr0 + 8u];
   const unsigned G = (B + kTcBeams - 1u) / kTcBeams;
+  // output rows: beam b's power cell at pw + b N, its beam word at bn + b
+  uint32_t* const pw0 = p.power ? p.power + ((uint64_t)f0 * B) * N + bin0 : nullptr;
+  uint32_t* const pw1 = p.power ? p.power + ((uint64_t)f1 * B) * N + bin1 : nullptr;
+  uint32_t* const bn0 = p.beams_bn ? p.beams_bn + ((uint64_t)f0 * N + bin0) * B : nullptr;
+  uint32_t* const bn1 = p.beams_bn ? p.beams_bn + ((uint64_t)f1 * N + bin1) * B : nullptr;
   unsigned fl_any = 0;
   unsigned long long nsat = 0;
   for (unsigned grp = 0; grp < G; ++grp) {
@@ -229,7 +234,10 @@ __global__ void __launch_bounds__(256, 2) k_beam_tc(BeamParams p) {
       }
     }
     // epilogue: lane t of each quad holds beam 4 t3 + t of the group for
-    // rows g (h = 0) and g + 8 (h = 1)
+    // rows g (h = 0) and g + 8 (h = 1). The fp32 estimate of a sum is off by
+    // less than 2^8 + 2^-24 of itself, so a sum estimated below 1e9 in
+    // magnitude is below 2^31 - 2^15: recombined modulo 2^32 it is exact, and
+    // rounds in 32 bits
 #pragma unroll
     for (int t3 = 0; t3 < 4; ++t3) {
       const unsigned b = grp * kTcBeams + (unsigned)t3 * 4u + tig;
@@ -238,24 +246,41 @@ __global__ void __launch_bounds__(256, 2) k_beam_tc(BeamParams p) {
         const float* c0 = d[3 * t3];
         const float* c1 = d[3 * t3 + 1];
         const float* c2 = d[3 * t3 + 2];
-        const long long re_v = fold3(c0[2 * h], c0[2 * h + 1], c1[2 * h]);
-        const long long im_v = fold3(c1[2 * h + 1], c2[2 * h], c2[2 * h + 1]);
+        const float cr16 = c0[2 * h], cr8 = c0[2 * h + 1], cr0 = c1[2 * h];
+        const float ci16 = c1[2 * h + 1], ci8 = c2[2 * h], ci0 = c2[2 * h + 1];
         const unsigned long long off = h ? off1 : off0;
         if (b < B && off != ~0ull) {
           unsigned fr = 0, fi = 0;
-          const int32_t yr = q15_out64(re_v, &fr), yi = q15_out64(im_v, &fi);
+          long long re_v, im_v;
+          int32_t yr, yi;
+          const float est = fmaxf(fabsf(fmaf(cr16, 65536.f, fmaf(cr8, 256.f, cr0))),
+                                  fabsf(fmaf(ci16, 65536.f, fmaf(ci8, 256.f, ci0))));
+          if (est < 1.0e9f) {
+            const int32_t re32 = (int32_t)((uint32_t)__float2int_rn(cr16) * 65536u +
+                                           (uint32_t)__float2int_rn(cr8) * 256u +
+                                           (uint32_t)__float2int_rn(cr0));
+            const int32_t im32 = (int32_t)((uint32_t)__float2int_rn(ci16) * 65536u +
+                                           (uint32_t)__float2int_rn(ci8) * 256u +
+                                           (uint32_t)__float2int_rn(ci0));
+            yr = q15_out32(re32, &fr);
+            yi = q15_out32(im32, &fi);
+            re_v = re32;
+            im_v = im32;
+          } else {
+            re_v = fold3(cr16, cr8, cr0);
+            im_v = fold3(ci16, ci8, ci0);
+            yr = q15_out64(re_v, &fr);
+            yi = q15_out64(im_v, &fi);
+          }
           if (fr | fi) {
             fl_any |= fr | fi;
             ++nsat;
           }
-          cplx y;
-          y.re = (int16_t)yr;
-          y.im = (int16_t)yi;
-          const uint64_t f = h ? f1 : f0, bin = h ? bin1 : bin0;
+          const uint32_t y = pack2(yr, yi);
+          if (p.power) (h ? pw1 : pw0)[b * N] = power_u32(unpack(y));
+          if (p.beams_bn) (h ? bn1 : bn0)[b] = y;
           const uint64_t r = r0 + rr0 + 8u * (unsigned)h;
-          if (p.power) p.power[(f * B + b) * N + bin] = power_u32(y);
-          if (p.beams_bn) p.beams_bn[(f * N + bin) * B + b] = pack(y);
-          if (p.y_rows) p.y_rows[r * B + b] = pack(y);
+          if (p.y_rows) p.y_rows[r * B + b] = y;
           if (p.acc_rows) {
             p.acc_rows[(r * B + b) * 2] = re_v;
             p.acc_rows[(r * B + b) * 2 + 1] = im_v;
