@@ -41,7 +41,6 @@ __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
   unsigned slot = p.ring_base + (unsigned)f;
   if (slot >= p.ring_frames) slot -= p.ring_frames;
   for (unsigned k = tid; k < B * C; k += 256u) {
-    s_w[k] = p.w_limbs[k];
     const uint32_t w = p.weights[k];
     const int wr = (int)(int16_t)(uint16_t)(w & 0xFFFFu), wi = (int)w >> 16;
     s_w3[k] = make_int4(wr, wi, wr + wi, 0);
@@ -80,6 +79,10 @@ __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
   // every sum is at most max|x| x the largest beam L1 norm of the weights:
   // within x_safe the plain int32 sum is exact
   const bool wide = __syncthreads_or(xmax > (int)p.x_safe) != 0;
+  if (wide) {  // the limb weights of the exact int64 path (block-uniform)
+    for (unsigned k = tid; k < B * C; k += 256u) s_w[k] = p.w_limbs[k];
+    __syncthreads();
+  }
   const unsigned bl = tid & 63u, bg = tid >> 6;
   const unsigned bin = bin0 + bl;
   unsigned fl_any = 0;
