@@ -29,9 +29,13 @@
 // with ns(a, b) = (-b, a). Three m16n8 tiles cover four y channels, column
 // 2t + e of tile j being class 2j + e of channel t (the layout of the tensor
 // beamformer), so after the three tiles the accumulator lane with columns
-// 2t, 2t+1 holds all six classes of (x, y) for its two x rows. Each lane's
-// B words are two of {hi, ns(lo), lo, ns(hi)}, stored adjacently per
-// (frame, channel) in that order and read as one 64-bit load.
+// 2t, 2t+1 holds all six classes of (x, y) for its two x rows. A lane with
+// e = g & 1 (its column's class parity) and h = tg & 1 (parts 0-1 or 2-3)
+// takes, for tiles 0, 1, 2:
+//   (h, e) = (0, 0) and (1, 1): hi, 0, ns(lo)     (0, 1): lo, ns(hi), 0
+//   (h, e) = (1, 0):            0, lo, ns(hi)
+// The staging writes these three word triples per (frame, channel), so a
+// lane's B fragment for all three tiles is one 16-byte load per k half.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -43,17 +47,20 @@
 
 namespace rd {
 
-constexpr unsigned kCtFrames = 32u;  // frames per staged chunk
-constexpr unsigned kCtFold = 4u;     // chunks per fp32 accumulation: 128 frames
-constexpr unsigned kCtPre = 16u;     // staged elements per thread per chunk
+constexpr unsigned kCtFrames = 16u;  // frames per staged chunk
+constexpr unsigned kCtLog2 = 4u;     // log2 kCtFrames
+constexpr unsigned kCtFold = 8u;     // chunks per fp32 accumulation: 128 frames
+constexpr unsigned kCtPre = 8u;      // staged elements per thread per chunk (NB Sp <= 128)
 
 template <int UPW>
 __global__ void __launch_bounds__(256, 2) k_cov_tc(CovParams p, CovTcPlan t) {
   extern __shared__ __align__(16) uint32_t sm[];
   const unsigned S = p.S, Sp = t.Sp, NB = t.NB, lsp = t.log2_sp;
-  const unsigned FSA = 2u * Sp + 16u, FSB = 4u * Sp + 16u;  // frame strides (words)
-  uint32_t* sA = sm;                                       // [NB][32][FSA]
-  uint32_t* sB = sA + NB * kCtFrames * FSA;                // [NB][32][FSB]
+  // frame strides (words); FSB = 16 mod 32 keeps the two frames of a B load
+  // on different banks
+  const unsigned FSA = 2u * Sp + 16u, FSB = 12u * Sp + 16u;
+  uint32_t* sA = sm;                                       // [NB][16][FSA]
+  uint32_t* sB = sA + NB * kCtFrames * FSA;                // [NB][16][FSB]
   long long* sAcc = reinterpret_cast<long long*>(sB + NB * kCtFrames * FSB);  // [8][UPW][32][4]
   const unsigned tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
   const unsigned g = lane >> 2, tg = lane & 3u;
@@ -78,13 +85,9 @@ __global__ void __launch_bounds__(256, 2) k_cov_tc(CovParams p, CovTcPlan t) {
   for (int u = 0; u < UPW; ++u)
     for (int e = 0; e < 4; ++e) acc[u * 128 + e] = 0;
 
-  // B word selection of this lane (see the header comment): the pair
-  // {hi, ns(lo)} or {lo, ns(hi)}, then per tile first, first/second or zero
-  const unsigned pair = (g ^ tg) & 1u;
-  const uint32_t m0 = ((g & 1u) == 0u && (tg & 1u)) ? 0u : ~0u;
-  const uint32_t m1 = pair ? ~0u : 0u;
-  const bool sel1 = (g & 1u) != 0u;
-  const uint32_t m2 = ((g & 1u) && (tg & 1u) == 0u) ? 0u : ~0u;
+  // this lane's B word triple (see the header comment): 0 for (h, e) = (0, 0)
+  // and (1, 1), 1 for (0, 1), 2 for (1, 0)
+  const unsigned bslot = ((g ^ tg) & 1u) == 0u ? 0u : ((tg & 1u) == 0u ? 1u : 2u);
 
   const unsigned per_chunk = (NB * kCtFrames) << lsp;
   uint32_t pre[kCtPre];
@@ -95,7 +98,7 @@ __global__ void __launch_bounds__(256, 2) k_cov_tc(CovParams p, CovTcPlan t) {
       uint32_t v = 0;
       if (e < per_chunk) {
         const unsigned c = e & (Sp - 1u), r = e >> lsp;
-        const unsigned f = f0 + (r & (kCtFrames - 1u)), bin = bin0 + (r >> 5);
+        const unsigned f = f0 + (r & (kCtFrames - 1u)), bin = bin0 + (r >> kCtLog2);
         if (f < hi && bin < p.N && c < S) {
           if (p.src_beam) {
             v = __ldg(p.beams_bn + ((size_t)f * p.N + bin) * S + c);
@@ -114,11 +117,15 @@ __global__ void __launch_bounds__(256, 2) k_cov_tc(CovParams p, CovTcPlan t) {
     for (unsigned j = 0; j < kCtPre; ++j) {
       const unsigned e = tid + j * 256u;
       if (e < per_chunk) {
-        const unsigned c = e & (Sp - 1u), r = e >> lsp;  // r = bl * 32 + frame
+        const unsigned c = e & (Sp - 1u), r = e >> lsp;  // r = bl * 16 + frame
         uint32_t h, l;
         limb_words(pre[j], h, l);
         *reinterpret_cast<uint2*>(sA + r * FSA + 2u * c) = make_uint2(h, l);
-        *reinterpret_cast<uint4*>(sB + r * FSB + 4u * c) = make_uint4(h, negswap(l), l, negswap(h));
+        const uint32_t nl = negswap(l), nh = negswap(h);
+        uint4* b = reinterpret_cast<uint4*>(sB + r * FSB + 12u * c);
+        b[0] = make_uint4(h, 0u, nl, 0u);
+        b[1] = make_uint4(l, nh, 0u, 0u);
+        b[2] = make_uint4(0u, l, nh, 0u);
       }
     }
   };
@@ -157,15 +164,15 @@ __global__ void __launch_bounds__(256, 2) k_cov_tc(CovParams p, CovTcPlan t) {
         const uint32_t* pa = sA + fr * FSA + 2u * (16u * mi + g) + (tg & 1u);
         const uint32_t a[4] = {pa[0], pa[16], pa[2u * FSA], pa[2u * FSA + 16u]};
         if (u == 0 || ((un ^ unit[u > 0 ? u - 1 : 0]) & 0xFFFF00FFu) != 0u) {
-          const uint32_t* pb = sB + fr * FSB + 4u * (4u * tri + (g >> 1)) + 2u * pair;
-          const uint2 w0 = *reinterpret_cast<const uint2*>(pb);
-          const uint2 w1 = *reinterpret_cast<const uint2*>(pb + 2u * FSB);
-          b00 = w0.x & m0;
-          b01 = (sel1 ? w0.y : w0.x) & m1;
-          b02 = w0.y & m2;
-          b10 = w1.x & m0;
-          b11 = (sel1 ? w1.y : w1.x) & m1;
-          b12 = w1.y & m2;
+          const uint32_t* pb = sB + fr * FSB + 12u * (4u * tri + (g >> 1)) + 4u * bslot;
+          const uint4 w0 = *reinterpret_cast<const uint4*>(pb);
+          const uint4 w1 = *reinterpret_cast<const uint4*>(pb + 2u * FSB);
+          b00 = w0.x;
+          b01 = w0.y;
+          b02 = w0.z;
+          b10 = w1.x;
+          b11 = w1.y;
+          b12 = w1.z;
         }
         mma_f16(d[u][0], a, b00, b10);
         mma_f16(d[u][1], a, b01, b11);
@@ -244,7 +251,7 @@ bool cov_tc_plan(uint32_t S, const uint32_t* px, const uint32_t* py, uint32_t P,
 }
 
 size_t cov_tc_smem(const CovTcPlan& t) {
-  const size_t fs = (2u * t.Sp + 16u) + (4u * t.Sp + 16u);
+  const size_t fs = (2u * t.Sp + 16u) + (12u * t.Sp + 16u);
   return (size_t)t.NB * kCtFrames * fs * 4u + (size_t)8u * t.UPW * 32u * 4u * 8u;
 }
 
