@@ -59,6 +59,17 @@ def peaks() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
+def bf16_peak() -> tuple[float, str]:
+    """Dense bf16 TFLOP/s for a kernel timed alone: the measured burst figure,
+    else the recipe's fallback."""
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        v = json.loads(f.read_text()).get("bf16_tflops")
+        if v:
+            return float(v), "of measured"
+    return 1900.0, "of fallback"
+
+
 class Clocks:
     """nvidia-smi sampling of SM clocks and throttle reasons during the run."""
 
@@ -214,13 +225,27 @@ def run_forms(torch, a, stream) -> dict:
         coeff = sc.coefficients(p.n_fft, p.taps)
         w = sc.steering_weights(p.n_chan, p.n_beams)
         r = {"samples_per_step": p.n_chan * n}
+        pairs = sc.pair_table(p)
+        rows = 1024 * p.n_fft  # (frame, bin) rows of one 1024-frame launch
+        # int MACs a launch (4 B C a bin-frame for the beams, 4 per pair for the
+        # covariance) and the limb GEMM's fp16 flops (6 B columns, 4 C depth)
+        beam_mac, cov_mac = 4 * p.n_beams * p.n_chan * rows, 4 * len(pairs[0]) * rows
+        beam_tc_flop = 2 * rows * (6 * p.n_beams) * (4 * p.n_chan)
         for name, form in (("cuda_core", abi.RD_FORM_CUDA_CORE), ("tensor", abi.RD_FORM_TENSOR)):
-            ch = gc.Chain(sc.make_config(p, max_frames=1024, form=form), coeff, w,
-                          sc.pair_table(p))
+            ch = gc.Chain(sc.make_config(p, max_frames=1024, form=form), coeff, w, pairs)
             ms, ks = time_chain(torch, ch, dev, n, stream, steps=3, warmup=3)
             r[name] = {"value": round(p.n_chan * n / (ms / 1e3) / 1e6, 3), "unit": UNIT,
                        "ms_per_step": round(ms, 3), "k_beam_us": ks.get("k_beam"),
                        "k_cov_us": ks.get("k_cov")}
+            if ks.get("k_beam") and ks.get("k_cov"):
+                r[name]["beam_int_gmac_s"] = round(beam_mac / ks["k_beam"] / 1e3, 1)
+                r[name]["cov_int_gmac_s"] = round(cov_mac / ks["k_cov"] / 1e3, 1)
+                if form == abi.RD_FORM_TENSOR:
+                    tf = beam_tc_flop / ks["k_beam"] / 1e6
+                    peak, src = bf16_peak()
+                    r[name]["beam_fp16_tflop_s"] = round(tf, 1)
+                    r[name]["beam_fp16_frac"] = round(tf / peak, 4)
+                    r[name]["beam_fp16_peak"] = f"{peak} TFLOP/s dense bf16, {src}"
             ch.close()
         cc, tc = r["cuda_core"], r["tensor"]
         r["chain_speedup"] = round(tc["value"] / cc["value"], 3)
@@ -309,10 +334,11 @@ def abi_ptr(v: int):
     return abi.C.c_void_p(v)
 
 
-def run_serving(torch, n_streams: int = 32, n_req: int = 400) -> dict:
+def run_serving(torch, n_streams: int = 32, n_req: int = 2000, n_burst: int = 400) -> dict:
     """32 resident streams of mixed tiny / medium / full geometry; a request
-    is 4096 samples per channel; Poisson arrivals at 25/50/80/100 % of the
-    measured saturation rate; latency = completion - arrival."""
+    is 4096 samples per channel; the saturation rate is the median of three
+    bursts of n_burst requests all due at once; then n_req Poisson arrivals
+    at 25/50/80/100 % of it; latency = completion - arrival."""
     from rdgb import abi, scenario as sc
     from rdgb.serve import Server
 
@@ -340,8 +366,7 @@ def run_serving(torch, n_streams: int = 32, n_req: int = 400) -> dict:
         return lat, mk, samples
 
     trace(64, None)  # warm
-    lat, mk, samples = trace(n_req, None)
-    sat = n_req / mk  # requests per microsecond
+    sat = float(np.median([n_burst / trace(n_burst, None)[1] for _ in range(3)]))  # req / us
     loads = []
     for load in (0.25, 0.5, 0.8, 1.0):
         lat, mk, samples = trace(n_req, sat * load)
@@ -352,6 +377,7 @@ def run_serving(torch, n_streams: int = 32, n_req: int = 400) -> dict:
     srv.close()
     return {"streams": n_streams, "mix": "tiny / medium / full in turn, tensor form",
             "request": "4096 samples per channel", "max_inflight": 16,
+            "requests_per_load": n_req, "saturation": f"median of 3 bursts of {n_burst}",
             "saturation_req_per_s": round(sat * 1e6, 1), "loads": loads,
             "p99_us_at_80pct": next(x["p99_us"] for x in loads if x["load"] == 0.8)}
 

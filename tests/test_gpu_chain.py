@@ -228,6 +228,25 @@ def test_chain_medium_cpi_vs_oracle(gpulib, port):
     assert (event_fields(rg["events"][:50])["alpha"] == p.alpha).all()
 
 
+def test_medium_bench_step_vs_oracle(gpulib, port):
+    # the medium workload at the bench's size: 64 CPIs of 65536 samples on
+    # each of 16 channels (16384 frames, 64 covariance windows, 1.3 M events)
+    # in the bench's 1024-frame launches, bit-exact against the oracle
+    import os
+
+    p = sc.preset("medium")
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    x = sc.adc(p, 64 * p.cpi_samples)
+    g = gc.Chain(sc.make_config(p, max_frames=1024), coeff, w, (px, py))
+    rg = g.process(x)
+    o = port.chain(sc.make_config(p, max_frames=1024), coeff, w, px, py)
+    ro = o.process(x, taps=False, threads=os.cpu_count() or 1)
+    assert len(rg["cov_windows"]) == 64 and len(rg["events"]) > 16384 * p.n_beams
+    assert diff(rg, ro) == []
+    assert diff_stats(g.stats(), o.stats()) == []
+
+
 def test_chain_full_geometry_slice_vs_oracle(gpulib, port):
     # the full workload's geometry (64 ch, 1024-point PFB x 16 taps, 64 beams,
     # 2080 covariance pairs), 20 frames with an 8-frame window

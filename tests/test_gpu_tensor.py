@@ -2,7 +2,7 @@
 the C ABI: bit-exact against the CPU oracle and against the CUDA-core form,
 per block (bf::dot, beamformer_model.hpp:162-179) and inside the chain
 (the committed fixtures made by the reference's model headers, seeded random
-chains, the full workload's geometry). The limb split makes every partial sum
+chains, the full workload's geometry, one full-size CPI of it). The limb split makes every partial sum
 an integer below 2^24, so any difference at all is a bug, not rounding."""
 import numpy as np
 import pytest
@@ -107,6 +107,28 @@ def test_chain_tensor_full_geometry_vs_oracle(gpulib, port):
     ro = o.process(x, taps=True, threads=8)
     assert diff(rg, ro, CHAIN_KEYS + TAP_KEYS) == []
     assert diff_stats(g.stats(), o.stats()) == []
+
+
+def test_full_cpi_vs_oracle_both_forms(gpulib, port):
+    # one CPI of the full workload at its full size (2^20 samples on each of
+    # 64 channels: 1024 frames of 1024 bins, 64 beams, four 256-frame windows
+    # of 2080 pairs, 512-bit packets): both forms, in launches of 1024 and of
+    # 333 frames, bit-exact against the oracle on the same CPI
+    import os
+
+    p = sc.preset("full")
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    x = sc.adc(p, p.cpi_samples)
+    o = port.chain(sc.make_config(p, max_frames=1024), coeff, w, px, py)
+    ro = o.process(x, taps=False, threads=os.cpu_count() or 1)
+    assert len(ro["cov_windows"]) == 4 and len(ro["events"]) > 1024 * p.n_beams
+    for form, mf in ((abi.RD_FORM_CUDA_CORE, 1024), (TC, 1024), (TC, 333)):
+        g = gc.Chain(sc.make_config(p, max_frames=mf, form=form), coeff, w, (px, py))
+        rg = g.process(x)
+        assert diff(rg, ro) == [], (form, mf)
+        assert diff_stats(g.stats(), o.stats()) == [], (form, mf)
+        g.close()
 
 
 @pytest.mark.parametrize("seed", range(3))
