@@ -824,23 +824,23 @@ __device__ __forceinline__ unsigned decide_frame(const CfarParams& p, uint64_t u
   for (unsigned r = 0; r < words; ++r) {
     const unsigned i = r * 32u + lane;
     bool dt = false;
-    uint64_t cut = 0, sum = 0;
+    Tp cut = 0, sum = 0;  // in Tp: every window sum fits (see warp_prefix)
     unsigned nref = 0;
     const bool ok = live && (int)i >= lo_b && (int)i < hi_b;  // i < n follows
     if (ok) {
-      cut = (Tp)(pre[i + 1] - pre[i]);
-      const uint64_t sl = (Tp)(pre[i + p.gl + p.rl + 1] - pre[i + p.gl + 1]);
-      const uint64_t sg = (Tp)(pre[i - p.gg] - pre[i - p.gg - p.rg]);
+      cut = pre[i + 1] - pre[i];
+      const Tp sl = pre[i + p.gl + p.rl + 1] - pre[i + p.gl + 1];
+      const Tp sg = pre[i - p.gg] - pre[i - p.gg - p.rg];
       uint64_t lhs;
       if (p.go) {
-        const bool lead = (sl * p.rg) >= (sg * p.rl);
+        const bool lead = ((uint64_t)sl * p.rg) >= ((uint64_t)sg * p.rl);
         sum = lead ? sl : sg;
         nref = lead ? p.rl : p.rg;
-        lhs = (cut * nref) << 8;
+        lhs = ((uint64_t)cut * nref) << 8;
       } else {
         sum = sl + sg;
         nref = p.rl + p.rg;
-        lhs = cut * ca_n8;
+        lhs = (uint64_t)cut * ca_n8;
       }
       dt = lhs > (uint64_t)p.alpha * sum;
     }
@@ -850,14 +850,15 @@ __device__ __forceinline__ unsigned decide_frame(const CfarParams& p, uint64_t u
     if (p.dense) {  // every cell emits; the detected ones still count
       em = i < p.n;
       m = __ballot_sync(0xffffffffu, em);
-      if (em && !ok) cut = (Tp)(pre[i + 1] - pre[i]);
+      if (em && !ok) cut = pre[i + 1] - pre[i];
     }
     if (lane == (r & 31u)) mword = m;
     if (em) {  // the frame's k-th event, while it fits the frame's slots
       const unsigned k = emitted + __popc(m & ((1u << lane) - 1u));
       if (k < kCfarSlots)
         p.slots[u * kCfarSlots + k] =
-            pack_detection(cut, i, dt ? 0u : (!ok ? 2u : 1u), ok ? sum : 0ull, ok ? nref : 0u);
+            pack_detection((uint64_t)cut, i, dt ? 0u : (!ok ? 2u : 1u), ok ? (uint64_t)sum : 0ull,
+                           ok ? nref : 0u);
     }
     emitted += __popc(m);
   }

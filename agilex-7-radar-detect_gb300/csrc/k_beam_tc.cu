@@ -325,9 +325,9 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 __global__ void __launch_bounds__(256, 2) k_beam_tc_pipe(BeamParams p, unsigned n_tiles) {
   extern __shared__ __align__(16) uint32_t sm[];
   const unsigned C = p.C, N = p.N;
-  const unsigned ks = C / 4u, S = 8u * ks + 4u;
+  const unsigned ks = C / 4u, S = 8u * ks + 4u, RS = C + 4u;
   uint32_t* s_x = sm;                  // [128][S] limb words of tile t
-  uint32_t* s_raw = sm + kTcRows * S;  // [128][C] samples of the next tile
+  uint32_t* s_raw = sm + kTcRows * S;  // [128][RS] samples of the next tile
   const unsigned tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u, gid = lane >> 2;
   const unsigned q4 = kTcRows * ks;    // 16-byte pieces of a tile
   auto fetch = [&](unsigned t) {
@@ -336,7 +336,10 @@ __global__ void __launch_bounds__(256, 2) k_beam_tc_pipe(BeamParams p, unsigned 
     unsigned slot = p.ring_base + f;
     if (slot >= p.ring_frames) slot -= p.ring_frames;
     const uint32_t* src = p.ring + ((size_t)slot * N + bin0) * C;
-    for (unsigned i = tid; i < q4; i += 256u) cp_async16(s_raw + 4u * i, src + 4u * i);
+    for (unsigned i = tid; i < q4; i += 256u) {
+      const unsigned rr = i / ks, j = i - rr * ks;
+      cp_async16(s_raw + rr * RS + 4u * j, src + 4u * i);
+    }
     cp_async_commit();
   };
   unsigned fl_any = 0;
@@ -346,9 +349,12 @@ __global__ void __launch_bounds__(256, 2) k_beam_tc_pipe(BeamParams p, unsigned 
   for (; t < n_tiles; t += gridDim.x) {
     cp_async_wait_all();
     __syncthreads();  // tile t landed for every thread; the last tile's products are done
+    // row-fastest, so that both the padded raw rows (stride C + 4) and the
+    // limb rows (stride 8 ks + 4) put a quarter-warp's 16-byte accesses on
+    // distinct banks
     for (unsigned i = tid; i < q4; i += 256u) {
-      const uint4 v = *reinterpret_cast<const uint4*>(s_raw + 4u * i);
-      const unsigned rr = i / ks, j = i - rr * ks;
+      const unsigned rr = i & (kTcRows - 1u), j = i / kTcRows;
+      const uint4 v = *reinterpret_cast<const uint4*>(s_raw + rr * RS + 4u * j);
       uint4 w0, w1;
       limb_words(v.x, w0.x, w0.y);
       limb_words(v.y, w0.z, w0.w);
@@ -380,7 +386,7 @@ size_t beam_tc_smem(uint32_t C) {
 }
 
 static size_t pipe_smem(uint32_t C) {
-  return (kTcRows * (8u * (C / 4u) + 4u) + (size_t)kTcRows * C) * sizeof(uint32_t);
+  return (kTcRows * (8u * (C / 4u) + 4u) + (size_t)kTcRows * (C + 4u)) * sizeof(uint32_t);
 }
 
 // the dynamic shared-memory opt-in is per device
