@@ -248,6 +248,21 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
     if (ok && p.tap_pfb)
       p.tap_pfb[((size_t)f * p.C + c) * N + ph0 + (j & 1) * dph1 + (j >> 1) * dph2] = pk(E[j]);
   };
+  // round_sat(acc, 15, 16) of an int32 sum (|acc| <= 2^31 - 2^15, pfb32). The
+  // exact pass saturates and flags; the bound-checked pass only rounds: a
+  // value that would saturate is at least 32768 in magnitude, above any
+  // safe_in (<= 32767), so the pass fails its check below and reruns exactly,
+  // and the flags and counts come from that rerun
+  auto round_out = [&](int j, int vr, int vi) {
+    if constexpr (FL) {
+      unsigned fr = 0, fi = 0;
+      const int yr = q15_out32(vr, &fr), yi = q15_out32(vi, &fi);
+      finish(j, yr, yi, fr, fi);
+    } else {
+      finish(j, (vr + 0x3FFF + ((vr >> 15) & 1)) >> 15, (vi + 0x3FFF + ((vi >> 15) & 1)) >> 15, 0u,
+             0u);
+    }
+  };
   if (p.pfb_dp) {
     // x h = 256 x hh + x hl with byte limbs: re = x.re hr + x.im (-hi),
     // im = x.re hi + x.im hr, two dp2a per limb on the packed sample. The
@@ -272,12 +287,9 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
       });
     }
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      unsigned fr = 0, fi = 0;
-      const int yr = q15_out32((int)((uint32_t)hr[j] * 256u + (uint32_t)lr[j]), &fr);
-      const int yi = q15_out32((int)((uint32_t)hi[j] * 256u + (uint32_t)li[j]), &fi);
-      finish(j, yr, yi, fr, fi);
-    }
+    for (int j = 0; j < 4; ++j)
+      round_out(j, (int)((uint32_t)hr[j] * 256u + (uint32_t)lr[j]),
+                (int)((uint32_t)hi[j] * 256u + (uint32_t)li[j]));
   } else if (p.pfb32) {
     // every partial sum is bounded by 2^15 x the phase's L1 norm < 2^31
     int ar[4] = {0, 0, 0, 0}, ai[4] = {0, 0, 0, 0};
@@ -298,11 +310,7 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
       });
     }
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      unsigned fr = 0, fi = 0;
-      const int yr = q15_out32(ar[j], &fr), yi = q15_out32(ai[j], &fi);
-      finish(j, yr, yi, fr, fi);
-    }
+    for (int j = 0; j < 4; ++j) round_out(j, ar[j], ai[j]);
   } else {
     long long ar[4] = {0, 0, 0, 0}, ai[4] = {0, 0, 0, 0};
     if (ok) {
@@ -324,9 +332,13 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
     }
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      unsigned fr = 0, fi = 0;
-      const int yr = q15_out64(ar[j], &fr), yi = q15_out64(ai[j], &fi);
-      finish(j, yr, yi, fr, fi);
+      if (FL) {
+        unsigned fr = 0, fi = 0;
+        const int yr = q15_out64(ar[j], &fr), yi = q15_out64(ai[j], &fi);
+        finish(j, yr, yi, fr, fi);
+      } else {
+        finish(j, (int)rne15_64(ar[j]), (int)rne15_64(ai[j]), 0u, 0u);
+      }
     }
   }
   // ---- the pass's bound check: every PFB output within safe_in means no
@@ -387,6 +399,14 @@ __device__ __noinline__ void front_pass_flags(const FrontParams& p, int T, int q
   front_pass_body<NL, SPC, TT, true, SH1>(p, T, q, tl, ok, f, c, twp, buf0, buf1, tile_row, cbp,
                                           pfl, psat, sf);
   *sf_out |= sf;
+  // the PFB flags and saturation count of the pass (the whole block runs
+  // this rerun, so every lane of the warp is here)
+  const unsigned a = __reduce_or_sync(0xffffffffu, pfl);
+  for (int o = 16; o > 0; o >>= 1) psat += __shfl_xor_sync(0xffffffffu, psat, o);
+  if ((threadIdx.x & 31u) == 0u) {
+    if (a) atomicOr(&p.stats->pfb_flags, a);
+    if (psat) atomicAdd(&p.stats->pfb_sat, psat);
+  }
 }
 
 template <int NL, int SPC, int TT, bool SH1>
