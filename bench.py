@@ -135,6 +135,20 @@ def kernel_bytes(cfg, name: str, frames: int) -> float:
     return 0.0
 
 
+def profile_instructions(kernel: str) -> float | None:
+    """Warp instructions per launch of `kernel` at the bench's launch size, from
+    the committed ncu summary (a line `instructions <kernel>
+    warp_inst_per_launch=<count>`, smsp__inst_executed.sum), or None."""
+    import re
+    f = ROOT / "profiles" / "kernels_medium_ncu_full.md"
+    if f.exists():
+        m = re.search(rf"^instructions {re.escape(kernel)} warp_inst_per_launch=(\d+)$",
+                      f.read_text(), re.M)
+        if m:
+            return float(m.group(1))
+    return None
+
+
 def profile_traffic(kernel: str) -> float | None:
     """dram read+write bytes per launch of `kernel` at the bench's launch size,
     from the committed ncu summary of the medium chain (a line
@@ -509,6 +523,18 @@ def run_gpu(a, rank: int, world: int, local: int) -> None:
                 "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": f"of {which}",
                 "traffic": profile_traffic(dom),
                 "algorithmic_bytes_per_launch": alg}
+    # the ceiling that binds these integer kernels: one warp instruction per
+    # SM sub-partition per cycle, at the SM clock sampled during the run
+    inst = profile_instructions(dom)
+    if inst:
+        n_smsp = 4 * torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz") or 2070.0
+        got = inst / (kernels[dom]["avg_ms"] / 1e3) / 1e9
+        top = n_smsp * mhz / 1e3
+        roofline["issue"] = {"achieved": round(got, 1), "peak": round(top, 1),
+                             "unit": "G warp instructions/s", "frac": round(got / top, 4),
+                             "inst_per_launch": inst, "sm_mhz": mhz,
+                             "source": "ncu smsp__inst_executed.sum of the same launch"}
 
     # e2e through the C ABI from pinned host memory
     e2e = None
