@@ -43,7 +43,8 @@ def args_():
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--workload", default="medium")
     ap.add_argument("--cpis", type=int, default=None, help="CPIs per step (default: the workload's)")
-    ap.add_argument("--max-frames", type=int, default=1024)
+    ap.add_argument("--max-frames", type=int, default=2048,
+                    help="frames per launch (the default gives the best end-to-end rate)")
     ap.add_argument("--form", choices=["cuda_core", "tensor"], default="cuda_core")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -227,26 +228,28 @@ def time_chain(torch, chain, dev, n: int, stream, steps: int, warmup: int):
 
 def run_forms(torch, a, stream) -> dict:
     """The chain in the CUDA-core integer form and in the limb-split
-    tensor-core form, on the medium workload and on the full-scale one."""
+    tensor-core form, on the medium workload (the bench's frames per launch)
+    and on the full-scale one (1024 frames, 67 M samples, per launch)."""
     from rdgb import abi, chain as gc, scenario as sc
 
     out = {}
-    for wl, cpis in (("medium", 64), ("full", 2)):
+    medium_frames = a.max_frames if a is not None else 2048
+    for wl, cpis, frames in (("medium", 64, medium_frames), ("full", 2, 1024)):
         p = sc.preset(wl)
         n = cpis * p.cpi_samples
         x = tiled_adc(p, n)
         dev = torch.from_numpy(x.view(np.int32)).cuda()
         coeff = sc.coefficients(p.n_fft, p.taps)
         w = sc.steering_weights(p.n_chan, p.n_beams)
-        r = {"samples_per_step": p.n_chan * n}
+        r = {"samples_per_step": p.n_chan * n, "frames_per_launch": frames}
         pairs = sc.pair_table(p)
-        rows = 1024 * p.n_fft  # (frame, bin) rows of one 1024-frame launch
+        rows = frames * p.n_fft  # (frame, bin) rows of one launch
         # int MACs a launch (4 B C a bin-frame for the beams, 4 per pair for the
         # covariance) and the limb GEMM's fp16 flops (6 B columns, 4 C depth)
         beam_mac, cov_mac = 4 * p.n_beams * p.n_chan * rows, 4 * len(pairs[0]) * rows
         beam_tc_flop = 2 * rows * (6 * p.n_beams) * (4 * p.n_chan)
         for name, form in (("cuda_core", abi.RD_FORM_CUDA_CORE), ("tensor", abi.RD_FORM_TENSOR)):
-            ch = gc.Chain(sc.make_config(p, max_frames=1024, form=form), coeff, w, pairs)
+            ch = gc.Chain(sc.make_config(p, max_frames=frames, form=form), coeff, w, pairs)
             ms, ks = time_chain(torch, ch, dev, n, stream, steps=3, warmup=3)
             r[name] = {"value": round(p.n_chan * n / (ms / 1e3) / 1e6, 3), "unit": UNIT,
                        "ms_per_step": round(ms, 3), "k_beam_us": ks.get("k_beam"),
