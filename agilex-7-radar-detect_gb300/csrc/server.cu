@@ -57,6 +57,15 @@ struct NoInit {
 template <typename T>
 using RawVec = std::vector<T, NoInit<T>>;
 
+// A page-locked block for a request's covariance window sums: they are the
+// one large output (34 MB for a full-scale window), and a page-locked
+// destination takes them by DMA instead of through a staging copy.
+struct PinnedBuf {
+  int64_t* p = nullptr;
+  size_t cap = 0;  // int64 words
+  size_t len = 0;
+};
+
 struct Request {
   uint64_t id = 0;
   uint32_t stream = 0;
@@ -69,9 +78,17 @@ struct Request {
   RawVec<rd_event> events;
   RawVec<uint32_t> flits;
   RawVec<rd_cov_window> windows;
-  RawVec<int64_t> cov;
+  PinnedBuf cov;
   uint64_t n_events = 0, n_flits = 0;
   uint32_t n_windows = 0, flit_words = 0;
+};
+
+// Output buffers of a finished request, kept (capacity included) for the
+// next one, so that steady serving allocates nothing.
+struct OutBufs {
+  RawVec<rd_event> events;
+  RawVec<uint32_t> flits;
+  RawVec<rd_cov_window> windows;
 };
 
 struct StreamState {
@@ -103,6 +120,8 @@ struct rd_server {
   std::vector<rd_cplx16*> host;   // pinned staging, queue_cap buffers
   std::vector<int> free_host;
   std::unordered_map<uint64_t, Request> reqs;
+  std::vector<OutBufs> pool;      // output buffers of finished requests, reused
+  std::vector<PinnedBuf> cov_pool;  // page-locked window-sum blocks, reused
   std::deque<uint64_t> waiting;   // submitted, not started (submission order)
   std::vector<rd_completion> finished;
   uint64_t next_id = 1;
@@ -113,6 +132,21 @@ struct rd_server {
 };
 
 namespace {
+
+// Removes request `it`, keeping its output buffers (capacity included) for
+// later requests.
+void retire(rd_server* s, std::unordered_map<uint64_t, Request>::iterator it) {
+  if (it == s->reqs.end()) return;
+  Request& r = it->second;
+  const size_t keep = (size_t)s->cfg.queue_cap + s->cfg.max_inflight;
+  if (s->pool.size() < keep)
+    s->pool.push_back(OutBufs{std::move(r.events), std::move(r.flits), std::move(r.windows)});
+  if (r.cov.p) {
+    if (s->cov_pool.size() < keep) s->cov_pool.push_back(PinnedBuf{r.cov.p, r.cov.cap, 0});
+    else cudaFreeHost(r.cov.p);
+  }
+  s->reqs.erase(it);
+}
 
 rd_status start_ready(rd_server* s) {
   for (auto it = s->waiting.begin(); it != s->waiting.end();) {
@@ -158,14 +192,33 @@ rd_status collect(rd_server* s, Request& r) {
   r.events.resize(q.n_events);
   r.flits.resize(q.n_events * nfl * words);
   r.windows.resize(q.n_cov_windows);
-  r.cov.resize((size_t)q.n_cov_windows * per);
+  const size_t need = (size_t)q.n_cov_windows * per;
+  if (need > r.cov.cap) {  // a kept block that holds it, else a new one
+    size_t best = s->cov_pool.size();
+    for (size_t k = 0; k < s->cov_pool.size(); ++k)
+      if (s->cov_pool[k].cap >= need && (best == s->cov_pool.size() ||
+                                         s->cov_pool[k].cap < s->cov_pool[best].cap))
+        best = k;
+    PinnedBuf b{};
+    if (best < s->cov_pool.size()) {
+      b = s->cov_pool[best];
+      s->cov_pool.erase(s->cov_pool.begin() + (ptrdiff_t)best);
+    } else if (cudaMallocHost(&b.p, need * sizeof(int64_t)) == cudaSuccess) {
+      b.cap = need;
+    } else {
+      return rd::set_error(RD_ENOMEM, "rd_server: no page-locked memory for window sums");
+    }
+    if (r.cov.p) s->cov_pool.push_back(PinnedBuf{r.cov.p, r.cov.cap, 0});
+    r.cov = b;
+  }
+  r.cov.len = need;
   rd_output o{};
   o.events = r.events.data();
   o.cap_events = q.n_events;
   o.flits = r.flits.data();
   o.cap_flits = q.n_events * nfl;
   o.cov_windows = r.windows.data();
-  o.cov_acc = r.cov.data();
+  o.cov_acc = r.cov.p;
   o.cap_cov_windows = q.n_cov_windows;
   rs = rd_chain_fetch(st.ch, &o);
   r.n_events = o.n_events;
@@ -227,6 +280,9 @@ void rd_server_destroy(rd_server* s) {
   }
   for (rd_cplx16* h : s->host)
     if (h) cudaFreeHost(h);
+  for (PinnedBuf& b : s->cov_pool) cudaFreeHost(b.p);
+  for (auto& kv : s->reqs)
+    if (kv.second.cov.p) cudaFreeHost(kv.second.cov.p);
   delete s;
 }
 
@@ -278,6 +334,17 @@ rd_status rd_stream_open(rd_server* s, const rd_config* cfg, const rd_cplx16* co
   }
   ss.open = true;
   s->used += fp;
+  // one page-locked block for the most window sums a request of this stream
+  // can close, so that requests take them without allocating
+  if (ss.n_pairs && cfg->cov_source != RD_COV_OFF && frames) {
+    const uint64_t wl = cfg->cov_window ? cfg->cov_window : 1u;
+    const size_t words = (size_t)(frames / wl + 1u) * cfg->n_fft * ss.n_pairs * 2u;
+    PinnedBuf b{};
+    if (cudaMallocHost(&b.p, words * sizeof(int64_t)) == cudaSuccess) {
+      b.cap = words;
+      s->cov_pool.push_back(b);
+    }
+  }
   uint32_t id = 0;
   while (id < s->streams.size() && s->streams[id].open) ++id;
   if (id == s->streams.size()) s->streams.push_back(ss);
@@ -317,6 +384,13 @@ rd_status rd_server_submit(rd_server* s, uint32_t id, const rd_cplx16* adc, uint
   s->free_host.pop_back();
   rd_cplx16* h = s->host[r.host_buf];
   for (uint32_t c = 0; c < st.cfg.n_chan; ++c) std::memcpy(h + (size_t)c * n, adc + (size_t)c * ld, n * 4);
+  if (!s->pool.empty()) {  // buffers of an earlier request
+    OutBufs& b = s->pool.back();
+    r.events = std::move(b.events);
+    r.flits = std::move(b.flits);
+    r.windows = std::move(b.windows);
+    s->pool.pop_back();
+  }
   r.t_submit = s->now();
   *req_id = r.id;
   st.outstanding++;
@@ -391,11 +465,11 @@ rd_status rd_server_take(rd_server* s, uint64_t req_id, rd_output* out) {
     const uint32_t k = std::min<uint32_t>(r.n_windows, out->cap_cov_windows);
     trunc |= k < r.n_windows;
     if (out->cov_windows) std::memcpy(out->cov_windows, r.windows.data(), k * sizeof(rd_cov_window));
-    const size_t per = r.n_windows ? r.cov.size() / r.n_windows : 0;
-    if (out->cov_acc) std::memcpy(out->cov_acc, r.cov.data(), k * per * 8);
+    const size_t per = r.n_windows ? r.cov.len / r.n_windows : 0;
+    if (out->cov_acc) std::memcpy(out->cov_acc, r.cov.p, k * per * 8);
   }
   const rd_status st = r.status;
-  s->reqs.erase(it);
+  retire(s, it);
   if (st != RD_OK) return st;
   return trunc ? rd::set_error(RD_ETRUNC, "rd_server_take: output capacity exceeded") : RD_OK;
 }
@@ -438,7 +512,7 @@ rd_status rd_server_run_trace(rd_server* s, uint64_t n_req, const uint32_t* stre
       const uint64_t j = idx[comp[i].req_id];
       latency_us[j] = (comp[i].t_done_us - t0) - arrival_us[j];
       if (comp[i].status != RD_OK && first_err == RD_OK) first_err = (rd_status)comp[i].status;
-      s->reqs.erase(comp[i].req_id);  // the outputs are not kept
+      retire(s, s->reqs.find(comp[i].req_id));  // the outputs are not kept
       ++done;
     }
   }

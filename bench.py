@@ -353,7 +353,7 @@ def abi_ptr(v: int):
 
 def run_serving(torch, n_streams: int = 32, n_req: int = 2000, n_burst: int = 400) -> dict:
     """32 resident streams of mixed tiny / medium / full geometry; a request
-    is 4096 samples per channel; the saturation rate is the median of three
+    is 4096 samples per channel; the saturation rate is the median of five
     bursts of n_burst requests all due at once; then n_req Poisson arrivals
     at 25/50/80/100 % of it; latency = completion - arrival."""
     from rdgb import abi, scenario as sc
@@ -382,8 +382,8 @@ def run_serving(torch, n_streams: int = 32, n_req: int = 2000, n_burst: int = 40
         samples = sum(streams[s][1].n_chan * 4096 for s in idx)
         return lat, mk, samples
 
-    trace(64, None)  # warm
-    sat = float(np.median([n_burst / trace(n_burst, None)[1] for _ in range(3)]))  # req / us
+    trace(n_burst, None)  # warm: every stream's buffers and the output pools
+    sat = float(np.median([n_burst / trace(n_burst, None)[1] for _ in range(5)]))  # req / us
     loads = []
     for load in (0.25, 0.5, 0.8, 1.0):
         lat, mk, samples = trace(n_req, sat * load)
@@ -394,7 +394,7 @@ def run_serving(torch, n_streams: int = 32, n_req: int = 2000, n_burst: int = 40
     srv.close()
     return {"streams": n_streams, "mix": "tiny / medium / full in turn, tensor form",
             "request": "4096 samples per channel", "max_inflight": 16,
-            "requests_per_load": n_req, "saturation": f"median of 3 bursts of {n_burst}",
+            "requests_per_load": n_req, "saturation": f"median of 5 bursts of {n_burst}",
             "saturation_req_per_s": round(sat * 1e6, 1), "loads": loads,
             "p99_us_at_80pct": next(x["p99_us"] for x in loads if x["load"] == 0.8)}
 
