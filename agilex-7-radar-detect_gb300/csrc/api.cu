@@ -965,7 +965,35 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
   const bool dev_ev = !taps && pinned(out->events), dev_fl = !taps && pinned(out->flits);
   const bool dev_cov = !taps && pinned(out->cov_acc);
   const bool drain = dev_ev || dev_fl || dev_cov;
-  const uint64_t n_chunks = (frames + ch->launch_frames - 1) / ch->launch_frames;
+  // chunk sizes: a quarter-size first chunk, so that compute starts after a
+  // quarter of a full copy, and a quarter-size last one, so that less compute
+  // and fewer results follow the last copy; full chunks between (the results
+  // do not depend on the chunking)
+  std::vector<uint32_t> sizes;
+  {
+    const uint64_t L = ch->launch_frames, q = std::max<uint64_t>(L / 4u, 1u);
+    uint64_t left = frames;
+    if (frames >= 2u * L) {
+      sizes.push_back((uint32_t)q);
+      left -= q;
+      while (left > L + q) {
+        sizes.push_back((uint32_t)L);
+        left -= L;
+      }
+      if (left > q) {
+        sizes.push_back((uint32_t)(left - q));
+        left = q;
+      }
+      sizes.push_back((uint32_t)left);
+    } else {
+      while (left) {
+        const uint64_t F = std::min(L, left);
+        sizes.push_back((uint32_t)F);
+        left -= F;
+      }
+    }
+  }
+  const uint64_t n_chunks = sizes.size();
   const uint32_t nfl = rd_detection_flits(c.packet_w);
   const size_t pk = (size_t)nfl * rd_flit_words(c.packet_w);
   if (drain) {
@@ -1006,8 +1034,8 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
     return RD_OK;
   };
   unsigned bi = 0, chunk = 0;
-  for (uint64_t f = 0; f < frames; f += ch->launch_frames, bi ^= 1u, ++chunk) {
-    const uint32_t F = (uint32_t)std::min<uint64_t>(ch->launch_frames, frames - f);
+  for (uint64_t f = 0; chunk < n_chunks; f += sizes[chunk], bi ^= 1u, ++chunk) {
+    const uint32_t F = sizes[chunk];
     uint32_t* stg = bi ? ch->stage2.p : ch->stage.p;
     CK(cudaStreamWaitEvent(ch->copy_stream, ch->ev_free[bi], 0));
     CK(cudaMemcpy2DAsync(stg, sld * 4, adc + f * N, ld * 4, (size_t)F * N * 4, C,
