@@ -966,16 +966,20 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
   const bool dev_cov = !taps && pinned(out->cov_acc);
   const bool drain = dev_ev || dev_fl || dev_cov;
   // chunk sizes: a quarter-size first chunk, so that compute starts after a
-  // quarter of a full copy, and a quarter-size last one, so that less compute
-  // and fewer results follow the last copy; full chunks between (the results
-  // do not depend on the chunking)
+  // quarter of a full copy, then chunks growing by half each time (a chunk's
+  // copy, at ~1.5x the chain's sample rate, then ends while its predecessor
+  // computes), full chunks, and a quarter-size last one, so that less compute
+  // and fewer results follow the last copy (the results do not depend on the
+  // chunking)
   std::vector<uint32_t> sizes;
   {
     const uint64_t L = ch->launch_frames, q = std::max<uint64_t>(L / 4u, 1u);
     uint64_t left = frames;
     if (frames >= 2u * L) {
-      sizes.push_back((uint32_t)q);
-      left -= q;
+      for (uint64_t s0 = q; s0 < L && left > s0 + L + q; s0 = std::min<uint64_t>(L, s0 * 3u / 2u)) {
+        sizes.push_back((uint32_t)s0);
+        left -= s0;
+      }
       while (left > L + q) {
         sizes.push_back((uint32_t)L);
         left -= L;

@@ -43,7 +43,7 @@ def args_():
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--workload", default="medium")
     ap.add_argument("--cpis", type=int, default=None, help="CPIs per step (default: the workload's)")
-    ap.add_argument("--max-frames", type=int, default=2048,
+    ap.add_argument("--max-frames", type=int, default=4096,
                     help="frames per launch (the default gives the best end-to-end rate)")
     ap.add_argument("--form", choices=["cuda_core", "tensor"], default="cuda_core")
     ap.add_argument("--no-e2e", action="store_true")
@@ -233,7 +233,7 @@ def run_forms(torch, a, stream) -> dict:
     from rdgb import abi, chain as gc, scenario as sc
 
     out = {}
-    medium_frames = a.max_frames if a is not None else 2048
+    medium_frames = a.max_frames if a is not None else 4096
     for wl, cpis, frames in (("medium", 64, medium_frames), ("full", 2, 1024)):
         p = sc.preset(wl)
         n = cpis * p.cpi_samples
