@@ -79,6 +79,35 @@ __device__ __forceinline__ void bfly(C2& a, C2& t, unsigned sh, unsigned& ovf, u
   t = hi;
 }
 
+// The halving butterflies of a bound-checked pass on the FMA pipe, exactly.
+// An integer v with |v| < 2^22 is held as the float 1.5 x 2^23 + v (bit
+// pattern 0x4B400000 + v): around 1.5 x 2^23 the float spacing is 1, so
+// fma(s, 0.5, 1.5 x 2^23) of an integer s below 2^17 in magnitude is
+// 1.5 x 2^23 + RNE(s / 2) - IEEE round-to-nearest-even on the sum, whose
+// integer part has the parity of RNE(s / 2) because 1.5 x 2^23 is even (the
+// "magic number" rounding). Every other step (a + (t - 3 x 2^23) = a + t,
+// a - t, 3 x 2^23 - t) is exact, and each is written with an explicitly
+// rounded intrinsic so that no contraction changes it. Values never depend
+// on which pipe computed them.
+struct F2 {
+  float re, im;
+};
+constexpr float kMg = 12582912.0f, kMg2 = 25165824.0f;  // 1.5 x 2^23, 3 x 2^23
+__device__ __forceinline__ float mg(int v) { return __int_as_float(v + 0x4B400000); }
+__device__ __forceinline__ int ung(float f) { return __float_as_int(f) - 0x4B400000; }
+
+// a, t <- (RNE((a + u) / 2), RNE((a - u) / 2)), u = t or -j t, on held values
+template <bool K1>
+__device__ __forceinline__ void bfly_mg(F2& a, F2& t) {
+  const F2 u = K1 ? F2{t.im, __fsub_rn(kMg2, t.re)} : t;
+  const F2 lo{__fmaf_rn(__fadd_rn(a.re, __fsub_rn(u.re, kMg2)), 0.5f, kMg),
+              __fmaf_rn(__fadd_rn(a.im, __fsub_rn(u.im, kMg2)), 0.5f, kMg)};
+  const F2 hi{__fmaf_rn(__fsub_rn(a.re, u.re), 0.5f, kMg),
+              __fmaf_rn(__fsub_rn(a.im, u.im), 0.5f, kMg)};
+  a = lo;
+  t = hi;
+}
+
 // a * w rounded once (cmul_q15, fxp.hpp:314-318) for a twiddle w {re, im}
 // (kept unpacked in shared memory)
 template <bool FL>
@@ -147,10 +176,22 @@ __device__ __forceinline__ void lane_stages(C2 (&E)[4], int q, int tl, unsigned 
     unsigned f0 = 0, f1 = 0;
     const unsigned sh0 = SH1 ? 1u : (sched >> S) & 1u;
     const unsigned sh1 = SH1 ? 1u : (sched >> (S + 1)) & 1u;
-    bfly<FL, false>(E[0], E[2], sh0, ovf, f0);  // BF2I, distance d0
-    bfly<FL, false>(E[1], E[3], sh0, ovf, f0);
-    bfly<FL, false>(E[0], E[1], sh1, ovf, f1);  // BF2II, distance d1
-    bfly<FL, true>(E[2], E[3], sh1, ovf, f1);   // odd block: -j on the lower half
+    if constexpr (!FL && SH1) {  // both sub-stages halve, nothing saturates
+      F2 G[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) G[j] = F2{mg(E[j].re), mg(E[j].im)};
+      bfly_mg<false>(G[0], G[2]);  // BF2I, distance d0
+      bfly_mg<false>(G[1], G[3]);
+      bfly_mg<false>(G[0], G[1]);  // BF2II, distance d1
+      bfly_mg<true>(G[2], G[3]);   // odd block: -j on the lower half
+#pragma unroll
+      for (int j = 0; j < 4; ++j) E[j] = C2{ung(G[j].re), ung(G[j].im)};
+    } else {
+      bfly<FL, false>(E[0], E[2], sh0, ovf, f0);  // BF2I, distance d0
+      bfly<FL, false>(E[1], E[3], sh0, ovf, f0);
+      bfly<FL, false>(E[0], E[1], sh1, ovf, f1);  // BF2II, distance d1
+      bfly<FL, true>(E[2], E[3], sh1, ovf, f1);   // odd block: -j on the lower half
+    }
     if constexpr (S + 2 < NL) {                 // group-closing twiddle
       const int2* tw = twp + (S / 2) * M;
       E[0] = twm<FL>(E[0], tw[base], ovf, f1);
