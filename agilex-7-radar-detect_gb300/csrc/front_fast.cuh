@@ -223,8 +223,18 @@ __device__ __forceinline__ void lane_stages(C2 (&E)[4], int q, int tl, unsigned 
     // final single stage (NL odd), distance 1, quad = 4*tl .. 4*tl+3
     unsigned f0 = 0;
     const unsigned sh0 = SH1 ? 1u : (sched >> S) & 1u;
-    bfly<FL, false>(E[0], E[1], sh0, ovf, f0);
-    bfly<FL, false>(E[2], E[3], sh0, ovf, f0);
+    if constexpr (!FL && SH1) {
+      F2 G[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) G[j] = F2{mg(E[j].re), mg(E[j].im)};
+      bfly_mg<false>(G[0], G[1]);
+      bfly_mg<false>(G[2], G[3]);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) E[j] = C2{ung(G[j].re), ung(G[j].im)};
+    } else {
+      bfly<FL, false>(E[0], E[1], sh0, ovf, f0);
+      bfly<FL, false>(E[2], E[3], sh0, ovf, f0);
+    }
     if (FL) sf |= f0 << (2 * S);
     uint32_t* b = cur ? buf1 : buf0;
     const int base = 4 * tl;
@@ -407,7 +417,14 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
       const uint2 eo = *reinterpret_cast<const uint2*>(b + 2 * j);  // phases 2j, 2j + 1
       C2 e = unpk(eo.x);
       C2 o = twm<FL>(unpk(eo.y), tw[j], ovf, fm);
-      bfly<FL, false>(e, o, shm, ovf, fm);
+      if constexpr (!FL && SH1) {
+        F2 ge{mg(e.re), mg(e.im)}, go{mg(o.re), mg(o.im)};
+        bfly_mg<false>(ge, go);
+        e = C2{ung(ge.re), ung(ge.im)};
+        o = C2{ung(go.re), ung(go.im)};
+      } else {
+        bfly<FL, false>(e, o, shm, ovf, fm);
+      }
       const int bin = (int)bitrev((unsigned)j, NL);
       if (ok) {
         tile_row[bin * cbp] = pk(e);
