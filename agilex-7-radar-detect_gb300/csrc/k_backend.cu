@@ -813,15 +813,17 @@ __device__ __forceinline__ uint4 pack_detection(uint64_t cut, unsigned bin, unsi
 // the products and comparisons in 64 bits either way): the ballot mask of the
 // emitting cells, the detection slots, the frame's counts. Returns the
 // frame's event count (detections + SUMMARY) and adds its detections to det.
-template <class Tp>
+template <int R, class Tp>
 __device__ __forceinline__ unsigned decide_frame(const CfarParams& p, uint64_t u, const Tp* pre,
                                                  bool live, int lo_b, int hi_b, unsigned n_ok,
                                                  unsigned& det) {
   const unsigned lane = threadIdx.x & 31u;
-  const unsigned words = (p.n + 31u) / 32u;
+  const unsigned words = (p.n + 31u) / 32u;  // at most 4 R
   const unsigned ca_n8 = (p.rl + p.rg) << 8;
   unsigned emitted = 0, mword = 0;
-  for (unsigned r = 0; r < words; ++r) {
+#pragma unroll
+  for (unsigned r = 0; r < 4u * R; ++r) {
+    if (r >= words) break;
     const unsigned i = r * 32u + lane;
     bool dt = false;
     Tp cut = 0, sum = 0;  // in Tp: every window sum fits (see warp_prefix)
@@ -903,11 +905,11 @@ __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_decide(CfarParams p) {
     if (narrow) {  // pre[0] three words past the boundary: pre + 1 on it
       uint32_t* pre = reinterpret_cast<uint32_t*>(wbase) + 3;
       warp_prefix<R>(p, c, pre, p.vec);
-      count = decide_frame(p, u, pre, live, lo_b, hi_b, n_ok, det);
+      count = decide_frame<R>(p, u, pre, live, lo_b, hi_b, n_ok, det);
     } else {  // pre[0] one word past the boundary
       uint64_t* pre = wbase + 1;
       warp_prefix<R>(p, c, pre, p.vec);
-      count = decide_frame(p, u, pre, live, lo_b, hi_b, n_ok, det);
+      count = decide_frame<R>(p, u, pre, live, lo_b, hi_b, n_ok, det);
     }
   }
   if (lane == 0) {
