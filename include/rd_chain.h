@@ -197,7 +197,11 @@ rd_status rd_chain_set_pairs(rd_chain* ch, const uint32_t* x, const uint32_t* y,
  * The copies overlap the kernels chunk by chunk: each chunk's input is copied
  * while the previous chunk computes, and results into page-locked host
  * buffers (cudaHostAlloc, cudaHostRegister) are copied as each chunk
- * finishes; into pageable buffers they are copied at the end. */
+ * finishes; into pageable buffers they are copied at the end. A call of at
+ * least two launches' worth of frames starts with a quarter-size chunk,
+ * grows the next chunks by half up to the launch size and ends with a
+ * quarter-size chunk, so that little of the first copy and of the last
+ * results stays uncovered. */
 rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n,
                            uint64_t ld, rd_output* out);
 
@@ -238,7 +242,9 @@ rd_status rd_chain_stats(const rd_chain* ch, rd_stats* st);
 rd_status rd_chain_reset(rd_chain* ch, void* stream);
 
 /* Frames per kernel launch, 1..max_frames (default max_frames). Results do
- * not depend on it; the batch autotuner varies it. */
+ * not depend on it; the batch autotuner varies it. Longer launches fill
+ * more waves of every kernel (medium workload on a GB300: 27 Gsamples/s at
+ * 1024 frames, 36 at 4096, 38 at 16384 with the input on the device). */
 rd_status rd_chain_set_launch_frames(rd_chain* ch, uint32_t frames);
 
 /* Device bytes a chain of this configuration holds, with the output
