@@ -337,6 +337,12 @@ typedef struct {
 } rd_server_info;
 rd_status rd_server_create(const rd_server_config* cfg, rd_server** out);
 void rd_server_destroy(rd_server* s);
+/* Admits a stream (RD_ENOMEM when its chain does not fit the budget). Besides
+ * the chain's device state it reserves one page-locked host block for the
+ * most covariance window sums a request of the stream can close (34 MB for a
+ * 64-channel, 1024-bin stream), so that requests read them by DMA without
+ * allocating; blocks stay with the server for later requests and streams
+ * until rd_server_destroy. */
 rd_status rd_stream_open(rd_server* s, const rd_config* cfg, const rd_cplx16* coeff,
                          const rd_cplx16* weights, uint32_t* stream_id);
 rd_status rd_stream_close(rd_server* s, uint32_t stream_id);
