@@ -163,3 +163,41 @@ def test_history_reads(port, refo):
             assert [np.asarray(v).tolist() for v in a.read_history(bin_, off)] == \
                    [np.asarray(v).tolist() for v in b.read_history(bin_, off)]
     assert a.stats()["hist_reads"] == b.stats()["hist_reads"]
+
+
+@pytest.mark.parametrize("case", ["full_slice", "medium_exp_go", "medium_saturating_block"])
+def test_port_matches_reference_modes(port, refo, case):
+    # the restatement against the reference model's own chain on the full
+    # geometry (64 channels, 1024 bins, 64 beams, 2080 pairs, 512-bit packets)
+    # and on the covariance and CFAR modes the presets leave at their defaults
+    rng = np.random.default_rng(len(case))
+    if case == "full_slice":
+        p = sc.preset("full", cov_window=2)
+        cfg = sc.make_config(p)
+        frames = 5
+        coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+        x = sc.adc(p, frames * p.n_fft)
+    else:
+        p = sc.preset("medium", cov_window=7)
+        cfg = sc.make_config(p)
+        frames = 24
+        coeff = sc.coefficients(p.n_fft, p.taps)
+        w = rng.integers(0, 2**32, size=p.n_chan * p.n_beams, dtype=np.uint64).astype(np.uint32)
+        x = rng.integers(0, 2**32, size=(p.n_chan, frames * p.n_fft),
+                         dtype=np.uint64).astype(np.uint32)
+        if case == "medium_exp_go":
+            cfg.cov_mode, cfg.cov_exp_k, cfg.cov_acc_w = abi.RD_COV_EXP, 3, 40
+            cfg.cfar_mode, cfg.cfar_out_mode = abi.RD_CFAR_GO, abi.RD_CFAR_DENSE
+        else:  # an unscaled FFT fills the spectrum; 7-frame block sums pass
+            cfg.scale_sched = 0  # 33-bit integrators, which saturate
+            cfg.cov_acc_w = 33
+    px, py = sc.pair_table(p)
+    a = port.chain(cfg, coeff, w, px, py)
+    b = refo.chain(cfg, coeff, w, px, py)
+    ra, rb = a.process(x, taps=True, threads=4), b.process(x, taps=True)
+    assert diff(ra, rb, CHAIN_KEYS + TAP_KEYS) == [], case
+    assert diff_stats(a.stats(), b.stats()) == [], case
+    fa, fb = a.flush_cov(), b.flush_cov()
+    assert diff(fa, fb, ("cov_windows", "cov_acc")) == [], case
+    if case == "medium_saturating_block":
+        assert a.stats()["cov_sat_steps"] > 0
