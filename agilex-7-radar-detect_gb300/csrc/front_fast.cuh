@@ -573,12 +573,11 @@ void launch_fast(const FrontParams& p, cudaStream_t s) {
   while (FB * CB * N > 8192u && CB > 1u) CB /= 2;
   const unsigned twn = G::NTW * G::M + (SPC == 2 ? G::M : 0);
   const size_t smem = (2u * twn + 2u * IPP * N + (size_t)FB * N * (CB + 1u)) * sizeof(uint32_t);
-  static bool attr = false;
-  if (!attr) {
+  static PerDevice attr;
+  attr.once([] {
     cudaFuncSetAttribute(k_front_fast<NL, SPC, TT, SH1>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
-    attr = true;
-  }
+  });
   const dim3 grid((p.F + FB - 1) / FB, (p.C + CB - 1) / CB);
   k_front_fast<NL, SPC, TT, SH1><<<grid, 256, smem, s>>>(p, FB, CB);
 }

@@ -186,11 +186,10 @@ __global__ void __launch_bounds__(256) k_beam(BeamParams p) {
 
 template <int BPT, int CC>
 static void launch_beam_k(const BeamParams& p, dim3 grid, size_t smem, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
+  static PerDevice attr;
+  attr.once([] {
     cudaFuncSetAttribute(k_beam<BPT, CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr = true;
-  }
+  });
   k_beam<BPT, CC><<<grid, 256, smem, s>>>(p);
 }
 
@@ -1075,16 +1074,15 @@ __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_emit(CfarParams p) {
 }
 
 // Decide: 8 frames x (n + 2) words of shared memory; n <= 1024 needs the
-// opt-in above 48 KB, set once per instantiation.
+// opt-in above 48 KB, set once per instantiation and device.
 template <int R>
 static void launch_cfar_r(const CfarParams& p, cudaStream_t s) {
-  static bool attr = false;
+  static PerDevice attr;
   const size_t sm = (size_t)kCfarWarps * (p.n + 2u) * sizeof(uint64_t);
-  if (!attr) {
+  attr.once([] {
     const int most = (int)((size_t)kCfarWarps * (128u * R + 2u) * sizeof(uint64_t));
     cudaFuncSetAttribute(k_cfar_decide<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
-    attr = true;
-  }
+  });
   const unsigned tiles = cfar_tiles(p.frames);
   const unsigned emits = (unsigned)((p.frames + kEmitFrames - 1u) / kEmitFrames);
   k_cfar_decide<R><<<tiles, kCfarWarps * 32, sm, s>>>(p);

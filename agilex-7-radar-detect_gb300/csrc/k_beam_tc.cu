@@ -405,9 +405,11 @@ void launch_beam_tc(const BeamParams& p, cudaStream_t s) {
     if (dev >= 0 && dev < 64) g_tc_attr[dev].store(true);
   }
   if (p.N % kTcRows == 0u && p.C % 4u == 0u && p.C <= 64u && p.ring_frames >= 1u) {
-    static int n_sm = 0;
-    if (!n_sm && cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    int n_sm = 0;
+    if (cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+      cudaGetLastError();
       n_sm = 0;
+    }
     const uint64_t tiles = rows / kTcRows;  // N a multiple of 128: every tile full
     const uint64_t grid = n_sm > 0 ? std::min<uint64_t>(tiles, 2ull * (unsigned)n_sm) : tiles;
     k_beam_tc_pipe<<<(unsigned)grid, 256, pipe_smem(p.C), s>>>(p, (unsigned)tiles);

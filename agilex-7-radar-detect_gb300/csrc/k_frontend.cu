@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(MAXT) k_front(FrontParams p, unsigned FB, unsi
   reduce_stats(p.stats, pfl, psat, sf);
 }
 
-static bool g_front_attr = false;
+static PerDevice g_front_attr;
 
 unsigned launch_front(const FrontParams& p, cudaStream_t s) {
   if (launch_front_fast(p, s)) return 1;  // it writes tail_out too
@@ -313,7 +313,7 @@ unsigned launch_front(const FrontParams& p, cudaStream_t s) {
   const unsigned twn = ((nl - 1u) / 2u) * m + (p.spc == 2u ? m : 0u);
   const dim3 grid((p.F + FB - 1) / FB, (p.C + CB - 1) / CB);
   const size_t smem = (twn + nth + (size_t)FB * p.N * (CB + 1u)) * sizeof(uint32_t);
-  if (!g_front_attr) {
+  g_front_attr.once([] {
     const int lim = 96 * 1024;
     cudaFuncSetAttribute(k_front<0, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     cudaFuncSetAttribute(k_front<4, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
@@ -323,8 +323,7 @@ unsigned launch_front(const FrontParams& p, cudaStream_t s) {
     cudaFuncSetAttribute(k_front<4, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     cudaFuncSetAttribute(k_front<8, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     cudaFuncSetAttribute(k_front<16, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    g_front_attr = true;
-  }
+  });
   if (nth <= 256u) {
     switch (p.T) {
       case 4: k_front<4, 256><<<grid, nth, smem, s>>>(p, FB, CB, twn); break;

@@ -5,11 +5,32 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <vector>
 
 #include "../../include/rd_chain.h"
 
 namespace rd {
+
+// Set-up that belongs to one device's context (a kernel's dynamic
+// shared-memory opt-in): once() runs f the first time it is reached with a
+// given device current, so every device the process uses gets its own call.
+// Devices past the 64 the mask tracks run f every time (it is cheap).
+struct PerDevice {
+  std::atomic<unsigned long long> done{0};
+  template <class F>
+  void once(F&& f) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+      cudaGetLastError();
+      dev = -1;
+    }
+    const unsigned long long bit = (dev >= 0 && dev < 64) ? 1ull << dev : 0ull;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) return;
+    f();
+    if (bit) done.fetch_or(bit, std::memory_order_acq_rel);
+  }
+};
 
 // Device-side cumulative statistics of one stream (zeroed at create).
 struct DevStats {

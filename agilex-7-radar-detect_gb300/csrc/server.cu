@@ -335,12 +335,29 @@ rd_status rd_stream_open(rd_server* s, const rd_config* cfg, const rd_cplx16* co
   ss.open = true;
   s->used += fp;
   // one page-locked block for the most window sums a request of this stream
-  // can close, so that requests take them without allocating
+  // can close, so that requests take them without allocating. The pool keeps
+  // at most as many blocks as requests can be outstanding (retire() keeps the
+  // same cap): when it is full, its smallest block makes room for this one if
+  // it is too small for this stream, else nothing is added, so repeated
+  // open / close cycles do not grow page-locked memory.
   if (ss.n_pairs && cfg->cov_source != RD_COV_OFF && frames) {
     const uint64_t wl = cfg->cov_window ? cfg->cov_window : 1u;
     const size_t words = (size_t)(frames / wl + 1u) * cfg->n_fft * ss.n_pairs * 2u;
+    const size_t keep = (size_t)s->cfg.queue_cap + s->cfg.max_inflight;
+    bool add = true;
+    if (s->cov_pool.size() >= keep && !s->cov_pool.empty()) {
+      size_t sm = 0;
+      for (size_t k = 1; k < s->cov_pool.size(); ++k)
+        if (s->cov_pool[k].cap < s->cov_pool[sm].cap) sm = k;
+      if (s->cov_pool[sm].cap >= words) {
+        add = false;
+      } else {
+        cudaFreeHost(s->cov_pool[sm].p);
+        s->cov_pool.erase(s->cov_pool.begin() + (ptrdiff_t)sm);
+      }
+    }
     PinnedBuf b{};
-    if (cudaMallocHost(&b.p, words * sizeof(int64_t)) == cudaSuccess) {
+    if (add && cudaMallocHost(&b.p, words * sizeof(int64_t)) == cudaSuccess) {
       b.cap = words;
       s->cov_pool.push_back(b);
     }
@@ -486,6 +503,8 @@ rd_status rd_server_info_get(rd_server* s, rd_server_info* info) {
   return RD_OK;
 }
 
+static constexpr double kTraceStallUs = 30e6;
+
 rd_status rd_server_run_trace(rd_server* s, uint64_t n_req, const uint32_t* stream_ids,
                               const double* arrival_us, const rd_cplx16* const* adc,
                               const uint64_t* n, double* latency_us, double* makespan_us) {
@@ -496,8 +515,21 @@ rd_status rd_server_run_trace(rd_server* s, uint64_t n_req, const uint32_t* stre
   const double t0 = s->now();
   uint64_t next = 0, done = 0;
   rd_status first_err = RD_OK;
+  // the loop gives up when requests are outstanding and none has completed
+  // for kTraceStallUs of wall-clock time (a device that stopped answering)
+  double t_progress = t0;
+  uint64_t done_seen = 0;
   while (done < n_req) {
     const double t = s->now() - t0;
+    if (done != done_seen) {
+      done_seen = done;
+      t_progress = t + t0;
+    } else if (next > done && t + t0 - t_progress > kTraceStallUs) {
+      if (makespan_us) *makespan_us = s->now() - t0;
+      return rd::set_error(RD_ETIMEOUT, "rd_server_run_trace: no request completed for %.0f s "
+                           "with %llu outstanding", kTraceStallUs * 1e-6,
+                           (unsigned long long)(next - done));
+    }
     while (next < n_req && arrival_us[next] <= t) {
       uint64_t id = 0;
       const rd_status st = rd_server_submit(s, stream_ids[next], adc[next], n[next], n[next], &id);

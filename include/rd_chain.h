@@ -242,9 +242,9 @@ rd_status rd_chain_stats(const rd_chain* ch, rd_stats* st);
 rd_status rd_chain_reset(rd_chain* ch, void* stream);
 
 /* Frames per kernel launch, 1..max_frames (default max_frames). Results do
- * not depend on it; the batch autotuner varies it. Longer launches fill
- * more waves of every kernel (medium workload on a GB300: 27 Gsamples/s at
- * 1024 frames, 36 at 4096, 38 at 16384 with the input on the device). */
+ * not depend on it; the batch autotuner varies it. Longer launches fill more
+ * waves of every kernel and pay fewer launch gaps, at the cost of device
+ * memory (the spectrum ring and the CFAR buffers grow with it). */
 rd_status rd_chain_set_launch_frames(rd_chain* ch, uint32_t frames);
 
 /* Device bytes a chain of this configuration holds, with the output
@@ -342,7 +342,8 @@ void rd_server_destroy(rd_server* s);
  * most covariance window sums a request of the stream can close (34 MB for a
  * 64-channel, 1024-bin stream), so that requests read them by DMA without
  * allocating; blocks stay with the server for later requests and streams
- * until rd_server_destroy. */
+ * until rd_server_destroy, at most queue_cap + max_inflight of them (a full
+ * pool gives up its smallest block for a larger one). */
 rd_status rd_stream_open(rd_server* s, const rd_config* cfg, const rd_cplx16* coeff,
                          const rd_cplx16* weights, uint32_t* stream_id);
 rd_status rd_stream_close(rd_server* s, uint32_t stream_id);
@@ -360,7 +361,9 @@ rd_status rd_server_info_get(rd_server* s, rd_server_info* info);
 /* A native request loop for measurement: request k (stream stream_ids[k],
  * samples adc[k], n[k] per channel) arrives at arrival_us[k] after the
  * start; each is submitted when it arrives (or as soon as the queue has
- * room) and polled to completion. latency_us[k] = completion - arrival. */
+ * room) and polled to completion. latency_us[k] = completion - arrival.
+ * Returns RD_ETIMEOUT when requests are outstanding and none completes for
+ * 30 s of wall-clock time. */
 rd_status rd_server_run_trace(rd_server* s, uint64_t n_req, const uint32_t* stream_ids,
                               const double* arrival_us, const rd_cplx16* const* adc,
                               const uint64_t* n, double* latency_us, double* makespan_us);
@@ -436,18 +439,22 @@ rd_status rd_cfar_run(const int64_t* cells, uint32_t n, uint32_t frames,
                       const rd_config* cfg, const uint32_t* frame_ids,
                       rd_event* events, uint64_t cap, uint64_t* n_events);
 
-/* cfar::run_frame like rd_cfar_run, but on caller-provided DEVICE buffers and
- * without allocating anything. It has no counterpart in the reference: it is
- * for callers that are handed device memory but may not call cudaMalloc
- * (code inside another framework's memory pool, real-time loops where an
+/* The CFAR detector of rd_cfar_run on caller-provided DEVICE buffers, without
+ * allocating anything. It has no counterpart in the reference. It is for
+ * callers that are handed device memory but may not call cudaMalloc (code
+ * inside another framework's memory pool, real-time loops where an
  * allocation would synchronise the device, processes whose allocator is
- * locked after start-up). Its scratch is a static device array shared by
- * every call on a device: at most RD_STATIC_CFAR_MAX_FRAMES frames of at most
+ * locked after start-up). Its scratch is a static device array of about
+ * 1.6 MB that every GPU loading the library holds until exit, shared by every
+ * call on a device: at most RD_STATIC_CFAR_MAX_FRAMES frames of at most
  * RD_STATIC_CFAR_MAX_CELLS cells (larger sizes return RD_EINVAL); calls whose
  * work overlaps on the GPU race on it. The first call on each device looks up
  * the scratch address and should come before any stream capture. cells,
  * frame_ids, events and n_events (one uint64) are device pointers; the call
- * is asynchronous on `stream` (a cudaStream_t, NULL = legacy stream). */
+ * is asynchronous on `stream` (a cudaStream_t, NULL = legacy stream).
+ * Because nothing waits for the device, an overflow is not reported as
+ * RD_ETRUNC: *n_events receives the full event count, only the first `cap`
+ * events are written, and the caller compares *n_events with cap. */
 #define RD_STATIC_CFAR_MAX_FRAMES 4096u
 #define RD_STATIC_CFAR_MAX_CELLS 1024u
 rd_status rd_cfar_run_static(const int64_t* cells, uint32_t n, uint32_t frames,

@@ -5,13 +5,15 @@ file and its ground-truth JSON for each named scenario, medium geometry
 (config/medium.json: 4 antennas, 256-point FFT, 2 samples per cycle,
 16 frames), seed 1. Run here, where the reference checkout is present:
 
-    python tests/golden/make_scenes.py /root/reference
+    python tests/golden/make_scenes.py <reference checkout>
 """
 import gzip
 import sys
 from pathlib import Path
 
-ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    sys.exit("usage: make_scenes.py <reference checkout>")
+ref = Path(sys.argv[1])
 sys.path.insert(0, str(ref / "model" / "python"))
 
 import gen_target_iq as g  # noqa: E402
