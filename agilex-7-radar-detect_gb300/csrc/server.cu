@@ -383,6 +383,23 @@ rd_status rd_stream_close(rd_server* s, uint32_t id) {
   return RD_OK;
 }
 
+rd_status rd_stream_set_pairs(rd_server* s, uint32_t id, const uint32_t* x, const uint32_t* y,
+                              uint32_t n_pairs) {
+  if (!s || id >= s->streams.size() || !s->streams[id].open)
+    return rd::set_error(RD_EINVAL, "rd_stream_set_pairs: no such stream");
+  StreamState& st = s->streams[id];
+  if (st.outstanding || st.busy)
+    return rd::set_error(RD_EINVAL, "rd_stream_set_pairs: the stream has requests");
+  if (n_pairs != st.n_pairs)
+    return rd::set_error(RD_EINVAL, "rd_stream_set_pairs: %u pairs, the stream was admitted with "
+                         "cov_n_pairs %u", n_pairs, st.n_pairs);
+  // the open's warm-up left the chain reset on its stream; the table goes in
+  // before the stream's first request
+  if (cudaStreamSynchronize(st.cs) != cudaSuccess)
+    return rd::set_error(RD_EDEVICE, "rd_stream_set_pairs: stream sync failed");
+  return rd_chain_set_pairs(st.ch, x, y, n_pairs);
+}
+
 rd_status rd_server_submit(rd_server* s, uint32_t id, const rd_cplx16* adc, uint64_t n,
                            uint64_t ld, uint64_t* req_id) {
   if (!s || !adc || !req_id || id >= s->streams.size() || !s->streams[id].open)

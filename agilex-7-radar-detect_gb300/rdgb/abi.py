@@ -199,6 +199,7 @@ def declare_rd(lib) -> None:
     _proto(lib, "rd_server_destroy", None, [VP])
     _proto(lib, "rd_stream_open", I32, [VP, P(RdConfig), VP, VP, P(U32)])
     _proto(lib, "rd_stream_close", I32, [VP, U32])
+    _proto(lib, "rd_stream_set_pairs", I32, [VP, U32, VP, VP, U32])
     _proto(lib, "rd_server_submit", I32, [VP, U32, VP, U64, U64, P(U64)])
     _proto(lib, "rd_server_poll", I32, [VP, P(RdCompletion), U32, P(U32)])
     _proto(lib, "rd_server_take", I32, [VP, U64, P(RdOutput)])
@@ -230,7 +231,7 @@ EXPORTED = [
     "rd_batch_create", "rd_batch_destroy", "rd_batch_run", "rd_batch_run_sequential",
     "rd_batch_fetch", "rd_batch_tune", "rd_batch_egress", "rd_server_create",
     "rd_server_destroy", "rd_stream_open",
-    "rd_stream_close", "rd_server_submit", "rd_server_poll", "rd_server_take",
+    "rd_stream_close", "rd_stream_set_pairs", "rd_server_submit", "rd_server_poll", "rd_server_take",
     "rd_server_info_get", "rd_server_run_trace", "rd_chain_read_history", "rd_pfb_run",
     "rd_fft_run", "rd_bf_run", "rd_power_run", "rd_cross_power_run", "rd_cfar_run", "rd_cfar_run_static",
     "rd_packetize", "rd_fxp_apply", "rd_last_error", "rd_device_ok", "rd_version",

@@ -251,37 +251,62 @@ def scene(p: Preset, seed: int | None = None) -> list[Tone]:
 TW_RE, TW_IM = unpack(np.array(TWIDDLES, dtype=np.uint32))
 
 
+def _adc_row(tones, s: int, a: int, idx: np.ndarray, out_row: np.ndarray) -> None:
+    """Channel a of the ADC samples at time indices idx, into out_row."""
+    n = idx.size
+    re = np.zeros(n, dtype=np.int64)
+    im = np.zeros(n, dtype=np.int64)
+    for t in tones:
+        with np.errstate(over="ignore"):
+            ph = (np.uint64(t.phi0) + np.uint64(t.dphi) * np.uint64(a)
+                  + np.uint64(t.freq) * idx)
+            if t.chirp:
+                ph = ph + np.uint64(t.chirp) * ((idx * (idx - np.uint64(1))) >> np.uint64(1))
+        e = ((ph & np.uint64(0xFFFFFFFF)) >> np.uint64(22)).astype(np.int64)
+        # exp(+j phase) = conj(W^e)
+        re += (t.amp * TW_RE[e] + (1 << 14)) >> 15
+        im += (-t.amp * TW_IM[e] + (1 << 14)) >> 15
+    key = (np.uint64(s & 0xFFFFFFFF) << np.uint64(32)) ^ (np.uint64(a) << np.uint64(40))
+    h1 = _mix64(key ^ (idx * np.uint64(2)))
+    h2 = _mix64(key ^ (idx * np.uint64(2) + np.uint64(1)))
+    for h, acc in ((h1, re), (h2, im)):
+        u = sum(((h >> np.uint64(16 * k)) & np.uint64(0xFFFF)).astype(np.int64) for k in range(4))
+        acc += ((u - 2 * 65535) * 111) >> 16     # sigma ~ 64
+    np.clip(re, -2047, 2047, out=re)
+    np.clip(im, -2047, 2047, out=im)
+    out_row[:] = pack(re, im)
+
+
 def adc(p: Preset, n: int, start: int = 0, seed: int | None = None,
-        chans: slice | None = None) -> np.ndarray:
+        chans: slice | None = None, threads: int | None = None) -> np.ndarray:
     """ADC samples [n_chan][n] (packed complex int16) for sample indices
-    start .. start+n-1 of the stream. Integer-only, deterministic."""
+    start .. start+n-1 of the stream. Integer-only, deterministic. Large
+    requests spread the channels over host threads (the values do not depend
+    on it)."""
+    import os
     s = p.seed if seed is None else seed
     tones = scene(p, s)
     ch = range(p.n_chan)[chans] if chans is not None else range(p.n_chan)
     out = np.empty((len(ch), n), dtype=np.uint32)
-    idx = np.arange(start, start + n, dtype=np.uint64)
-    for row, a in enumerate(ch):
-        re = np.zeros(n, dtype=np.int64)
-        im = np.zeros(n, dtype=np.int64)
-        for t in tones:
-            with np.errstate(over="ignore"):
-                ph = (np.uint64(t.phi0) + np.uint64(t.dphi) * np.uint64(a)
-                      + np.uint64(t.freq) * idx)
-                if t.chirp:
-                    ph = ph + np.uint64(t.chirp) * ((idx * (idx - np.uint64(1))) >> np.uint64(1))
-            e = ((ph & np.uint64(0xFFFFFFFF)) >> np.uint64(22)).astype(np.int64)
-            # exp(+j phase) = conj(W^e)
-            re += (t.amp * TW_RE[e] + (1 << 14)) >> 15
-            im += (-t.amp * TW_IM[e] + (1 << 14)) >> 15
-        key = (np.uint64(s & 0xFFFFFFFF) << np.uint64(32)) ^ (np.uint64(a) << np.uint64(40))
-        h1 = _mix64(key ^ (idx * np.uint64(2)))
-        h2 = _mix64(key ^ (idx * np.uint64(2) + np.uint64(1)))
-        for h, acc in ((h1, re), (h2, im)):
-            u = sum(((h >> np.uint64(16 * k)) & np.uint64(0xFFFF)).astype(np.int64) for k in range(4))
-            acc += ((u - 2 * 65535) * 111) >> 16     # sigma ~ 64
-        np.clip(re, -2047, 2047, out=re)
-        np.clip(im, -2047, 2047, out=im)
-        out[row] = pack(re, im)
+    # rows in pieces of at most 2^20 samples keep the temporaries small
+    piece = 1 << 20
+    jobs = [(row, a, lo) for row, a in enumerate(ch) for lo in range(0, n, piece)]
+
+    def run(job):
+        row, a, lo = job
+        hi = min(n, lo + piece)
+        idx = np.arange(start + lo, start + hi, dtype=np.uint64)
+        _adc_row(tones, s, a, idx, out[row, lo:hi])
+
+    if threads is None:
+        threads = min(os.cpu_count() or 1, 16) if len(ch) * n >= (1 << 22) else 1
+    if threads > 1 and len(jobs) > 1:
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(threads) as ex:
+            list(ex.map(run, jobs))
+    else:
+        for j in jobs:
+            run(j)
     return out
 
 

@@ -22,13 +22,21 @@ class Server:
         self.streams: dict[int, tuple] = {}   # id -> (cfg, n_pairs)
         self._keep = []
 
-    def open(self, cfg: abi.RdConfig, coeff, weights) -> tuple[int, int]:
-        """(status, stream id); the id is valid when status is RD_OK."""
+    def open(self, cfg: abi.RdConfig, coeff, weights, pairs=None) -> tuple[int, int]:
+        """(status, stream id); the id is valid when status is RD_OK. `pairs`
+        (x, y): the covariance pair table, else the default one."""
         co = np.ascontiguousarray(coeff, np.uint32)
         w = np.ascontiguousarray(weights, np.uint32)
         sid = C.c_uint32()
         st = self.L.rd_stream_open(self.h, C.byref(cfg), co.ctypes.data, w.ctypes.data,
                                    C.byref(sid))
+        if st == abi.RD_OK and pairs is not None and cfg.cov_source:
+            x = np.ascontiguousarray(pairs[0], np.uint32)
+            y = np.ascontiguousarray(pairs[1], np.uint32)
+            st = self.L.rd_stream_set_pairs(self.h, sid.value, x.ctypes.data, y.ctypes.data,
+                                            len(x))
+            if st != abi.RD_OK:
+                self.L.rd_stream_close(self.h, sid.value)
         if st == abi.RD_OK:
             self.streams[sid.value] = (cfg, self.L.rd_cov_pairs(C.byref(cfg)))
         return st, sid.value

@@ -347,6 +347,10 @@ void rd_server_destroy(rd_server* s);
 rd_status rd_stream_open(rd_server* s, const rd_config* cfg, const rd_cplx16* coeff,
                          const rd_cplx16* weights, uint32_t* stream_id);
 rd_status rd_stream_close(rd_server* s, uint32_t stream_id);
+/* The stream's covariance pair table, as rd_chain_set_pairs; only before the
+ * stream's first request, with the cov_n_pairs it was admitted with. */
+rd_status rd_stream_set_pairs(rd_server* s, uint32_t stream_id, const uint32_t* x,
+                              const uint32_t* y, uint32_t n_pairs);
 /* Copies the request's samples ([C][n], row stride ld) and queues it;
  * RD_EAGAIN when queue_cap requests are outstanding. */
 rd_status rd_server_submit(rd_server* s, uint32_t stream_id, const rd_cplx16* adc, uint64_t n,

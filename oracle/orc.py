@@ -248,11 +248,12 @@ class OracleChain:
             self.orc.lib.orc_chain_destroy(self.h)
             self.h = None
 
-    def process(self, adc: np.ndarray, taps: bool = True, threads: int = 1) -> dict:
+    def process(self, adc: np.ndarray, taps: bool = True, threads: int = 1,
+                cap_events: int | None = None) -> dict:
         adc = np.ascontiguousarray(adc, np.uint32)
         n = adc.shape[1]
         frames = n // self.cfg.n_fft
-        out = Outputs(self.cfg, frames, self.n_pairs, taps)
+        out = Outputs(self.cfg, frames, self.n_pairs, taps, cap_events)
         r = self.orc.lib.orc_chain_process(self.h, abi.ptr(adc), n, n, C.byref(out.c), threads)
         if r != 0:
             raise RuntimeError(f"orc_chain_process: {r}")

@@ -65,3 +65,26 @@ def event_fields(ev: np.ndarray) -> dict:
     return {"kind": f(0, 2), "bin": f(2, 16), "frame_id": f(18, 16), "ref_cnt": f(34, 7),
             "alpha": f(41, 16), "det": f(57, 16), "sup": f(73, 16), "cut": f(89, 40),
             "sum": f(129, 47)}
+
+
+def rnd(rng, n):
+    return rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
+
+
+def banks(p, rng):
+    """Coefficient banks that take the PFB's three integer paths: a small-norm
+    bank (byte-limb dot products), a full-range random one (int64 sums), one
+    holding an imaginary -32768 (int32 multiplies), then the first again."""
+    n = p.n_fft * p.taps
+    small = sc.coefficients(p.n_fft, p.taps)
+    re, im = sc.unpack(sc.coefficients(p.n_fft, p.taps, window="hamming"))
+    im[1::p.taps] = -32768  # no int8 high limb for its negation
+    re[::p.taps] = 0
+    return [small, rnd(rng, n), sc.pack(re, im), small]
+
+
+def weight_sets(p, rng):
+    """Steering weights (int32 beam sums), full-range random weights
+    (limb-split sums) and weaker steering weights."""
+    return [sc.steering_weights(p.n_chan, p.n_beams), rnd(rng, p.n_chan * p.n_beams),
+            sc.steering_weights(p.n_chan, p.n_beams, gain=0.5)]

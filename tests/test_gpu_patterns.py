@@ -24,16 +24,21 @@ def _batch_inputs(n, torch, log2_max=14):
     return ps, cfgs, coeffs, ws, xs, devs
 
 
-def test_batch_matches_standalone_chains(gpulib):
+def test_batch_matches_oracle(gpulib, port):
+    # 16 scenarios of uneven geometry (channels 4..64, FFT 16..1024, taps
+    # 4..16, 2^12..2^14 samples per channel): every batched scenario, in every
+    # run mode and after autotuning, equals the CPU oracle's chain on the same
+    # input, bit for bit
     torch = pytest.importorskip("torch")
-    ps, cfgs, coeffs, ws, xs, devs = _batch_inputs(12, torch)
+    ps, cfgs, coeffs, ws, xs, devs = _batch_inputs(16, torch)
     ptrs = [d.data_ptr() for d in devs]
     ns = [p.cpi_samples for p in ps]
     b = Batch(cfgs, coeffs, ws, n_streams=4, use_graph=True)
     want = []
     for i, p in enumerate(ps):
-        r = gc.Chain(cfgs[i], coeffs[i], ws[i]).process(xs[i])
-        want.append(r)
+        px, py = sc.pair_table(p)
+        want.append(port.chain(cfgs[i], coeffs[i], ws[i], px, py).process(xs[i], taps=False,
+                                                                           threads=8))
     n_pairs = [gc.lib().rd_cov_pairs(gc.C.byref(c)) for c in cfgs]
     for mode in ("eager-first", "graph", "graph-again", "sequential"):
         b.run(ptrs, ns, sequential=(mode == "sequential"))
@@ -45,6 +50,9 @@ def test_batch_matches_standalone_chains(gpulib):
     b.run(ptrs, ns)
     for i, p in enumerate(ps):
         assert diff(b.fetch(i, p.frames_per_cpi, n_pairs[i]), want[i], CHAIN_KEYS) == [], i
+    # the scenarios cover every FFT size and channel count of the workload
+    assert {p.n_fft for p in ps} == {16, 64, 256, 1024}
+    assert {p.n_chan for p in ps} == {4, 16, 32, 64}
     b.close()
 
 
@@ -97,6 +105,57 @@ def test_serving_results_equal_alone(gpulib):
             assert diff(done[(s, k)], alone, CHAIN_KEYS) == [], (s, k)
     info = srv.info()
     assert info["streams"] == len(streams) and info["inflight"] == 0
+    srv.close()
+
+
+def test_serving_full_tensor_vs_oracle(gpulib, port):
+    # a mix with a full-scale stream in the tensor form (64 channels, 1024
+    # bins, 64 beams, 2080 pairs; its 8-frame covariance windows close every
+    # second request): every served request equals the CPU oracle's chain fed
+    # the same request sequence, bit for bit
+    mix = [("tiny", abi.RD_FORM_CUDA_CORE, {}), ("full", abi.RD_FORM_TENSOR, {"cov_window": 8}),
+           ("medium", abi.RD_FORM_TENSOR, {}), ("ref_tiny", abi.RD_FORM_CUDA_CORE, {}),
+           ("full", abi.RD_FORM_CUDA_CORE, {"cov_window": 4})]
+    srv = Server(hbm_budget=6 << 30, max_inflight=3, queue_cap=32, max_chan=64,
+                 max_request_samples=4096)
+    streams, ids = [], []
+    for name, form, over in mix:
+        p = sc.preset(name, **over)
+        cfg = sc.make_config(p, max_frames=64, form=form)
+        co, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+        st, sid = srv.open(cfg, co, w, pairs=sc.pair_table(p))
+        assert st == abi.RD_OK, gc.lib().rd_last_error()
+        streams.append((p, cfg, co, w))
+        ids.append(sid)
+    n_req = 4
+    reqs, done = {}, {}
+    pending = [(s, k) for k in range(n_req) for s in range(len(streams))]
+    while pending:
+        s, k = pending[0]
+        p = streams[s][0]
+        x = sc.adc(p, 4096, start=k * 4096, seed=p.seed + 11 * s)
+        st, rid = srv.submit(ids[s], x)
+        if st == abi.RD_EAGAIN:
+            srv.poll()
+            continue
+        assert st == abi.RD_OK
+        reqs[rid] = (s, k)
+        pending.pop(0)
+    while len(done) < len(reqs):
+        for c in srv.poll():
+            assert c["status"] == abi.RD_OK
+            s, k = reqs[c["req_id"]]
+            done[(s, k)] = srv.take(c["req_id"], ids[s], 4096 // streams[s][0].n_fft)
+    windows = 0
+    for s, (p, cfg, co, w) in enumerate(streams):
+        px, py = sc.pair_table(p)
+        o = port.chain(cfg, co, w, px, py)
+        for k in range(n_req):
+            x = sc.adc(p, 4096, start=k * 4096, seed=p.seed + 11 * s)
+            want = o.process(x, taps=False, threads=8)
+            assert diff(done[(s, k)], want, CHAIN_KEYS) == [], (s, k)
+            windows += len(want["cov_windows"]) if p.n_fft == 1024 else 0
+    assert windows >= 4  # the full-scale streams closed windows
     srv.close()
 
 

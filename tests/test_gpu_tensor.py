@@ -131,6 +131,39 @@ def test_full_cpi_vs_oracle_both_forms(gpulib, port):
         g.close()
 
 
+def test_full_bench_step_vs_oracle(gpulib, port):
+    # the full workload at the bench's launch size: 2 CPIs of 2^20 samples on
+    # each of 64 channels (2048 frames of 1024 bins, 64 beams, eight 256-frame
+    # windows of 2080 pairs, 512-bit packets) in 1024-frame launches, both
+    # forms, through the host-buffer call into page-locked result buffers (the
+    # bench's end-to-end path), bit-exact against the oracle on the same input
+    import os
+
+    torch = pytest.importorskip("torch")
+    p = sc.preset("full")
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    x = sc.adc(p, 2 * p.cpi_samples)
+    frames = 2 * p.frames_per_cpi
+    cap = frames * p.n_beams * (2 + p.n_fft // 16)
+    o = port.chain(sc.make_config(p, max_frames=1024), coeff, w, px, py)
+    ro = o.process(x, taps=False, threads=os.cpu_count() or 1, cap_events=cap)
+    assert len(ro["cov_windows"]) == 8 and len(ro["events"]) > frames * p.n_beams
+
+    def pinned(shape, dtype):
+        dt = np.dtype(dtype)
+        k = int(np.prod(shape)) * dt.itemsize
+        return torch.empty(max(k, 1), dtype=torch.uint8, pin_memory=True).numpy()[:k] \
+            .view(dt).reshape(shape)
+
+    for form in (abi.RD_FORM_CUDA_CORE, TC):
+        g = gc.Chain(sc.make_config(p, max_frames=1024, form=form), coeff, w, (px, py))
+        rg = g.process(x, cap_events=cap, alloc=pinned)
+        assert diff(rg, ro) == [], form
+        assert diff_stats(g.stats(), o.stats()) == [], form
+        g.close()
+
+
 @pytest.mark.parametrize("seed", range(3))
 def test_chain_tensor_equals_cuda_core(gpulib, seed):
     # random weights over the full int16 range and a medium CPI: both forms

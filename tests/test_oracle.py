@@ -6,7 +6,8 @@ import numpy as np
 import pytest
 
 from conftest import load_chain_fixture
-from helpers import CHAIN_KEYS, TAP_KEYS, cfg_from_fixture, diff, diff_stats, fixture_stats
+from helpers import (CHAIN_KEYS, TAP_KEYS, banks, cfg_from_fixture, diff, diff_stats,
+                     fixture_stats, weight_sets)
 from rdgb import abi, scenario as sc
 from rdgb.twiddle import DIGEST, TWIDDLES
 
@@ -201,3 +202,32 @@ def test_port_matches_reference_modes(port, refo, case):
     assert diff(fa, fb, ("cov_windows", "cov_acc")) == [], case
     if case == "medium_saturating_block":
         assert a.stats()["cov_sat_steps"] > 0
+
+
+@pytest.mark.parametrize("name", ["tiny", "medium"])
+def test_port_matches_reference_bank_swaps(port, refo, name):
+    # mid-stream coefficient and weight swaps (pfb_model.hpp:225-233,
+    # beamformer_model.hpp:271-279) between calls of uneven length, inside
+    # covariance windows: the restatement against the reference's own models
+    rng = np.random.default_rng(len(name))
+    p = sc.preset(name, cov_window=6)
+    cfg = sc.make_config(p, max_frames=7)
+    px, py = sc.pair_table(p)
+    cb, ws = banks(p, rng), weight_sets(p, rng)
+    a = port.chain(cfg, cb[0], ws[0], px, py)
+    b = refo.chain(cfg, cb[0], ws[0], px, py)
+    start = 0
+    for k, (nf, c, w) in enumerate([(4, None, None), (9, 1, None), (2, None, 1), (9, 2, None),
+                                    (5, 3, 2), (1, 1, 0), (6, None, None)]):
+        for ch in (a, b):
+            if c is not None:
+                ch.set_coeff(cb[c])
+            if w is not None:
+                ch.set_weights(ws[w])
+        x = sc.adc(p, nf * p.n_fft, start=start * p.n_fft)
+        ra, rb = a.process(x, taps=True, threads=4), b.process(x, taps=True)
+        assert diff(ra, rb, CHAIN_KEYS + TAP_KEYS) == [], (name, k)
+        start += nf
+    assert diff_stats(a.stats(), b.stats()) == []
+    fa, fb = a.flush_cov(), b.flush_cov()
+    assert diff(fa, fb, ("cov_windows", "cov_acc")) == []
