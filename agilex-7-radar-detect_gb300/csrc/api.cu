@@ -192,7 +192,9 @@ struct rd_chain {
   uint32_t pfb_dp = 0;
   uint32_t x_safe = 0;      // beamformer: |x| bound for exact int32 sums
   uint32_t pfb32 = 0;       // 1: int32 PFB accumulation is exact for this bank
-  DevBuf<uint32_t> w_frag;  // tensor form: mma fragments of the limb-split weights
+  DevBuf<uint32_t> w_frag;  // warp-level tensor form: mma fragments of the limb-split weights
+  DevBuf<uint32_t> w_t5;    // tcgen05 form: the canonical-layout weight operand
+  bool t5 = false;          // the beamformer runs on tcgen05
   // tensor form of the exact covariance: plan, unit lists and pair map
   CovTcHost cov_tc{};
   bool cov_tc_ok = false;
@@ -350,7 +352,7 @@ rd_status rd_config_validate(const rd_config* c) {
     if (c->cov_window > 65535) return fail(RD_EINVAL, "cov_window must fit 16 bits");
   }
   if (c->max_frames < 1 || c->max_frames > 65536) return fail(RD_EINVAL, "max_frames 1..65536");
-  if (c->form > RD_FORM_TENSOR) return fail(RD_EINVAL, "bad form");
+  if (c->form > RD_FORM_TENSOR_WARP) return fail(RD_EINVAL, "bad form");
   if (c->form != RD_FORM_CUDA_CORE && c->n_chan > RD_TC_MAX_CHAN)
     return fail(RD_EINVAL, "the tensor form takes at most %u channels", RD_TC_MAX_CHAN);
   if (c->vc > 3 || c->src_id > 31 || c->dest > 15) return fail(RD_EINVAL, "packet header field out of range");
@@ -401,6 +403,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
   ch->R = F + c.hist_frames;
   ch->launch_frames = F;
   ch->safe_in = front_safe_input(N, c.spc, c.scale_sched);
+  ch->t5 = c.form == RD_FORM_TENSOR && beam_t5_ok(C, B);
   auto bad = [&](cudaError_t e) {
     if (e == cudaSuccess) return false;
     fail(e == cudaErrorMemoryAllocation ? RD_ENOMEM : RD_EDEVICE, "allocation failed: %s",
@@ -415,7 +418,9 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
       bad(ch->coeff_dp.ensure((size_t)T * N)) ||
       bad(ch->weights.ensure((size_t)B * C)) ||
       bad(ch->w_limbs.ensure((size_t)B * C)) ||
-      (c.form == RD_FORM_TENSOR && bad(ch->w_frag.ensure(beam_tc_fragment_words(C, B)))) ||
+      (c.form != RD_FORM_CUDA_CORE && !ch->t5 &&
+       bad(ch->w_frag.ensure(beam_tc_fragment_words(C, B)))) ||
+      (ch->t5 && bad(ch->w_t5.ensure(beam_t5_operand_words(C, B)))) ||
       bad(ch->tail[0].ensure((size_t)C * D * N)) || bad(ch->tail[1].ensure((size_t)C * D * N)) ||
       bad(ch->ring.ensure((size_t)ch->R * N * C)) || bad(ch->power.ensure((size_t)F * B * N)) ||
       bad(ch->counts.ensure((size_t)F * B)) || bad(ch->detsup.ensure((size_t)F * B)) ||
@@ -431,8 +436,9 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
   cudaMemset(ch->coeff_dp.p, 0, (size_t)T * N * sizeof(uint2));
   cudaMemset(ch->weights.p, 0, (size_t)B * C * 4);
   cudaMemset(ch->w_limbs.p, 0, (size_t)B * C * sizeof(int4));
-  if (c.form == RD_FORM_TENSOR)
+  if (c.form != RD_FORM_CUDA_CORE && !ch->t5)
     cudaMemset(ch->w_frag.p, 0, (size_t)beam_tc_fragment_words(C, B) * 4);
+  if (ch->t5) cudaMemset(ch->w_t5.p, 0, (size_t)beam_t5_operand_words(C, B) * 4);
   cudaMemset(ch->tail[0].p, 0, (size_t)C * D * N * 4);
   cudaMemset(ch->tail[1].p, 0, (size_t)C * D * N * 4);
   cudaMemset(ch->ring.p, 0, (size_t)ch->R * N * C * 4);
@@ -487,7 +493,7 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
 void rd_chain_destroy(rd_chain* ch) {
   if (!ch) return;
   if (ch->stream) cudaStreamSynchronize(ch->stream);
-  ch->coeff_t.release(); ch->coeff2.release(); ch->coeff_dp.release(); ch->weights.release(); ch->w_limbs.release(); ch->w_frag.release(); ch->tail[0].release(); ch->tail[1].release();
+  ch->coeff_t.release(); ch->coeff2.release(); ch->coeff_dp.release(); ch->weights.release(); ch->w_limbs.release(); ch->w_frag.release(); ch->w_t5.release(); ch->tail[0].release(); ch->tail[1].release();
   ch->ring.release(); ch->power.release(); ch->beams_bn.release(); ch->stage.release();
   ch->stage2.release();
   if (ch->copy_stream) cudaStreamSynchronize(ch->copy_stream);
@@ -589,7 +595,12 @@ rd_status rd_chain_set_weights(rd_chain* ch, const rd_cplx16* w) {
   CK(cudaMemcpyAsync(ch->w_limbs.p, limbs.data(), n * sizeof(int4), cudaMemcpyHostToDevice,
                      ch->stream));
   std::vector<uint32_t> frag;
-  if (ch->cfg.form == RD_FORM_TENSOR) {
+  if (ch->t5) {
+    frag.resize(beam_t5_operand_words(ch->cfg.n_chan, ch->cfg.n_beams));
+    beam_t5_operand(w, ch->cfg.n_chan, ch->cfg.n_beams, frag.data());
+    CK(cudaMemcpyAsync(ch->w_t5.p, frag.data(), frag.size() * 4, cudaMemcpyHostToDevice,
+                       ch->stream));
+  } else if (ch->cfg.form != RD_FORM_CUDA_CORE) {
     frag.resize(beam_tc_fragment_words(ch->cfg.n_chan, ch->cfg.n_beams));
     beam_tc_fragments(w, ch->cfg.n_chan, ch->cfg.n_beams, frag.data());
     CK(cudaMemcpyAsync(ch->w_frag.p, frag.data(), frag.size() * 4, cudaMemcpyHostToDevice,
@@ -666,6 +677,7 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   bp.x_safe = ch->x_safe;
   bp.cshift = (C & (C - 1u)) == 0u ? __builtin_ctz(C) : -1;
   bp.w_frag = ch->w_frag.p;
+  bp.w_t5 = ch->w_t5.p;
   bp.power = ch->power.p;
   bp.beams_bn = ch->beams_bn.p;
   bp.F = F;
@@ -675,7 +687,9 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   bp.stats = st;
   {
     KTimer t(ch, KT_BEAM);
-    if (c.form == RD_FORM_TENSOR)
+    if (ch->t5)
+      launch_beam_t5(bp, s);
+    else if (c.form != RD_FORM_CUDA_CORE)
       launch_beam_tc(bp, s);
     else
       launch_beam(bp, s);
@@ -876,6 +890,8 @@ rd_status rd_chain_fetch(rd_chain* ch, rd_output* out) {
   if (ch->out_stream) CK(cudaStreamSynchronize(ch->out_stream));
   DevStats ds;
   CK(cudaMemcpy(&ds, ch->stats.p, sizeof(ds), cudaMemcpyDeviceToHost));
+  if (ds.dev_timeout)
+    return fail(RD_ETIMEOUT, "a bounded wait inside a tensor-core kernel gave up; results invalid");
   const uint64_t n_ev = ds.scan_scratch[0];
   const uint32_t nfl = rd_detection_flits(c.packet_w), words = rd_flit_words(c.packet_w);
   bool trunc = n_ev > ch->call_cap_events;
@@ -1248,7 +1264,9 @@ uint64_t rd_chain_footprint(const rd_config* cfg, uint64_t frames_per_call) {
   const uint64_t R = F + c.hist_frames, D = T > 1 ? T - 1 : 1;
   uint64_t b = 0;
   b += T * N * 4 + B * C * (4 + 16);                         // coefficients, weights
-  if (c.form == RD_FORM_TENSOR) b += (uint64_t)beam_tc_fragment_words(c.n_chan, c.n_beams) * 4;
+  if (c.form != RD_FORM_CUDA_CORE)
+    b += (uint64_t)std::max(beam_tc_fragment_words(c.n_chan, c.n_beams),
+                            beam_t5_operand_words(c.n_chan, c.n_beams)) * 4;
   b += 2 * C * D * N * 4 + R * N * C * 4;                    // delay lines, spectrum ring
   b += F * B * N * 4 + F * B * (4 + 8 + 8) + F * B * ((N + 31) / 32) * 4;  // power, CFAR
   b += sizeof(DevStats) + 5 * N * 4;
@@ -1256,7 +1274,7 @@ uint64_t rd_chain_footprint(const rd_config* cfg, uint64_t frames_per_call) {
     const uint64_t S = c.cov_source == RD_COV_CHANNEL ? C : B;
     const uint64_t P = rd_cov_pairs(cfg);
     b += P * 8 + N * P * (2 * 2 * 8 + 4 + 8);                // pairs, state
-    if (c.form == RD_FORM_TENSOR) b += S * S * 4 + 4096;      // pair map, unit lists
+    if (c.form != RD_FORM_CUDA_CORE) b += S * S * 4 + 4096;   // pair map, unit lists
     if (c.cov_source == RD_COV_BEAM) b += F * N * B * 4;
     const uint64_t wl = c.cov_window ? c.cov_window : 1;
     b += (frames_per_call / wl + 1) * (N * P * 16 + 4);       // closed windows of a call
@@ -1272,6 +1290,8 @@ rd_status rd_chain_stats(const rd_chain* ch, rd_stats* st) {
   CK(cudaStreamSynchronize(ch->stream));
   DevStats ds;
   CK(cudaMemcpy(&ds, ch->stats.p, sizeof(ds), cudaMemcpyDeviceToHost));
+  if (ds.dev_timeout)
+    return fail(RD_ETIMEOUT, "a bounded wait inside a tensor-core kernel gave up");
   *st = ch->host_st;
   st->frames = ch->frame;
   st->pfb_flags = ds.pfb_flags;
@@ -1415,7 +1435,7 @@ rd_status rd_fft_run(uint32_t n_fft, uint32_t spc, uint32_t sched, int reorder,
 
 rd_status rd_bf_run(uint32_t n_ant, uint32_t n_beams, const rd_cplx16* w, const rd_cplx16* x,
                     uint64_t n_vec, rd_cplx16* y, int64_t* acc, uint8_t* flags, uint32_t form) {
-  if (!w || !x || !y || n_ant == 0 || n_beams == 0 || form > RD_FORM_TENSOR)
+  if (!w || !x || !y || n_ant == 0 || n_beams == 0 || form > RD_FORM_TENSOR_WARP)
     return fail(RD_EINVAL, "bad argument");
   if (form != RD_FORM_CUDA_CORE && n_ant > RD_TC_MAX_CHAN)
     return fail(RD_EINVAL, "the tensor form takes at most %u antennas", RD_TC_MAX_CHAN);
@@ -1424,17 +1444,25 @@ rd_status rd_bf_run(uint32_t n_ant, uint32_t n_beams, const rd_cplx16* w, const 
   uint32_t *dw, *dx, *dy;
   long long* dacc = nullptr;
   uint8_t* df = nullptr;
+  DevStats* dst;
   CK(sc.alloc(&dw, (size_t)n_ant * n_beams));
   CK(sc.alloc(&dx, n_vec * n_ant));
   CK(sc.alloc(&dy, n_vec * n_beams));
+  CK(sc.alloc(&dst, 1));
   if (acc) CK(sc.alloc(&dacc, n_vec * n_beams * 2));
   if (flags) CK(sc.alloc(&df, n_vec * n_beams));
   CK(cudaMemcpy(dw, w, (size_t)n_ant * n_beams * 4, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(dx, x, n_vec * n_ant * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemset(dst, 0, sizeof(DevStats)));
   if (form != RD_FORM_CUDA_CORE) {
     // the vectors as a one-bin "ring" of n_vec frames, in launches of < 2^31 rows
-    std::vector<uint32_t> frag(beam_tc_fragment_words(n_ant, n_beams));
-    beam_tc_fragments(w, n_ant, n_beams, frag.data());
+    const bool t5 = form == RD_FORM_TENSOR && beam_t5_ok(n_ant, n_beams);
+    std::vector<uint32_t> frag(t5 ? beam_t5_operand_words(n_ant, n_beams)
+                                  : beam_tc_fragment_words(n_ant, n_beams));
+    if (t5)
+      beam_t5_operand(w, n_ant, n_beams, frag.data());
+    else
+      beam_tc_fragments(w, n_ant, n_beams, frag.data());
     uint32_t* dfrag;
     CK(sc.alloc(&dfrag, frag.size()));
     CK(cudaMemcpy(dfrag, frag.data(), frag.size() * 4, cudaMemcpyHostToDevice));
@@ -1445,6 +1473,7 @@ rd_status rd_bf_run(uint32_t n_ant, uint32_t n_beams, const rd_cplx16* w, const 
       bp.ring = dx + v0 * n_ant;
       bp.ring_frames = F;
       bp.w_frag = dfrag;
+      bp.w_t5 = dfrag;
       bp.y_rows = dy + v0 * n_beams;
       bp.acc_rows = dacc ? dacc + v0 * n_beams * 2 : nullptr;
       bp.flag_rows = df ? df + v0 * n_beams : nullptr;
@@ -1452,12 +1481,19 @@ rd_status rd_bf_run(uint32_t n_ant, uint32_t n_beams, const rd_cplx16* w, const 
       bp.C = n_ant;
       bp.N = 1;
       bp.B = n_beams;
-      launch_beam_tc(bp, 0);
+      bp.stats = dst;
+      if (t5)
+        launch_beam_t5(bp, 0);
+      else
+        launch_beam_tc(bp, 0);
     }
   } else {
     launch_bf_block(n_ant, n_beams, dw, dx, n_vec, dy, dacc, df, 0);
   }
   CK(cudaGetLastError());
+  DevStats hs;
+  CK(cudaMemcpy(&hs, dst, sizeof(hs), cudaMemcpyDeviceToHost));
+  if (hs.dev_timeout) return fail(RD_ETIMEOUT, "a bounded wait inside the tensor-core kernel gave up");
   CK(cudaMemcpy(y, dy, n_vec * n_beams * 4, cudaMemcpyDeviceToHost));
   if (acc) CK(cudaMemcpy(acc, dacc, n_vec * n_beams * 16, cudaMemcpyDeviceToHost));
   if (flags) CK(cudaMemcpy(flags, df, n_vec * n_beams, cudaMemcpyDeviceToHost));

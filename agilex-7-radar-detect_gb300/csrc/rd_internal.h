@@ -46,6 +46,7 @@ struct DevStats {
   unsigned long long events_total;   // events emitted so far (packet seq base)
   unsigned long long events_call;    // events of the current call
   unsigned long long scan_scratch[4];
+  unsigned dev_timeout;              // a bounded device wait gave up (tcgen05 kernels)
 };
 
 // ---- front end: PFB + FFT + corner turn into the spectrum ring ------------
@@ -109,7 +110,8 @@ struct BeamParams {
   uint64_t g0;
   const uint32_t* weights;  // [B][C]
   const int4* w_limbs;      // [B][C] {wh.re, wh.im, wl.re, wl.im}, w = 256 wh + wl
-  const uint32_t* w_frag;   // tensor form: beam_tc_fragments() of the weights
+  const uint32_t* w_frag;   // warp-level tensor form: beam_tc_fragments() of the weights
+  const uint32_t* w_t5;     // tcgen05 form: beam_t5_operand() of the weights
   uint32_t* power;          // [F][B][N] (or null)
   uint32_t* beams_bn;       // [F][N][B] beam samples (null unless needed)
   uint32_t* y_rows;         // per-block entry: [rows][B] y, acc, flags (or null)
@@ -126,6 +128,12 @@ void launch_beam_tc(const BeamParams& p, cudaStream_t s);
 uint32_t beam_tc_fragment_words(uint32_t C, uint32_t B);
 size_t beam_tc_smem(uint32_t C);
 void beam_tc_fragments(const uint32_t* w, uint32_t C, uint32_t B, uint32_t* out);
+// tcgen05 form (k_beam_t5.cu): whether the geometry fits it (C <= 64 and the
+// shared-memory plan), the weight operand image and the launch.
+bool beam_t5_ok(uint32_t C, uint32_t B);
+uint32_t beam_t5_operand_words(uint32_t C, uint32_t B);
+void beam_t5_operand(const uint32_t* w, uint32_t C, uint32_t B, uint32_t* out);
+void launch_beam_t5(const BeamParams& p, cudaStream_t s);
 
 struct CovParams {
   const uint32_t* ring;     // channel source: [R][N][C]

@@ -26,6 +26,19 @@ __device__ __forceinline__ void limb_words(uint32_t v, uint32_t& hi, uint32_t& l
   lo = hsub2((v & 0x00FF00FFu) | 0x64006400u, 0x64006400u);
 }
 
+// Balanced 8-bit limbs of v = {im, re}: x = 256 xh + xl with xl the
+// sign-extended low byte of x, in [-128, 127], and xh = (x >> 8) + bit 7 of
+// x, in [-128, 128]; every limb and limb product is then at most 2^7 and 2^14
+// in magnitude. As fp16 pairs, the real part in the low half: xl + 128 is the
+// low byte with bit 7 flipped, xh + 128 is the high byte with bit 7 flipped
+// plus bit 7 of x (at most 256, so no carry crosses into the other half);
+// placed under the exponent of 1024 and the bias 1024 + 128 subtracted.
+__device__ __forceinline__ void limb_words_bal(uint32_t v, uint32_t& hi, uint32_t& lo) {
+  const uint32_t t = (((v >> 8) & 0x00FF00FFu) ^ 0x00800080u) + ((v >> 7) & 0x00010001u);
+  hi = hsub2(t | 0x64006400u, 0x64806480u);
+  lo = hsub2(((v ^ 0x00800080u) & 0x00FF00FFu) | 0x64006400u, 0x64806480u);
+}
+
 // (-b, a) from the fp16 pair (a, b): the halves swapped, the new low half negated
 __device__ __forceinline__ uint32_t negswap(uint32_t w) {
   return __byte_perm(w, 0u, 0x1032) ^ 0x00008000u;

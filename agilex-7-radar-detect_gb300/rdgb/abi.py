@@ -25,7 +25,7 @@ RD_CFAR_EVENTS, RD_CFAR_DENSE = 0, 1
 RD_EV_DETECT, RD_EV_BIN, RD_EV_SUPPRESSED, RD_EV_SUMMARY = 0, 1, 2, 3
 RD_COV_OFF, RD_COV_CHANNEL, RD_COV_BEAM = 0, 1, 2
 RD_COV_BLOCK, RD_COV_EXP = 0, 1
-RD_FORM_CUDA_CORE, RD_FORM_TENSOR = 0, 1
+RD_FORM_CUDA_CORE, RD_FORM_TENSOR, RD_FORM_TENSOR_WARP = 0, 1, 2
 RD_TC_MAX_CHAN = 128
 RD_STATIC_CFAR_MAX_FRAMES, RD_STATIC_CFAR_MAX_CELLS = 4096, 1024
 

@@ -154,15 +154,23 @@ def kernel_bytes(cfg, name: str, frames: int) -> float:
 
 
 def kernel_tensor_flops(cfg, name: str, frames: int, n_pairs: int) -> float:
-    """fp16 tensor-core flops of one launch of a limb-split contraction: the
-    beamformer's GEMM has (frame, bin) rows, 6 class columns per beam and 4
-    limb parts per channel of depth; the covariance's per-bin Gram matrix has
-    the channels as rows, 6 class columns per channel and 4 parts per frame of
-    depth, over the 16-channel tiles that hold a requested pair (the whole
-    triangle of tiles for the full table)."""
+    """fp16 tensor-core flops of one launch of a limb-split contraction. The
+    tcgen05 beamformer (up to 64 channels) runs four GEMMs per 128-row tile
+    (high x high, low x low and the two cross terms) of (frame, bin) rows,
+    2 columns per beam (re, im; beams padded to groups of up to 32) and 2
+    parts per channel of depth (padded to 16); the warp-level one has 6
+    class columns per beam and 4 limb parts per channel. The covariance's
+    per-bin Gram matrix has the channels as rows, 6 class columns per channel
+    and 4 parts per frame of depth, over the 16-channel tiles that hold a
+    requested pair (the whole triangle of tiles for the full table)."""
     N, C, B = cfg.n_fft, cfg.n_chan, cfg.n_beams
     rows = frames * N
     if name == "k_beam":
+        if cfg.form == 1 and C <= 64:
+            nb = min(32, -(-B // 8) * 8)
+            cols = 2 * nb * -(-B // nb)
+            depth = -(-2 * C // 16) * 16
+            return 2.0 * rows * 4 * cols * depth
         return 2.0 * rows * (6 * B) * (4 * C)
     if name == "k_cov":
         t = -(-C // 16)

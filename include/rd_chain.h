@@ -55,14 +55,17 @@ enum { RD_EV_DETECT = 0, RD_EV_BIN = 1, RD_EV_SUPPRESSED = 2, RD_EV_SUMMARY = 3 
 enum { RD_COV_OFF = 0, RD_COV_CHANNEL = 1, RD_COV_BEAM = 2 };
 enum { RD_COV_BLOCK = 0, RD_COV_EXP = 1 };
 
-/* Form of the beamforming and covariance contractions. Both are bit-exact.
+/* Form of the beamforming and covariance contractions. All are bit-exact.
  * RD_FORM_CUDA_CORE: integer multiply-accumulate on the CUDA cores.
  * RD_FORM_TENSOR: the int16 operands split into 8-bit limbs held exactly in
- * fp16, multiplied on the tensor cores (warp-level mma) with fp32
- * accumulation whose every partial sum is an integer below 2^24 (hence
- * n_chan <= RD_TC_MAX_CHAN), recombined in int64; the covariance in this
- * form for its exact block mode. */
-enum { RD_FORM_CUDA_CORE = 0, RD_FORM_TENSOR = 1 };
+ * fp16, multiplied on the tensor cores with fp32 accumulation whose every
+ * partial sum is an integer below 2^24 (hence n_chan <= RD_TC_MAX_CHAN),
+ * recombined in int64; the covariance in this form for its exact block mode.
+ * The beamformer runs on the 5th-generation tensor cores (tcgen05, TMEM
+ * accumulators) for up to 64 channels, else as RD_FORM_TENSOR_WARP.
+ * RD_FORM_TENSOR_WARP: the same limb split on the warp-level mma
+ * instruction. */
+enum { RD_FORM_CUDA_CORE = 0, RD_FORM_TENSOR = 1, RD_FORM_TENSOR_WARP = 2 };
 #define RD_TC_MAX_CHAN 128u
 
 /* Stream geometry and block configuration. Zero-initialise, then fill;

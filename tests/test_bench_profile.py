@@ -51,8 +51,9 @@ def test_bench_defaults_full_scale():
     assert (a.workload, a.form, a.max_frames, a.gpus) == ("full", "tensor", 1024, 1)
     p = sc.preset("full")
     cfg = sc.make_config(p, max_frames=1024, form=1)
-    # the limb GEMMs of one launch: 1024 x 1024 rows x 384 columns x 256 deep
-    assert bench.kernel_tensor_flops(cfg, "k_beam", 1024, 2080) == 2.0 * 1024 * 1024 * 384 * 256
+    # the tcgen05 beamformer's four limb GEMMs of one launch: 1024 x 1024 rows
+    # x 128 columns (64 beams, re and im) x 128 deep (64 channels, re and im)
+    assert bench.kernel_tensor_flops(cfg, "k_beam", 1024, 2080) == 2.0 * 1024 * 1024 * 4 * 128 * 128
     # the covariance's Gram tiles: 10 of the 16 16x16 channel tiles hold a pair
     assert bench.kernel_tensor_flops(cfg, "k_cov", 1024, 2080) == \
         2.0 * 1024 * 1024 * 4 * 10 * 16 * 16 * 6

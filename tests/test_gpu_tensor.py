@@ -19,7 +19,7 @@ def rnd(rng, n):
     return rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
 
 
-FORMS = [abi.RD_FORM_TENSOR]
+FORMS = [abi.RD_FORM_TENSOR, abi.RD_FORM_TENSOR_WARP]
 
 
 @pytest.mark.parametrize("form", FORMS)
