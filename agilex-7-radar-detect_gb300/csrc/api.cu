@@ -736,10 +736,14 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
     cp.stats = st;
     {
       KTimer t(ch, KT_COV);
-      if (ch->cov_tc_ok && cp.exact && !cp.exp_mode)
-        launch_cov_tc(cp, ch->cov_tc.plan, s);
-      else
+      if (ch->cov_tc_ok && cp.exact && !cp.exp_mode) {
+        if (c.form == RD_FORM_TENSOR && cov_t5_ok(ch->S, wl))
+          launch_cov_t5(cp, ch->cov_tc.plan.pq, s);
+        else
+          launch_cov_tc(cp, ch->cov_tc.plan, s);
+      } else {
         launch_cov(cp, s);
+      }
     }
     ch->acc_cur ^= 1u;
     ch->launches++;

@@ -181,6 +181,10 @@ bool cov_tc_plan(uint32_t S, const uint32_t* px, const uint32_t* py, uint32_t P,
                  CovTcHost* out);
 size_t cov_tc_smem(const CovTcPlan& t);
 void launch_cov_tc(const CovParams& p, const CovTcPlan& t, cudaStream_t s);
+// tcgen05 form of the exact block covariance (k_cov_t5.cu): for up to 64
+// source channels and windows of 64 to 256 frames; pq is the plan's pair map.
+bool cov_t5_ok(uint32_t S, uint32_t wl);
+void launch_cov_t5(const CovParams& p, const int32_t* pq, cudaStream_t s);
 
 // Detections a CFAR frame keeps from its decision for the emit pass; a frame
 // with more (DENSE output, clutter) re-decides its events there.

@@ -143,7 +143,8 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t cols) {
 
 // Warp-collective: three runs of 16 consecutive 32-bit TMEM columns of this
 // thread's lane (the warp's lane quadrant), and the wait for them in the same
-// statement, so no use of the registers can move above the wait.
+// statement, so no use of the registers can move above the wait. The column
+// addresses must be the same in every lane of the warp: the load uses one.
 __device__ __forceinline__ void tmem_ld3x16(uint32_t ta, uint32_t tb, uint32_t tc,
                                             uint32_t (&a)[16], uint32_t (&b)[16],
                                             uint32_t (&c)[16]) {
