@@ -745,6 +745,7 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
         launch_cov(cp, s);
       }
     }
+    CK(cudaGetLastError());  // a rejected launch (resources, configuration)
     ch->acc_cur ^= 1u;
     ch->launches++;
     // window headers, known on the host (covar_model.hpp:229-235)

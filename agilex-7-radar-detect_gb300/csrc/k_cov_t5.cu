@@ -27,17 +27,20 @@
 // 4 such terms a frame, so over a window segment of at most 256 frames every
 // partial sum is an integer of magnitude <= 2^24: exact in the fp32
 // accumulators. The epilogue recombines 2^16 D16 + 2^8 D8 + D0 in int64 - the
-// integer the Integrator adds - then adds the carried-in sum (first segment
-// of the launch), writes each window that closes, and the carried-out sum.
+// integer the Integrator adds, each class read off its fp32 value with adds
+// (exact_int24) - then adds the carried-in sum (first segment of the
+// launch), writes each window that closes, and the carried-out sum.
 //
-// Kernel: persistent, one CTA per SM, warp-specialised (384 threads): warp 0
-// allocates TMEM and issues the MMAs; warps 1-7 stage 64-frame chunks of the
-// spectrum (double-buffered in shared memory, and in two register sets, so a
-// thread's loads of the next chunk are in flight while it converts this
-// one); warps 8-11 read the accumulators back (warp 8 + q: TMEM lanes 32q ..
-// 32q + 31 = A rows) and finish the sums. A work unit is
-// (window segment, bin group); its accumulators alternate between two TMEM
-// buffers. Every wait is bounded (DevStats::dev_timeout on a timeout).
+// Kernel: persistent, one CTA per SM, warp-specialised (544 threads): warp 0
+// allocates TMEM and issues the MMAs; warps 1-8 stage 64-frame chunks of the
+// spectrum (16-byte cp.async copies of 4 channels a frame into a ring of raw
+// stages, three chunks ahead, then converted into double-buffered operand
+// tiles); warps 9-16 read the accumulators
+// back (warp w: TMEM lanes 32 (w % 4) .. + 31 = A rows, half of the columns)
+// and finish the sums.
+// A work unit is (window segment, bin group); its accumulators alternate
+// between two TMEM buffers. Every wait is bounded (DevStats::dev_timeout on a
+// timeout).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -54,13 +57,19 @@ constexpr unsigned kRowsC = 128u;   // M: [U; V] rows
 constexpr unsigned kColsC = 64u;    // N: U rows
 constexpr unsigned kChunk = 64u;    // frames per staged chunk (K = 128)
 constexpr unsigned kKp = 2u * kChunk;
-constexpr unsigned kSboC = 16u * kKp;               // bytes per 8-row group
-constexpr unsigned kMatC = kRowsC * kKp * 2u;       // one limb matrix: 32 KB
-constexpr unsigned kProdC = 7u;                     // producer warps 1 .. 7
-constexpr unsigned kEpiC = 8u;                      // epilogue warps 8 .. 11
-constexpr unsigned kThreadsC = 384u;
-// items (row, 4-frame quad) of a chunk per producer thread
-constexpr unsigned kItemsC = (kColsC * (kChunk / 4u) + kProdC * 32u - 1u) / (kProdC * 32u);
+// bytes per 8-row group: the group's 16 core matrices (2 KB) and a 16-byte
+// skew, so that the 8 row groups a quarter-warp's stores touch (rows 4 g + j,
+// g = 0 .. 7) start in 8 different 16-byte bank slots
+constexpr unsigned kSboC = 16u * kKp + 16u;
+constexpr unsigned kMatC = 16u * kSboC;             // one limb matrix (128 rows)
+constexpr unsigned kProdC = 8u;                     // producer warps 1 .. 8
+constexpr unsigned kEpiC = 9u;                      // epilogue warps 9 .. 16
+constexpr unsigned kThreadsC = 544u;
+// a chunk's items: (4-row group g, 4-frame quad) = 16 x 16, one per producer
+constexpr unsigned kItemsC = 16u * (kChunk / 4u);
+static_assert(kItemsC == kProdC * 32u, "one item per producer thread");
+constexpr unsigned kStages = 4u;                    // chunks of raw words in flight
+constexpr unsigned kStageBytes = kItemsC * 4u * 16u;  // 16 KB: [frame e][item] uint4
 
 __host__ __device__ inline unsigned sp_of(unsigned S) {
   unsigned sp = 16u;
@@ -70,78 +79,96 @@ __host__ __device__ inline unsigned sp_of(unsigned S) {
 
 }  // namespace
 
-// One producer thread's items of one 64-frame chunk: item m is A row r
-// (bin bin0 + r / Sp, channel r % Sp) and 4-frame quad fq; consecutive threads
-// take consecutive rows (the 8 rows of a core matrix, and consecutive channels
-// in memory). Loads them into v (zero outside the chunk, the bins, the
-// channels).
-__device__ __forceinline__ void c5_load(const CovParams& p, unsigned pt, unsigned Sp, bool ok,
-                                        unsigned f0, unsigned hi, unsigned bin0,
-                                        uint32_t (&v)[kItemsC][4]) {
+// One producer thread's item of one 64-frame chunk: A rows 4 g .. 4 g + 3
+// (bin bin0 + 4 g / Sp, channels 4 g % Sp ..) over frames 4 fq .. 4 fq + 3,
+// g = pt % 16 and fq = pt / 16, so a warp's 16-byte copies of one frame cover
+// 64 consecutive rows (256 contiguous bytes when S = Sp). Copies frame
+// 4 fq + e of the 4 channels to stage word [e][pt] with cp.async, zero-filled
+// outside the chunk, the bins, the channels. vec: S is a multiple of 4 and the
+// source 16-byte aligned, so a group of 4 channels is whole and aligned.
+__device__ __forceinline__ void c5_issue(const CovParams& p, unsigned pt, unsigned Sp, bool vec,
+                                         unsigned f0, unsigned hi, unsigned bin0, uint32_t stage) {
   const uint32_t* src = p.src_beam ? p.beams_bn : p.ring;
+  const unsigned r0 = 4u * (pt & 15u), fq = pt >> 4;
+  const unsigned ch0 = r0 & (Sp - 1u), bin = bin0 + r0 / Sp;
+  const bool rok = ch0 < p.S && bin < p.N;
 #pragma unroll
-  for (unsigned m = 0; m < kItemsC; ++m) {
-    const unsigned it = pt + m * kProdC * 32u;
-    const unsigned r = it & (kColsC - 1u), fq = it / kColsC;
-    const unsigned ch = r & (Sp - 1u), bin = bin0 + r / Sp;
-    const bool rok = ok && fq < kChunk / 4u && ch < p.S && bin < p.N;
+  for (unsigned e = 0; e < 4u; ++e) {
+    const unsigned f = f0 + 4u * fq + e;
+    const bool fok = rok && f < hi;
+    const uint32_t* a = src;  // any valid address when nothing is read
+    if (fok) {
+      unsigned slot = p.src_beam ? f : p.ring_base + f;
+      if (!p.src_beam && slot >= p.ring_frames) slot -= p.ring_frames;
+      a = src + ((size_t)slot * p.N + bin) * p.S + ch0;
+    }
+    const uint32_t d = stage + (e * kItemsC + pt) * 16u;
+    if (vec) {
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(a),
+                   "r"(fok ? 16 : 0)
+                   : "memory");
+    } else {
 #pragma unroll
-    for (unsigned e = 0; e < 4u; ++e) {
-      const unsigned f = f0 + 4u * fq + e;
-      uint32_t x = 0u;
-      if (rok && f < hi) {
-        unsigned slot = p.src_beam ? f : p.ring_base + f;
-        if (!p.src_beam && slot >= p.ring_frames) slot -= p.ring_frames;
-        x = __ldg(src + ((size_t)slot * p.N + bin) * p.S + ch);
+      for (unsigned j = 0; j < 4u; ++j) {
+        const bool ok = fok && ch0 + j < p.S;
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d + 4u * j),
+                     "l"(ok ? a + j : src), "r"(ok ? 4 : 0)
+                     : "memory");
       }
-      v[m][e] = x;
     }
   }
 }
 
-// The same items as [U; V] balanced limb words into one chunk buffer: row r
-// (U) and row 64 + r (V) of the high- and low-limb matrices, K chunk fq
-// (frames 4 fq .. 4 fq + 3).
+// Channel j of the four frames as one 16-byte row of each limb matrix: row
+// r = 4 g + j (U) and 64 + r (V), K chunk fq (frames 4 fq .. 4 fq + 3).
+__device__ __forceinline__ void c5_row(uint8_t* ah, uint8_t* al, unsigned r, unsigned fq,
+                                       uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3) {
+  uint4 uh, ul;
+  limb_words_bal(w0, uh.x, ul.x);
+  limb_words_bal(w1, uh.y, ul.y);
+  limb_words_bal(w2, uh.z, ul.z);
+  limb_words_bal(w3, uh.w, ul.w);
+  const uint4 vh = make_uint4(negswap(uh.x), negswap(uh.y), negswap(uh.z), negswap(uh.w));
+  const uint4 vl = make_uint4(negswap(ul.x), negswap(ul.y), negswap(ul.z), negswap(ul.w));
+  const unsigned ou = (r >> 3) * kSboC + fq * t5::kLbo + (r & 7u) * 16u;
+  const unsigned ov = ou + 8u * kSboC;
+  *reinterpret_cast<uint4*>(ah + ou) = uh;
+  *reinterpret_cast<uint4*>(al + ou) = ul;
+  *reinterpret_cast<uint4*>(ah + ov) = vh;
+  *reinterpret_cast<uint4*>(al + ov) = vl;
+}
+
+// The item as [U; V] balanced limb words into one chunk buffer.
 __device__ __forceinline__ void c5_store(unsigned pt, uint8_t* ah, uint8_t* al,
-                                         const uint32_t (&v)[kItemsC][4]) {
-#pragma unroll
-  for (unsigned m = 0; m < kItemsC; ++m) {
-    const unsigned it = pt + m * kProdC * 32u;
-    const unsigned r = it & (kColsC - 1u), fq = it / kColsC;
-    if (fq >= kChunk / 4u) continue;
-    uint4 uh, ul;
-    limb_words_bal(v[m][0], uh.x, ul.x);
-    limb_words_bal(v[m][1], uh.y, ul.y);
-    limb_words_bal(v[m][2], uh.z, ul.z);
-    limb_words_bal(v[m][3], uh.w, ul.w);
-    const uint4 vh = make_uint4(negswap(uh.x), negswap(uh.y), negswap(uh.z), negswap(uh.w));
-    const uint4 vl = make_uint4(negswap(ul.x), negswap(ul.y), negswap(ul.z), negswap(ul.w));
-    const unsigned ou = (r >> 3) * kSboC + fq * t5::kLbo + (r & 7u) * 16u;
-    const unsigned ov = ou + 8u * kSboC;
-    *reinterpret_cast<uint4*>(ah + ou) = uh;
-    *reinterpret_cast<uint4*>(al + ou) = ul;
-    *reinterpret_cast<uint4*>(ah + ov) = vh;
-    *reinterpret_cast<uint4*>(al + ov) = vl;
-  }
+                                         const uint4 (&v)[4]) {
+  const unsigned r0 = 4u * (pt & 15u), fq = pt >> 4;
+  c5_row(ah, al, r0 + 0u, fq, v[0].x, v[1].x, v[2].x, v[3].x);
+  c5_row(ah, al, r0 + 1u, fq, v[0].y, v[1].y, v[2].y, v[3].y);
+  c5_row(ah, al, r0 + 2u, fq, v[0].z, v[1].z, v[2].z, v[3].z);
+  c5_row(ah, al, r0 + 3u, fq, v[0].w, v[1].w, v[2].w, v[3].w);
 }
 
 bool cov_t5_ok(uint32_t S, uint32_t wl) { return S >= 1 && S <= 64 && wl >= 64 && wl <= 256; }
 
 size_t cov_t5_smem(uint32_t S) {
-  // two chunk buffers (high, low limbs), the pair map, barriers; at least
-  // 120 KB so that two CTAs never share an SM (and its TMEM)
-  const size_t need = 4u * kMatC + (size_t)S * S * 4u + 128u;
+  // two chunk buffers (high, low limbs), the raw-word stages, the pair map,
+  // barriers; at least 120 KB so that two CTAs never share an SM (and its
+  // TMEM)
+  const size_t need = 4u * kMatC + kStages * kStageBytes + (size_t)S * S * 4u + 128u;
   return std::max<size_t>(need, 120u * 1024u);
 }
 
 __global__ void __launch_bounds__(kThreadsC, 1) k_cov_t5(CovParams p, const int32_t* pq,
-                                                          unsigned n_groups, unsigned nz) {
+                                                          unsigned n_groups, unsigned nz,
+                                                          unsigned vec) {
   extern __shared__ __align__(1024) uint8_t smc[];
   __shared__ uint32_t s_abort;
   const unsigned S = p.S, Sp = sp_of(S), Pb = kColsC / Sp;  // channels padded, bins per tile
   uint8_t* sA = smc;                                   // [2 buffers][hi, lo]
-  int32_t* s_pq = reinterpret_cast<int32_t*>(smc + 4u * kMatC);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smc + 4u * kMatC + ((S * S * 4u + 15u) & ~15u));
+  uint8_t* sStg = smc + 4u * kMatC;                    // [kStages] raw words
+  int32_t* s_pq = reinterpret_cast<int32_t*>(sStg + kStages * kStageBytes);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sStg + kStages * kStageBytes +
+                                               ((S * S * 4u + 15u) & ~15u));
   uint64_t* a_full = bars;        // [2]
   uint64_t* a_empty = bars + 2;   // [2]
   uint64_t* t_full = bars + 4;    // [2]
@@ -156,7 +183,7 @@ __global__ void __launch_bounds__(kThreadsC, 1) k_cov_t5(CovParams p, const int3
       t5::bar_init(&a_full[i], kProdC * 32u);
       t5::bar_init(&a_empty[i], 1);
       t5::bar_init(&t_full[i], 1);
-      t5::bar_init(&t_empty[i], 128u);
+      t5::bar_init(&t_empty[i], 256u);
     }
     t5::bar_init(done, 1);
     t5::bar_init_fence();
@@ -229,51 +256,54 @@ __global__ void __launch_bounds__(kThreadsC, 1) k_cov_t5(CovParams p, const int3
   } else if (warp <= kProdC) {
     // ---- producers: 64-frame chunks of the unit's bins -> [U; V] limbs ----
     // The CTA's chunk sequence: unit i's frames [lo, hi) in 64-frame chunks,
-    // units one after another. Chunk c + 1's loads are issued before chunk c
-    // is converted (two register sets), so they overlap the conversion and
-    // the wait for the buffer.
+    // units one after another. Each thread copies its item of chunk
+    // c + kStages - 1 (cp.async, one commit group a chunk) before it converts
+    // chunk c from the stage its own copies filled, so kStages - 1 chunks of
+    // loads are in flight while it converts and waits for a buffer.
     const unsigned pt = tid - 32u;
-    unsigned i_a = 0, f_a = 0, hi_a = 0, b_a = 0, i_b = 0, f_b = 0, hi_b = 0, b_b = 0;
-    bool ok_a = false, ok_b = false;
-    auto unit_start = [&](unsigned i, unsigned& f0, unsigned& hi, unsigned& bin0) {
+    const uint32_t stg0 = t5::saddr(sStg);
+    unsigned ii = 0, f_i = 0, hi_i = 0, b_i = 0;  // the next chunk to copy
+    auto unit_start = [&](unsigned i) {
       if (i >= n_local) return false;
       const unsigned unit = blockIdx.x + i * gridDim.x, z = unit / n_groups;
-      seg(z, f0, hi);
-      bin0 = (unit - z * n_groups) * Pb;
+      seg(z, f_i, hi_i);
+      b_i = (unit - z * n_groups) * Pb;
       return true;
     };
-    ok_a = unit_start(0u, f_a, hi_a, b_a);
-    uint32_t va[kItemsC][4], vb[kItemsC][4];
-    c5_load(p, pt, Sp, ok_a, f_a, hi_a, b_a, va);
-    for (unsigned c = 0; ok_a && !*abort; c += 2u) {
-      // chunk c + 1 follows chunk c (a)
-      i_b = i_a;
-      f_b = f_a + kChunk;
-      hi_b = hi_a;
-      b_b = b_a;
-      ok_b = f_b < hi_b || (i_b = i_a + 1u, unit_start(i_b, f_b, hi_b, b_b));
-      c5_load(p, pt, Sp, ok_b, f_b, hi_b, b_b, vb);
+    bool more = unit_start(0u);
+    unsigned n_issued = 0;
+    auto issue_next = [&]() {
+      if (more) {
+        c5_issue(p, pt, Sp, vec != 0u, f_i, hi_i, b_i, stg0 + (n_issued % kStages) * kStageBytes);
+        ++n_issued;
+        f_i += kChunk;
+        if (f_i >= hi_i) more = unit_start(++ii);
+      }
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+#pragma unroll 1
+    for (unsigned d = 0; d + 1u < kStages; ++d) issue_next();
+#pragma unroll 1
+    for (unsigned c = 0; c < n_issued && !*abort; ++c) {
+      issue_next();
+      // groups committed: c + kStages; chunk c's is complete when at most
+      // kStages - 1 are pending
+      asm volatile("cp.async.wait_group %0;\n" ::"n"(kStages - 1u) : "memory");
+      const uint8_t* st = sStg + (c % kStages) * kStageBytes + pt * 16u;
+      uint4 v[4];
+#pragma unroll
+      for (unsigned e = 0; e < 4u; ++e) v[e] = *reinterpret_cast<const uint4*>(st + e * kItemsC * 16u);
       if (!t5::bar_wait(&a_empty[c & 1u], ((c >> 1) & 1u) ^ 1u, abort)) break;
-      c5_store(pt, sA + (c & 1u) * 2u * kMatC, sA + (c & 1u) * 2u * kMatC + kMatC, va);
+      c5_store(pt, sA + (c & 1u) * 2u * kMatC, sA + (c & 1u) * 2u * kMatC + kMatC, v);
       t5::fence_proxy_async();
       t5::bar_arrive(&a_full[c & 1u]);
-      if (!ok_b) break;
-      // chunk c + 2 follows chunk c + 1 (b)
-      i_a = i_b;
-      f_a = f_b + kChunk;
-      hi_a = hi_b;
-      b_a = b_b;
-      ok_a = f_a < hi_a || (i_a = i_b + 1u, unit_start(i_a, f_a, hi_a, b_a));
-      c5_load(p, pt, Sp, ok_a, f_a, hi_a, b_a, va);
-      const unsigned c1 = c + 1u;
-      if (!t5::bar_wait(&a_empty[c1 & 1u], ((c1 >> 1) & 1u) ^ 1u, abort)) break;
-      c5_store(pt, sA + (c1 & 1u) * 2u * kMatC, sA + (c1 & 1u) * 2u * kMatC + kMatC, vb);
-      t5::fence_proxy_async();
-      t5::bar_arrive(&a_full[c1 & 1u]);
     }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
   } else {
     // ---- epilogue: D rows -> window sums of the pairs ----
-    const unsigned q = warp - kEpiC, row = 32u * q + lane;
+    // warp w reads TMEM lanes 32 (w % 4) .. + 31; two warps share a lane
+    // quarter, each taking half of the columns
+    const unsigned q = warp & 3u, half = (warp - kEpiC) >> 2, row = 32u * q + lane;
     const unsigned comp = row >> 6, rl = row & 63u;  // 0: re rows (U), 1: im rows (V)
     const unsigned bl = rl / Sp, y = rl & (Sp - 1u);
     // A TMEM load takes one column address for the whole warp, and the
@@ -281,6 +311,7 @@ __global__ void __launch_bounds__(kThreadsC, 1) k_cov_t5(CovParams p, const int3
     // columns of every bin among its rows, and each lane uses its own bin's
     const unsigned wcol0 = (((32u * q) & 63u) / Sp) * Sp;
     const unsigned wcols = Sp < 32u ? 32u : Sp;
+    const unsigned xa = half * (wcols / 2u), xe = xa + wcols / 2u;
     for (unsigned i = 0; i < n_local && !*abort; ++i) {
       const unsigned unit = blockIdx.x + i * gridDim.x, z = unit / n_groups;
       const unsigned bin = (unit - z * n_groups) * Pb + bl;
@@ -289,30 +320,49 @@ __global__ void __launch_bounds__(kThreadsC, 1) k_cov_t5(CovParams p, const int3
       if (!__all_sync(0xffffffffu, got)) break;
       t5::fence_after();
       const bool carry_in = z == 0u, carry_out = z + 1u == nz, closes = z < p.n_windows;
+      const bool lane_ok = y < S && bin < p.N;
+      // the unit's rows of the carried-in and carried-out sums and of the
+      // window output (pair pi at [pi], [pi], [2 pi])
+      const size_t kb = (size_t)bin * p.P;
+      const long long* acc_in = (comp ? p.acc_im : p.acc_re) + kb;
+      long long* acc_out = (comp ? p.acc_im_out : p.acc_re_out) + kb;
+      long long* outw = p.out + ((size_t)z * p.N * p.P + kb) * 2u + comp;
       const uint32_t tq = tmem + ((32u * q) << 16) + tb * 3u * kColsC + wcol0;
-      for (unsigned x0 = 0; x0 < wcols; x0 += 16u) {
-        uint32_t c16[16], c8[16], c0[16];
-        t5::tmem_ld3x16(tq + x0, tq + kColsC + x0, tq + 2u * kColsC + x0, c16, c8, c0);
-        // this chunk's columns wcol0 + x0 .. + 15 against the lane's bin's
-        // columns bl Sp .. bl Sp + Sp - 1
+      for (unsigned x0 = xa; x0 < xe; x0 += 8u) {
+        // columns wcol0 + x0 .. + 7 against the lane's bin's columns
+        // bl Sp .. bl Sp + Sp - 1: their pair indices, and the block is
+        // skipped when no lane of the warp has a pair in it
         const int xb = (int)(wcol0 + x0) - (int)(bl * Sp);
-        if (y >= S || bin >= p.N || xb < 0 || xb >= (int)Sp) continue;
+        const bool blk_ok = lane_ok && xb >= 0 && xb < (int)Sp;
+        int pis[8];
+        bool any = false;
 #pragma unroll
-        for (unsigned k = 0; k < 16u; ++k) {
+        for (unsigned k = 0; k < 8u; ++k) {
           const unsigned x = (unsigned)xb + k;
-          if (x >= S) break;
-          const int pi = s_pq[x * S + y];
+          pis[k] = blk_ok && x < S ? s_pq[x * S + y] : -1;
+          any |= pis[k] >= 0;
+        }
+        if (!__any_sync(0xffffffffu, any)) continue;
+        // carried-in sums loaded all at once, ahead of the stores (which may
+        // alias them for the compiler), and in flight during the TMEM load
+        long long cin[8];
+#pragma unroll
+        for (unsigned k = 0; k < 8u; ++k)
+          cin[k] = carry_in && pis[k] >= 0 ? __ldg(acc_in + pis[k]) : 0ll;
+        uint32_t c16[8], c8[8], c0[8];
+        t5::tmem_ld3x8(tq + x0, tq + kColsC + x0, tq + 2u * kColsC + x0, c16, c8, c0);
+#pragma unroll
+        for (unsigned k = 0; k < 8u; ++k) {
+          const int pi = pis[k];
           if (pi < 0) continue;
-          long long v = (long long)__float2int_rn(__uint_as_float(c16[k])) * 65536 +
-                        (long long)__float2int_rn(__uint_as_float(c8[k])) * 256 +
-                        (long long)__float2int_rn(__uint_as_float(c0[k]));
-          const size_t kq = (size_t)bin * p.P + (unsigned)pi;
-          if (carry_in) v += comp ? p.acc_im[kq] : p.acc_re[kq];
+          long long v = fold3_24(__uint_as_float(c16[k]), __uint_as_float(c8[k]),
+                                 __uint_as_float(c0[k])) +
+                        cin[k];
           if (closes) {
-            p.out[(((size_t)z * p.N + bin) * p.P + (unsigned)pi) * 2u + comp] = v;
+            outw[2 * pi] = v;
             v = 0;
           }
-          if (carry_out) (comp ? p.acc_im_out : p.acc_re_out)[kq] = v;
+          if (carry_out) acc_out[pi] = v;
         }
       }
       t5::fence_before();
@@ -343,12 +393,18 @@ void launch_cov_t5(const CovParams& p, const int32_t* pq, cudaStream_t s) {
     cudaGetLastError();
     n_sm = 1;
   }
+  // the opt-in covers the largest channel count; with the kernel's static
+  // shared memory it stays within the 227 KB a block may have
   g_c5_attr.once([] {
-    cudaFuncSetAttribute(k_cov_t5, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_cov_t5, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)cov_t5_smem(64));
   });
   const unsigned units = nz * n_groups;
   const unsigned grid = std::min<unsigned>(units, (unsigned)(n_sm > 0 ? n_sm : 1));
-  k_cov_t5<<<grid, kThreadsC, cov_t5_smem(p.S), s>>>(p, pq, n_groups, nz);
+  // 16-byte loads when every group of 4 channels starts on a 16-byte boundary
+  const void* src = p.src_beam ? (const void*)p.beams_bn : (const void*)p.ring;
+  const unsigned vec = (p.S % 4u == 0u && reinterpret_cast<uintptr_t>(src) % 16u == 0u) ? 1u : 0u;
+  k_cov_t5<<<grid, kThreadsC, cov_t5_smem(p.S), s>>>(p, pq, n_groups, nz, vec);
 }
 
 }  // namespace rd

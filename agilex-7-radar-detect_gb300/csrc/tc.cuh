@@ -59,4 +59,24 @@ __device__ __forceinline__ long long fold3(float c16, float c8, float c0) {
          (long long)__float2int_rn(c0);
 }
 
+// The integer held exactly by an fp32 value v with |v| <= 2^24, with adds
+// only (no float-to-int conversion instruction): v + 1.5 2^25 lies in
+// [2^25, 2^26], where fp32 values are the multiples of 4, so it rounds v to
+// a multiple of 4 whose quarter is the difference of the bit patterns; the
+// rest, v minus that multiple (exact, |r| <= 2), is read the same way off
+// r + 1.5 2^23, where the values are the integers.
+__device__ __forceinline__ int exact_int24(float v) {
+  const float m25 = 50331648.0f, m23 = 12582912.0f;
+  const float t = __fadd_rn(v, m25);
+  const int q = __float_as_int(t) - __float_as_int(m25);
+  const float r = __fsub_rn(v, __fsub_rn(t, m25));
+  return q * 4 + (__float_as_int(__fadd_rn(r, m23)) - __float_as_int(m23));
+}
+
+// fold3 for accumulators of magnitude <= 2^24
+__device__ __forceinline__ long long fold3_24(float c16, float c8, float c0) {
+  return (long long)exact_int24(c16) * 65536 + (long long)exact_int24(c8) * 256 +
+         (long long)exact_int24(c0);
+}
+
 }  // namespace rd

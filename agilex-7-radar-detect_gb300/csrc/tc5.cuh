@@ -167,5 +167,22 @@ __device__ __forceinline__ void tmem_ld3x16(uint32_t ta, uint32_t tb, uint32_t t
       : "memory");
 }
 
+// The same for 8 columns of each of three accumulators.
+__device__ __forceinline__ void tmem_ld3x8(uint32_t ta, uint32_t tb, uint32_t tc,
+                                           uint32_t (&a)[8], uint32_t (&b)[8],
+                                           uint32_t (&c)[8]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%24];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8,%9,%10,%11,%12,%13,%14,%15}, [%25];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%16,%17,%18,%19,%20,%21,%22,%23}, [%26];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(a[0]), "=r"(a[1]), "=r"(a[2]), "=r"(a[3]), "=r"(a[4]), "=r"(a[5]), "=r"(a[6]),
+        "=r"(a[7]), "=r"(b[0]), "=r"(b[1]), "=r"(b[2]), "=r"(b[3]), "=r"(b[4]), "=r"(b[5]),
+        "=r"(b[6]), "=r"(b[7]), "=r"(c[0]), "=r"(c[1]), "=r"(c[2]), "=r"(c[3]), "=r"(c[4]),
+        "=r"(c[5]), "=r"(c[6]), "=r"(c[7])
+      : "r"(ta), "r"(tb), "r"(tc)
+      : "memory");
+}
+
 }  // namespace t5
 }  // namespace rd

@@ -159,9 +159,12 @@ def kernel_tensor_flops(cfg, name: str, frames: int, n_pairs: int) -> float:
     (high x high, low x low and the two cross terms) of (frame, bin) rows,
     2 columns per beam (re, im; beams padded to groups of up to 32) and 2
     parts per channel of depth (padded to 16); the warp-level one has 6
-    class columns per beam and 4 limb parts per channel. The covariance's
-    per-bin Gram matrix has the channels as rows, 6 class columns per channel
-    and 4 parts per frame of depth, over the 16-channel tiles that hold a
+    class columns per beam and 4 limb parts per channel. The tcgen05
+    covariance (up to 64 channels, windows of 64-256 frames) runs four
+    128 x 64 GEMMs ([U; V] rows against U columns, 64 // Sp bins of Sp
+    channels a tile, Sp the channel count rounded up to a power of two >= 16)
+    of depth 2 per frame; the warp-level one has 6 class columns per channel
+    and 4 parts per frame of depth over the 16-channel tiles that hold a
     requested pair (the whole triangle of tiles for the full table)."""
     N, C, B = cfg.n_fft, cfg.n_chan, cfg.n_beams
     rows = frames * N
@@ -173,8 +176,15 @@ def kernel_tensor_flops(cfg, name: str, frames: int, n_pairs: int) -> float:
             return 2.0 * rows * 4 * cols * depth
         return 2.0 * rows * (6 * B) * (4 * C)
     if name == "k_cov":
-        t = -(-C // 16)
-        tiles = t * (t + 1) // 2 if n_pairs >= C * (C + 1) // 2 else t * t
+        S = B if cfg.cov_source == 2 else C
+        if cfg.form == 1 and S <= 64 and 64 <= cfg.cov_window <= 256:
+            sp = 16
+            while sp < S:
+                sp *= 2
+            tiles = -(-N // (64 // sp))
+            return 2.0 * tiles * frames * 4 * 128 * 64 * 2
+        t = -(-S // 16)
+        tiles = t * (t + 1) // 2 if n_pairs >= S * (S + 1) // 2 else t * t
         return 2.0 * N * frames * 4 * tiles * 16 * 16 * 6
     return 0.0
 

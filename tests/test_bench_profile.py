@@ -54,8 +54,12 @@ def test_bench_defaults_full_scale():
     # the tcgen05 beamformer's four limb GEMMs of one launch: 1024 x 1024 rows
     # x 128 columns (64 beams, re and im) x 128 deep (64 channels, re and im)
     assert bench.kernel_tensor_flops(cfg, "k_beam", 1024, 2080) == 2.0 * 1024 * 1024 * 4 * 128 * 128
-    # the covariance's Gram tiles: 10 of the 16 16x16 channel tiles hold a pair
+    # the tcgen05 covariance: per bin and frame, four 128 x 64 GEMMs of depth 2
     assert bench.kernel_tensor_flops(cfg, "k_cov", 1024, 2080) == \
+        2.0 * 1024 * 1024 * 4 * 128 * 64 * 2
+    # the warp-level covariance's Gram tiles: 10 of the 16 16x16 channel tiles
+    cfg_w = sc.make_config(p, max_frames=1024, form=2)
+    assert bench.kernel_tensor_flops(cfg_w, "k_cov", 1024, 2080) == \
         2.0 * 1024 * 1024 * 4 * 10 * 16 * 16 * 6
 
 
