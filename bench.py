@@ -56,7 +56,7 @@ def args_():
     ap.add_argument("--cpis", type=int, default=None, help="CPIs per step (default: the workload's)")
     ap.add_argument("--max-frames", type=int, default=None,
                     help="frames per launch (default: 1024 at full scale, 4096 at medium)")
-    ap.add_argument("--form", choices=["cuda_core", "tensor"], default=None,
+    ap.add_argument("--form", choices=["cuda_core", "tensor", "tensor_warp"], default=None,
                     help="default: tensor at full scale, cuda_core at medium")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -331,9 +331,10 @@ def run_forms(torch, a, stream) -> dict:
         out[wl] = r
         del dev
     out["note"] = ("tensor form: int16 samples and weights split into 8-bit limbs held exactly "
-                   "in fp16, mma.sync with fp32 accumulation below 2^24, int64 recombine; "
-                   "per-launch stage times from CUDA events; inputs: one 65536-sample seeded "
-                   "block per channel repeated")
+                   "in fp16, products on the tensor cores with fp32 accumulation of exact "
+                   "integers, int64 recombine (tcgen05 with TMEM accumulators up to 64 "
+                   "channels, else warp-level mma); per-launch stage times from CUDA events; "
+                   "inputs: one 65536-sample seeded block per channel repeated")
     return out
 
 
@@ -531,7 +532,8 @@ def run_gpu(a, rank: int, world: int, local: int) -> None:
     p = sc.preset(a.workload)
     cpis = a.cpis or p.n_cpi
     n = cpis * p.cpi_samples
-    form = abi.RD_FORM_TENSOR if a.form == "tensor" else abi.RD_FORM_CUDA_CORE
+    form = {"tensor": abi.RD_FORM_TENSOR, "tensor_warp": abi.RD_FORM_TENSOR_WARP}.get(
+        a.form, abi.RD_FORM_CUDA_CORE)
     cfg = sc.make_config(p, max_frames=a.max_frames, form=form)
     pairs = sc.pair_table(p)
     coeff = sc.coefficients(p.n_fft, p.taps)
