@@ -10,6 +10,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstring>
 #include <numeric>
 #include <vector>
 
@@ -279,6 +281,93 @@ rd_status rd_batch_tune(rd_batch* b, const rd_cplx16* const* adc_dev, const uint
   drop_graph(b);
   if (chosen) *chosen = best;
   if (best_ms) *best_ms = best_t;
+  return RD_OK;
+}
+
+namespace {
+
+uint64_t fnv1a(uint64_t h, const void* p, size_t n) {
+  const unsigned char* c = static_cast<const unsigned char*>(p);
+  for (size_t i = 0; i < n; ++i) h = (h ^ c[i]) * 1099511628211ull;
+  return h;
+}
+
+// What the tuner's choice depends on: the device, this library, and every
+// scenario's configuration and sample count (rd_config is all 32-bit fields,
+// no padding).
+uint64_t tune_key(const rd_batch* b, const uint64_t* n_samples) {
+  uint64_t h = 1469598103934665603ull;
+  int dev = 0;
+  cudaDeviceProp pr{};
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaGetDeviceProperties(&pr, dev) == cudaSuccess) {
+    h = fnv1a(h, pr.name, strnlen(pr.name, sizeof(pr.name)));
+    h = fnv1a(h, &pr.multiProcessorCount, sizeof(int));
+    h = fnv1a(h, &pr.major, sizeof(int));
+    h = fnv1a(h, &pr.minor, sizeof(int));
+  } else {
+    cudaGetLastError();
+  }
+  const char* v = rd_version();
+  h = fnv1a(h, v, strlen(v));
+  const uint32_t n = (uint32_t)b->cfgs.size();
+  h = fnv1a(h, &n, sizeof(n));
+  for (uint32_t i = 0; i < n; ++i) {
+    h = fnv1a(h, &b->cfgs[i], sizeof(rd_config));
+    h = fnv1a(h, &n_samples[i], sizeof(uint64_t));
+  }
+  return h;
+}
+
+}  // namespace
+
+rd_status rd_batch_tune_cached(rd_batch* b, const rd_cplx16* const* adc_dev,
+                               const uint64_t* n_samples, uint32_t reps, const char* cache_path,
+                               rd_batch_options* chosen, double* best_ms, int* hit) {
+  if (!b || !adc_dev || !n_samples || !cache_path)
+    return rd::set_error(RD_EINVAL, "rd_batch_tune_cached: bad argument");
+  if (hit) *hit = 0;
+  const uint64_t key = tune_key(b, n_samples);
+  // one line per tuned batch: key, streams, frames per launch, milliseconds;
+  // the last line of a key wins
+  bool found = false;
+  unsigned f_ns = 0, f_lf = 0;
+  double f_ms = 0;
+  if (FILE* f = std::fopen(cache_path, "r")) {
+    char line[256];
+    while (std::fgets(line, sizeof(line), f)) {
+      unsigned long long k = 0;
+      unsigned ns = 0, lf = 0;
+      double ms = 0;
+      if (std::sscanf(line, "%llx %u %u %lf", &k, &ns, &lf, &ms) == 4 && k == key && ns >= 1 &&
+          ns <= kMaxStreams && lf >= 1) {
+        found = true;
+        f_ns = ns;
+        f_lf = lf;
+        f_ms = ms;
+      }
+    }
+    std::fclose(f);
+  }
+  if (found) {
+    b->opt = rd_batch_options{f_ns, f_lf, 1};
+    drop_graph(b);
+    if (chosen) *chosen = b->opt;
+    if (best_ms) *best_ms = f_ms;
+    if (hit) *hit = 1;
+    return RD_OK;
+  }
+  rd_batch_options o{};
+  double ms = 0;
+  const rd_status st = rd_batch_tune(b, adc_dev, n_samples, reps, &o, &ms);
+  if (st != RD_OK) return st;
+  // a cache that cannot be written costs the next caller a tuning, nothing more
+  if (FILE* f = std::fopen(cache_path, "a")) {
+    std::fprintf(f, "%016llx %u %u %.4f\n", (unsigned long long)key, o.n_streams,
+                 o.launch_frames, ms);
+    std::fclose(f);
+  }
+  if (chosen) *chosen = o;
+  if (best_ms) *best_ms = ms;
   return RD_OK;
 }
 

@@ -35,13 +35,25 @@ class Batch:
         fn = self.L.rd_batch_run_sequential if sequential else self.L.rd_batch_run
         abi.check(self.L, fn(self.h, p, q, C.c_void_p(stream)), "rd_batch_run")
 
-    def tune(self, ptrs, ns, reps: int = 3) -> tuple[dict, float]:
+    def tune(self, ptrs, ns, reps: int = 3, cache: str | None = None):
+        """Autotune (rd_batch_tune): the chosen options and their time. With
+        `cache` (a file path), rd_batch_tune_cached: a choice recorded there
+        for these scenarios on this device is applied without tuning, else the
+        tuning's choice is appended; the result then also says whether the
+        cache answered (`hit`)."""
         p, q = self._args(ptrs, ns)
         o = abi.RdBatchOptions()
         ms = C.c_double()
-        abi.check(self.L, self.L.rd_batch_tune(self.h, p, q, reps, C.byref(o), C.byref(ms)),
-                  "rd_batch_tune")
-        return {"n_streams": o.n_streams, "launch_frames": o.launch_frames}, ms.value
+        if cache is None:
+            abi.check(self.L, self.L.rd_batch_tune(self.h, p, q, reps, C.byref(o), C.byref(ms)),
+                      "rd_batch_tune")
+            return {"n_streams": o.n_streams, "launch_frames": o.launch_frames}, ms.value
+        hit = C.c_int(0)
+        abi.check(self.L, self.L.rd_batch_tune_cached(self.h, p, q, reps, str(cache).encode(),
+                                                      C.byref(o), C.byref(ms), C.byref(hit)),
+                  "rd_batch_tune_cached")
+        return ({"n_streams": o.n_streams, "launch_frames": o.launch_frames, "hit": bool(hit.value)},
+                ms.value)
 
     def fetch(self, i: int, frames: int, n_pairs: int) -> dict:
         out = Outputs(self.cfgs[i], frames, n_pairs, False, None)

@@ -359,7 +359,9 @@ def run_batching(torch, n_scen: int = 256, runs: int = 5) -> dict:
     st = torch.cuda.Stream()
     b.run(ptrs, ns, st.cuda_stream)  # sizes every chain's buffers
     t = time.perf_counter()
-    opt, tuned_ms = b.tune(ptrs, ns, reps=3)
+    # the tuner's choice is kept on disk, keyed by the scenarios and the device
+    opt, tuned_ms = b.tune(ptrs, ns, reps=3, cache=ROOT / "agilex-7-radar-detect_gb300" /
+                           "_build" / "batch_tune_cache.txt")
     tune_s = time.perf_counter() - t
 
     def timed(sequential: bool) -> float:
@@ -376,6 +378,20 @@ def run_batching(torch, n_scen: int = 256, runs: int = 5) -> dict:
 
     batched = timed(False)
     seq = timed(True)
+    # the batched run with every scenario's results read back to the host, the
+    # work of the per-scenario arm below
+    n_pairs = [gc.lib().rd_cov_pairs(gc.C.byref(c)) for c in cfgs]
+
+    def batched_fetch_once() -> float:
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        b.run(ptrs, ns, st.cuda_stream)
+        for i, p in enumerate(ps):
+            b.fetch(i, p.frames_per_cpi, n_pairs[i])
+        return 1e3 * (time.perf_counter() - t)
+
+    batched_fetch_once()
+    batched_fetch = min(batched_fetch_once() for _ in range(3))
     # the per-scenario API as a caller uses it: process, then read the results
     chains = [gc.Chain(c, co, w) for c, co, w in zip(cfgs, coeffs, ws)]
     for ch, d, n in zip(chains, devs, ns):  # warm
@@ -395,15 +411,17 @@ def run_batching(torch, n_scen: int = 256, runs: int = 5) -> dict:
             "geometry": "channels {4,16,32,64}, PFB/FFT {16,64,256,1024}, taps {4,8,16}, "
                         "CPI log-uniform 2^12..2^18 samples/ch, beams = channels",
             "batched_ms": round(batched, 3), "sequential_ms": round(seq, 3),
+            "batched_with_fetch_ms": round(batched_fetch, 3),
             "sequential_with_fetch_ms": round(seq_fetch, 3),
             "speedup_vs_sequential": round(seq / batched, 3),
-            "speedup_vs_sequential_with_fetch": round(seq_fetch / batched, 3),
+            "speedup_vs_sequential_with_fetch": round(seq_fetch / batched_fetch, 3),
             "batched_msamples_s": round(samples / (batched / 1e3) / 1e6, 1),
             "autotuned": opt, "tune_s": round(tune_s, 2),
             "note": "batched: one CUDA graph replay of every scenario's launches spread "
                     "largest-first over the tuned number of streams; sequential: the same "
                     "launches stream-ordered on one stream, no host waits; with_fetch: "
-                    "each scenario processed and its results read before the next"}
+                    "every scenario's results read to the host - after the one replay "
+                    "(batched), or each before the next scenario starts (sequential)"}
 
 
 def abi_ptr(v: int):

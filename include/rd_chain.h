@@ -302,6 +302,15 @@ rd_status rd_batch_fetch(rd_batch* b, uint32_t i, rd_output* out);
  * it. */
 rd_status rd_batch_tune(rd_batch* b, const rd_cplx16* const* adc_dev, const uint64_t* n_samples,
                         uint32_t reps, rd_batch_options* chosen, double* best_ms);
+/* rd_batch_tune with an on-disk cache: when the text file `cache_path` holds
+ * a choice for these scenarios (the device, this library, every scenario's
+ * rd_config and sample count) it is applied without timing anything
+ * (*hit = 1, *best_ms the time recorded with it); otherwise the batch is
+ * tuned and the choice appended to the file (created if missing; a file that
+ * cannot be written is not an error). */
+rd_status rd_batch_tune_cached(rd_batch* b, const rd_cplx16* const* adc_dev,
+                               const uint64_t* n_samples, uint32_t reps, const char* cache_path,
+                               rd_batch_options* chosen, double* best_ms, int* hit);
 /* The detection packets of the last run, every scenario a source (index i,
  * port cfgs[i].dest), merged by rd_egress_merge on `stream` - the stream the
  * run was given, or one ordered after it. Counts are read on the device, so

@@ -56,6 +56,47 @@ def test_batch_matches_oracle(gpulib, port):
     b.close()
 
 
+def test_batch_tune_cache(gpulib, port, tmp_path):
+    # the on-disk autotune cache: the first batch tunes and records its choice,
+    # a second batch of the same scenarios takes it from the file without
+    # timing anything, and its results are unchanged
+    torch = pytest.importorskip("torch")
+    ps, cfgs, coeffs, ws, xs, devs = _batch_inputs(6, torch, log2_max=13)
+    ptrs = [d.data_ptr() for d in devs]
+    ns = [p.cpi_samples for p in ps]
+    n_pairs = [gc.lib().rd_cov_pairs(gc.C.byref(c)) for c in cfgs]
+    cache = tmp_path / "batch_tune.txt"
+    b = Batch(cfgs, coeffs, ws, n_streams=4, use_graph=True)
+    b.run(ptrs, ns)
+    opt1, ms1 = b.tune(ptrs, ns, reps=2, cache=cache)
+    assert not opt1["hit"] and ms1 > 0
+    lines = cache.read_text().splitlines()
+    assert len(lines) == 1 and lines[0].split()[1:3] == [str(opt1["n_streams"]),
+                                                         str(opt1["launch_frames"])]
+    b.close()
+    b2 = Batch(cfgs, coeffs, ws, n_streams=1, use_graph=True)
+    b2.run(ptrs, ns)
+    opt2, ms2 = b2.tune(ptrs, ns, reps=2, cache=cache)
+    assert opt2["hit"] and (opt2["n_streams"], opt2["launch_frames"]) == \
+        (opt1["n_streams"], opt1["launch_frames"]) and ms2 == pytest.approx(ms1, rel=1e-3)
+    assert len(cache.read_text().splitlines()) == 1
+    b2.run(ptrs, ns)
+    for i, p in enumerate(ps):
+        px, py = sc.pair_table(p)
+        want = port.chain(cfgs[i], coeffs[i], ws[i], px, py).process(xs[i], taps=False, threads=8)
+        assert diff(b2.fetch(i, p.frames_per_cpi, n_pairs[i]), want, CHAIN_KEYS) == [], i
+    # other scenarios (one sample count changed: a frame fewer) miss the
+    # cache and append
+    ns3 = list(ns)
+    ns3[0] = ns[0] - cfgs[0].n_fft
+    b3 = Batch(cfgs, coeffs, ws, n_streams=2, use_graph=True)
+    b3.run(ptrs, ns3)
+    opt3, _ = b3.tune(ptrs, ns3, reps=1, cache=cache)
+    assert not opt3["hit"] and len(cache.read_text().splitlines()) == 2
+    b3.close()
+    b2.close()
+
+
 def _serve_streams():
     # mixed stream sizes; every request is 4096 samples per channel
     out = []
