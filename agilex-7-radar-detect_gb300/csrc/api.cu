@@ -176,6 +176,7 @@ struct rd_chain {
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;  // ordering with the caller's stream
 
   DevBuf<uint32_t> coeff_t, weights, tail[2], ring, power, beams_bn, stage, tw_pos;
+  DevBuf<int2> tw2;
   DevBuf<uint32_t> stage2;                 // host-input staging: two buffers, so the
   cudaStream_t copy_stream = nullptr;      // next chunk's copy overlaps this chunk
   cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
@@ -473,6 +474,14 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
       return RD_ENOMEM;
     }
     if (words) cudaMemcpy(ch->tw_pos.p, tp.data(), words * 4, cudaMemcpyHostToDevice);
+    std::vector<int2> t2(words ? words : 1u, int2{0, 0});
+    for (uint32_t k = 0; k < words; ++k)
+      t2[k] = int2{(int)(int16_t)(uint16_t)(tp[k] & 0xFFFFu), (int)tp[k] >> 16};
+    if (bad(ch->tw2.ensure(t2.size()))) {
+      rd_chain_destroy(ch);
+      return RD_ENOMEM;
+    }
+    cudaMemcpy(ch->tw2.p, t2.data(), t2.size() * sizeof(int2), cudaMemcpyHostToDevice);
   }
   ch->hist.n_ant = C;
   ch->hist.n = N;
@@ -509,7 +518,7 @@ void rd_chain_destroy(rd_chain* ch) {
   if (ch->h_snaps) cudaFreeHost(ch->h_snaps);
   for (int b = 0; b < 2; ++b)
     if (ch->ev_snap[b]) cudaEventDestroy(ch->ev_snap[b]);
-  ch->tw_pos.release(); ch->ct_units.release(); ch->ct_pq.release();
+  ch->tw_pos.release(); ch->tw2.release(); ch->ct_units.release(); ch->ct_pq.release();
   ch->px.release(); ch->py.release(); ch->acc_re.release(); ch->acc_im.release();
   ch->cov_out.release(); ch->sticky.release(); ch->satcnt.release(); ch->win_flags.release();
   ch->counts.release(); ch->detsup.release(); ch->mask.release(); ch->totals.release();
@@ -652,6 +661,7 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   fp.ring_base = ring_base;
   fp.g0 = ch->frame;
   fp.tw_pos = ch->tw_pos.p;
+  fp.tw2 = ch->tw2.p;
   fp.tap_pfb = d_tap_pfb;
   fp.F = F;
   fp.C = C;

@@ -160,13 +160,25 @@ __device__ __forceinline__ int sidx(int q, int pos) {
   return SPC == 2 ? 2 * pos + q : pos;
 }
 
+// Word k of this item's exchange buffer, the item's words starting at word
+// ioff of the pass's buffer. The exchanges after the first stage pairs access
+// words at strides of 8 to 64 (their lanes differ in address bits 3-6), which
+// hit 2 to 4 words in one bank; an XOR of bits 1-4 with (b5, b6, b5, b6) maps
+// every such warp access onto distinct banks at spc 2 (a CPU model of every
+// instantiation's accesses checked it), keeps bit 0 (the merge reads phase
+// pairs as 8-byte words) and is a permutation of each 128-word block.
+__device__ __forceinline__ int xw(int ioff, int k) {
+  const int a = ioff + k;
+  return a ^ (((a >> 4) & 6) * 5);
+}
+
 // The lane sub-stages of one item after the PFB. E[j] holds lane element
 // quad_base<NL-2>(tl) + {0, d1, d0, d0+d1}[j] of lane q on entry. On return,
 // the lane values are in buf[cur] (smem, phase order), cur updated.
 template <int NL, int SPC, bool FL, bool SH1, int S>
 __device__ __forceinline__ void lane_stages(C2 (&E)[4], int q, int tl, unsigned sched,
                                             const int2* twp, uint32_t* buf0, uint32_t* buf1,
-                                            int& cur, unsigned& ovf, unsigned& sf) {
+                                            int ioff, int& cur, unsigned& ovf, unsigned& sf) {
   constexpr int M = 1 << NL;
   if constexpr (S + 1 < NL) {
     // stage pair (S, S+1): distances d0 = 2^(P+1), d1 = 2^P
@@ -194,30 +206,30 @@ __device__ __forceinline__ void lane_stages(C2 (&E)[4], int q, int tl, unsigned 
     }
     if constexpr (S + 2 < NL) {                 // group-closing twiddle
       const int2* tw = twp + (S / 2) * M;
-      E[0] = twm<FL>(E[0], tw[base], ovf, f1);
-      E[1] = twm<FL>(E[1], tw[base + d1], ovf, f1);
-      E[2] = twm<FL>(E[2], tw[base + d0], ovf, f1);
-      E[3] = twm<FL>(E[3], tw[base + d0 + d1], ovf, f1);
+      E[0] = twm<FL>(E[0], __ldg(tw + base), ovf, f1);
+      E[1] = twm<FL>(E[1], __ldg(tw + base + d1), ovf, f1);
+      E[2] = twm<FL>(E[2], __ldg(tw + base + d0), ovf, f1);
+      E[3] = twm<FL>(E[3], __ldg(tw + base + d0 + d1), ovf, f1);
     }
     if (FL) sf |= (f0 << (2 * S)) | (f1 << (2 * (S + 1)));
     // exchange into the next quad layout (or the final layout)
     uint32_t* b = cur ? buf1 : buf0;
-    b[sidx<SPC>(q, base)] = pk(E[0]);
-    b[sidx<SPC>(q, base + d1)] = pk(E[1]);
-    b[sidx<SPC>(q, base + d0)] = pk(E[2]);
-    b[sidx<SPC>(q, base + d0 + d1)] = pk(E[3]);
+    b[xw(ioff, sidx<SPC>(q, base))] = pk(E[0]);
+    b[xw(ioff, sidx<SPC>(q, base + d1))] = pk(E[1]);
+    b[xw(ioff, sidx<SPC>(q, base + d0))] = pk(E[2]);
+    b[xw(ioff, sidx<SPC>(q, base + d0 + d1))] = pk(E[3]);
     __syncthreads();
     if constexpr (S + 2 < NL) {
       constexpr int PN = (S + 3 < NL) ? NL - 4 - S : 0;  // next pair, or a single stage
       constexpr int e1 = (S + 3 < NL) ? (1 << PN) : 1;
       constexpr int e0 = (S + 3 < NL) ? (2 << PN) : 2;
       const int nb = (S + 3 < NL) ? quad_base<PN>(tl) : 4 * tl;
-      E[0] = unpk(b[sidx<SPC>(q, nb)]);
-      E[1] = unpk(b[sidx<SPC>(q, nb + e1)]);
-      E[2] = unpk(b[sidx<SPC>(q, nb + e0)]);
-      E[3] = unpk(b[sidx<SPC>(q, nb + e0 + e1)]);
+      E[0] = unpk(b[xw(ioff, sidx<SPC>(q, nb))]);
+      E[1] = unpk(b[xw(ioff, sidx<SPC>(q, nb + e1))]);
+      E[2] = unpk(b[xw(ioff, sidx<SPC>(q, nb + e0))]);
+      E[3] = unpk(b[xw(ioff, sidx<SPC>(q, nb + e0 + e1))]);
       cur ^= 1;
-      lane_stages<NL, SPC, FL, SH1, S + 2>(E, q, tl, sched, twp, buf0, buf1, cur, ovf, sf);
+      lane_stages<NL, SPC, FL, SH1, S + 2>(E, q, tl, sched, twp, buf0, buf1, ioff, cur, ovf, sf);
     }
   } else if constexpr (S + 1 == NL) {
     // final single stage (NL odd), distance 1, quad = 4*tl .. 4*tl+3
@@ -239,7 +251,7 @@ __device__ __forceinline__ void lane_stages(C2 (&E)[4], int q, int tl, unsigned 
     uint32_t* b = cur ? buf1 : buf0;
     const int base = 4 * tl;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) b[sidx<SPC>(q, base + j)] = pk(E[j]);
+    for (int j = 0; j < 4; ++j) b[xw(ioff, sidx<SPC>(q, base + j))] = pk(E[j]);
     __syncthreads();
   }
 }
@@ -273,7 +285,7 @@ __device__ __forceinline__ void for_taps(const FrontParams& p, int T, unsigned f
 template <int NL, int SPC, int TT, bool FL, bool SH1>
 __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int q, int tl, bool ok,
                                                 unsigned f, unsigned c, const int2* twp,
-                                                uint32_t* buf0, uint32_t* buf1,
+                                                uint32_t* buf0, uint32_t* buf1, int ioff,
                                                 uint32_t* tile_row, unsigned cbp, unsigned& pfl,
                                                 unsigned long long& psat, unsigned& sf_out) {
   using G = Geo<NL, SPC>;
@@ -402,7 +414,7 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
   }
   // ---- lane sub-stages (fft_ref.hpp:269-276) ----
   int cur = 0;
-  lane_stages<NL, SPC, FL, SH1, 0>(E, q, tl, p.sched, twp, buf0, buf1, cur, ovf, sf);
+  lane_stages<NL, SPC, FL, SH1, 0>(E, q, tl, p.sched, twp, buf0, buf1, ioff, cur, ovf, sf);
   uint32_t* b = cur ? buf1 : buf0;
   // ---- merge (fft_ref.hpp:380-406) and natural bins (:291-296) ----
   if constexpr (SPC == 2) {
@@ -414,9 +426,9 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
 #pragma unroll
     for (int h2 = 0; h2 < 2; ++h2) {
       const int j = t + h2 * (M / 2);
-      const uint2 eo = *reinterpret_cast<const uint2*>(b + 2 * j);  // phases 2j, 2j + 1
+      const uint2 eo = *reinterpret_cast<const uint2*>(b + xw(ioff, 2 * j));  // phases 2j, 2j + 1
       C2 e = unpk(eo.x);
-      C2 o = twm<FL>(unpk(eo.y), tw[j], ovf, fm);
+      C2 o = twm<FL>(unpk(eo.y), __ldg(tw + j), ovf, fm);
       if constexpr (!FL && SH1) {
         F2 ge{mg(e.re), mg(e.im)}, go{mg(o.re), mg(o.im)};
         bfly_mg<false>(ge, go);
@@ -437,7 +449,7 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int bin = (int)bitrev((unsigned)(base + j), NL);
-      if (ok) tile_row[bin * cbp] = b[base + j];
+      if (ok) tile_row[bin * cbp] = b[xw(ioff, base + j)];
     }
   }
   if (FL && ok) sf_out |= sf;
@@ -450,11 +462,12 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
 template <int NL, int SPC, int TT, bool SH1>
 __device__ __noinline__ void front_pass_flags(const FrontParams& p, int T, int q, int tl, bool ok,
                                               unsigned f, unsigned c, const int2* twp,
-                                              uint32_t* buf0, uint32_t* buf1, uint32_t* tile_row,
+                                              uint32_t* buf0, uint32_t* buf1, int ioff,
+                                              uint32_t* tile_row,
                                               unsigned cbp, unsigned* sf_out) {
   unsigned pfl = 0, sf = 0;
   unsigned long long psat = 0;
-  front_pass_body<NL, SPC, TT, true, SH1>(p, T, q, tl, ok, f, c, twp, buf0, buf1, tile_row, cbp,
+  front_pass_body<NL, SPC, TT, true, SH1>(p, T, q, tl, ok, f, c, twp, buf0, buf1, ioff, tile_row, cbp,
                                           pfl, psat, sf);
   *sf_out |= sf;
   // the PFB flags and saturation count of the pass (the whole block runs
@@ -473,22 +486,21 @@ __global__ void __launch_bounds__(256, 3) k_front_fast(FrontParams p, unsigned F
   constexpr int N = G::N, M = G::M, TPI = G::TPI;
   constexpr int IPP = 256 / TPI;  // items per pass
   extern __shared__ __align__(16) uint32_t sm[];
-  const unsigned twn = G::NTW * M + (SPC == 2 ? M : 0);
-  int2* s_tw = reinterpret_cast<int2*>(sm);  // [twn] {re, im}
-  uint32_t* s_buf = sm + 2 * twn;         // [2][IPP][N]
+  // the twiddles {re, im} are read from global memory through L1 (20 KB at
+  // N = 1024: in shared memory they cost a CTA per SM)
+  const int2* s_tw = p.tw2;
+  uint32_t* s_buf = sm;                   // [2][IPP][N]
   uint32_t* s_tile = s_buf + 2 * IPP * N; // [FB][N][CB+1]
   const unsigned cbp = CB + 1u;
   const int tid = threadIdx.x;
-  for (unsigned k = tid; k < twn; k += 256u) {
-    const uint32_t w = p.tw_pos[k];
-    s_tw[k] = make_int2(sext16(w), (int)w >> 16);
-  }
   const int item = tid / TPI, t = tid % TPI;
   const int q = SPC == 2 ? (t & 1) : 0;
   const int tl = SPC == 2 ? (t >> 1) : t;
   const int T = TT ? TT : (int)p.T;
-  uint32_t* buf0 = s_buf + item * N;
-  uint32_t* buf1 = s_buf + (IPP + item) * N;
+  // the two exchange buffers of the pass; this item's words start at ioff
+  uint32_t* buf0 = s_buf;
+  uint32_t* buf1 = s_buf + IPP * N;
+  const int ioff = item * N;
   const unsigned f0 = blockIdx.x * FB, c0 = blockIdx.y * CB;
   const unsigned n_items = FB * CB;
   unsigned pfl = 0, sf = 0;
@@ -514,9 +526,9 @@ __global__ void __launch_bounds__(256, 3) k_front_fast(FrontParams p, unsigned F
     const bool ok = it < n_items && f < p.F && c < p.C;
     uint32_t* tile_row = s_tile + (size_t)fb * N * cbp + cc;
     const bool big = front_pass_body<NL, SPC, TT, false, SH1>(p, T, q, tl, ok, f, c, s_tw, buf0,
-                                                              buf1, tile_row, cbp, pfl, psat, sf);
+                                                              buf1, ioff, tile_row, cbp, pfl, psat, sf);
     if (big)  // the exact path: saturation and per-sub-stage flags
-      front_pass_flags<NL, SPC, TT, SH1>(p, T, q, tl, ok, f, c, s_tw, buf0, buf1, tile_row, cbp,
+      front_pass_flags<NL, SPC, TT, SH1>(p, T, q, tl, ok, f, c, s_tw, buf0, buf1, ioff, tile_row, cbp,
                                          &sf);
   }
   __syncthreads();
@@ -571,8 +583,7 @@ void launch_fast(const FrontParams& p, cudaStream_t s) {
   while (FB * CB < (unsigned)IPP) FB *= 2;   // at least one full pass of items
   while (FB * CB * N > 8192u && FB > 1u) FB /= 2;
   while (FB * CB * N > 8192u && CB > 1u) CB /= 2;
-  const unsigned twn = G::NTW * G::M + (SPC == 2 ? G::M : 0);
-  const size_t smem = (2u * twn + 2u * IPP * N + (size_t)FB * N * (CB + 1u)) * sizeof(uint32_t);
+  const size_t smem = (2u * IPP * N + (size_t)FB * N * (CB + 1u)) * sizeof(uint32_t);
   static PerDevice attr;
   attr.once([] {
     cudaFuncSetAttribute(k_front_fast<NL, SPC, TT, SH1>,

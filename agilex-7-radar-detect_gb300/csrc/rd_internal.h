@@ -65,6 +65,7 @@ struct FrontParams {
   uint32_t ring_base;       // ring slot of chunk frame 0 (g0 mod R)
   uint64_t g0;              // stream frame index of chunk frame 0
   const uint32_t* tw_pos;   // per-position twiddles, twiddle_positions()
+  const int2* tw2;          // the same unpacked {re, im}
   uint32_t* tap_pfb;        // [F][C][N] chunk-relative, or null
   uint32_t F, C, N, T, spc, sched;
   uint32_t safe_in;         // PFB outputs within this bound cannot saturate the FFT
