@@ -1664,3 +1664,57 @@ rd_egress_source rd::chain_egress_source(const rd_chain* ch) {
 
 uint32_t rd::chain_packet_w(const rd_chain* ch) { return ch->cfg.packet_w; }
 
+namespace {
+
+static_assert(sizeof(rd_event) == 32, "an event is two 16-byte words");
+
+// The call's count and flag, and its first min(count, call_cap, cap) events
+// and packets, into mapped host memory (grid-stride, 16-byte words for the
+// events)
+__global__ void k_export(const DevStats* st, const rd_event* ev, const uint32_t* fl,
+                         uint64_t call_cap, uint64_t cap, uint32_t pk_words, rd::ExportHdr* hdr,
+                         rd_event* ev_out, uint32_t* fl_out) {
+  const uint64_t n = st->scan_scratch[0];
+  const uint64_t k = n < call_cap ? (n < cap ? n : cap) : (call_cap < cap ? call_cap : cap);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    hdr->n_events = n;
+    hdr->dev_timeout = st->dev_timeout;
+  }
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t nth = (uint64_t)gridDim.x * blockDim.x;
+  const uint4* es = reinterpret_cast<const uint4*>(ev);
+  uint4* ed = reinterpret_cast<uint4*>(ev_out);
+  for (uint64_t i = t; i < 2u * k; i += nth) ed[i] = es[i];
+  if (fl)
+    for (uint64_t i = t; i < k * pk_words; i += nth) fl_out[i] = fl[i];
+}
+
+}  // namespace
+
+rd_status rd::chain_export(rd_chain* ch, const ExportDst& d, cudaStream_t s) {
+  const rd_config& c = ch->cfg;
+  const uint32_t pk_words = rd_detection_flits(c.packet_w) * rd_flit_words(c.packet_w);
+  const uint32_t nw = (uint32_t)ch->call_windows.size();
+  const size_t per = (size_t)c.n_fft * ch->P * 2;
+  if (nw > d.cap_windows || (size_t)nw * per > d.cov_words)
+    return fail(RD_EINVAL, "chain_export: %u windows do not fit", nw);
+  k_export<<<32, 256, 0, s>>>(ch->stats.p, ch->events.p, ch->flits.p, ch->call_cap_events,
+                              d.cap_events, pk_words, d.hdr, d.events, d.flits);
+  CK(cudaGetLastError());
+  if (nw) {
+    CK(cudaMemcpyAsync(d.win_flags, ch->win_flags.p, nw * sizeof(unsigned), cudaMemcpyDeviceToHost,
+                       s));
+    if (per)
+      CK(cudaMemcpyAsync(d.cov, ch->cov_out.p, (size_t)nw * per * 8, cudaMemcpyDeviceToHost, s));
+  }
+  return RD_OK;
+}
+
+const std::vector<rd_cov_window>& rd::chain_call_windows(const rd_chain* ch) {
+  return ch->call_windows;
+}
+
+uint64_t rd::chain_call_cap(const rd_chain* ch) { return ch->call_cap_events; }
+
+size_t rd::chain_window_words(const rd_chain* ch) { return (size_t)ch->cfg.n_fft * ch->P * 2; }
+

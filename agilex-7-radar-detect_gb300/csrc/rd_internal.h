@@ -243,6 +243,36 @@ void launch_doppler_gather(const uint32_t* ring, uint32_t R, uint64_t g_first, u
 rd_egress_source chain_egress_source(const rd_chain* ch);
 uint32_t chain_packet_w(const rd_chain* ch);
 
+// The outputs of a chain's last call exported into host memory on a stream,
+// so that a host loop reads them without a synchronous copy (server.cu): a
+// kernel writes the call's event count, its dev_timeout flag and at most
+// cap_events events and their packets into mapped page-locked memory, and
+// the closed windows' flags and sums follow by DMA into page-locked memory.
+struct ExportHdr {
+  unsigned long long n_events;  // the call's events (may exceed what was kept)
+  unsigned dev_timeout;
+  unsigned pad;
+};
+struct ExportDst {
+  ExportHdr* hdr;        // device views of mapped page-locked memory
+  rd_event* events;      // cap_events entries
+  uint32_t* flits;       // cap_events packets
+  uint64_t cap_events;
+  unsigned* win_flags;   // page-locked host memory, cap_windows entries
+  uint32_t cap_windows;
+  int64_t* cov;          // page-locked host memory, cov_words
+  size_t cov_words;
+};
+// Enqueued on s, which must be ordered after the call (the stream given to
+// rd_chain_process_device). RD_EINVAL when the call's windows do not fit.
+rd_status chain_export(rd_chain* ch, const ExportDst& d, cudaStream_t s);
+// The window headers of the chain's last call (their sat_flags are on the
+// device until exported) and its event capacity.
+const std::vector<rd_cov_window>& chain_call_windows(const rd_chain* ch);
+uint64_t chain_call_cap(const rd_chain* ch);
+// Words of one closed window's sums: n_fft x pairs x (re, im).
+size_t chain_window_words(const rd_chain* ch);
+
 // rd_egress_merge on a stream (fabric.cu)
 rd_status egress_merge(const rd_egress_source* src, uint32_t n_src, uint32_t packet_w,
                        uint32_t n_ports, uint32_t* ring_dev, uint64_t cap_per_port,

@@ -13,8 +13,15 @@
 // overlap on the device and are admitted the moment a slot frees, without
 // waiting for a batch to drain (continuous batching); requests of one stream
 // run in order, because each one continues the stream's state. Polling
-// collects finished requests, reads their outputs and starts whatever can
-// start next.
+// collects finished requests and starts whatever can start next.
+//
+// Outputs. Behind each request's launches its stream also exports the
+// outputs into host memory (rd::chain_export): the event count and up to
+// kExpEvents events and packets into a mapped page-locked block, the closed
+// windows' sums by DMA into a page-locked block, so that polling reads counts
+// from host memory and never waits on a copy. A request with more events
+// than a block holds is read with synchronous copies instead (its stream
+// starts nothing before it is collected, so the chain still holds them).
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -66,6 +73,27 @@ struct PinnedBuf {
   size_t len = 0;
 };
 
+// A mapped page-locked block a request's events and packets are exported
+// into: header, kExpEvents events, their packets at the widest packet format,
+// kExpWindows window flags.
+constexpr uint64_t kExpEvents = 4096;
+constexpr uint32_t kExpWindows = 1024;
+constexpr uint32_t kExpPkWords = 34;  // detection packet words at 512-bit flits, the most
+struct ExportBlock {
+  void* host = nullptr;
+  rd::ExportHdr* hdr = nullptr;  // host views
+  rd_event* ev = nullptr;
+  uint32_t* fl = nullptr;
+  unsigned* wf = nullptr;
+  rd::ExportHdr* d_hdr = nullptr;  // device views
+  rd_event* d_ev = nullptr;
+  uint32_t* d_fl = nullptr;
+};
+constexpr size_t kExpHdrBytes = 256;
+constexpr size_t kExpEvBytes = kExpEvents * sizeof(rd_event);
+constexpr size_t kExpFlBytes = kExpEvents * kExpPkWords * 4;
+constexpr size_t kExpBytes = kExpHdrBytes + kExpEvBytes + kExpFlBytes + kExpWindows * 4;
+
 struct Request {
   uint64_t id = 0;
   uint32_t stream = 0;
@@ -79,7 +107,8 @@ struct Request {
   RawVec<uint32_t> flits;
   RawVec<rd_cov_window> windows;
   PinnedBuf cov;
-  uint64_t n_events = 0, n_flits = 0;
+  ExportBlock* xb = nullptr;  // the exported outputs (null: read synchronously)
+  uint64_t n_events = 0, n_flits = 0, n_kept = 0;
   uint32_t n_windows = 0, flit_words = 0;
 };
 
@@ -122,6 +151,7 @@ struct rd_server {
   std::unordered_map<uint64_t, Request> reqs;
   std::vector<OutBufs> pool;      // output buffers of finished requests, reused
   std::vector<PinnedBuf> cov_pool;  // page-locked window-sum blocks, reused
+  std::vector<ExportBlock*> xpool;  // mapped export blocks, reused
   std::deque<uint64_t> waiting;   // submitted, not started (submission order)
   std::vector<rd_completion> finished;
   uint64_t next_id = 1;
@@ -145,7 +175,70 @@ void retire(rd_server* s, std::unordered_map<uint64_t, Request>::iterator it) {
     if (s->cov_pool.size() < keep) s->cov_pool.push_back(PinnedBuf{r.cov.p, r.cov.cap, 0});
     else cudaFreeHost(r.cov.p);
   }
+  if (r.xb) {
+    if (s->xpool.size() < keep) {
+      s->xpool.push_back(r.xb);
+    } else {
+      cudaFreeHost(r.xb->host);
+      delete r.xb;
+    }
+  }
   s->reqs.erase(it);
+}
+
+ExportBlock* take_xblock(rd_server* s) {
+  if (!s->xpool.empty()) {
+    ExportBlock* b = s->xpool.back();
+    s->xpool.pop_back();
+    return b;
+  }
+  ExportBlock* b = new ExportBlock();
+  if (cudaHostAlloc(&b->host, kExpBytes, cudaHostAllocMapped) != cudaSuccess) {
+    cudaGetLastError();
+    delete b;
+    return nullptr;
+  }
+  void* d = nullptr;
+  if (cudaHostGetDevicePointer(&d, b->host, 0) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFreeHost(b->host);
+    delete b;
+    return nullptr;
+  }
+  char* h = static_cast<char*>(b->host);
+  char* g = static_cast<char*>(d);
+  b->hdr = reinterpret_cast<rd::ExportHdr*>(h);
+  b->d_hdr = reinterpret_cast<rd::ExportHdr*>(g);
+  b->ev = reinterpret_cast<rd_event*>(h + kExpHdrBytes);
+  b->d_ev = reinterpret_cast<rd_event*>(g + kExpHdrBytes);
+  b->fl = reinterpret_cast<uint32_t*>(h + kExpHdrBytes + kExpEvBytes);
+  b->d_fl = reinterpret_cast<uint32_t*>(g + kExpHdrBytes + kExpEvBytes);
+  b->wf = reinterpret_cast<unsigned*>(h + kExpHdrBytes + kExpEvBytes + kExpFlBytes);
+  return b;
+}
+
+// A page-locked block of at least `need` words for the request's window
+// sums: a kept block that holds it (the smallest), else a new one.
+rd_status take_cov(rd_server* s, Request& r, size_t need) {
+  if (need <= r.cov.cap) return RD_OK;
+  size_t best = s->cov_pool.size();
+  for (size_t k = 0; k < s->cov_pool.size(); ++k)
+    if (s->cov_pool[k].cap >= need &&
+        (best == s->cov_pool.size() || s->cov_pool[k].cap < s->cov_pool[best].cap))
+      best = k;
+  PinnedBuf b{};
+  if (best < s->cov_pool.size()) {
+    b = s->cov_pool[best];
+    s->cov_pool.erase(s->cov_pool.begin() + (ptrdiff_t)best);
+  } else if (cudaMallocHost(&b.p, need * sizeof(int64_t)) == cudaSuccess) {
+    b.cap = need;
+  } else {
+    cudaGetLastError();
+    return rd::set_error(RD_ENOMEM, "rd_server: no page-locked memory for window sums");
+  }
+  if (r.cov.p) s->cov_pool.push_back(PinnedBuf{r.cov.p, r.cov.cap, 0});
+  r.cov = b;
+  return RD_OK;
 }
 
 rd_status start_ready(rd_server* s) {
@@ -168,6 +261,28 @@ rd_status start_ready(rd_server* s) {
     SK(cudaMemcpyAsync(sl.dev, s->host[r.host_buf], words * 4, cudaMemcpyHostToDevice, st.cs));
     rd_status rs = rd_chain_process_device(st.ch, sl.dev, r.n, r.n, st.cs);
     if (rs != RD_OK) return rs;
+    // the outputs follow the launches into host memory (see the top of the
+    // file); without a block the request is read synchronously when it ends
+    {
+      const std::vector<rd_cov_window>& w = rd::chain_call_windows(st.ch);
+      const size_t per = rd::chain_window_words(st.ch);
+      const uint32_t pk = rd_detection_flits(st.cfg.packet_w) * rd_flit_words(st.cfg.packet_w);
+      ExportBlock* xb = w.size() <= kExpWindows && pk <= kExpPkWords ? take_xblock(s) : nullptr;
+      if (xb && take_cov(s, r, w.size() * per) == RD_OK) {
+        r.windows.assign(w.begin(), w.end());
+        r.cov.len = w.size() * per;
+        rd::ExportDst d{xb->d_hdr, xb->d_ev, xb->d_fl, kExpEvents, xb->wf, kExpWindows,
+                        r.cov.p, r.cov.cap};
+        rs = rd::chain_export(st.ch, d, st.cs);
+        if (rs != RD_OK) {
+          s->xpool.push_back(xb);
+          return rs;
+        }
+        r.xb = xb;
+      } else if (xb) {
+        s->xpool.push_back(xb);
+      }
+    }
     SK(cudaEventRecord(sl.done, st.cs));
     sl.used = true;
     sl.req = r.id;
@@ -228,6 +343,32 @@ rd_status collect(rd_server* s, Request& r) {
   return rs;  // RD_ETRUNC: the chain's own event buffer overflowed
 }
 
+// A finished request whose outputs were exported: counts from host memory;
+// more events than the block kept means the synchronous read after all.
+rd_status finish_export(rd_server* s, Request& r) {
+  StreamState& st = s->streams[r.stream];
+  const rd_config& c = st.cfg;
+  const rd::ExportHdr h = *r.xb->hdr;
+  if (h.dev_timeout)
+    return rd::set_error(RD_ETIMEOUT, "a bounded wait inside a tensor-core kernel gave up; "
+                         "results invalid");
+  const uint64_t cap = rd::chain_call_cap(st.ch);
+  const uint64_t avail = std::min<uint64_t>(h.n_events, cap);
+  if (avail > kExpEvents) {
+    s->xpool.push_back(r.xb);
+    r.xb = nullptr;
+    return collect(s, r);
+  }
+  const uint32_t nfl = rd_detection_flits(c.packet_w);
+  r.n_events = h.n_events;
+  r.n_flits = h.n_events * nfl;
+  r.n_kept = avail;
+  r.flit_words = rd_flit_words(c.packet_w);
+  r.n_windows = (uint32_t)r.windows.size();
+  for (uint32_t w = 0; w < r.n_windows; ++w) r.windows[w].sat_flags = (uint8_t)r.xb->wf[w];
+  return h.n_events > cap ? rd::set_error(RD_ETRUNC, "output capacity exceeded") : RD_OK;
+}
+
 }  // namespace
 
 rd_status rd_server_create(const rd_server_config* cfg, rd_server** out) {
@@ -281,8 +422,17 @@ void rd_server_destroy(rd_server* s) {
   for (rd_cplx16* h : s->host)
     if (h) cudaFreeHost(h);
   for (PinnedBuf& b : s->cov_pool) cudaFreeHost(b.p);
-  for (auto& kv : s->reqs)
+  for (ExportBlock* b : s->xpool) {
+    cudaFreeHost(b->host);
+    delete b;
+  }
+  for (auto& kv : s->reqs) {
     if (kv.second.cov.p) cudaFreeHost(kv.second.cov.p);
+    if (kv.second.xb) {
+      cudaFreeHost(kv.second.xb->host);
+      delete kv.second.xb;
+    }
+  }
   delete s;
 }
 
@@ -441,7 +591,7 @@ rd_status rd_server_poll(rd_server* s, rd_completion* out, uint32_t cap, uint32_
     if (q == cudaErrorNotReady) continue;
     Request& r = s->reqs[sl.req];
     StreamState& st = s->streams[r.stream];
-    r.status = q == cudaSuccess ? collect(s, r)
+    r.status = q == cudaSuccess ? (r.xb ? finish_export(s, r) : collect(s, r))
                                 : rd::set_error(RD_EDEVICE, "request failed: %s", cudaGetErrorString(q));
     r.t_done = s->now();
     r.done = true;
@@ -485,15 +635,21 @@ rd_status rd_server_take(rd_server* s, uint64_t req_id, rd_output* out) {
   out->flit_words = r.flit_words;
   out->n_cov_windows = r.n_windows;
   out->n_frames = r.n / s->streams[r.stream].cfg.n_fft;
+  // exported outputs sit in the request's block (n_kept of them), else in
+  // its vectors
+  const rd_event* ev = r.xb ? r.xb->ev : r.events.data();
+  const uint32_t* fl = r.xb ? r.xb->fl : r.flits.data();
+  const uint64_t n_ev = r.xb ? r.n_kept : r.events.size();
+  const uint64_t n_fl = r.xb ? r.n_kept * (r.n_events ? r.n_flits / r.n_events : 0) : r.n_flits;
   if (out->events) {
-    const uint64_t k = std::min<uint64_t>(r.events.size(), out->cap_events);
-    trunc |= k < r.events.size();
-    std::memcpy(out->events, r.events.data(), k * sizeof(rd_event));
+    const uint64_t k = std::min<uint64_t>(n_ev, out->cap_events);
+    trunc |= k < r.n_events;
+    std::memcpy(out->events, ev, k * sizeof(rd_event));
   }
   if (out->flits && r.flit_words) {
-    const uint64_t k = std::min<uint64_t>(r.n_flits, out->cap_flits);
+    const uint64_t k = std::min<uint64_t>(n_fl, out->cap_flits);
     trunc |= k < r.n_flits;
-    std::memcpy(out->flits, r.flits.data(), k * r.flit_words * 4);
+    std::memcpy(out->flits, fl, k * r.flit_words * 4);
   }
   if (r.n_windows) {
     const uint32_t k = std::min<uint32_t>(r.n_windows, out->cap_cov_windows);
