@@ -59,6 +59,13 @@ void sat_bump(uint32_t* c, uint64_t by) {
   *c = v > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)v;
 }
 
+// Whether chains of this configuration run the PFB as its own pass before the
+// FFT kernel (then they hold its outputs: F x C x N words): taps the pass is
+// specialised for and an FFT geometry with a specialised kernel.
+bool pfb_pass(const rd_config& c) {
+  return (c.taps == 4u || c.taps == 8u || c.taps == 16u) && front_fast_ok(c.n_fft, c.spc);
+}
+
 unsigned clog2(unsigned v) {
   unsigned w = 0;
   while ((1u << w) < v) ++w;
@@ -177,6 +184,8 @@ struct rd_chain {
 
   DevBuf<uint32_t> coeff_t, weights, tail[2], ring, power, beams_bn, stage, tw_pos;
   DevBuf<int2> tw2;
+  DevBuf<uint32_t> pfb_buf;  // the PFB pass's outputs, [max_frames][C][N]
+  uint32_t coeff_real = 0;   // 1: the bank's imaginary parts are all 0
   DevBuf<uint32_t> stage2;                 // host-input staging: two buffers, so the
   cudaStream_t copy_stream = nullptr;      // next chunk's copy overlaps this chunk
   cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
@@ -427,7 +436,8 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
       bad(ch->counts.ensure((size_t)F * B)) || bad(ch->detsup.ensure((size_t)F * B)) ||
       bad(ch->mask.ensure((size_t)F * B * ((N + 31) / 32))) ||
       bad(ch->totals.ensure(cfar_tiles(F * B))) ||
-      bad(ch->slots.ensure((size_t)F * B * kCfarSlots)) || bad(ch->stats.ensure(1))) {
+      bad(ch->slots.ensure((size_t)F * B * kCfarSlots)) || bad(ch->stats.ensure(1)) ||
+      (pfb_pass(c) && bad(ch->pfb_buf.ensure((size_t)F * C * N)))) {
     rd_chain_destroy(ch);
     return RD_ENOMEM;
   }
@@ -518,7 +528,7 @@ void rd_chain_destroy(rd_chain* ch) {
   if (ch->h_snaps) cudaFreeHost(ch->h_snaps);
   for (int b = 0; b < 2; ++b)
     if (ch->ev_snap[b]) cudaEventDestroy(ch->ev_snap[b]);
-  ch->tw_pos.release(); ch->tw2.release(); ch->ct_units.release(); ch->ct_pq.release();
+  ch->tw_pos.release(); ch->tw2.release(); ch->pfb_buf.release(); ch->ct_units.release(); ch->ct_pq.release();
   ch->px.release(); ch->py.release(); ch->acc_re.release(); ch->acc_im.release();
   ch->cov_out.release(); ch->sticky.release(); ch->satcnt.release(); ch->win_flags.release();
   ch->counts.release(); ch->detsup.release(); ch->mask.release(); ch->totals.release();
@@ -570,6 +580,7 @@ rd_status rd_chain_set_coeff(rd_chain* ch, const rd_cplx16* coeff) {
   }
   ch->pfb32 = worst <= 65535u ? 1u : 0u;
   ch->pfb_dp = ch->pfb32 && neg_ok ? 1u : 0u;
+  ch->coeff_real = std::all_of(t2.begin(), t2.end(), [](const int2& h) { return h.y == 0; }) ? 1u : 0u;
   CK(cudaMemcpyAsync(ch->coeff2.p, t2.data(), t2.size() * sizeof(int2), cudaMemcpyHostToDevice,
                      ch->stream));
   CK(cudaMemcpyAsync(ch->coeff_dp.p, tdp.data(), tdp.size() * sizeof(uint2),
@@ -656,6 +667,9 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
   fp.coeff_dp = ch->coeff_dp.p;
   fp.pfb_dp = ch->pfb_dp;
   fp.pfb32 = ch->pfb32;
+  fp.coeff_real = ch->coeff_real;
+  fp.pfb_buf = ch->pfb_buf.p;
+  fp.pfb_in = nullptr;
   fp.ring = ch->ring.p;
   fp.ring_frames = ch->R;
   fp.ring_base = ring_base;
@@ -1285,6 +1299,7 @@ uint64_t rd_chain_footprint(const rd_config* cfg, uint64_t frames_per_call) {
   b += 2 * C * D * N * 4 + R * N * C * 4;                    // delay lines, spectrum ring
   b += F * B * N * 4 + F * B * (4 + 8 + 8) + F * B * ((N + 31) / 32) * 4;  // power, CFAR
   b += sizeof(DevStats) + 5 * N * 4;
+  if (pfb_pass(c)) b += F * C * N * 4;                          // PFB pass outputs
   if (c.cov_source != RD_COV_OFF) {
     const uint64_t S = c.cov_source == RD_COV_CHANNEL ? C : B;
     const uint64_t P = rd_cov_pairs(cfg);

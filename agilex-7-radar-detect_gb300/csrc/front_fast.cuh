@@ -1,7 +1,9 @@
 // front_fast.cuh - the PFB + FFT + corner-turn kernel specialised per FFT
 // geometry (lane length 2^NL, SPC lanes, taps TT, and whether every
 // sub-stage of the scaling schedule halves). Same arithmetic, same outputs,
-// as k_front in k_frontend.cu, organised for instruction count:
+// as k_front in k_frontend.cu, organised for instruction count. With EXT the
+// PFB has run as its own frame-blocked pass (k_pfb_rows.cu) and this kernel
+// loads its outputs; otherwise it computes the PFB itself:
 //
 //  * every thread owns 4 elements of a lane, so each pair of radix-2^2
 //    sub-stages (BF2I at s, BF2II at s+1, fft_ref.hpp:334-365) runs in
@@ -279,10 +281,11 @@ __device__ __forceinline__ void for_taps(const FrontParams& p, int T, unsigned f
   }
 }
 
-// One pass over IPP items: PFB into registers, the lane sub-stages, the merge,
-// natural-order outputs into the corner-turn tile. Returns whether any value
-// of the pass saturated (block-uniform).
-template <int NL, int SPC, int TT, bool FL, bool SH1>
+// One pass over IPP items: PFB into registers (EXT: the PFB pass's outputs,
+// k_pfb_rows.cu, loaded), the lane sub-stages, the merge, natural-order
+// outputs into the corner-turn tile. Returns whether any value of the pass
+// saturated (block-uniform).
+template <int NL, int SPC, int TT, bool FL, bool SH1, bool EXT>
 __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int q, int tl, bool ok,
                                                 unsigned f, unsigned c, const int2* twp,
                                                 uint32_t* buf0, uint32_t* buf1, int ioff,
@@ -300,7 +303,7 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
   // the chunk's last T - 1 frames become the next chunk's delay line
   // (pfb_model.hpp:170-175): this frame's samples go there as they are read
   uint32_t* tail_row = nullptr;
-  if (!FL && ok && p.tail_out && f + (unsigned)T > p.F)
+  if (!FL && !EXT && ok && p.tail_out && f + (unsigned)T > p.F)
     tail_row = p.tail_out + ((size_t)c * (T - 1) + (p.F - 1u - f)) * N + ph0;
   auto finish = [&](int j, int yr, int yi, unsigned fr, unsigned fi) {
     if (fr | fi) {
@@ -326,7 +329,15 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
              0u);
     }
   };
-  if (p.pfb_dp) {
+  if constexpr (EXT) {
+    // already rounded and saturated by the PFB pass, which also counted its
+    // flags and wrote the delay line and the taps
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      E[j] = ok ? unpk(__ldg(p.pfb_in + ((size_t)f * p.C + c) * N + ph0 + (j & 1) * dph1 +
+                            (j >> 1) * dph2))
+                : C2{0, 0};
+  } else if (p.pfb_dp) {
     // x h = 256 x hh + x hl with byte limbs: re = x.re hr + x.im (-hi),
     // im = x.re hi + x.im hr, two dp2a per limb on the packed sample. The
     // limb sums stay below 2^28; the true sums are below 2^31 (pfb32), so
@@ -459,7 +470,7 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
 
 // The exact-flags recomputation, kept out of line so it does not weigh on the
 // register allocation of the common path.
-template <int NL, int SPC, int TT, bool SH1>
+template <int NL, int SPC, int TT, bool SH1, bool EXT>
 __device__ __noinline__ void front_pass_flags(const FrontParams& p, int T, int q, int tl, bool ok,
                                               unsigned f, unsigned c, const int2* twp,
                                               uint32_t* buf0, uint32_t* buf1, int ioff,
@@ -467,7 +478,7 @@ __device__ __noinline__ void front_pass_flags(const FrontParams& p, int T, int q
                                               unsigned cbp, unsigned* sf_out) {
   unsigned pfl = 0, sf = 0;
   unsigned long long psat = 0;
-  front_pass_body<NL, SPC, TT, true, SH1>(p, T, q, tl, ok, f, c, twp, buf0, buf1, ioff, tile_row, cbp,
+  front_pass_body<NL, SPC, TT, true, SH1, EXT>(p, T, q, tl, ok, f, c, twp, buf0, buf1, ioff, tile_row, cbp,
                                           pfl, psat, sf);
   *sf_out |= sf;
   // the PFB flags and saturation count of the pass (the whole block runs
@@ -480,8 +491,10 @@ __device__ __noinline__ void front_pass_flags(const FrontParams& p, int T, int q
   }
 }
 
-template <int NL, int SPC, int TT, bool SH1>
-__global__ void __launch_bounds__(256, 3) k_front_fast(FrontParams p, unsigned FB, unsigned CB) {
+// EXT (the PFB computed by its own pass) holds no PFB accumulators: four
+// CTAs an SM; the fused form keeps three (80 registers)
+template <int NL, int SPC, int TT, bool SH1, bool EXT>
+__global__ void __launch_bounds__(256, EXT ? 4 : 3) k_front_fast(FrontParams p, unsigned FB, unsigned CB) {
   using G = Geo<NL, SPC>;
   constexpr int N = G::N, M = G::M, TPI = G::TPI;
   constexpr int IPP = 256 / TPI;  // items per pass
@@ -525,10 +538,10 @@ __global__ void __launch_bounds__(256, 3) k_front_fast(FrontParams p, unsigned F
     const unsigned f = f0 + fb, c = c0 + cc;
     const bool ok = it < n_items && f < p.F && c < p.C;
     uint32_t* tile_row = s_tile + (size_t)fb * N * cbp + cc;
-    const bool big = front_pass_body<NL, SPC, TT, false, SH1>(p, T, q, tl, ok, f, c, s_tw, buf0,
+    const bool big = front_pass_body<NL, SPC, TT, false, SH1, EXT>(p, T, q, tl, ok, f, c, s_tw, buf0,
                                                               buf1, ioff, tile_row, cbp, pfl, psat, sf);
     if (big)  // the exact path: saturation and per-sub-stage flags
-      front_pass_flags<NL, SPC, TT, SH1>(p, T, q, tl, ok, f, c, s_tw, buf0, buf1, ioff, tile_row, cbp,
+      front_pass_flags<NL, SPC, TT, SH1, EXT>(p, T, q, tl, ok, f, c, s_tw, buf0, buf1, ioff, tile_row, cbp,
                                          &sf);
   }
   __syncthreads();
@@ -574,7 +587,7 @@ __global__ void __launch_bounds__(256, 3) k_front_fast(FrontParams p, unsigned F
   }
 }
 
-template <int NL, int SPC, int TT, bool SH1>
+template <int NL, int SPC, int TT, bool SH1, bool EXT = false>
 void launch_fast(const FrontParams& p, cudaStream_t s) {
   using G = Geo<NL, SPC>;
   constexpr int N = G::N, TPI = G::TPI, IPP = 256 / TPI;
@@ -586,11 +599,11 @@ void launch_fast(const FrontParams& p, cudaStream_t s) {
   const size_t smem = (2u * IPP * N + (size_t)FB * N * (CB + 1u)) * sizeof(uint32_t);
   static PerDevice attr;
   attr.once([] {
-    cudaFuncSetAttribute(k_front_fast<NL, SPC, TT, SH1>,
+    cudaFuncSetAttribute(k_front_fast<NL, SPC, TT, SH1, EXT>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
   });
   const dim3 grid((p.F + FB - 1) / FB, (p.C + CB - 1) / CB);
-  k_front_fast<NL, SPC, TT, SH1><<<grid, 256, smem, s>>>(p, FB, CB);
+  k_front_fast<NL, SPC, TT, SH1, EXT><<<grid, 256, smem, s>>>(p, FB, CB);
 }
 
 // The taps specialised at compile time (and, for them, the schedule that
@@ -600,6 +613,14 @@ template <int NL, int SPC>
 bool dispatch_t(const FrontParams& p, cudaStream_t s) {
   const uint32_t all = (2u << NL) - 1u;  // sub-stages 0 .. NL (the merge at NL)
   const bool sh1 = (p.sched & all) == all;
+  if (p.pfb_in) {  // the PFB pass ran (k_pfb_rows.cu: taps 4, 8, 16)
+    switch (p.T) {
+      case 4: sh1 ? launch_fast<NL, SPC, 4, true, true>(p, s) : launch_fast<NL, SPC, 4, false, true>(p, s); return true;
+      case 8: sh1 ? launch_fast<NL, SPC, 8, true, true>(p, s) : launch_fast<NL, SPC, 8, false, true>(p, s); return true;
+      case 16: sh1 ? launch_fast<NL, SPC, 16, true, true>(p, s) : launch_fast<NL, SPC, 16, false, true>(p, s); return true;
+      default: return false;
+    }
+  }
   switch (p.T) {
     case 4: sh1 ? launch_fast<NL, SPC, 4, true>(p, s) : launch_fast<NL, SPC, 4, false>(p, s); return true;
     case 8: sh1 ? launch_fast<NL, SPC, 8, true>(p, s) : launch_fast<NL, SPC, 8, false>(p, s); return true;

@@ -13,6 +13,17 @@ bool launch_front_fast_small(const FrontParams& p, cudaStream_t s) {
   return p.N == 64 ? dispatch_t<6, 1>(p, s) : false;
 }
 
+// Whether launch_front_fast has a specialisation for the geometry.
+bool front_fast_ok(uint32_t n, uint32_t spc) {
+  switch (n) {
+    case 16: return spc == 2;
+    case 64: return spc == 1 || spc == 2;
+    case 256:
+    case 1024: return spc == 1 || spc == 2;
+    default: return false;
+  }
+}
+
 // Launches the specialised kernel when the geometry has one; returns false
 // otherwise (the caller then uses the generic k_front).
 bool launch_front_fast(const FrontParams& p, cudaStream_t s) {

@@ -300,6 +300,14 @@ __global__ void __launch_bounds__(MAXT) k_front(FrontParams p, unsigned FB, unsi
 static PerDevice g_front_attr;
 
 unsigned launch_front(const FrontParams& p, cudaStream_t s) {
+  // the PFB as its own pass, then the FFT kernel on its outputs
+  if ((p.pfb_buf || p.tap_pfb) && pfb_rows_ok(p) && front_fast_ok(p.N, p.spc)) {
+    uint32_t* out = p.tap_pfb ? p.tap_pfb : p.pfb_buf;
+    launch_pfb_rows(p, out, s);  // it writes tail_out too
+    FrontParams q = p;
+    q.pfb_in = out;
+    if (launch_front_fast(q, s)) return 2;
+  }
   if (launch_front_fast(p, s)) return 1;  // it writes tail_out too
   const unsigned nth = p.N > 256u ? p.N : 256u;
   const unsigned ipp = nth / p.N;

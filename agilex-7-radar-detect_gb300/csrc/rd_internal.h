@@ -60,6 +60,9 @@ struct FrontParams {
   uint32_t pfb32;           // 1: the bank's phase L1 norms keep every sum in int32
   const uint2* coeff_dp;    // [T][N] byte limbs {hh: re, -im, im, re}, {hl: ...} for dp2a
   uint32_t pfb_dp;          // 1: pfb32 and the limbs hold (no im = -32768): dp2a path
+  uint32_t coeff_real;      // 1: every coefficient's imaginary part is 0
+  uint32_t* pfb_buf;        // [max_frames][C][N] for the PFB pass's outputs (or null)
+  const uint32_t* pfb_in;   // the PFB pass's outputs, [F][C][N], when it ran
   uint32_t* ring;           // [R][N][C]
   uint32_t ring_frames;     // R
   uint32_t ring_base;       // ring slot of chunk frame 0 (g0 mod R)
@@ -81,6 +84,12 @@ uint32_t front_safe_input(uint32_t n, uint32_t spc, uint32_t sched);
 // The geometry-specialised kernel (k_front_fast.cu); false when the geometry
 // has no specialisation.
 bool launch_front_fast(const FrontParams& p, cudaStream_t s);
+bool front_fast_ok(uint32_t n, uint32_t spc);
+// The PFB as its own frame-blocked pass (k_pfb_rows.cu), for banks whose sums
+// stay in int32 and 4, 8 or 16 taps; writes [F][C][N] to out and the next
+// delay line.
+bool pfb_rows_ok(const FrontParams& p);
+void launch_pfb_rows(const FrontParams& p, uint32_t* out, cudaStream_t s);
 void launch_tail_update(const uint32_t* adc, uint64_t ld, const uint32_t* old_tail,
                         uint32_t* new_tail, uint32_t F, uint32_t C, uint32_t N,
                         uint32_t T, cudaStream_t s);
