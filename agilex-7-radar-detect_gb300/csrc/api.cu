@@ -186,14 +186,16 @@ struct rd_chain {
   DevBuf<int2> tw2;
   DevBuf<uint32_t> pfb_buf;  // the PFB pass's outputs, [max_frames][C][N]
   uint32_t coeff_real = 0;   // 1: the bank's imaginary parts are all 0
-  DevBuf<uint32_t> stage2;                 // host-input staging: two buffers, so the
-  cudaStream_t copy_stream = nullptr;      // next chunk's copy overlaps this chunk
-  cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
+  // host-input staging: three buffers (stage, stage2, stage3), so a chunk's
+  // copy may run up to two chunks ahead of the compute
+  DevBuf<uint32_t> stage2, stage3;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_ready[3] = {nullptr, nullptr, nullptr}, ev_free[3] = {nullptr, nullptr, nullptr};
   // results drained into page-locked host buffers chunk by chunk
   cudaStream_t out_stream = nullptr;
   unsigned long long* h_snaps = nullptr;   // page-locked: events of the call after each chunk
   size_t h_snaps_n = 0;
-  cudaEvent_t ev_snap[2] = {nullptr, nullptr};
+  cudaEvent_t ev_snap[3] = {nullptr, nullptr, nullptr};
   bool drained_events = false, drained_flits = false;
   uint32_t drained_windows = 0;
   DevBuf<int4> w_limbs;
@@ -515,8 +517,9 @@ void rd_chain_destroy(rd_chain* ch) {
   ch->coeff_t.release(); ch->coeff2.release(); ch->coeff_dp.release(); ch->weights.release(); ch->w_limbs.release(); ch->w_frag.release(); ch->w_t5.release(); ch->tail[0].release(); ch->tail[1].release();
   ch->ring.release(); ch->power.release(); ch->beams_bn.release(); ch->stage.release();
   ch->stage2.release();
+  ch->stage3.release();
   if (ch->copy_stream) cudaStreamSynchronize(ch->copy_stream);
-  for (int b = 0; b < 2; ++b) {
+  for (int b = 0; b < 3; ++b) {
     if (ch->ev_ready[b]) cudaEventDestroy(ch->ev_ready[b]);
     if (ch->ev_free[b]) cudaEventDestroy(ch->ev_free[b]);
   }
@@ -526,7 +529,7 @@ void rd_chain_destroy(rd_chain* ch) {
     cudaStreamDestroy(ch->out_stream);
   }
   if (ch->h_snaps) cudaFreeHost(ch->h_snaps);
-  for (int b = 0; b < 2; ++b)
+  for (int b = 0; b < 3; ++b)
     if (ch->ev_snap[b]) cudaEventDestroy(ch->ev_snap[b]);
   ch->tw_pos.release(); ch->tw2.release(); ch->pfb_buf.release(); ch->ct_units.release(); ch->ct_pq.release();
   ch->px.release(); ch->py.release(); ch->acc_re.release(); ch->acc_im.release();
@@ -974,9 +977,10 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
   const uint64_t sld = (uint64_t)c.max_frames * N;
   CK(ch->stage.ensure((size_t)C * sld));
   CK(ch->stage2.ensure((size_t)C * sld));
+  CK(ch->stage3.ensure((size_t)C * sld));
   if (!ch->copy_stream) {
     CK(cudaStreamCreateWithFlags(&ch->copy_stream, cudaStreamNonBlocking));
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < 3; ++b) {
       CK(cudaEventCreateWithFlags(&ch->ev_ready[b], cudaEventDisableTiming));
       CK(cudaEventCreateWithFlags(&ch->ev_free[b], cudaEventDisableTiming));
     }
@@ -989,10 +993,10 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
   const uint64_t cap = out->events ? out->cap_events : default_cap(c, frames);
   rd_status st = begin_call(ch, frames, std::max<uint64_t>(cap, 1));
   if (st != RD_OK) return st;
-  // chunk i is copied into staging buffer i % 2 on the copy stream once the
-  // chain has finished with that buffer's previous chunk, so the copy of chunk
-  // i + 1 runs while chunk i computes
-  for (int b = 0; b < 2; ++b) CK(cudaEventRecord(ch->ev_free[b], ch->stream));
+  // chunk i is copied into staging buffer i % 3 on the copy stream once the
+  // chain has finished with that buffer's previous chunk, so the copies of
+  // chunks i + 1 and i + 2 may run while chunk i computes
+  for (int b = 0; b < 3; ++b) CK(cudaEventRecord(ch->ev_free[b], ch->stream));
   std::vector<uint32_t> hb;
   // results into page-locked host buffers are copied chunk by chunk on a third
   // stream while later chunks compute: once chunk i - 1 has finished, the
@@ -1048,7 +1052,7 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
   if (drain) {
     if (!ch->out_stream) {
       CK(cudaStreamCreateWithFlags(&ch->out_stream, cudaStreamNonBlocking));
-      for (int b = 0; b < 2; ++b) CK(cudaEventCreateWithFlags(&ch->ev_snap[b], cudaEventDisableTiming));
+      for (int b = 0; b < 3; ++b) CK(cudaEventCreateWithFlags(&ch->ev_snap[b], cudaEventDisableTiming));
     }
     if (ch->h_snaps_n < n_chunks) {
       if (ch->h_snaps) CK(cudaFreeHost(ch->h_snaps));
@@ -1065,7 +1069,7 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
   std::vector<uint32_t> win_end(n_chunks, 0);  // windows closed by the end of each chunk
   // queue the copies of chunk k's results (its snapshot has landed)
   auto drain_chunk = [&](uint64_t k) -> rd_status {
-    CK(cudaEventSynchronize(ch->ev_snap[k & 1]));  // chunk k is done: its results are final
+    CK(cudaEventSynchronize(ch->ev_snap[k % 3]));  // chunk k is done: its results are final
     const uint64_t lo = k ? ch->h_snaps[k - 1] : 0, hi = ch->h_snaps[k];
     const uint64_t e1 = std::min(hi, cap_ev), f1 = std::min(hi, cap_fl);
     if (dev_ev && e1 > lo)
@@ -1083,9 +1087,9 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
     return RD_OK;
   };
   unsigned bi = 0, chunk = 0;
-  for (uint64_t f = 0; chunk < n_chunks; f += sizes[chunk], bi ^= 1u, ++chunk) {
+  for (uint64_t f = 0; chunk < n_chunks; f += sizes[chunk], bi = bi == 2u ? 0u : bi + 1u, ++chunk) {
     const uint32_t F = sizes[chunk];
-    uint32_t* stg = bi ? ch->stage2.p : ch->stage.p;
+    uint32_t* stg = bi == 0u ? ch->stage.p : (bi == 1u ? ch->stage2.p : ch->stage3.p);
     CK(cudaStreamWaitEvent(ch->copy_stream, ch->ev_free[bi], 0));
     CK(cudaMemcpy2DAsync(stg, sld * 4, adc + f * N, ld * 4, (size_t)F * N * 4, C,
                          cudaMemcpyHostToDevice, ch->copy_stream));
@@ -1100,10 +1104,12 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
       win_end[chunk] = (uint32_t)ch->call_windows.size();
       CK(cudaMemcpyAsync(ch->h_snaps + chunk, &ch->stats.p->events_call,
                          sizeof(unsigned long long), cudaMemcpyDeviceToHost, ch->stream));
-      CK(cudaEventRecord(ch->ev_snap[chunk & 1], ch->stream));
-      // chunk + 1 is queued behind this one; the previous chunk's results go now
-      if (chunk) {
-        st = drain_chunk(chunk - 1);
+      CK(cudaEventRecord(ch->ev_snap[chunk % 3], ch->stream));
+      // the results of the chunk two back go now: waiting for it (not for the
+      // previous one) leaves this chunk and the previous one queued, so the
+      // next chunk's input copy is issued two chunks ahead of its compute
+      if (chunk >= 2) {
+        st = drain_chunk(chunk - 2);
         if (st != RD_OK) return st;
       }
     }
@@ -1131,10 +1137,11 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
       }
     }
   }
-  if (drain && chunk) {
-    st = drain_chunk(chunk - 1);
-    if (st != RD_OK) return st;
-  }
+  if (drain)
+    for (uint64_t k = chunk >= 2 ? chunk - 2 : 0; k < chunk; ++k) {
+      st = drain_chunk(k);
+      if (st != RD_OK) return st;
+    }
   st = end_call(ch);
   if (st != RD_OK) return st;
   ch->drained_events = dev_ev;
