@@ -64,14 +64,16 @@ def test_bench_defaults_full_scale():
 
 
 def test_full_profile_lines():
-    # the full-scale summary: the front kernel's launch of 1024 frames x 64
-    # channels x 1024 phases, its DRAM bytes within a tenth of the algorithmic
-    # 8 B a sample, and a few hundred thread instructions a sample
+    # the full-scale summary: the front stage's launch of 1024 frames x 64
+    # channels x 1024 phases (the PFB pass and the FFT kernel), its DRAM bytes
+    # the algorithmic 8 B a sample plus the PFB outputs written and read back
+    # (within a tenth of 16 B a sample), and a few hundred thread
+    # instructions a sample
     p = sc.preset("full")
     cfg = sc.make_config(p, max_frames=1024)
     alg = bench.kernel_bytes(cfg, "k_front", 1024)
     traffic = bench.profile_line("full", "traffic", "k_front")
     inst = bench.profile_line("full", "instructions", "k_front")
-    assert 0.9 * alg < traffic < 1.1 * alg
+    assert 1.8 * alg < traffic < 2.2 * alg
     assert 100 < inst * 32 / (1024 * 1024 * 64) < 1000
     assert "1024 frames" in (ROOT / "profiles" / "chain_full_ncu.md").read_text()
