@@ -29,7 +29,7 @@ constexpr unsigned kPfbThreads = 128u;
 constexpr int kRF = 16;  // output frames per thread
 
 template <int TT, bool REAL>
-__global__ void __launch_bounds__(kPfbThreads) k_pfb_rows(FrontParams p, uint32_t* out) {
+__global__ void __launch_bounds__(kPfbThreads, 4) k_pfb_rows(FrontParams p, uint32_t* out) {
   constexpr int NI = kRF + TT - 1;  // input frames of the block
   const unsigned N = p.N;
   const unsigned ph = blockIdx.x * kPfbThreads + threadIdx.x;
@@ -98,18 +98,21 @@ __global__ void __launch_bounds__(kPfbThreads) k_pfb_rows(FrontParams p, uint32_
       }
     }
   }
-  // round_sat(v, 15, 16) (q15_out32): the clamp always, the flags only when
-  // some output of the warp saturated
+  // round_sat(v, 15, 16) (q15_out32): rounded in 32 bits, saturated and
+  // packed {im, re} by one cvt.pack.sat; the flags only when some output of
+  // the warp saturated
   bool sat = false;
+  const size_t ostep = (size_t)p.C * N;
+  uint32_t* o = out + ((size_t)f0 * p.C + c) * N + ph;
 #pragma unroll
-  for (int r = 0; r < kRF; ++r) {
-    const int f = f0 + r;
+  for (int r = 0; r < kRF; ++r, o += ostep) {
     const int yr = (ar[r] + 0x3FFF + ((ar[r] >> 15) & 1)) >> 15;
     const int yi = (ai[r] + 0x3FFF + ((ai[r] >> 15) & 1)) >> 15;
-    const int cr = min(max(yr, -32768), 32767), ci = min(max(yi, -32768), 32767);
-    sat |= live && f < F && (cr != yr || ci != yi);
-    if (live && f < F)
-      out[((size_t)f * p.C + c) * N + ph] = ((uint32_t)(uint16_t)ci << 16) | (uint16_t)cr;
+    uint32_t w;
+    asm("cvt.pack.sat.s16.s32 %0, %1, %2;" : "=r"(w) : "r"(yi), "r"(yr));
+    const bool in = live && f0 + r < F;
+    sat |= in && (((unsigned)(yr + 32768) | (unsigned)(yi + 32768)) > 65535u);
+    if (in) *o = w;
   }
   if (__any_sync(0xffffffffu, sat)) {
     unsigned fl = 0, nsat = 0;
