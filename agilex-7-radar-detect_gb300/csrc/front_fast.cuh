@@ -173,6 +173,12 @@ __device__ __forceinline__ int xw(int ioff, int k) {
   const int a = ioff + k;
   return a ^ (((a >> 4) & 6) * 5);
 }
+// The swizzle is linear over XOR, and within an exchange a thread's words are
+// one base plus offsets in bit positions the base leaves zero (the quad's d0,
+// d1 or the merge's lane half; a CPU model checked every access of every
+// instantiation), so word base + o sits at xw(base) ^ xk(o): one swizzle a
+// stage, then an XOR with a constant for each access.
+constexpr int xk(int o) { return o ^ (((o >> 4) & 6) * 5); }
 
 // The lane sub-stages of one item after the PFB. E[j] holds lane element
 // quad_base<NL-2>(tl) + {0, d1, d0, d0+d1}[j] of lane q on entry. On return,
@@ -216,20 +222,22 @@ __device__ __forceinline__ void lane_stages(C2 (&E)[4], int q, int tl, unsigned 
     if (FL) sf |= (f0 << (2 * S)) | (f1 << (2 * (S + 1)));
     // exchange into the next quad layout (or the final layout)
     uint32_t* b = cur ? buf1 : buf0;
-    b[xw(ioff, sidx<SPC>(q, base))] = pk(E[0]);
-    b[xw(ioff, sidx<SPC>(q, base + d1))] = pk(E[1]);
-    b[xw(ioff, sidx<SPC>(q, base + d0))] = pk(E[2]);
-    b[xw(ioff, sidx<SPC>(q, base + d0 + d1))] = pk(E[3]);
+    const int A = xw(ioff, sidx<SPC>(q, base));
+    b[A] = pk(E[0]);
+    b[A ^ xk(SPC * d1)] = pk(E[1]);
+    b[A ^ xk(SPC * d0)] = pk(E[2]);
+    b[A ^ xk(SPC * (d0 + d1))] = pk(E[3]);
     __syncthreads();
     if constexpr (S + 2 < NL) {
       constexpr int PN = (S + 3 < NL) ? NL - 4 - S : 0;  // next pair, or a single stage
       constexpr int e1 = (S + 3 < NL) ? (1 << PN) : 1;
       constexpr int e0 = (S + 3 < NL) ? (2 << PN) : 2;
       const int nb = (S + 3 < NL) ? quad_base<PN>(tl) : 4 * tl;
-      E[0] = unpk(b[xw(ioff, sidx<SPC>(q, nb))]);
-      E[1] = unpk(b[xw(ioff, sidx<SPC>(q, nb + e1))]);
-      E[2] = unpk(b[xw(ioff, sidx<SPC>(q, nb + e0))]);
-      E[3] = unpk(b[xw(ioff, sidx<SPC>(q, nb + e0 + e1))]);
+      const int An = xw(ioff, sidx<SPC>(q, nb));
+      E[0] = unpk(b[An]);
+      E[1] = unpk(b[An ^ xk(SPC * e1)]);
+      E[2] = unpk(b[An ^ xk(SPC * e0)]);
+      E[3] = unpk(b[An ^ xk(SPC * (e0 + e1))]);
       cur ^= 1;
       lane_stages<NL, SPC, FL, SH1, S + 2>(E, q, tl, sched, twp, buf0, buf1, ioff, cur, ovf, sf);
     }
@@ -251,9 +259,9 @@ __device__ __forceinline__ void lane_stages(C2 (&E)[4], int q, int tl, unsigned 
     }
     if (FL) sf |= f0 << (2 * S);
     uint32_t* b = cur ? buf1 : buf0;
-    const int base = 4 * tl;
+    const int A = xw(ioff, sidx<SPC>(q, 4 * tl));
 #pragma unroll
-    for (int j = 0; j < 4; ++j) b[xw(ioff, sidx<SPC>(q, base + j))] = pk(E[j]);
+    for (int j = 0; j < 4; ++j) b[A ^ xk(SPC * j)] = pk(E[j]);
     __syncthreads();
   }
 }
@@ -437,7 +445,8 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
 #pragma unroll
     for (int h2 = 0; h2 < 2; ++h2) {
       const int j = t + h2 * (M / 2);
-      const uint2 eo = *reinterpret_cast<const uint2*>(b + xw(ioff, 2 * j));  // phases 2j, 2j + 1
+      // phases 2j, 2j + 1 (j = t + h2 M / 2)
+      const uint2 eo = *reinterpret_cast<const uint2*>(b + (xw(ioff, 2 * t) ^ xk(h2 * M)));
       C2 e = unpk(eo.x);
       C2 o = twm<FL>(unpk(eo.y), __ldg(tw + j), ovf, fm);
       if constexpr (!FL && SH1) {
@@ -460,7 +469,7 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int bin = (int)bitrev((unsigned)(base + j), NL);
-      if (ok) tile_row[bin * cbp] = b[xw(ioff, base + j)];
+      if (ok) tile_row[bin * cbp] = b[xw(ioff, base) ^ xk(j)];
     }
   }
   if (FL && ok) sf_out |= sf;
