@@ -596,12 +596,28 @@ __device__ __forceinline__ void cells4(const CfarParams& p, uint64_t u, unsigned
   for (int k = 0; k < 4; ++k) c[k] = i0 + k < p.n ? cell_at(p, u, i0 + k) : 0ull;
 }
 
+// The chain's 32-bit power cells kept in 32 bits: half the registers of the
+// 64-bit form, so a 1024-cell frame's 32 cells a lane leave room for two CTAs
+// an SM.
+__device__ __forceinline__ void cells4(const CfarParams& p, uint64_t u, unsigned i0, bool vec,
+                                       uint32_t* c) {
+  const uint32_t* row = p.power_u32 + u * p.n;
+  if (vec && i0 < p.n) {
+    const uint4 v = __ldcs(reinterpret_cast<const uint4*>(row + i0));
+    c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
+    return;
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) c[k] = i0 + k < p.n ? row[i0 + k] : 0u;
+}
+
 // The frame's cells, 4 a lane per row: lane l of row r holds cells
 // 128 r + 4 l .. + 3 (zero past the frame). R >= ceil(n / 128) bounds the
 // rows at compile time; every row is loaded before the first scan step.
-template <int R>
+// Tc = uint32_t reads the 32-bit power cells only.
+template <int R, class Tc>
 __device__ __forceinline__ void load_cells(const CfarParams& p, uint64_t u, bool vec,
-                                           uint64_t (&c)[R][4]) {
+                                           Tc (&c)[R][4]) {
   const unsigned lane = threadIdx.x & 31u;
 #pragma unroll
   for (int r = 0; r < R; ++r) cells4(p, u, (unsigned)r * 128u + lane * 4u, vec, c[r]);
@@ -622,8 +638,8 @@ __device__ __forceinline__ void store4(uint32_t* d, uint32_t a, uint32_t b, uint
 // window sum the decisions take is below 2^32 (a difference of two wrapped
 // prefixes is then the exact sum). pre + 1 sits on a 16-byte boundary, so
 // lane l's pre[4l + 1 .. 4l + 4] are aligned 16-byte stores.
-template <int R, class Tp>
-__device__ __forceinline__ void warp_prefix(const CfarParams& p, const uint64_t (&c)[R][4], Tp* pre,
+template <int R, class Tp, class Tc>
+__device__ __forceinline__ void warp_prefix(const CfarParams& p, const Tc (&c)[R][4], Tp* pre,
                                             bool vec) {
   const unsigned lane = threadIdx.x & 31u;
   if (lane == 0) pre[0] = 0;
@@ -871,12 +887,15 @@ __device__ __forceinline__ unsigned decide_frame(const CfarParams& p, uint64_t u
   return emitted + 1u;  // + SUMMARY
 }
 
-template <int R>
-__global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_decide(CfarParams p) {
+// Persistent: each CTA's 8 warps take 8-frame groups g = blockIdx.x,
+// blockIdx.x + gridDim.x, ... (warp w the group's frame w), so warps never
+// wait for each other and the grid is one wave; a frame's event count goes
+// into its group's total (zeroed before the launch) by one atomic, and each
+// warp adds its detected and suppressed counts once at the end.
+template <int R, class Tc>
+__global__ void __launch_bounds__(kCfarWarps * 32, sizeof(Tc) == 4 ? 3 : 2) k_cfar_decide(CfarParams p) {
   extern __shared__ __align__(16) uint64_t s_pre[];
-  __shared__ unsigned s_cnt[kCfarWarps], s_det[kCfarWarps];
   const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  const uint64_t u = (uint64_t)blockIdx.x * kCfarWarps + warp;
   // the warp's n + 2 words (on a 16-byte boundary when n is even, as the
   // 16-byte stores need)
   uint64_t* wbase = s_pre + (size_t)warp * (p.n + 2u);
@@ -886,18 +905,23 @@ __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_decide(CfarParams p) {
   const bool usable = p.go ? (p.rl != 0u && p.rg != 0u) : (p.rl + p.rg) != 0u;
   const bool live = p.enable && usable;
   const unsigned n_ok = live && hi_b > lo_b ? (unsigned)(hi_b - lo_b) : 0u;
-  unsigned count = 0, det = 0;
-  if (u < p.frames) {
-    uint64_t c[R][4];
+  // the emit pass counts from the events before this launch
+  if (blockIdx.x == 0 && threadIdx.x == 0) p.stats->scan_scratch[1] = p.stats->events_call;
+  unsigned long long det_w = 0, sup_w = 0;
+  for (uint64_t g = blockIdx.x; g * kCfarWarps < p.frames; g += gridDim.x) {
+    const uint64_t u = g * kCfarWarps + warp;
+    if (u >= p.frames) break;  // warp-uniform
+    unsigned det = 0, count;
+    Tc c[R][4];
     load_cells<R>(p, u, p.vec, c);
     // every window sum (and the cell) below 2^32 when the largest cell times
     // the reference cells plus one is: the scan then runs in 32 bits
-    uint64_t mx = 0;
+    Tc mx = 0;
 #pragma unroll
     for (int r = 0; r < R; ++r)
 #pragma unroll
       for (int k = 0; k < 4; ++k) mx = c[r][k] > mx ? c[r][k] : mx;
-    bool narrow = !__any_sync(0xffffffffu, (mx >> 32) != 0ull);
+    bool narrow = !__any_sync(0xffffffffu, ((uint64_t)mx >> 32) != 0ull);
     if (narrow)
       narrow = (uint64_t)__reduce_max_sync(0xffffffffu, (unsigned)mx) * (p.rl + p.rg + 1u) <=
                0xFFFFFFFFull;
@@ -910,24 +934,14 @@ __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_decide(CfarParams p) {
       warp_prefix<R>(p, c, pre, p.vec);
       count = decide_frame<R>(p, u, pre, live, lo_b, hi_b, n_ok, det);
     }
+    if (lane == 0) atomicAdd(&p.totals[g], (unsigned long long)count);
+    det_w += det;
+    sup_w += p.n - n_ok;  // every frame has its SUMMARY
+    __syncwarp();  // the warp's words are rewritten by its next frame
   }
   if (lane == 0) {
-    s_cnt[warp] = count;
-    s_det[warp] = det;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long tot = 0, d = 0, q = 0;
-    for (unsigned k = 0; k < kCfarWarps; ++k) {
-      tot += s_cnt[k];
-      d += s_det[k];
-      if (s_cnt[k]) q += p.n - n_ok;
-    }
-    p.totals[blockIdx.x] = tot;
-    if (d) atomicAdd(&p.stats->cfar_det, d);
-    if (q) atomicAdd(&p.stats->cfar_sup, q);
-    // the emit pass counts from the events before this launch
-    if (blockIdx.x == 0) p.stats->scan_scratch[1] = p.stats->events_call;
+    if (det_w) atomicAdd(&p.stats->cfar_det, det_w);
+    if (sup_w) atomicAdd(&p.stats->cfar_sup, sup_w);
   }
 }
 
@@ -1074,18 +1088,38 @@ __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_emit(CfarParams p) {
 }
 
 // Decide: 8 frames x (n + 2) words of shared memory; n <= 1024 needs the
-// opt-in above 48 KB, set once per instantiation and device.
-template <int R>
-static void launch_cfar_r(const CfarParams& p, cudaStream_t s) {
+// opt-in above 48 KB, set once per instantiation and device. One wave of
+// persistent CTAs (as many as fit an SM, times the SMs), the group totals
+// zeroed first.
+template <int R, class Tc>
+static void launch_decide(const CfarParams& p, size_t sm, unsigned tiles, cudaStream_t s) {
   static PerDevice attr;
-  const size_t sm = (size_t)kCfarWarps * (p.n + 2u) * sizeof(uint64_t);
   attr.once([] {
     const int most = (int)((size_t)kCfarWarps * (128u * R + 2u) * sizeof(uint64_t));
-    cudaFuncSetAttribute(k_cfar_decide<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+    cudaFuncSetAttribute(k_cfar_decide<R, Tc>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
   });
+  int dev = 0, n_sm = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cfar_decide<R, Tc>,
+                                                    kCfarWarps * 32, sm) != cudaSuccess) {
+    cudaGetLastError();
+    n_sm = 0;
+  }
+  const unsigned wave = n_sm > 0 && per_sm > 0 ? (unsigned)(n_sm * per_sm) : tiles;
+  cudaMemsetAsync(p.totals, 0, (size_t)tiles * sizeof(unsigned long long), s);
+  k_cfar_decide<R, Tc><<<std::min(tiles, wave), kCfarWarps * 32, sm, s>>>(p);
+}
+
+template <int R>
+static void launch_cfar_r(const CfarParams& p, cudaStream_t s) {
+  const size_t sm = (size_t)kCfarWarps * (p.n + 2u) * sizeof(uint64_t);
   const unsigned tiles = cfar_tiles(p.frames);
   const unsigned emits = (unsigned)((p.frames + kEmitFrames - 1u) / kEmitFrames);
-  k_cfar_decide<R><<<tiles, kCfarWarps * 32, sm, s>>>(p);
+  if (p.power_u32)
+    launch_decide<R, uint32_t>(p, sm, tiles, s);
+  else
+    launch_decide<R, uint64_t>(p, sm, tiles, s);
   const size_t esm = (size_t)kCfarWarps * 32 * p.nfl * p.flit_words * 4;
   switch (p.packet_w) {  // the common widths with their word layout fixed
     case 64: k_cfar_emit<64><<<emits, kCfarWarps * 32, esm, s>>>(p); break;
