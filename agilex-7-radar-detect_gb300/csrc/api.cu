@@ -221,7 +221,7 @@ struct rd_chain {
   uint32_t acc_cur = 0;
   DevBuf<unsigned> sticky, satcnt, win_flags;
   DevBuf<uint32_t> counts, detsup, mask;   // CFAR per-frame decisions
-  DevBuf<unsigned long long> totals;       // CFAR events per decide CTA
+  DevBuf<unsigned long long> totals;       // CFAR events per 8-frame group and per 64 groups
   DevBuf<uint4> slots;                     // CFAR detections per frame
   DevBuf<rd_event> events;
   DevBuf<uint32_t> flits;

@@ -59,16 +59,23 @@ void drop_graph(rd_batch* b) {
   b->exec = nullptr;
 }
 
+// A chain's frames per launch for the option's launch_frames, which counts
+// frames of a 1024-point FFT: an N-point scenario takes launch_frames x 1024 /
+// N frames (the same samples per launch), capped by its max_frames; 0 takes
+// max_frames.
+uint32_t scaled_frames(const rd_config& c, uint32_t launch_frames) {
+  if (!launch_frames) return std::max(1u, c.max_frames);
+  const uint64_t f = (uint64_t)launch_frames * 1024u / std::max(1u, c.n_fft);
+  return (uint32_t)std::max<uint64_t>(1u, std::min<uint64_t>(f, c.max_frames));
+}
+
 // Enqueues one full run on `root`: fork to the worker streams, reset and
 // process every scenario on its stream, join back.
 rd_status enqueue(rd_batch* b, const rd_cplx16* const* adc, const uint64_t* n, cudaStream_t root,
                   const rd_batch_options& o) {
   const uint32_t ns = std::max(1u, std::min<uint32_t>(o.n_streams, (uint32_t)b->streams.size()));
-  for (size_t i = 0; i < b->chains.size(); ++i) {
-    const uint32_t lf = std::max(1u, std::min(o.launch_frames ? o.launch_frames : b->cfgs[i].max_frames,
-                                              b->cfgs[i].max_frames));
-    BS(rd_chain_set_launch_frames(b->chains[i], lf));
-  }
+  for (size_t i = 0; i < b->chains.size(); ++i)
+    BS(rd_chain_set_launch_frames(b->chains[i], scaled_frames(b->cfgs[i], o.launch_frames)));
   // largest first onto the least-loaded stream (cost ~ samples x channels x beams)
   std::vector<uint32_t> order(b->chains.size());
   std::iota(order.begin(), order.end(), 0u);
@@ -234,15 +241,17 @@ rd_status rd_batch_tune(rd_batch* b, const rd_cplx16* const* adc_dev, const uint
                         uint32_t reps, rd_batch_options* chosen, double* best_ms) {
   if (!b || !adc_dev || !n_samples) return rd::set_error(RD_EINVAL, "rd_batch_tune: bad argument");
   if (reps == 0) reps = 3;
-  uint32_t maxf = 0;
-  for (const rd_config& c : b->cfgs) maxf = std::max(maxf, c.max_frames);
+  // candidates in frames of a 1024-point FFT, up to the largest any chain takes
+  uint64_t maxf = 1;
+  for (const rd_config& c : b->cfgs)
+    maxf = std::max<uint64_t>(maxf, ((uint64_t)c.max_frames * c.n_fft + 1023u) / 1024u);
   const uint32_t n = (uint32_t)b->chains.size();
   std::vector<uint32_t> stream_c, frame_c;
   for (uint32_t s : {1u, 4u, 8u, 16u, 32u})
     if (s <= std::max(1u, n)) stream_c.push_back(s);
-  for (uint32_t f : {128u, 256u, 512u, 1024u, 4096u})
+  for (uint32_t f : {32u, 64u, 128u, 256u, 512u, 1024u, 4096u})
     if (f <= maxf) frame_c.push_back(f);
-  if (frame_c.empty()) frame_c.push_back(maxf);
+  if (frame_c.empty() || frame_c.back() < maxf) frame_c.push_back((uint32_t)std::min<uint64_t>(maxf, 1u << 30));
   cudaEvent_t t0, t1;
   BK(cudaEventCreate(&t0));
   BK(cudaEventCreate(&t1));

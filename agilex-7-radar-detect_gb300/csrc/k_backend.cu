@@ -553,21 +553,29 @@ void launch_cov(const CovParams& p, cudaStream_t s) {
 
 // ---------------------------------------------------------------------------
 // CFAR (cfar_model.hpp:243-340) in two launches.
-// Decide: one warp per CFAR frame (frame x beam), 8 frames per CTA. The warp
-// loads its frame with 16-byte loads (4 cells a lane), builds the prefix sums
-// in shared memory, decides every cell (the lead/lag reference sums as prefix
-// differences - the same integers the model's loops add) and keeps a ballot
-// mask of the cells that emit, the frame's event count and its detected /
-// suppressed counts; the CTA writes its event total.
-// Emit: a CTA takes 64 frames. Its first event's offset is the sum of the
-// totals of all earlier decide CTAs (read in parallel, no scan pass); a scan
-// of its frames' counts gives each frame's offset. Every frame's SUMMARY is
-// written by one thread (64 frames at once); frames with detections are
-// re-read (from L2) by a warp, which writes each detection from the lane that
-// owns its cell, in bin order.
+// Decide: a warp per CFAR frame (frame x beam), or for frames of at most 64
+// cells several frames a warp. The warp loads its cells with 16-byte loads
+// (4 cells a lane), builds the prefix sums in shared memory, decides every
+// cell (the lead/lag reference sums as prefix differences - the same integers
+// the model's loops add) and keeps a ballot mask of the cells that emit, the
+// frame's event count, its detected / suppressed counts and its first
+// detections. The grid is one persistent wave; the event counts are summed
+// per 8-frame group and per 64 groups.
+// Emit: a CTA takes 32 frames (256 when frames are at most 64 cells). Its
+// first event's offset sums the block totals and group totals before it; a
+// scan of its frames' counts places every event, and each thread writes one
+// event and builds its packet in shared memory, the round's packets leaving
+// as one coalesced run.
 // ---------------------------------------------------------------------------
-constexpr unsigned kCfarWarps = 8;        // decide: frames per CTA
-constexpr unsigned kEmitFrames = 32;      // emit: frames per CTA (4 decide CTAs)
+constexpr unsigned kCfarWarps = 8;        // decide: warps per CTA, frames per group
+constexpr unsigned kEmitFrames = 32;      // emit: frames per CTA (frames of 65+ cells)
+constexpr unsigned kCfarBlock = 64;       // groups per block total
+
+// 8-frame groups of a launch; the totals array holds their counts, then one
+// total per 64 groups (cfar_tiles words)
+__host__ __device__ __forceinline__ uint64_t cfar_groups(uint64_t frames) {
+  return (frames + kCfarWarps - 1u) / kCfarWarps;
+}
 
 __device__ __forceinline__ uint64_t cell_at(const CfarParams& p, uint64_t u, unsigned i) {
   if (p.power_u32) return p.power_u32[u * p.n + i];
@@ -890,8 +898,9 @@ __device__ __forceinline__ unsigned decide_frame(const CfarParams& p, uint64_t u
 // Persistent: each CTA's 8 warps take 8-frame groups g = blockIdx.x,
 // blockIdx.x + gridDim.x, ... (warp w the group's frame w), so warps never
 // wait for each other and the grid is one wave; a frame's event count goes
-// into its group's total (zeroed before the launch) by one atomic, and each
-// warp adds its detected and suppressed counts once at the end.
+// into its group's total and its 64-group block's total (zeroed before the
+// launch) by two atomics, and each warp adds its detected and suppressed
+// counts once at the end.
 template <int R, class Tc>
 __global__ void __launch_bounds__(kCfarWarps * 32, sizeof(Tc) == 4 ? 3 : 2) k_cfar_decide(CfarParams p) {
   extern __shared__ __align__(16) uint64_t s_pre[];
@@ -908,6 +917,7 @@ __global__ void __launch_bounds__(kCfarWarps * 32, sizeof(Tc) == 4 ? 3 : 2) k_cf
   // the emit pass counts from the events before this launch
   if (blockIdx.x == 0 && threadIdx.x == 0) p.stats->scan_scratch[1] = p.stats->events_call;
   unsigned long long det_w = 0, sup_w = 0;
+  const uint64_t groups = cfar_groups(p.frames);
   for (uint64_t g = blockIdx.x; g * kCfarWarps < p.frames; g += gridDim.x) {
     const uint64_t u = g * kCfarWarps + warp;
     if (u >= p.frames) break;  // warp-uniform
@@ -934,10 +944,158 @@ __global__ void __launch_bounds__(kCfarWarps * 32, sizeof(Tc) == 4 ? 3 : 2) k_cf
       warp_prefix<R>(p, c, pre, p.vec);
       count = decide_frame<R>(p, u, pre, live, lo_b, hi_b, n_ok, det);
     }
-    if (lane == 0) atomicAdd(&p.totals[g], (unsigned long long)count);
+    if (lane == 0) {
+      atomicAdd(&p.totals[g], (unsigned long long)count);
+      atomicAdd(&p.totals[groups + g / kCfarBlock], (unsigned long long)count);
+    }
     det_w += det;
     sup_w += p.n - n_ok;  // every frame has its SUMMARY
     __syncwarp();  // the warp's words are rewritten by its next frame
+  }
+  if (lane == 0) {
+    if (det_w) atomicAdd(&p.stats->cfar_det, det_w);
+    if (sup_w) atomicAdd(&p.stats->cfar_sup, sup_w);
+  }
+}
+
+// Frames of at most 64 cells, several to a warp. A warp pass holds 128 / NP
+// frames of NP cells (NP = 16, 32 or 64; a frame's cells past n are zero):
+// lane l loads cells 4 (l % (NP / 4)) .. + 3 of frame l / (NP / 4), a scan
+// segmented at the frame boundaries writes each frame's prefix sums, and the
+// 128 cells are decided 32 a step exactly as k_cfar_decide decides them, each
+// frame keeping its own mask words, slots and counts. For NP = 16 a 32-cell
+// step spans two frames, whose ballot halves are taken apart by a mask.
+template <int NP, class Tp, class Tc>
+__device__ __forceinline__ void packed_pass(const CfarParams& p, const Tc (&c)[4], uint64_t u0,
+                                            uint64_t* wbase, bool live, int lo_b, int hi_b,
+                                            unsigned n_ok, unsigned long long& det_w) {
+  constexpr unsigned LPF = NP / 4u;       // lanes a frame holds
+  constexpr unsigned STRIDE = NP + 4u;    // prefix words a frame (a multiple of 4)
+  constexpr unsigned OFF = sizeof(Tp) == 4 ? 3u : 1u;  // pre + 1 on a 16-byte boundary
+  const unsigned lane = threadIdx.x & 31u;
+  Tp* base = reinterpret_cast<Tp*>(wbase);
+  {  // segmented scan: inclusive prefixes pre[1..n] of lane l's frame
+    const unsigned a = lane / LPF, i0 = 4u * (lane % LPF);
+    Tp* pre = base + a * STRIDE + OFF;
+    const Tp t0 = (Tp)c[0], t1 = t0 + (Tp)c[1], t2 = t1 + (Tp)c[2], t3 = t2 + (Tp)c[3];
+    Tp x = t3;
+#pragma unroll
+    for (unsigned o = 1; o < LPF; o <<= 1) {
+      const Tp t = __shfl_up_sync(0xffffffffu, x, o);
+      if ((lane % LPF) >= o) x += t;
+    }
+    const Tp b = x - t3;
+    if (i0 == 0u) pre[0] = 0;
+    if (p.vec && i0 < p.n) {
+      store4(pre + i0 + 1, b + t0, b + t1, b + t2, b + t3);
+    } else {
+      if (i0 < p.n) pre[i0 + 1] = b + t0;
+      if (i0 + 1 < p.n) pre[i0 + 2] = b + t1;
+      if (i0 + 2 < p.n) pre[i0 + 3] = b + t2;
+      if (i0 + 3 < p.n) pre[i0 + 4] = b + t3;
+    }
+  }
+  __syncwarp();
+  const unsigned words = (p.n + 31u) / 32u;  // mask words a frame: 1, or 2 for NP = 64
+  const unsigned ca_n8 = (p.rl + p.rg) << 8;
+  // this lane's frame's bits of a ballot, and the bits below the lane
+  const unsigned fmask = NP >= 32 ? 0xFFFFFFFFu : (0xFFFFu << (lane & 16u));
+  const unsigned below = (1u << lane) - 1u;
+  unsigned emitted = 0, detf = 0;
+#pragma unroll
+  for (unsigned r = 0; r < 4u; ++r) {
+    const unsigned j = r * 32u + lane;
+    const unsigned a = j / NP, i = j % NP;
+    const uint64_t u = u0 + a;
+    const bool valid = u < p.frames;
+    const Tp* pre = base + a * STRIDE + OFF;
+    if ((r * 32u) % NP == 0u) emitted = detf = 0;  // a frame starts with this step
+    bool dt = false;
+    Tp cut = 0, sum = 0;
+    unsigned nref = 0;
+    const bool ok = live && valid && (int)i >= lo_b && (int)i < hi_b;  // i < n follows
+    if (ok) {
+      cut = pre[i + 1] - pre[i];
+      const Tp sl = pre[i + p.gl + p.rl + 1] - pre[i + p.gl + 1];
+      const Tp sg = pre[i - p.gg] - pre[i - p.gg - p.rg];
+      uint64_t lhs;
+      if (p.go) {
+        const bool lead = ((uint64_t)sl * p.rg) >= ((uint64_t)sg * p.rl);
+        sum = lead ? sl : sg;
+        nref = lead ? p.rl : p.rg;
+        lhs = ((uint64_t)cut * nref) << 8;
+      } else {
+        sum = sl + sg;
+        nref = p.rl + p.rg;
+        lhs = (uint64_t)cut * ca_n8;
+      }
+      dt = lhs > (uint64_t)p.alpha * sum;
+    }
+    bool em = dt;
+    const unsigned dm = __ballot_sync(0xffffffffu, dt);
+    unsigned m = dm;
+    if (lane == 0) det_w += __popc(dm);
+    if (p.dense) {  // every cell emits; the detected ones still count
+      em = valid && i < p.n;
+      m = __ballot_sync(0xffffffffu, em);
+      if (em && !ok) cut = pre[i + 1] - pre[i];
+    }
+    const unsigned mf = m & fmask;
+    if (em) {
+      const unsigned k = emitted + __popc(mf & below);
+      if (k < kCfarSlots)
+        p.slots[u * kCfarSlots + k] =
+            pack_detection((uint64_t)cut, i, dt ? 0u : (!ok ? 2u : 1u), ok ? (uint64_t)sum : 0ull,
+                           ok ? nref : 0u);
+    }
+    emitted += __popc(mf);
+    detf += __popc(dm & fmask);
+    const bool first = (i % 32u) == 0u;  // the frame's first lane in this step
+    if (valid && first) p.mask[u * words + i / 32u] = NP >= 32 ? mf : mf >> (lane & 16u);
+    if (valid && first && ((r * 32u + 32u) % NP == 0u || NP < 32)) {  // the frame's last step
+      p.counts[u] = emitted + 1u;
+      p.detsup[u] = detf | ((p.n - n_ok) << 16);
+      atomicAdd(&p.totals[u / kCfarWarps], (unsigned long long)(emitted + 1u));
+      atomicAdd(&p.totals[cfar_groups(p.frames) + u / (kCfarWarps * kCfarBlock)],
+                (unsigned long long)(emitted + 1u));
+    }
+  }
+  __syncwarp();  // the warp's words are rewritten by its next pass
+}
+
+template <int NP, class Tc>
+__global__ void __launch_bounds__(kCfarWarps * 32, 4) k_cfar_decide_packed(CfarParams p) {
+  constexpr unsigned RW = 128u / NP;  // frames a warp pass
+  constexpr unsigned LPF = NP / 4u;
+  __shared__ __align__(16) uint64_t s_pre[kCfarWarps * RW * (NP + 4u)];
+  const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  uint64_t* wbase = s_pre + (size_t)warp * RW * (NP + 4u);
+  const int lo_b = (int)(p.gg + p.rg), hi_b = (int)p.n - (int)(p.gl + p.rl);
+  const bool usable = p.go ? (p.rl != 0u && p.rg != 0u) : (p.rl + p.rg) != 0u;
+  const bool live = p.enable && usable;
+  const unsigned n_ok = live && hi_b > lo_b ? (unsigned)(hi_b - lo_b) : 0u;
+  if (blockIdx.x == 0 && threadIdx.x == 0) p.stats->scan_scratch[1] = p.stats->events_call;
+  unsigned long long det_w = 0, sup_w = 0;
+  const uint64_t passes = ((uint64_t)p.frames + RW - 1u) / RW;
+  for (uint64_t q = (uint64_t)blockIdx.x * kCfarWarps + warp; q < passes;
+       q += (uint64_t)gridDim.x * kCfarWarps) {
+    const uint64_t u0 = q * RW;
+    const uint64_t ul = u0 + lane / LPF;
+    Tc c[4] = {0, 0, 0, 0};
+    if (ul < p.frames) cells4(p, ul, 4u * (lane % LPF), p.vec, c);
+    Tc mx = c[0] > c[1] ? c[0] : c[1];
+    mx = c[2] > mx ? c[2] : mx;
+    mx = c[3] > mx ? c[3] : mx;
+    bool narrow = !__any_sync(0xffffffffu, ((uint64_t)mx >> 32) != 0ull);
+    if (narrow)
+      narrow = (uint64_t)__reduce_max_sync(0xffffffffu, (unsigned)mx) * (p.rl + p.rg + 1u) <=
+               0xFFFFFFFFull;
+    if (narrow)
+      packed_pass<NP, uint32_t>(p, c, u0, wbase, live, lo_b, hi_b, n_ok, det_w);
+    else
+      packed_pass<NP, uint64_t>(p, c, u0, wbase, live, lo_b, hi_b, n_ok, det_w);
+    const uint64_t left = p.frames - u0;
+    sup_w += (uint64_t)(p.n - n_ok) * (left < RW ? left : RW);  // every frame has its SUMMARY
   }
   if (lane == 0) {
     if (det_w) atomicAdd(&p.stats->cfar_det, det_w);
@@ -991,14 +1149,14 @@ __device__ uint4 redecide(const CfarParams& p, uint64_t u, unsigned k) {
 // Event j of an emit CTA (frame f of the CTA, its k-th event): the SUMMARY
 // from the frame's counts, a detection from the frame's slot (or
 // re-decided); the event goes straight out, its packet to `pkt`.
-template <unsigned PW>
+template <unsigned PW, unsigned EF>
 __device__ __forceinline__ void emit_one(const CfarParams& p, unsigned long long j,
                                          unsigned long long base, unsigned long long seq0,
                                          size_t pk, uint64_t f0, const unsigned long long* s_fbase,
                                          const unsigned* s_c, uint32_t* pkt) {
   unsigned f = 0;  // the frame holding event j: s_fbase[f] <= j < s_fbase[f + 1]
 #pragma unroll
-  for (unsigned step = kEmitFrames / 2; step > 0; step >>= 1)
+  for (unsigned step = EF / 2; step > 0; step >>= 1)
     if (s_fbase[f + step] <= j) f += step;
   const unsigned k = (unsigned)(j - s_fbase[f]), c = s_c[f];
   const uint64_t u = f0 + f;
@@ -1027,44 +1185,65 @@ __device__ __forceinline__ void emit_one(const CfarParams& p, unsigned long long
                  (unsigned)((seq0 + idx) & 0xFFFFu));
 }
 
-template <unsigned PW>
+// EF frames a CTA: 32, or 256 for frames of at most 64 cells (a frame then
+// holds an event or two, and 32 frames would leave most threads idle).
+template <unsigned PW, unsigned EF>
 __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_emit(CfarParams p) {
-  __shared__ unsigned long long s_red[kCfarWarps], s_fbase[kEmitFrames + 1];
-  __shared__ unsigned s_c[kEmitFrames];
+  static_assert(EF == 32u || EF == kCfarWarps * 32u, "a warp's or the CTA's frames");
+  __shared__ unsigned long long s_red[kCfarWarps + 1], s_fbase[EF + 1];
+  __shared__ unsigned s_c[EF];
   const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, tid = threadIdx.x;
-  const uint64_t f0 = (uint64_t)blockIdx.x * kEmitFrames;
-  // events before this CTA: the launch's base plus every earlier decide CTA's total
-  const uint64_t t_end = f0 / kCfarWarps;
-  unsigned long long part = 0;
-  for (uint64_t t0 = 0; t0 < t_end; t0 += 8ull * blockDim.x) {
-    unsigned long long v[8];  // eight independent loads in flight
+  const uint64_t f0 = (uint64_t)blockIdx.x * EF;
+  // events before this CTA: the launch's base, the totals of the 64-group
+  // blocks before its first group's block and of that block's groups before
+  // it (read in parallel; G / 128 + 32 words a CTA on average)
+  {
+    const uint64_t g = f0 / kCfarWarps, blk = g / kCfarBlock, groups = cfar_groups(p.frames);
+    unsigned long long part = 0;
+    for (uint64_t i = tid; i < blk; i += blockDim.x) part += p.totals[groups + i];
+    for (uint64_t i = blk * kCfarBlock + tid; i < g; i += blockDim.x) part += p.totals[i];
+    part = warp_sum64(part);
+    if (lane == 0) s_red[warp] = part;
+    __syncthreads();
+    if (tid == 0) {
+      unsigned long long b = p.stats->scan_scratch[1];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const uint64_t t = t0 + (uint64_t)q * blockDim.x + tid;
-      v[q] = t < t_end ? p.totals[t] : 0ull;
+      for (unsigned w = 0; w < kCfarWarps; ++w) b += s_red[w];
+      s_red[kCfarWarps] = b;
     }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) part += v[q];
+    __syncthreads();  // s_red[0..7] are rewritten by the frame scan
   }
-  part = warp_sum64(part);
-  if (lane == 0) s_red[warp] = part;
-  // this CTA's frames: counts and their exclusive scan (warp 0)
-  if (warp == 0) {
-    const unsigned c = f0 + lane < p.frames ? p.counts[f0 + lane] : 0u;
-    s_c[lane] = c;
+  // this CTA's frames: counts and their exclusive scan (a warp per 32 frames)
+  if (warp < EF / 32u) {
+    const unsigned fl = warp * 32u + lane;
+    const unsigned c = f0 + fl < p.frames ? p.counts[f0 + fl] : 0u;
+    s_c[fl] = c;
     unsigned long long x = c;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const unsigned long long t = __shfl_up_sync(0xffffffffu, x, o);
       if ((int)lane >= o) x += t;
     }
-    s_fbase[lane] = x - c;
-    if (lane == 31) s_fbase[kEmitFrames] = x;
+    s_fbase[fl] = x - c;
+    if (lane == 31) s_red[warp] = x;
   }
   __syncthreads();
-  unsigned long long base = p.stats->scan_scratch[1];
-  for (unsigned k = 0; k < kCfarWarps; ++k) base += s_red[k];
-  const unsigned long long total = s_fbase[kEmitFrames];
+  if (EF > 32u) {  // add the earlier warps' frame totals
+    unsigned long long add = 0, all = 0;
+#pragma unroll
+    for (unsigned w = 0; w < EF / 32u; ++w) {
+      add += w < warp ? s_red[w] : 0ull;
+      all += s_red[w];
+    }
+    s_fbase[tid] += add;  // EF = blockDim.x: a frame a thread
+    if (tid == 0) s_fbase[EF] = all;
+    __syncthreads();
+  } else if (tid == 0) {
+    s_fbase[EF] = s_red[0];
+  }
+  if (EF == 32u) __syncthreads();
+  const unsigned long long base = s_red[kCfarWarps];
+  const unsigned long long total = s_fbase[EF];
   if (blockIdx.x == gridDim.x - 1 && tid == 0)  // the launch's last frame is here
     p.stats->events_call = base + total;
   const unsigned long long seq0 = p.stats->events_total;
@@ -1076,7 +1255,8 @@ __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_emit(CfarParams p) {
     const unsigned long long j = j0 + tid;
     const unsigned long long end = base + (total < j0 + blockDim.x ? total : j0 + blockDim.x);
     const unsigned long long stop = end < p.cap ? end : p.cap;  // events of the round kept
-    if (j < total) emit_one<PW>(p, j, base, seq0, pk, f0, s_fbase, s_c, s_pk + (size_t)tid * pk);
+    if (j < total)
+      emit_one<PW, EF>(p, j, base, seq0, pk, f0, s_fbase, s_c, s_pk + (size_t)tid * pk);
     __syncthreads();
     if (p.flits && stop > base + j0) {
       const size_t nw = (size_t)(stop - (base + j0)) * pk;
@@ -1091,6 +1271,41 @@ __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_emit(CfarParams p) {
 // opt-in above 48 KB, set once per instantiation and device. One wave of
 // persistent CTAs (as many as fit an SM, times the SMs), the group totals
 // zeroed first.
+// CTAs of `kernel` an SM at `sm` bytes of dynamic shared memory, and the
+// device's SM count; the occupancy answer is kept per device and shared
+// memory size in `memo` (one word per device: sm << 8 | CTAs).
+template <class K>
+static void decide_fit(K kernel, size_t sm, std::atomic<unsigned long long>* memo, int& per_sm,
+                       int& n_sm) {
+  int dev = 0;
+  per_sm = n_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    n_sm = 0;
+    return;
+  }
+  const unsigned long long m = dev >= 0 && dev < 64 ? memo[dev].load(std::memory_order_relaxed) : 0ull;
+  if (m && (m >> 8) == (unsigned long long)sm) {
+    per_sm = (int)(m & 0xFFull);
+    return;
+  }
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kCfarWarps * 32, sm) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    per_sm = 0;
+    return;
+  }
+  if (dev >= 0 && dev < 64 && per_sm > 0 && per_sm < 256)
+    memo[dev].store(((unsigned long long)sm << 8) | (unsigned)per_sm, std::memory_order_relaxed);
+}
+
+// The decide grid: one wave (as many CTAs as fit), at most one per `work` unit.
+static unsigned decide_grid(unsigned work, int per_sm, int n_sm) {
+  const unsigned wave = n_sm > 0 && per_sm > 0 ? (unsigned)(n_sm * per_sm) : work;
+  return std::max(1u, std::min(work, wave));
+}
+
 template <int R, class Tc>
 static void launch_decide(const CfarParams& p, size_t sm, unsigned tiles, cudaStream_t s) {
   static PerDevice attr;
@@ -1098,47 +1313,78 @@ static void launch_decide(const CfarParams& p, size_t sm, unsigned tiles, cudaSt
     const int most = (int)((size_t)kCfarWarps * (128u * R + 2u) * sizeof(uint64_t));
     cudaFuncSetAttribute(k_cfar_decide<R, Tc>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
   });
-  int dev = 0, n_sm = 0, per_sm = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess ||
-      cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cfar_decide<R, Tc>,
-                                                    kCfarWarps * 32, sm) != cudaSuccess) {
-    cudaGetLastError();
-    n_sm = 0;
-  }
-  const unsigned wave = n_sm > 0 && per_sm > 0 ? (unsigned)(n_sm * per_sm) : tiles;
+  static std::atomic<unsigned long long> memo[64];
+  int per_sm, n_sm;
+  decide_fit(k_cfar_decide<R, Tc>, sm, memo, per_sm, n_sm);
+  const unsigned grid = decide_grid((unsigned)cfar_groups(p.frames), per_sm, n_sm);
   cudaMemsetAsync(p.totals, 0, (size_t)tiles * sizeof(unsigned long long), s);
-  k_cfar_decide<R, Tc><<<std::min(tiles, wave), kCfarWarps * 32, sm, s>>>(p);
+  k_cfar_decide<R, Tc><<<grid, kCfarWarps * 32, sm, s>>>(p);
 }
 
 template <int R>
-static void launch_cfar_r(const CfarParams& p, cudaStream_t s) {
+static void launch_decide_r(const CfarParams& p, cudaStream_t s) {
   const size_t sm = (size_t)kCfarWarps * (p.n + 2u) * sizeof(uint64_t);
   const unsigned tiles = cfar_tiles(p.frames);
-  const unsigned emits = (unsigned)((p.frames + kEmitFrames - 1u) / kEmitFrames);
   if (p.power_u32)
     launch_decide<R, uint32_t>(p, sm, tiles, s);
   else
     launch_decide<R, uint64_t>(p, sm, tiles, s);
-  const size_t esm = (size_t)kCfarWarps * 32 * p.nfl * p.flit_words * 4;
-  switch (p.packet_w) {  // the common widths with their word layout fixed
-    case 64: k_cfar_emit<64><<<emits, kCfarWarps * 32, esm, s>>>(p); break;
-    case 128: k_cfar_emit<128><<<emits, kCfarWarps * 32, esm, s>>>(p); break;
-    case 256: k_cfar_emit<256><<<emits, kCfarWarps * 32, esm, s>>>(p); break;
-    case 512: k_cfar_emit<512><<<emits, kCfarWarps * 32, esm, s>>>(p); break;
-    default: k_cfar_emit<0><<<emits, kCfarWarps * 32, esm, s>>>(p); break;
-  }
 }
 
-unsigned cfar_tiles(uint32_t frames) { return (frames + kCfarWarps - 1u) / kCfarWarps; }
+// Frames of at most 64 cells: 128 / NP frames a warp pass, persistent as above.
+template <int NP, class Tc>
+static void launch_decide_packed(const CfarParams& p, cudaStream_t s) {
+  const unsigned tiles = cfar_tiles(p.frames);
+  static std::atomic<unsigned long long> memo[64];
+  int per_sm, n_sm;
+  decide_fit(k_cfar_decide_packed<NP, Tc>, 0, memo, per_sm, n_sm);
+  const uint64_t passes = ((uint64_t)p.frames + 128u / NP - 1u) / (128u / NP);
+  const unsigned grid =
+      decide_grid((unsigned)((passes + kCfarWarps - 1u) / kCfarWarps), per_sm, n_sm);
+  cudaMemsetAsync(p.totals, 0, (size_t)tiles * sizeof(unsigned long long), s);
+  k_cfar_decide_packed<NP, Tc><<<grid, kCfarWarps * 32, 0, s>>>(p);
+}
+
+template <int NP>
+static void launch_decide_np(const CfarParams& p, cudaStream_t s) {
+  if (p.power_u32)
+    launch_decide_packed<NP, uint32_t>(p, s);
+  else
+    launch_decide_packed<NP, uint64_t>(p, s);
+}
+
+unsigned cfar_tiles(uint32_t frames) {
+  const uint64_t g = cfar_groups(frames);
+  return (unsigned)(g + (g + kCfarBlock - 1u) / kCfarBlock);
+}
+
+template <unsigned EF>
+static void launch_emit(const CfarParams& p, cudaStream_t s) {
+  const unsigned emits = (unsigned)((p.frames + EF - 1u) / EF);
+  const size_t esm = (size_t)kCfarWarps * 32 * p.nfl * p.flit_words * 4;
+  switch (p.packet_w) {  // the common widths with their word layout fixed
+    case 64: k_cfar_emit<64, EF><<<emits, kCfarWarps * 32, esm, s>>>(p); break;
+    case 128: k_cfar_emit<128, EF><<<emits, kCfarWarps * 32, esm, s>>>(p); break;
+    case 256: k_cfar_emit<256, EF><<<emits, kCfarWarps * 32, esm, s>>>(p); break;
+    case 512: k_cfar_emit<512, EF><<<emits, kCfarWarps * 32, esm, s>>>(p); break;
+    default: k_cfar_emit<0, EF><<<emits, kCfarWarps * 32, esm, s>>>(p); break;
+  }
+}
 
 void launch_cfar(const CfarParams& p, cudaStream_t s) {
   if (!p.frames) return;
   const unsigned rows = (p.n + 127u) / 128u;
-  if (rows <= 1) launch_cfar_r<1>(p, s);
-  else if (rows <= 2) launch_cfar_r<2>(p, s);
-  else if (rows <= 4) launch_cfar_r<4>(p, s);
-  else launch_cfar_r<8>(p, s);
+  if (p.n >= 1u && p.n <= 16u) launch_decide_np<16>(p, s);
+  else if (p.n >= 1u && p.n <= 32u) launch_decide_np<32>(p, s);
+  else if (p.n >= 1u && p.n <= 64u) launch_decide_np<64>(p, s);
+  else if (rows <= 1) launch_decide_r<1>(p, s);
+  else if (rows <= 2) launch_decide_r<2>(p, s);
+  else if (rows <= 4) launch_decide_r<4>(p, s);
+  else launch_decide_r<8>(p, s);
+  if (p.n <= 64u)
+    launch_emit<kCfarWarps * 32u>(p, s);
+  else
+    launch_emit<kEmitFrames>(p, s);
 }
 
 // ---------------------------------------------------------------------------

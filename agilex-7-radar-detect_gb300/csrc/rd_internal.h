@@ -212,7 +212,7 @@ struct CfarParams {
   uint32_t* counts;           // [frames] events per CFAR frame (SUMMARY included)
   uint32_t* detsup;           // [frames] detected | suppressed << 16
   uint32_t* mask;             // [frames][ceil(n / 32)] emitted-cell bitmask
-  unsigned long long* totals; // [cfar_tiles(frames)] events per decide CTA
+  unsigned long long* totals; // [cfar_tiles(frames)] events per 8-frame group, then per 64 groups
   uint4* slots;               // [frames][kCfarSlots] the frame's first detections
   int vec;                    // n % 4 == 0 and the cells 16-byte aligned: 16-byte loads
   int ev16;                   // events 16-byte aligned: 16-byte stores

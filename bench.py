@@ -345,9 +345,10 @@ def run_batching(torch, n_scen: int = 256, runs: int = 5) -> dict:
     from rdgb.batch import Batch
 
     ps = sc.batch_scenarios(n_scen)
-    # the tensor form for every scenario (bit-identical to the CUDA-core one)
-    cfgs = [sc.make_config(p, max_frames=min(p.frames_per_cpi, 1024), form=abi.RD_FORM_TENSOR)
-            for p in ps]
+    # the tensor form for every scenario (bit-identical to the CUDA-core one);
+    # buffers for a whole CPI, the launch size the tuner's (equal samples per
+    # launch across FFT sizes), the sequential arm one launch per CPI
+    cfgs = [sc.make_config(p, max_frames=p.frames_per_cpi, form=abi.RD_FORM_TENSOR) for p in ps]
     coeffs = [sc.coefficients(p.n_fft, p.taps) for p in ps]
     ws = [sc.steering_weights(p.n_chan, p.n_beams) for p in ps]
     devs = [torch.from_numpy(tiled_adc(p, p.cpi_samples, 8192).view(np.int32)).cuda()
@@ -680,6 +681,7 @@ def run_gpu(a, rank: int, world: int, local: int) -> None:
         e2e = {"value": round(world * samples / (e2e_ms / 1e3) / 1e6, 3), "unit": UNIT,
                "h2d_bytes_per_step": samples * 4, "d2h_bytes_per_step": int(d2h),
                "ms_per_step": round(e2e_ms, 3),
+               "step_ms": [round(1e3 * x, 3) for x in times],
                "api": "rd_chain_process (host buffers in, page-locked result buffers out)"}
         del out
 

@@ -281,7 +281,10 @@ rd_status rd_chain_read_history(rd_chain* ch, uint32_t bin, uint32_t frame_off,
 typedef struct rd_batch rd_batch;
 typedef struct {
   uint32_t n_streams;          /* concurrent streams (0: autotune) */
-  uint32_t launch_frames;      /* frames per launch, capped per chain (0: autotune) */
+  uint32_t launch_frames;      /* frames per launch of a 1024-point FFT: an N-point
+                                  scenario takes launch_frames x 1024 / N (the same
+                                  samples per launch), capped by its max_frames
+                                  (0: autotune) */
   int use_graph;               /* 1: capture once, replay; 0: launch eagerly */
 } rd_batch_options;
 rd_status rd_batch_create(uint32_t n, const rd_config* cfgs, const rd_cplx16* const* coeff,

@@ -216,6 +216,41 @@ def test_cfar_large_cells_vs_oracle(gpulib, port, mode):
                 assert (event_fields(g)["kind"] == 0).any()
 
 
+@pytest.mark.parametrize("mode", [abi.RD_CFAR_CA, abi.RD_CFAR_GO])
+@pytest.mark.parametrize("out", [abi.RD_CFAR_EVENTS, abi.RD_CFAR_DENSE])
+def test_cfar_short_frames_vs_oracle(gpulib, port, mode, out):
+    # frames of at most 64 cells run several to a warp (16, 32 or 64 cells a
+    # frame slot): every length around the slot sizes, lengths that are not
+    # a multiple of 4 (scalar loads), frame counts that leave a warp's last
+    # slots empty, and cells past 32 bits in some frames (the 64-bit scan)
+    rng = np.random.default_rng(40 + mode * 2 + out)
+    for n in (1, 3, 5, 12, 15, 16, 17, 20, 31, 32, 33, 36, 47, 63, 64):
+        for frames in (1, 3, 9, 37):
+            cells = rng.exponential(1000.0, frames * n).astype(np.int64)
+            cells[rng.integers(0, cells.size, 8)] *= 40
+            if frames > 3:
+                cells[n + rng.integers(0, n)] = 2**33 + 7
+            fid = rng.integers(0, 2**16, frames).astype(np.uint32)
+            for geo in ((1, 1, 4, 4), (0, 2, 3, 0), (2, 0, 6, 6), (1, 1, 2, 1)):
+                cfg = cfar_cfg(mode, out, *geo, int(rng.integers(0, 3000)))
+                g, o = gc.cfar(cells, n, cfg, fid), port.cfar(cells, n, cfg, fid)
+                assert np.array_equal(g, o), (n, frames, geo)
+
+
+@pytest.mark.parametrize("n,frames", [(16, 50000), (48, 40000), (1024, 5000)])
+def test_cfar_many_frames_vs_oracle(gpulib, port, n, frames):
+    # more frames than one wave of the persistent decide grid holds, so warps
+    # take several frame groups each
+    rng = np.random.default_rng(n + frames)
+    cells = rng.exponential(1000.0, frames * n).astype(np.int64)
+    cells[rng.integers(0, cells.size, frames // 4)] *= 40
+    fid = (np.arange(frames) % 65536).astype(np.uint32)
+    for mode in (abi.RD_CFAR_CA, abi.RD_CFAR_GO):
+        cfg = cfar_cfg(mode, abi.RD_CFAR_EVENTS, 1, 1, 4, 4, 2600)
+        g, o = gc.cfar(cells, n, cfg, fid), port.cfar(cells, n, cfg, fid)
+        assert np.array_equal(g, o), mode
+
+
 def test_cfar_directed(gpulib, port):
     n = 128
     cells = np.full(n, 100, np.int64)
