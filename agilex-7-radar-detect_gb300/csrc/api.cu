@@ -1707,8 +1707,15 @@ __global__ void k_export(const DevStats* st, const rd_event* ev, const uint32_t*
   const uint4* es = reinterpret_cast<const uint4*>(ev);
   uint4* ed = reinterpret_cast<uint4*>(ev_out);
   for (uint64_t i = t; i < 2u * k; i += nth) ed[i] = es[i];
-  if (fl)
-    for (uint64_t i = t; i < k * pk_words; i += nth) fl_out[i] = fl[i];
+  if (fl) {  // 16 bytes a store where both ends allow it, the tail by words
+    const uint64_t nw = k * pk_words;
+    const bool v16 = ((reinterpret_cast<uintptr_t>(fl) | reinterpret_cast<uintptr_t>(fl_out)) & 15u) == 0;
+    const uint64_t nv = v16 ? nw / 4u : 0u;
+    const uint4* fs = reinterpret_cast<const uint4*>(fl);
+    uint4* fd = reinterpret_cast<uint4*>(fl_out);
+    for (uint64_t i = t; i < nv; i += nth) fd[i] = fs[i];
+    for (uint64_t i = 4u * nv + t; i < nw; i += nth) fl_out[i] = fl[i];
+  }
 }
 
 }  // namespace
@@ -1718,15 +1725,20 @@ rd_status rd::chain_export(rd_chain* ch, const ExportDst& d, cudaStream_t s) {
   const uint32_t pk_words = rd_detection_flits(c.packet_w) * rd_flit_words(c.packet_w);
   const uint32_t nw = (uint32_t)ch->call_windows.size();
   const size_t per = (size_t)c.n_fft * ch->P * 2;
-  if (nw > d.cap_windows || (size_t)nw * per > d.cov_words)
+  if (nw > d.cap_windows || (d.cov && (size_t)nw * per > d.cov_words))
     return fail(RD_EINVAL, "chain_export: %u windows do not fit", nw);
-  k_export<<<32, 256, 0, s>>>(ch->stats.p, ch->events.p, ch->flits.p, ch->call_cap_events,
-                              d.cap_events, pk_words, d.hdr, d.events, d.flits);
+  // a CTA per 64 KB of the most the call can export (8 to 256 CTAs)
+  const uint64_t most = std::min<uint64_t>(ch->call_cap_events, d.cap_events) *
+                        (sizeof(rd_event) + (d.flits ? pk_words * 4ull : 0ull));
+  const unsigned grid = (unsigned)std::min<uint64_t>(std::max<uint64_t>(most >> 16, 8u), 256u);
+  k_export<<<grid, 256, 0, s>>>(ch->stats.p, ch->events.p, d.flits ? ch->flits.p : nullptr,
+                                ch->call_cap_events, d.cap_events, pk_words, d.hdr, d.events,
+                                d.flits);
   CK(cudaGetLastError());
   if (nw) {
     CK(cudaMemcpyAsync(d.win_flags, ch->win_flags.p, nw * sizeof(unsigned), cudaMemcpyDeviceToHost,
                        s));
-    if (per)
+    if (per && d.cov)
       CK(cudaMemcpyAsync(d.cov, ch->cov_out.p, (size_t)nw * per * 8, cudaMemcpyDeviceToHost, s));
   }
   return RD_OK;
@@ -1737,6 +1749,8 @@ const std::vector<rd_cov_window>& rd::chain_call_windows(const rd_chain* ch) {
 }
 
 uint64_t rd::chain_call_cap(const rd_chain* ch) { return ch->call_cap_events; }
+
+uint64_t rd::chain_call_frames(const rd_chain* ch) { return ch->call_frames; }
 
 size_t rd::chain_window_words(const rd_chain* ch) { return (size_t)ch->cfg.n_fft * ch->P * 2; }
 

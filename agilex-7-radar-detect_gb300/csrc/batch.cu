@@ -46,8 +46,20 @@ struct rd_batch {
   std::vector<const rd_cplx16*> cap_adc;
   std::vector<uint64_t> cap_n;
   rd_batch_options cap_opt{};
+  uint64_t cap_out_gen = 0;
   bool warmed = false;
   cudaStream_t last = nullptr;        // the stream of the last run
+  // results exported by every run (rd_batch_set_outputs): the caller's
+  // buffers, the events' and flits' device views, and per scenario a mapped
+  // header (event count, timeout) and page-locked window flags
+  std::vector<rd_output> outs;
+  std::vector<rd_event*> out_ev;
+  std::vector<uint32_t*> out_fl;
+  rd::ExportHdr* hdr = nullptr;       // mapped, one per scenario
+  rd::ExportHdr* hdr_dev = nullptr;
+  unsigned* wflags = nullptr;         // page-locked, wf_off[i] + cap_cov_windows
+  std::vector<size_t> wf_off;
+  uint64_t out_gen = 0;
 };
 
 namespace {
@@ -69,8 +81,26 @@ uint32_t scaled_frames(const rd_config& c, uint32_t launch_frames) {
   return (uint32_t)std::max<uint64_t>(1u, std::min<uint64_t>(f, c.max_frames));
 }
 
+// Scenario i's results into its registered host buffers, on s after its
+// launches (rd::chain_export: the events and flits by a kernel through the
+// mapped views, the window flags and sums by copies).
+rd_status export_one(rd_batch* b, uint32_t i, cudaStream_t s) {
+  const rd_output& o = b->outs[i];
+  const rd_config& c = b->cfgs[i];
+  const uint32_t nfl = rd_detection_flits(c.packet_w);
+  uint64_t cap = o.cap_events;
+  if (b->out_fl[i]) cap = std::min<uint64_t>(cap, o.cap_flits / nfl);
+  const rd::ExportDst d{b->hdr_dev + i,         b->out_ev[i], b->out_fl[i],
+                        cap,                    b->wflags + b->wf_off[i],
+                        o.cap_cov_windows,      o.cov_acc,
+                        o.cov_acc ? (size_t)o.cap_cov_windows * rd::chain_window_words(b->chains[i])
+                                  : 0u};
+  return rd::chain_export(b->chains[i], d, s);
+}
+
 // Enqueues one full run on `root`: fork to the worker streams, reset and
-// process every scenario on its stream, join back.
+// process every scenario on its stream (exporting its results when outputs
+// are registered), join back.
 rd_status enqueue(rd_batch* b, const rd_cplx16* const* adc, const uint64_t* n, cudaStream_t root,
                   const rd_batch_options& o) {
   const uint32_t ns = std::max(1u, std::min<uint32_t>(o.n_streams, (uint32_t)b->streams.size()));
@@ -97,6 +127,7 @@ rd_status enqueue(rd_batch* b, const rd_cplx16* const* adc, const uint64_t* n, c
     for (uint32_t i : per[k]) {
       BS(rd_chain_reset(b->chains[i], b->streams[k]));
       BS(rd_chain_process_device(b->chains[i], adc[i], n[i], n[i], b->streams[k]));
+      if (!b->outs.empty()) BS(export_one(b, i, b->streams[k]));
     }
   for (uint32_t k = 0; k < ns; ++k) {
     BK(cudaEventRecord(b->ev, b->streams[k]));
@@ -127,6 +158,7 @@ rd_status capture(rd_batch* b, const rd_cplx16* const* adc, const uint64_t* n,
   b->cap_adc.assign(adc, adc + b->chains.size());
   b->cap_n.assign(n, n + b->chains.size());
   b->cap_opt = o;
+  b->cap_out_gen = b->out_gen;
   return RD_OK;
 }
 
@@ -148,7 +180,8 @@ rd_status run_with(rd_batch* b, const rd_cplx16* const* adc, const uint64_t* n, 
     drop_graph(b);
   } else {
     const bool reuse = b->exec && same_inputs(b, adc, n) && b->cap_opt.n_streams == o.n_streams &&
-                       b->cap_opt.launch_frames == o.launch_frames;
+                       b->cap_opt.launch_frames == o.launch_frames &&
+                       b->cap_out_gen == b->out_gen;
     if (!reuse) BS(capture(b, adc, n, o));
     BK(cudaGraphLaunch(b->exec, b->root));
   }
@@ -198,10 +231,27 @@ rd_status rd_batch_create(uint32_t n, const rd_config* cfgs, const rd_cplx16* co
   return RD_OK;
 }
 
+namespace {
+
+void free_outputs(rd_batch* b) {
+  if (b->hdr) cudaFreeHost(b->hdr);
+  if (b->wflags) cudaFreeHost(b->wflags);
+  b->hdr = b->hdr_dev = nullptr;
+  b->wflags = nullptr;
+  b->outs.clear();
+  b->out_ev.clear();
+  b->out_fl.clear();
+  b->wf_off.clear();
+}
+
+}  // namespace
+
 void rd_batch_destroy(rd_batch* b) {
   if (!b) return;
   if (b->root) cudaStreamSynchronize(b->root);
+  if (b->last) cudaStreamSynchronize(b->last);
   drop_graph(b);
+  free_outputs(b);
   for (rd_chain* ch : b->chains) rd_chain_destroy(ch);
   for (cudaStream_t s : b->streams)
     if (s) cudaStreamDestroy(s);
@@ -229,6 +279,98 @@ rd_status rd_batch_run_sequential(rd_batch* b, const rd_cplx16* const* adc_dev,
   }
   b->last = s;
   return RD_OK;
+}
+
+rd_status rd_batch_set_outputs(rd_batch* b, const rd_output* outs) {
+  if (!b) return rd::set_error(RD_EINVAL, "rd_batch_set_outputs: null batch");
+  if (b->last) BK(cudaStreamSynchronize(b->last));  // no run still writes the old ones
+  drop_graph(b);
+  free_outputs(b);
+  ++b->out_gen;
+  if (!outs) return RD_OK;
+  const size_t n = b->chains.size();
+  std::vector<rd_event*> ev(n, nullptr);
+  std::vector<uint32_t*> fl(n, nullptr);
+  std::vector<size_t> off(n + 1, 0);
+  for (size_t i = 0; i < n; ++i) {
+    const rd_output& o = outs[i];
+    void* d = nullptr;
+    if (!o.events || cudaHostGetDevicePointer(&d, o.events, 0) != cudaSuccess) {
+      cudaGetLastError();
+      return rd::set_error(RD_EINVAL, "rd_batch_set_outputs: scenario %zu: events are not "
+                           "mapped page-locked memory", i);
+    }
+    ev[i] = static_cast<rd_event*>(d);
+    if (o.flits) {
+      if (cudaHostGetDevicePointer(&d, o.flits, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return rd::set_error(RD_EINVAL, "rd_batch_set_outputs: scenario %zu: flits are not "
+                             "mapped page-locked memory", i);
+      }
+      fl[i] = static_cast<uint32_t*>(d);
+    }
+    if (o.cov_acc) {
+      cudaPointerAttributes a{};
+      if (cudaPointerGetAttributes(&a, o.cov_acc) != cudaSuccess || a.type != cudaMemoryTypeHost) {
+        cudaGetLastError();
+        return rd::set_error(RD_EINVAL, "rd_batch_set_outputs: scenario %zu: cov_acc is not "
+                             "page-locked memory", i);
+      }
+    }
+    off[i + 1] = off[i] + std::max<uint32_t>(o.cap_cov_windows, 1u);
+  }
+  void* h = nullptr;
+  BK(cudaHostAlloc(&h, n * sizeof(rd::ExportHdr), cudaHostAllocMapped));
+  b->hdr = static_cast<rd::ExportHdr*>(h);
+  std::memset(b->hdr, 0, n * sizeof(rd::ExportHdr));
+  void* hd = nullptr;
+  if (cudaHostGetDevicePointer(&hd, h, 0) != cudaSuccess) {
+    free_outputs(b);
+    return rd::set_error(RD_EDEVICE, "rd_batch_set_outputs: no device view of the headers");
+  }
+  b->hdr_dev = static_cast<rd::ExportHdr*>(hd);
+  void* w = nullptr;
+  if (cudaHostAlloc(&w, off[n] * sizeof(unsigned), cudaHostAllocDefault) != cudaSuccess) {
+    free_outputs(b);
+    return rd::set_error(RD_EDEVICE, "rd_batch_set_outputs: page-locked allocation failed");
+  }
+  b->wflags = static_cast<unsigned*>(w);
+  b->outs.assign(outs, outs + n);
+  b->out_ev = ev;
+  b->out_fl = fl;
+  b->wf_off.assign(off.begin(), off.end() - 1);
+  return RD_OK;
+}
+
+rd_status rd_batch_results(rd_batch* b, uint32_t i, rd_output* out) {
+  if (!b || !out || i >= b->chains.size())
+    return rd::set_error(RD_EINVAL, "rd_batch_results: bad argument");
+  if (b->outs.empty()) return rd::set_error(RD_EINVAL, "rd_batch_results: no outputs registered");
+  if (b->last) BK(cudaStreamSynchronize(b->last));
+  const rd::ExportHdr h = b->hdr[i];
+  if (h.dev_timeout)
+    return rd::set_error(RD_ETIMEOUT, "a bounded wait inside a tensor-core kernel gave up; "
+                         "results invalid");
+  const rd_config& c = b->cfgs[i];
+  const rd_output& o = b->outs[i];
+  const uint32_t nfl = rd_detection_flits(c.packet_w);
+  uint64_t kept = std::min<uint64_t>(h.n_events, rd::chain_call_cap(b->chains[i]));
+  kept = std::min<uint64_t>(kept, o.cap_events);
+  if (o.flits) kept = std::min<uint64_t>(kept, o.cap_flits / nfl);
+  out->n_events = h.n_events;
+  out->n_flits = h.n_events * nfl;
+  out->flit_words = rd_flit_words(c.packet_w);
+  out->n_frames = rd::chain_call_frames(b->chains[i]);
+  const std::vector<rd_cov_window>& w = rd::chain_call_windows(b->chains[i]);
+  out->n_cov_windows = (uint32_t)w.size();
+  const uint32_t nw = std::min<uint32_t>((uint32_t)w.size(), out->cap_cov_windows);
+  if (out->cov_windows)
+    for (uint32_t k = 0; k < nw; ++k) {
+      out->cov_windows[k] = w[k];
+      out->cov_windows[k].sat_flags = (uint8_t)b->wflags[b->wf_off[i] + k];
+    }
+  const bool trunc = kept < h.n_events || nw < w.size();
+  return trunc ? rd::set_error(RD_ETRUNC, "output capacity exceeded") : RD_OK;
 }
 
 rd_status rd_batch_fetch(rd_batch* b, uint32_t i, rd_output* out) {

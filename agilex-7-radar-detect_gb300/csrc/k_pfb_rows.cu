@@ -7,7 +7,7 @@
 // sample and the coefficient: every sample was read by T items and every
 // coefficient by every item, and those loads took most of the kernel's
 // L1 bandwidth. Here a thread owns one phase of one channel over RF
-// consecutive output frames: its T coefficients stay in registers, and each
+// consecutive output frames (threads run over channel x phase, phase fastest): its T coefficients stay in registers, and each
 // input sample is loaded once and used by every output frame it reaches.
 //
 // The sums are int32 multiply-adds (the bank's L1 norms keep every partial
@@ -31,12 +31,14 @@ constexpr int kRF = 16;  // output frames per thread
 template <int TT, bool REAL>
 __global__ void __launch_bounds__(kPfbThreads, 4) k_pfb_rows(FrontParams p, uint32_t* out) {
   constexpr int NI = kRF + TT - 1;  // input frames of the block
+  // threads over (channel, phase), the phase fastest: a 16- or 64-point
+  // bank fills the CTA with several channels
   const unsigned N = p.N;
-  const unsigned ph = blockIdx.x * kPfbThreads + threadIdx.x;
-  const unsigned c = blockIdx.y;
+  const unsigned t = blockIdx.x * kPfbThreads + threadIdx.x;
+  const unsigned c = t / N, ph = t - c * N;
   const int f0 = (int)(blockIdx.z * kRF);
   const int F = (int)p.F;
-  const bool live = ph < N;
+  const bool live = c < p.C;
   int hr[TT], hi[TT];
 #pragma unroll
   for (int k = 0; k < TT; ++k) {
@@ -138,7 +140,8 @@ __global__ void __launch_bounds__(kPfbThreads, 4) k_pfb_rows(FrontParams p, uint
 
 template <int TT>
 void launch_t(const FrontParams& p, uint32_t* out, cudaStream_t s) {
-  const dim3 grid((p.N + kPfbThreads - 1u) / kPfbThreads, p.C, (p.F + kRF - 1u) / kRF);
+  const dim3 grid((unsigned)(((uint64_t)p.C * p.N + kPfbThreads - 1u) / kPfbThreads), 1u,
+                  (p.F + kRF - 1u) / kRF);
   if (p.coeff_real)
     k_pfb_rows<TT, true><<<grid, kPfbThreads, 0, s>>>(p, out);
   else

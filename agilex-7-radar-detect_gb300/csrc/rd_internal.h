@@ -279,6 +279,8 @@ rd_status chain_export(rd_chain* ch, const ExportDst& d, cudaStream_t s);
 // device until exported) and its event capacity.
 const std::vector<rd_cov_window>& chain_call_windows(const rd_chain* ch);
 uint64_t chain_call_cap(const rd_chain* ch);
+// Frames of the chain's last call.
+uint64_t chain_call_frames(const rd_chain* ch);
 // Words of one closed window's sums: n_fft x pairs x (re, im).
 size_t chain_window_words(const rd_chain* ch);
 

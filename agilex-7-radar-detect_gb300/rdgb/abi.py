@@ -194,6 +194,8 @@ def declare_rd(lib) -> None:
     _proto(lib, "rd_batch_run", I32, [VP, VP, VP, VP])
     _proto(lib, "rd_batch_run_sequential", I32, [VP, VP, VP, VP])
     _proto(lib, "rd_batch_fetch", I32, [VP, U32, P(RdOutput)])
+    _proto(lib, "rd_batch_set_outputs", I32, [VP, P(RdOutput)])
+    _proto(lib, "rd_batch_results", I32, [VP, U32, P(RdOutput)])
     _proto(lib, "rd_batch_tune", I32, [VP, VP, VP, U32, P(RdBatchOptions), P(C.c_double)])
     _proto(lib, "rd_batch_tune_cached", I32, [VP, VP, VP, U32, C.c_char_p, P(RdBatchOptions),
                                               P(C.c_double), P(C.c_int)])
@@ -231,7 +233,7 @@ EXPORTED = [
     "rd_chain_reset", "rd_chain_set_launch_frames", "rd_chain_footprint", "rd_chain_doppler",
     "rd_egress_merge", "rd_route_path",
     "rd_batch_create", "rd_batch_destroy", "rd_batch_run", "rd_batch_run_sequential",
-    "rd_batch_fetch", "rd_batch_tune", "rd_batch_tune_cached", "rd_batch_egress", "rd_server_create",
+    "rd_batch_fetch", "rd_batch_set_outputs", "rd_batch_results", "rd_batch_tune", "rd_batch_tune_cached", "rd_batch_egress", "rd_server_create",
     "rd_server_destroy", "rd_stream_open",
     "rd_stream_close", "rd_stream_set_pairs", "rd_server_submit", "rd_server_poll", "rd_server_take",
     "rd_server_info_get", "rd_server_run_trace", "rd_chain_read_history", "rd_pfb_run",

@@ -22,6 +22,7 @@ class Batch:
         cp = (C.c_void_p * n)(*[c.ctypes.data for c in self._coeff])
         wp = (C.c_void_p * n)(*[w.ctypes.data for w in self._w])
         self.opt = abi.RdBatchOptions(n_streams, launch_frames, 1 if use_graph else 0)
+        self._outs = None
         self.h = C.c_void_p()
         abi.check(self.L, self.L.rd_batch_create(n, arr, cp, wp, C.byref(self.opt),
                                                  C.byref(self.h)), "rd_batch_create")
@@ -58,6 +59,26 @@ class Batch:
     def fetch(self, i: int, frames: int, n_pairs: int) -> dict:
         out = Outputs(self.cfgs[i], frames, n_pairs, False, None)
         abi.check(self.L, self.L.rd_batch_fetch(self.h, i, C.byref(out.c)), "rd_batch_fetch")
+        return out.result()
+
+    def set_outputs(self, outs: list | None) -> None:
+        """rd_batch_set_outputs: every run writes scenario i's results into
+        outs[i] (an Outputs over page-locked host arrays); None stops it."""
+        if outs is None:
+            abi.check(self.L, self.L.rd_batch_set_outputs(self.h, None), "rd_batch_set_outputs")
+            self._outs = None
+            return
+        arr = (abi.RdOutput * len(outs))(*[o.c for o in outs])
+        abi.check(self.L, self.L.rd_batch_set_outputs(self.h, arr), "rd_batch_set_outputs")
+        self._outs = list(outs)  # the arrays stay alive while registered
+
+    def results(self, i: int, check: bool = True) -> dict:
+        """rd_batch_results: scenario i's results of the last run, from its
+        registered Outputs (no device read)."""
+        out = self._outs[i]
+        st = self.L.rd_batch_results(self.h, i, C.byref(out.c))
+        if check:
+            abi.check(self.L, st, "rd_batch_results")
         return out.result()
 
     def egress(self, n_ports: int, ring: int, cap_per_port: int, port_count: int,

@@ -338,6 +338,16 @@ def run_forms(torch, a, stream) -> dict:
     return out
 
 
+def pinned_alloc(torch):
+    """An Outputs allocator of page-locked host arrays: the device writes
+    the results by DMA."""
+    def alloc(shape, dtype):
+        dt = np.dtype(dtype)
+        k = int(np.prod(shape)) * dt.itemsize
+        return torch.empty(k, dtype=torch.uint8, pin_memory=True).numpy().view(dt).reshape(shape)
+    return alloc
+
+
 def run_batching(torch, n_scen: int = 256, runs: int = 5) -> dict:
     """256 independent scenarios of seeded uneven geometry: one autotuned
     graph replay against the scenarios one after another on one stream."""
@@ -383,28 +393,45 @@ def run_batching(torch, n_scen: int = 256, runs: int = 5) -> dict:
     # work of the per-scenario arm below
     n_pairs = [gc.lib().rd_cov_pairs(gc.C.byref(c)) for c in cfgs]
 
+    # page-locked result buffers per scenario, sized from a first read and
+    # reused by both arms: each then times the GPU work and the results'
+    # device-to-host copies, not host allocation
+    first = [b.fetch(i, p.frames_per_cpi, n_pairs[i]) for i, p in enumerate(ps)]
+    outs = [gc.Outputs(c, p.frames_per_cpi, n_pairs[i], False,
+                       max(2 * len(f["events"]), 1024), alloc=pinned_alloc(torch))
+            for i, (c, p, f) in enumerate(zip(cfgs, ps, first))]
+    del first
+    L = gc.lib()
+
+    # the batched run writes every scenario's results into them itself, each
+    # as its launches end (rd_batch_set_outputs); the host then only reads
+    # the counts (rd_batch_results)
+    b.set_outputs(outs)
+
     def batched_fetch_once() -> float:
         torch.cuda.synchronize()
         t = time.perf_counter()
         b.run(ptrs, ns, st.cuda_stream)
-        for i, p in enumerate(ps):
-            b.fetch(i, p.frames_per_cpi, n_pairs[i])
+        for i, o in enumerate(outs):
+            abi.check(L, L.rd_batch_results(b.h, i, abi.C.byref(o.c)), "rd_batch_results")
         return 1e3 * (time.perf_counter() - t)
 
     batched_fetch_once()
     batched_fetch = min(batched_fetch_once() for _ in range(3))
     # the per-scenario API as a caller uses it: process, then read the results
     chains = [gc.Chain(c, co, w) for c, co, w in zip(cfgs, coeffs, ws)]
-    for ch, d, n in zip(chains, devs, ns):  # warm
-        ch.process_device(d.data_ptr(), n, n, st.cuda_stream)
-        ch.fetch(n // ch.cfg.n_fft)
-    torch.cuda.synchronize()
-    t = time.perf_counter()
-    for ch, d, n in zip(chains, devs, ns):
-        ch.L.rd_chain_reset(ch.h, abi_ptr(st.cuda_stream))
-        ch.process_device(d.data_ptr(), n, n, st.cuda_stream)
-        ch.fetch(n // ch.cfg.n_fft)
-    seq_fetch = 1e3 * (time.perf_counter() - t)
+
+    def sequential_fetch_once() -> float:
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for ch, d, n, o in zip(chains, devs, ns, outs):
+            ch.L.rd_chain_reset(ch.h, abi_ptr(st.cuda_stream))
+            ch.process_device(d.data_ptr(), n, n, st.cuda_stream)
+            abi.check(L, L.rd_chain_fetch(ch.h, abi.C.byref(o.c)), "rd_chain_fetch")
+        return 1e3 * (time.perf_counter() - t)
+
+    sequential_fetch_once()
+    seq_fetch = min(sequential_fetch_once() for _ in range(3))
     for ch in chains:
         ch.close()
     b.close()
@@ -421,8 +448,10 @@ def run_batching(torch, n_scen: int = 256, runs: int = 5) -> dict:
             "note": "batched: one CUDA graph replay of every scenario's launches spread "
                     "largest-first over the tuned number of streams; sequential: the same "
                     "launches stream-ordered on one stream, no host waits; with_fetch: "
-                    "every scenario's results read to the host - after the one replay "
-                    "(batched), or each before the next scenario starts (sequential)"}
+                    "every scenario's results in page-locked host buffers - written by the "
+                    "replay itself as each scenario ends (batched), or read after each "
+                    "scenario before the next starts (sequential, the per-scenario API as "
+                    "a caller uses it)"}
 
 
 def abi_ptr(v: int):
@@ -654,12 +683,7 @@ def run_gpu(a, rank: int, world: int, local: int) -> None:
     if not a.no_e2e:
         cap = max(2 * n_events, 1024)
 
-        def pinned(shape, dtype):  # page-locked result buffers: the D2H runs as DMA
-            dt = np.dtype(dtype)
-            k = int(np.prod(shape)) * dt.itemsize
-            return torch.empty(k, dtype=torch.uint8, pin_memory=True).numpy().view(dt).reshape(shape)
-
-        out = gc.Outputs(cfg, frames_total, chain.n_pairs, False, cap, alloc=pinned)
+        out = gc.Outputs(cfg, frames_total, chain.n_pairs, False, cap, alloc=pinned_alloc(torch))
         adc_ptr = abi.C.c_void_p(host.data_ptr())
         times = []
         for i in range(max(2, a.warmup) + a.steps):

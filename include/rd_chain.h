@@ -300,6 +300,18 @@ rd_status rd_batch_run(rd_batch* b, const rd_cplx16* const* adc_dev, const uint6
 rd_status rd_batch_run_sequential(rd_batch* b, const rd_cplx16* const* adc_dev,
                                   const uint64_t* n_samples, void* stream);
 rd_status rd_batch_fetch(rd_batch* b, uint32_t i, rd_output* out);
+/* Results written to host memory by every run itself, each scenario's as soon
+ * as its launches end (overlapping the other scenarios' work): outs[i] names
+ * scenario i's page-locked host buffers - events (required) and flits mapped
+ * into the device's address space (cudaHostAlloc, or cudaHostRegister with
+ * cudaHostRegisterMapped), cov_acc page-locked - and their capacities. The
+ * pointers are kept; NULL stops the export. RD_EINVAL for memory the device
+ * cannot reach. A run then needs no rd_batch_fetch: once its stream has
+ * completed, rd_batch_results fills out's counts and window headers (and
+ * returns RD_ETRUNC or RD_ETIMEOUT as rd_batch_fetch would) without reading
+ * the device. */
+rd_status rd_batch_set_outputs(rd_batch* b, const rd_output* outs);
+rd_status rd_batch_results(rd_batch* b, uint32_t i, rd_output* out);
 /* Autotuner: times every (n_streams, launch_frames) candidate on these
  * inputs (graph replays, median of `reps`), keeps the fastest and reports
  * it. */

@@ -97,6 +97,73 @@ def test_batch_tune_cache(gpulib, port, tmp_path):
     b2.close()
 
 
+def _pinned(torch):
+    def alloc(shape, dtype):
+        dt = np.dtype(dtype)
+        k = int(np.prod(shape)) * dt.itemsize
+        return torch.empty(max(k, 1), dtype=torch.uint8, pin_memory=True).numpy()[:k] \
+            .view(dt).reshape(shape)
+    return alloc
+
+
+def test_batch_exported_outputs(gpulib, port):
+    # results written to page-locked host buffers by the run itself (the graph
+    # carries the export): every scenario equals the oracle, a replay rewrites
+    # them identically, a scenario whose event capacity is too small keeps its
+    # first events and reports RD_ETRUNC, and unregistering stops the export
+    torch = pytest.importorskip("torch")
+    ps, cfgs, coeffs, ws, xs, devs = _batch_inputs(10, torch, log2_max=13)
+    ptrs = [d.data_ptr() for d in devs]
+    ns = [p.cpi_samples for p in ps]
+    n_pairs = [gc.lib().rd_cov_pairs(gc.C.byref(c)) for c in cfgs]
+    want = []
+    for i, p in enumerate(ps):
+        px, py = sc.pair_table(p)
+        want.append(port.chain(cfgs[i], coeffs[i], ws[i], px, py).process(xs[i], taps=False,
+                                                                           threads=8))
+    b = Batch(cfgs, coeffs, ws, n_streams=4, use_graph=True)
+    b.run(ptrs, ns)  # eager first run (sizes the chains' buffers)
+    small = 3  # this scenario keeps 5 events
+    outs = [gc.Outputs(c, p.frames_per_cpi, n_pairs[i], False,
+                       5 if i == small else max(2 * len(want[i]["events"]), 64),
+                       alloc=_pinned(torch))
+            for i, (c, p) in enumerate(zip(cfgs, ps))]
+    b.set_outputs(outs)
+    for rep in range(3):  # eager, captured, replayed
+        for o in outs:
+            o.events[...] = 0
+            o.flits[...] = 0
+        b.run(ptrs, ns)
+        for i in range(len(ps)):
+            if i == small:
+                st = b.L.rd_batch_results(b.h, i, gc.C.byref(outs[i].c))
+                assert st == abi.RD_ETRUNC, st
+                got = outs[i].result()
+                n_ev = len(want[i]["events"])
+                assert outs[i].c.n_events == n_ev > 5
+                assert np.array_equal(outs[i].events[:5], want[i]["events"][:5])
+                nfl = len(want[i]["flits"]) // n_ev
+                assert np.array_equal(outs[i].flits[:5 * nfl], want[i]["flits"][:5 * nfl])
+                continue
+            got = b.results(i)
+            assert diff(got, want[i], CHAIN_KEYS) == [], (rep, i)
+    # without registered outputs the run exports nothing
+    b.set_outputs(None)
+    for o in outs:
+        o.events[...] = 0
+    b.run(ptrs, ns)
+    torch.cuda.synchronize()
+    assert all(not o.events.view(np.uint8).any() for o in outs)
+    for i, p in enumerate(ps):
+        assert diff(b.fetch(i, p.frames_per_cpi, n_pairs[i]), want[i], CHAIN_KEYS) == [], i
+    # pageable memory is refused
+    bad = [gc.Outputs(c, p.frames_per_cpi, n_pairs[i], False, 64) for i, (c, p) in
+           enumerate(zip(cfgs, ps))]
+    assert b.L.rd_batch_set_outputs(b.h, (abi.RdOutput * len(bad))(*[o.c for o in bad])) == \
+        abi.RD_EINVAL
+    b.close()
+
+
 def _serve_streams():
     # mixed stream sizes; every request is 4096 samples per channel
     out = []
