@@ -863,7 +863,8 @@ static rd_status begin_call(rd_chain* ch, uint64_t frames, uint64_t cap_events) 
     // same-sized call that started on an empty window
     CK(ch->cov_out.ensure((n_win + 1) * per));
     CK(ch->win_flags.ensure(n_win + 1));
-    CK(cudaMemsetAsync(ch->win_flags.p, 0, std::max<uint64_t>(n_win, 1) * 4, ch->stream));
+    if (n_win)  // flags of the windows this call closes (none: nothing reads them)
+      CK(cudaMemsetAsync(ch->win_flags.p, 0, n_win * 4, ch->stream));
   }
   k_call_begin<<<1, 1, 0, ch->stream>>>(ch->stats.p);
   ch->launches++;
@@ -894,9 +895,13 @@ rd_status rd_chain_process_device(rd_chain* ch, const rd_cplx16* adc_dev, uint64
   // synchronise with it implicitly, so the order is made explicit both ways.
   cudaStream_t user = stream ? (cudaStream_t)stream : cudaStreamLegacy;
   // order the chain after the caller's stream (a wait uses the event's state
-  // at the call, so one event per direction serves every call)
-  CK(cudaEventRecord(ch->ev_in, user));
-  CK(cudaStreamWaitEvent(ch->stream, ch->ev_in, 0));
+  // at the call, so one event per direction serves every call); nothing to
+  // order when the caller enqueues on the chain's own stream
+  const bool same = user == ch->stream;
+  if (!same) {
+    CK(cudaEventRecord(ch->ev_in, user));
+    CK(cudaStreamWaitEvent(ch->stream, ch->ev_in, 0));
+  }
   const uint64_t frames = n / c.n_fft;
   rd_status st = begin_call(ch, frames, std::max<uint64_t>(ch->events.n, default_cap(c, frames)));
   if (st != RD_OK) return st;
@@ -908,8 +913,10 @@ rd_status rd_chain_process_device(rd_chain* ch, const rd_cplx16* adc_dev, uint64
   st = end_call(ch);
   if (st != RD_OK) return st;
   // and the caller's stream after the chain
-  CK(cudaEventRecord(ch->ev_out, ch->stream));
-  CK(cudaStreamWaitEvent(user, ch->ev_out, 0));
+  if (!same) {
+    CK(cudaEventRecord(ch->ev_out, ch->stream));
+    CK(cudaStreamWaitEvent(user, ch->ev_out, 0));
+  }
   return RD_OK;
 }
 
@@ -1751,6 +1758,8 @@ const std::vector<rd_cov_window>& rd::chain_call_windows(const rd_chain* ch) {
 uint64_t rd::chain_call_cap(const rd_chain* ch) { return ch->call_cap_events; }
 
 uint64_t rd::chain_call_frames(const rd_chain* ch) { return ch->call_frames; }
+
+cudaStream_t rd::chain_stream(const rd_chain* ch) { return ch->stream; }
 
 size_t rd::chain_window_words(const rd_chain* ch) { return (size_t)ch->cfg.n_fft * ch->P * 2; }
 

@@ -281,6 +281,9 @@ const std::vector<rd_cov_window>& chain_call_windows(const rd_chain* ch);
 uint64_t chain_call_cap(const rd_chain* ch);
 // Frames of the chain's last call.
 uint64_t chain_call_frames(const rd_chain* ch);
+// The chain's own stream: work enqueued on it is ordered with the chain's
+// launches without events (rd_chain_process_device skips its two waits).
+cudaStream_t chain_stream(const rd_chain* ch);
 // Words of one closed window's sums: n_fft x pairs x (re, im).
 size_t chain_window_words(const rd_chain* ch);
 

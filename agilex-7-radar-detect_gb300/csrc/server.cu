@@ -412,8 +412,7 @@ void rd_server_destroy(rd_server* s) {
   for (StreamState& st : s->streams)
     if (st.open) {
       cudaStreamSynchronize(st.cs);
-      rd_chain_destroy(st.ch);
-      cudaStreamDestroy(st.cs);
+      rd_chain_destroy(st.ch);  // and with it the stream
     }
   for (Slot& sl : s->slots) {
     if (sl.dev) cudaFree(sl.dev);
@@ -459,8 +458,9 @@ rd_status rd_stream_open(rd_server* s, const rd_config* cfg, const rd_cplx16* co
   st = rd_chain_create(cfg, &ss.ch);
   if (st == RD_OK) st = rd_chain_set_coeff(ss.ch, coeff);
   if (st == RD_OK) st = rd_chain_set_weights(ss.ch, weights);
-  if (st == RD_OK && cudaStreamCreateWithFlags(&ss.cs, cudaStreamNonBlocking) != cudaSuccess)
-    st = rd::set_error(RD_EDEVICE, "rd_stream_open: stream creation failed");
+  // the stream's copies, launches and export all go on the chain's own
+  // stream: no cross-stream events per request
+  if (st == RD_OK) ss.cs = rd::chain_stream(ss.ch);
   if (st == RD_OK && frames) {
     // size the chain's per-call buffers with one request of the largest
     // size, so that requests never allocate (cudaMalloc would stall the
@@ -478,7 +478,6 @@ rd_status rd_stream_open(rd_server* s, const rd_config* cfg, const rd_cplx16* co
     if (tmp) cudaFree(tmp);
   }
   if (st != RD_OK) {
-    if (ss.cs) cudaStreamDestroy(ss.cs);
     if (ss.ch) rd_chain_destroy(ss.ch);
     return st;
   }
@@ -526,8 +525,7 @@ rd_status rd_stream_close(rd_server* s, uint32_t id) {
   StreamState& st = s->streams[id];
   if (st.outstanding) return rd::set_error(RD_EAGAIN, "rd_stream_close: requests outstanding");
   cudaStreamSynchronize(st.cs);
-  rd_chain_destroy(st.ch);
-  cudaStreamDestroy(st.cs);
+  rd_chain_destroy(st.ch);  // and with it the stream
   s->used -= st.footprint;
   st = StreamState{};
   return RD_OK;
