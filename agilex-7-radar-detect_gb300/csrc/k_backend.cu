@@ -844,7 +844,9 @@ __device__ __forceinline__ unsigned decide_frame(const CfarParams& p, uint64_t u
   const unsigned words = (p.n + 31u) / 32u;  // at most 4 R
   const unsigned ca_n8 = (p.rl + p.rg) << 8;
   unsigned emitted = 0, mword = 0;
-#pragma unroll
+  // unrolled by 4, not fully: 32 copies of the step overflow the instruction
+  // cache at 1024 cells (warps then stall on instruction fetch)
+#pragma unroll 4
   for (unsigned r = 0; r < 4u * R; ++r) {
     if (r >= words) break;
     const unsigned i = r * 32u + lane;
