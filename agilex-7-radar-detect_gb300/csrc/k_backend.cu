@@ -561,14 +561,14 @@ void launch_cov(const CovParams& p, cudaStream_t s) {
 // frame's event count, its detected / suppressed counts and its first
 // detections. The grid is one persistent wave; the event counts are summed
 // per 8-frame group and per 64 groups.
-// Emit: a CTA takes 32 frames (256 when frames are at most 64 cells). Its
+// Emit: a CTA takes 64 frames (256 when frames are at most 64 cells). Its
 // first event's offset sums the block totals and group totals before it; a
 // scan of its frames' counts places every event, and each thread writes one
 // event and builds its packet in shared memory, the round's packets leaving
 // as one coalesced run.
 // ---------------------------------------------------------------------------
 constexpr unsigned kCfarWarps = 8;        // decide: warps per CTA, frames per group
-constexpr unsigned kEmitFrames = 32;      // emit: frames per CTA (frames of 65+ cells)
+constexpr unsigned kEmitFrames = 64;      // emit: frames per CTA (frames of 65+ cells)
 constexpr unsigned kCfarBlock = 64;       // groups per block total
 
 // 8-frame groups of a launch; the totals array holds their counts, then one
@@ -1191,31 +1191,24 @@ __device__ __forceinline__ void emit_one(const CfarParams& p, unsigned long long
 // holds an event or two, and 32 frames would leave most threads idle).
 template <unsigned PW, unsigned EF>
 __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_emit(CfarParams p) {
-  static_assert(EF == 32u || EF == kCfarWarps * 32u, "a warp's or the CTA's frames");
-  __shared__ unsigned long long s_red[kCfarWarps + 1], s_fbase[EF + 1];
+  static_assert(EF % 32u == 0 && EF <= kCfarWarps * 32u, "whole warps of frames, a CTA's at most");
+  __shared__ unsigned long long s_part[kCfarWarps], s_wtot[kCfarWarps], s_base, s_fbase[EF + 1];
   __shared__ unsigned s_c[EF];
   const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, tid = threadIdx.x;
   const uint64_t f0 = (uint64_t)blockIdx.x * EF;
   // events before this CTA: the launch's base, the totals of the 64-group
   // blocks before its first group's block and of that block's groups before
-  // it (read in parallel; G / 128 + 32 words a CTA on average)
+  // it (read in parallel; G / 128 + 32 words a CTA on average); and this
+  // CTA's frames' counts with their exclusive scan (a warp per 32 frames) -
+  // both behind one barrier
   {
     const uint64_t g = f0 / kCfarWarps, blk = g / kCfarBlock, groups = cfar_groups(p.frames);
     unsigned long long part = 0;
     for (uint64_t i = tid; i < blk; i += blockDim.x) part += p.totals[groups + i];
     for (uint64_t i = blk * kCfarBlock + tid; i < g; i += blockDim.x) part += p.totals[i];
     part = warp_sum64(part);
-    if (lane == 0) s_red[warp] = part;
-    __syncthreads();
-    if (tid == 0) {
-      unsigned long long b = p.stats->scan_scratch[1];
-#pragma unroll
-      for (unsigned w = 0; w < kCfarWarps; ++w) b += s_red[w];
-      s_red[kCfarWarps] = b;
-    }
-    __syncthreads();  // s_red[0..7] are rewritten by the frame scan
+    if (lane == 0) s_part[warp] = part;
   }
-  // this CTA's frames: counts and their exclusive scan (a warp per 32 frames)
   if (warp < EF / 32u) {
     const unsigned fl = warp * 32u + lane;
     const unsigned c = f0 + fl < p.frames ? p.counts[f0 + fl] : 0u;
@@ -1227,24 +1220,27 @@ __global__ void __launch_bounds__(kCfarWarps * 32) k_cfar_emit(CfarParams p) {
       if ((int)lane >= o) x += t;
     }
     s_fbase[fl] = x - c;
-    if (lane == 31) s_red[warp] = x;
+    if (lane == 31) s_wtot[warp] = x;
   }
   __syncthreads();
-  if (EF > 32u) {  // add the earlier warps' frame totals
+  {
     unsigned long long add = 0, all = 0;
 #pragma unroll
     for (unsigned w = 0; w < EF / 32u; ++w) {
-      add += w < warp ? s_red[w] : 0ull;
-      all += s_red[w];
+      add += w < warp ? s_wtot[w] : 0ull;
+      all += s_wtot[w];
     }
-    s_fbase[tid] += add;  // EF = blockDim.x: a frame a thread
-    if (tid == 0) s_fbase[EF] = all;
-    __syncthreads();
-  } else if (tid == 0) {
-    s_fbase[EF] = s_red[0];
+    if (tid < EF) s_fbase[tid] += add;  // a frame a thread
+    if (tid == 0) {
+      unsigned long long b = p.stats->scan_scratch[1];
+#pragma unroll
+      for (unsigned w = 0; w < kCfarWarps; ++w) b += s_part[w];
+      s_base = b;
+      s_fbase[EF] = all;
+    }
   }
-  if (EF == 32u) __syncthreads();
-  const unsigned long long base = s_red[kCfarWarps];
+  __syncthreads();
+  const unsigned long long base = s_base;
   const unsigned long long total = s_fbase[EF];
   if (blockIdx.x == gridDim.x - 1 && tid == 0)  // the launch's last frame is here
     p.stats->events_call = base + total;

@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(kPfbThreads, 4) k_pfb_rows(FrontParams p, uint
       xi[d] = (int)xw >> 16;
     }
   }
-  if (to && live) {
+  if (to && live && f0 + kRF + TT - 1 > F) {  // the block holds some of the last TT - 1 frames
 #pragma unroll
     for (int r = 0; r < kRF; ++r) {
       const int fi = f0 + r;
@@ -102,21 +102,25 @@ __global__ void __launch_bounds__(kPfbThreads, 4) k_pfb_rows(FrontParams p, uint
   }
   // round_sat(v, 15, 16) (q15_out32): rounded in 32 bits, saturated and
   // packed {im, re} by one cvt.pack.sat; the flags only when some output of
-  // the warp saturated
-  bool sat = false;
+  // the warp saturated. A sum v saturates exactly when v + 0x40004000 leaves
+  // [0, 2^31) (the rounded value passes 32767 from v = 0x3FFFC000 on and
+  // -32768 below v = -0x40004000), so one add and the sign bit tell it.
+  unsigned sacc = 0;
   const size_t ostep = (size_t)p.C * N;
   uint32_t* o = out + ((size_t)f0 * p.C + c) * N + ph;
+  const int nout = live ? min(kRF, F - f0) : 0;  // outputs of the thread in the chunk
 #pragma unroll
   for (int r = 0; r < kRF; ++r, o += ostep) {
     const int yr = (ar[r] + 0x3FFF + ((ar[r] >> 15) & 1)) >> 15;
     const int yi = (ai[r] + 0x3FFF + ((ai[r] >> 15) & 1)) >> 15;
     uint32_t w;
     asm("cvt.pack.sat.s16.s32 %0, %1, %2;" : "=r"(w) : "r"(yi), "r"(yr));
-    const bool in = live && f0 + r < F;
-    sat |= in && (((unsigned)(yr + 32768) | (unsigned)(yi + 32768)) > 65535u);
-    if (in) *o = w;
+    if (r < nout) {
+      *o = w;
+      sacc |= ((unsigned)ar[r] + 0x40004000u) | ((unsigned)ai[r] + 0x40004000u);
+    }
   }
-  if (__any_sync(0xffffffffu, sat)) {
+  if (__any_sync(0xffffffffu, (sacc >> 31) != 0u)) {
     unsigned fl = 0, nsat = 0;
 #pragma unroll
     for (int r = 0; r < kRF; ++r) {
