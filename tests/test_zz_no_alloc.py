@@ -51,6 +51,9 @@ def test_static_cfar_matches_allocating_entry_point(gpulib):
     cases = [
         (256, 64, _cfg(abi.RD_CFAR_CA, abi.RD_CFAR_EVENTS, 2, 2, 8, 8, 2000)),
         (1024, 37, _cfg(abi.RD_CFAR_GO, abi.RD_CFAR_DENSE, 4, 1, 16, 5, 3000)),
+        # short frames (several a warp) up to the scratch's frame limit
+        (16, abi.RD_STATIC_CFAR_MAX_FRAMES, _cfg(abi.RD_CFAR_CA, abi.RD_CFAR_EVENTS, 1, 1, 4, 4, 2600)),
+        (47, 301, _cfg(abi.RD_CFAR_GO, abi.RD_CFAR_DENSE, 1, 2, 6, 3, 1900)),
     ]
     for n, frames, cfg in cases:  # two calls in a row on the shared scratch
         cells = rng.exponential(1000.0, frames * n).astype(np.int64)
