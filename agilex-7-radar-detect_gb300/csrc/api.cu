@@ -195,7 +195,7 @@ struct rd_chain {
   cudaStream_t out_stream = nullptr;
   unsigned long long* h_snaps = nullptr;   // page-locked: events of the call after each chunk
   size_t h_snaps_n = 0;
-  cudaEvent_t ev_snap[3] = {nullptr, nullptr, nullptr};
+  std::vector<cudaEvent_t> ev_snap;        // one per chunk of a call: its snapshot landed
   bool drained_events = false, drained_flits = false;
   uint32_t drained_windows = 0;
   DevBuf<int4> w_limbs;
@@ -529,8 +529,7 @@ void rd_chain_destroy(rd_chain* ch) {
     cudaStreamDestroy(ch->out_stream);
   }
   if (ch->h_snaps) cudaFreeHost(ch->h_snaps);
-  for (int b = 0; b < 3; ++b)
-    if (ch->ev_snap[b]) cudaEventDestroy(ch->ev_snap[b]);
+  for (cudaEvent_t e : ch->ev_snap) cudaEventDestroy(e);
   ch->tw_pos.release(); ch->tw2.release(); ch->pfb_buf.release(); ch->ct_units.release(); ch->ct_pq.release();
   ch->px.release(); ch->py.release(); ch->acc_re.release(); ch->acc_im.release();
   ch->cov_out.release(); ch->sticky.release(); ch->satcnt.release(); ch->win_flags.release();
@@ -1057,9 +1056,11 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
   const uint32_t nfl = rd_detection_flits(c.packet_w);
   const size_t pk = (size_t)nfl * rd_flit_words(c.packet_w);
   if (drain) {
-    if (!ch->out_stream) {
-      CK(cudaStreamCreateWithFlags(&ch->out_stream, cudaStreamNonBlocking));
-      for (int b = 0; b < 3; ++b) CK(cudaEventCreateWithFlags(&ch->ev_snap[b], cudaEventDisableTiming));
+    if (!ch->out_stream) CK(cudaStreamCreateWithFlags(&ch->out_stream, cudaStreamNonBlocking));
+    while (ch->ev_snap.size() < n_chunks) {
+      cudaEvent_t e = nullptr;
+      CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      ch->ev_snap.push_back(e);
     }
     if (ch->h_snaps_n < n_chunks) {
       if (ch->h_snaps) CK(cudaFreeHost(ch->h_snaps));
@@ -1076,7 +1077,7 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
   std::vector<uint32_t> win_end(n_chunks, 0);  // windows closed by the end of each chunk
   // queue the copies of chunk k's results (its snapshot has landed)
   auto drain_chunk = [&](uint64_t k) -> rd_status {
-    CK(cudaEventSynchronize(ch->ev_snap[k % 3]));  // chunk k is done: its results are final
+    CK(cudaEventSynchronize(ch->ev_snap[k]));  // chunk k is done: its results are final
     const uint64_t lo = k ? ch->h_snaps[k - 1] : 0, hi = ch->h_snaps[k];
     const uint64_t e1 = std::min(hi, cap_ev), f1 = std::min(hi, cap_fl);
     if (dev_ev && e1 > lo)
@@ -1111,14 +1112,7 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
       win_end[chunk] = (uint32_t)ch->call_windows.size();
       CK(cudaMemcpyAsync(ch->h_snaps + chunk, &ch->stats.p->events_call,
                          sizeof(unsigned long long), cudaMemcpyDeviceToHost, ch->stream));
-      CK(cudaEventRecord(ch->ev_snap[chunk % 3], ch->stream));
-      // the results of the chunk two back go now: waiting for it (not for the
-      // previous one) leaves this chunk and the previous one queued, so the
-      // next chunk's input copy is issued two chunks ahead of its compute
-      if (chunk >= 2) {
-        st = drain_chunk(chunk - 2);
-        if (st != RD_OK) return st;
-      }
+      CK(cudaEventRecord(ch->ev_snap[chunk], ch->stream));
     }
     if (taps) {  // debug taps: copied out chunk by chunk
       CK(cudaStreamSynchronize(ch->stream));
@@ -1144,8 +1138,12 @@ rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint6
       }
     }
   }
+  // every chunk's copies and launches are queued before the first host wait
+  // (the input copies wait for their staging buffer on the device), so a
+  // stalled host thread stalls neither the copies in nor the compute; the
+  // results then leave chunk by chunk as each one ends
   if (drain)
-    for (uint64_t k = chunk >= 2 ? chunk - 2 : 0; k < chunk; ++k) {
+    for (uint64_t k = 0; k < n_chunks; ++k) {
       st = drain_chunk(k);
       if (st != RD_OK) return st;
     }
