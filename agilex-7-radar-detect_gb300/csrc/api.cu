@@ -268,11 +268,17 @@ enum { KT_FRONT = 0, KT_BEAM, KT_COV, KT_CFAR, KT_CALL = 7 };
 
 // Brackets one kernel launch with events on the chain's stream when stage
 // timing is on.
+// A stage's launches: an NVTX range always, CUDA events around them when
+// the chain is profiling.
+const char* const kStageNames[] = {"rd front (PFB + FFT)", "rd beamform + power",
+                                   "rd covariance", "rd CFAR + events + packets"};
+
 struct KTimer {
   rd_chain* ch;
   int id;
   cudaEvent_t a = nullptr;
-  KTimer(rd_chain* c, int i) : ch(c), id(i) {
+  rd::NvtxRange range;
+  KTimer(rd_chain* c, int i) : ch(c), id(i), range(i >= 0 && i < 4 ? kStageNames[i] : "rd call") {
     if (ch->profiling) {
       a = ch->ev_get();
       cudaEventRecord(a, ch->stream);
@@ -887,6 +893,7 @@ static uint64_t default_cap(const rd_config& c, uint64_t frames) {
 rd_status rd_chain_process_device(rd_chain* ch, const rd_cplx16* adc_dev, uint64_t n,
                                   uint64_t ld, void* stream) {
   if (!ch || !adc_dev) return fail(RD_EINVAL, "null argument");
+  rd::NvtxRange range("rd_chain_process_device");
   const rd_config& c = ch->cfg;
   if (n % c.n_fft) return fail(RD_EINVAL, "n=%llu is not a multiple of n_fft", (unsigned long long)n);
   if (ld < n) return fail(RD_EINVAL, "ld < n");
@@ -975,6 +982,7 @@ rd_status rd_chain_fetch(rd_chain* ch, rd_output* out) {
 rd_status rd_chain_process(rd_chain* ch, const rd_cplx16* adc, uint64_t n, uint64_t ld,
                            rd_output* out) {
   if (!ch || !adc || !out) return fail(RD_EINVAL, "null argument");
+  rd::NvtxRange range("rd_chain_process");
   const rd_config& c = ch->cfg;
   if (n % c.n_fft) return fail(RD_EINVAL, "n=%llu is not a multiple of n_fft", (unsigned long long)n);
   if (ld < n) return fail(RD_EINVAL, "ld < n");

@@ -172,6 +172,7 @@ bool same_inputs(const rd_batch* b, const rd_cplx16* const* adc, const uint64_t*
 // batch is eager so that every chain sizes its buffers outside a capture.
 rd_status run_with(rd_batch* b, const rd_cplx16* const* adc, const uint64_t* n, cudaStream_t s,
                    const rd_batch_options& o) {
+  rd::NvtxRange range("rd_batch_run");
   BK(cudaEventRecord(b->ev, s));
   BK(cudaStreamWaitEvent(b->root, b->ev, 0));
   if (!o.use_graph || !b->warmed) {

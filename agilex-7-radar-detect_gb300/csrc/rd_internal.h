@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <atomic>
@@ -30,6 +31,16 @@ struct PerDevice {
     f();
     if (bit) done.fetch_or(bit, std::memory_order_acq_rel);
   }
+};
+
+// A named NVTX range for its scope: the chain's stages, calls, batch runs
+// and served requests show on a profiler's timeline (nsys, ncu's range
+// filters). With no tool attached an NVTX call returns at once.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
 // Device-side cumulative statistics of one stream (zeroed at create).

@@ -257,6 +257,7 @@ rd_status start_ready(rd_server* s) {
       }
     if (slot < 0) break;
     Slot& sl = s->slots[slot];
+    rd::NvtxRange range("rd_server request start");
     const size_t words = (size_t)st.cfg.n_chan * r.n;
     SK(cudaMemcpyAsync(sl.dev, s->host[r.host_buf], words * 4, cudaMemcpyHostToDevice, st.cs));
     rd_status rs = rd_chain_process_device(st.ch, sl.dev, r.n, r.n, st.cs);
