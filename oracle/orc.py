@@ -23,7 +23,8 @@ sys.path.insert(0, str(REPO / "agilex-7-radar-detect_gb300"))
 
 from rdgb import abi  # noqa: E402
 
-LIBS = {"port": ROOT / "_build" / "liborc.so", "ref": ROOT / "_ref" / "liborc_ref.so"}
+LIBS = {"port": ROOT / "_build" / "liborc.so", "ref": ROOT / "_ref" / "liborc_ref.so",
+        "san": ROOT / "_build" / "liborc_san.so"}
 # the reference checkout: $RD_REFERENCE, else a directory named `reference`
 # beside the repository
 REF_SOURCES = Path(os.environ.get("RD_REFERENCE", str(REPO.parent / "reference")))

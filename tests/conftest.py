@@ -18,11 +18,16 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session")
 def port():
+    import os
+
     import orc
 
-    if not orc.available("port"):
-        orc.build("port")
-    return orc.Oracle("port")
+    # RD_ORACLE_LIB=san: the port built with ASan + UBSan (tests/test_sanitizers.py
+    # runs the oracle tests that way in a child process that preloads libasan)
+    which = os.environ.get("RD_ORACLE_LIB", "port")
+    if not orc.available(which):
+        orc.build(which)
+    return orc.Oracle(which)
 
 
 @pytest.fixture(scope="session")
