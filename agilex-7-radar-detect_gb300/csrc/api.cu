@@ -104,6 +104,12 @@ struct HistMirror {
   unsigned n_ant = 0, n = 0, lanes = 1, frames_max = 4, depth = 4;
   uint32_t frames_done = 0;
   unsigned done_slot = 0;
+  unsigned epoch = 0;       // depth changes so far
+  uint64_t base = 0;        // the stream frame of this epoch's frame 0 (ring slots)
+  // the stream frame last written to the model's slot 0, which a read returns
+  // when no frame is done in the epoch (the model never clears its store)
+  uint64_t slot0_frame = 0;
+  bool slot0_valid = false;
   uint32_t c_overwrite = 0, c_skew = 0, c_wbeat = 0, c_read = 0, c_collision = 0, c_error = 0;
 
   unsigned readable() const {
@@ -116,6 +122,10 @@ struct HistMirror {
     if (frames_done >= depth) sat_bump(&c_overwrite, 1);
     frames_done += 1;
     if (frames_done != 1) done_slot = (done_slot + 1 == depth) ? 0u : done_slot + 1u;
+    if ((frames_done - 1u) % depth == 0u) {  // frame j of the epoch went to slot j % depth
+      slot0_frame = base + frames_done - 1u;
+      slot0_valid = true;
+    }
   }
   struct Read {
     unsigned slot;
@@ -1298,12 +1308,194 @@ rd_status rd_chain_reset(rd_chain* ch, void* stream) {
   ch->hist.n = h0.n;
   ch->hist.lanes = h0.lanes;
   ch->hist.frames_max = h0.frames_max;
-  ch->hist.depth = h0.depth;
+  ch->hist.depth = h0.frames_max;  // a new model's depth
   ch->host_st = rd_stats{};
   ch->align_seq = 0;
   ch->call_frames = 0;
   ch->call_windows.clear();
   return RD_OK;
+}
+
+rd_status rd_chain_set_history_depth(rd_chain* ch, uint32_t frames) {
+  if (!ch) return fail(RD_EINVAL, "rd_chain_set_history_depth: null chain");
+  HistMirror& h = ch->hist;
+  h.depth = std::min<unsigned>(std::max<unsigned>(frames, 1u), h.frames_max);
+  h.epoch += 1;
+  h.frames_done = 0;
+  h.done_slot = 0;
+  h.base = ch->frame;  // the stored frames mean nothing now; new ones count from here
+  return RD_OK;
+}
+
+// ---- checkpoint / resume --------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+constexpr char kStateMagic[8] = {'r', 'd', 's', 't', 'a', 't', 'e', '1'};
+
+// The blob: this header, then DevStats, the current delay line, the current
+// covariance accumulators (re, im), sticky flags, saturation counts, and the
+// last `ring_frames` frames of the history ring, oldest first.
+struct StateHeader {
+  char magic[8];
+  uint32_t version, cfg_bytes;
+  rd_config cfg;
+  uint32_t P, ring_frames;
+  uint64_t frame;
+  uint32_t cov_count, cov_window_id, align_seq, pad;
+  HistMirror hist;
+  rd_stats host_st;
+  uint64_t tail_words, acc_words, total_bytes;
+};
+
+struct StateSizes {
+  uint64_t tail_words, acc_words, ring_frames, frame_words, total;
+};
+
+StateSizes state_sizes(const rd_chain* ch) {
+  const rd_config& c = ch->cfg;
+  StateSizes z{};
+  const uint64_t D = c.taps > 1 ? c.taps - 1u : 1u;
+  z.tail_words = (uint64_t)c.n_chan * D * c.n_fft;
+  z.acc_words = ch->P ? (uint64_t)c.n_fft * ch->P : 0u;
+  z.ring_frames = std::min<uint64_t>(std::min<uint64_t>(c.hist_frames, ch->R), ch->frame);
+  z.frame_words = (uint64_t)c.n_fft * c.n_chan;
+  z.total = sizeof(StateHeader) + sizeof(DevStats) + z.tail_words * 4 + z.acc_words * 16 +
+            z.acc_words * 4 * 3 + z.ring_frames * z.frame_words * 4;
+  return z;
+}
+
+// copies of the ring frames [frame - n, frame) between the ring and a
+// contiguous buffer, at most two runs of slots
+template <class Copy>
+rd_status ring_runs(const rd_chain* ch, uint64_t n, Copy&& copy) {
+  uint64_t f = ch->frame - n, done = 0;
+  while (done < n) {
+    const uint64_t slot = f % ch->R;
+    const uint64_t run = std::min<uint64_t>(n - done, ch->R - slot);
+    const rd_status st = copy(slot, done, run);
+    if (st != RD_OK) return st;
+    done += run;
+    f += run;
+  }
+  return RD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint64_t rd_chain_state_size(const rd_chain* ch) { return ch ? state_sizes(ch).total : 0u; }
+
+rd_status rd_chain_save_state(rd_chain* ch, void* buf, uint64_t cap) {
+  if (!ch || !buf) return fail(RD_EINVAL, "rd_chain_save_state: null argument");
+  const StateSizes z = state_sizes(ch);
+  if (cap < z.total)
+    return fail(RD_EINVAL, "rd_chain_save_state: %llu bytes, the state takes %llu",
+                (unsigned long long)cap, (unsigned long long)z.total);
+  CK(cudaStreamSynchronize(ch->stream));
+  if (ch->out_stream) CK(cudaStreamSynchronize(ch->out_stream));
+  unsigned char* p = static_cast<unsigned char*>(buf);
+  StateHeader h{};
+  std::memcpy(h.magic, kStateMagic, 8);
+  h.version = 1;
+  h.cfg_bytes = sizeof(rd_config);
+  h.cfg = ch->cfg;
+  h.P = ch->P;
+  h.ring_frames = (uint32_t)z.ring_frames;
+  h.frame = ch->frame;
+  h.cov_count = ch->cov_count;
+  h.cov_window_id = ch->cov_window_id;
+  h.align_seq = ch->align_seq;
+  h.hist = ch->hist;
+  h.host_st = ch->host_st;
+  h.tail_words = z.tail_words;
+  h.acc_words = z.acc_words;
+  h.total_bytes = z.total;
+  std::memcpy(p, &h, sizeof(h));
+  p += sizeof(h);
+  CK(cudaMemcpy(p, ch->stats.p, sizeof(DevStats), cudaMemcpyDeviceToHost));
+  p += sizeof(DevStats);
+  CK(cudaMemcpy(p, ch->tail[ch->tail_cur].p, z.tail_words * 4, cudaMemcpyDeviceToHost));
+  p += z.tail_words * 4;
+  if (z.acc_words) {
+    const size_t k = z.acc_words;
+    CK(cudaMemcpy(p, ch->acc_re.p + ch->acc_cur * k, k * 8, cudaMemcpyDeviceToHost));
+    p += k * 8;
+    CK(cudaMemcpy(p, ch->acc_im.p + ch->acc_cur * k, k * 8, cudaMemcpyDeviceToHost));
+    p += k * 8;
+    CK(cudaMemcpy(p, ch->sticky.p, k * 4, cudaMemcpyDeviceToHost));
+    p += k * 4;
+    CK(cudaMemcpy(p, ch->satcnt.p, 2 * k * 4, cudaMemcpyDeviceToHost));
+    p += 2 * k * 4;
+  }
+  const size_t fb = z.frame_words * 4;
+  return ring_runs(ch, z.ring_frames, [&](uint64_t slot, uint64_t at, uint64_t run) -> rd_status {
+    CK(cudaMemcpy(p + at * fb, ch->ring.p + slot * z.frame_words, run * fb,
+                  cudaMemcpyDeviceToHost));
+    return RD_OK;
+  });
+}
+
+rd_status rd_chain_load_state(rd_chain* ch, const void* buf, uint64_t len) {
+  if (!ch || !buf) return fail(RD_EINVAL, "rd_chain_load_state: null argument");
+  StateHeader h;
+  if (len < sizeof(h)) return fail(RD_EINVAL, "rd_chain_load_state: %llu bytes is no state",
+                                   (unsigned long long)len);
+  std::memcpy(&h, buf, sizeof(h));
+  if (std::memcmp(h.magic, kStateMagic, 8) != 0 || h.version != 1 ||
+      h.cfg_bytes != sizeof(rd_config))
+    return fail(RD_EINVAL, "rd_chain_load_state: not a chain state of this library");
+  if (std::memcmp(&h.cfg, &ch->cfg, sizeof(rd_config)) != 0 || h.P != ch->P)
+    return fail(RD_EINVAL, "rd_chain_load_state: the state is of another configuration");
+  const rd_config& c = ch->cfg;
+  const uint64_t D = c.taps > 1 ? c.taps - 1u : 1u;
+  const uint64_t frame_words = (uint64_t)c.n_fft * c.n_chan;
+  const uint64_t ring_frames =
+      std::min<uint64_t>(std::min<uint64_t>(c.hist_frames, ch->R), h.frame);
+  const uint64_t acc_words = ch->P ? (uint64_t)c.n_fft * ch->P : 0u;
+  const uint64_t total = sizeof(StateHeader) + sizeof(DevStats) +
+                         (uint64_t)c.n_chan * D * c.n_fft * 4 + acc_words * 28 +
+                         ring_frames * frame_words * 4;
+  if (h.tail_words != (uint64_t)c.n_chan * D * c.n_fft || h.acc_words != acc_words ||
+      h.ring_frames != ring_frames || h.total_bytes != total || len < total)
+    return fail(RD_EINVAL, "rd_chain_load_state: damaged or truncated state (%llu of %llu bytes)",
+                (unsigned long long)len, (unsigned long long)total);
+  CK(cudaStreamSynchronize(ch->stream));
+  if (ch->out_stream) CK(cudaStreamSynchronize(ch->out_stream));
+  const unsigned char* p = static_cast<const unsigned char*>(buf) + sizeof(h);
+  CK(cudaMemcpy(ch->stats.p, p, sizeof(DevStats), cudaMemcpyHostToDevice));
+  p += sizeof(DevStats);
+  CK(cudaMemcpy(ch->tail[0].p, p, h.tail_words * 4, cudaMemcpyHostToDevice));
+  p += h.tail_words * 4;
+  if (acc_words) {
+    const size_t k = acc_words;
+    CK(cudaMemcpy(ch->acc_re.p, p, k * 8, cudaMemcpyHostToDevice));
+    p += k * 8;
+    CK(cudaMemcpy(ch->acc_im.p, p, k * 8, cudaMemcpyHostToDevice));
+    p += k * 8;
+    CK(cudaMemcpy(ch->sticky.p, p, k * 4, cudaMemcpyHostToDevice));
+    p += k * 4;
+    CK(cudaMemcpy(ch->satcnt.p, p, 2 * k * 4, cudaMemcpyHostToDevice));
+    p += 2 * k * 4;
+  }
+  ch->tail_cur = 0;
+  ch->acc_cur = 0;
+  ch->frame = h.frame;
+  ch->cov_count = h.cov_count;
+  ch->cov_window_id = h.cov_window_id;
+  ch->align_seq = h.align_seq;
+  ch->hist = h.hist;
+  ch->host_st = h.host_st;
+  ch->call_frames = 0;
+  ch->call_windows.clear();
+  const size_t fb = frame_words * 4;
+  return ring_runs(ch, ring_frames, [&](uint64_t slot, uint64_t at, uint64_t run) -> rd_status {
+    CK(cudaMemcpy(ch->ring.p + slot * frame_words, p + at * fb, run * fb,
+                  cudaMemcpyHostToDevice));
+    return RD_OK;
+  });
 }
 
 uint64_t rd_chain_footprint(const rd_config* cfg, uint64_t frames_per_call) {
@@ -1358,6 +1550,8 @@ rd_status rd_chain_stats(const rd_chain* ch, rd_stats* st) {
   st->hist_errors = ch->hist.c_error;
   st->hist_overwrites = ch->hist.c_overwrite;
   st->hist_skew = ch->hist.c_skew;
+  st->hist_depth = ch->hist.depth;
+  st->hist_epoch = ch->hist.epoch;
   st->cfar_det = ds.cfar_det;
   st->cfar_sup = ds.cfar_sup;
   st->cfar_frames = ch->frame * ch->cfg.n_beams;
@@ -1405,10 +1599,13 @@ rd_status rd_chain_read_history(rd_chain* ch, uint32_t bin, uint32_t frame_off, 
   if (!ch || !vec || !frame_id || !flags) return fail(RD_EINVAL, "null argument");
   const HistMirror::Read r = ch->hist.locate(bin, frame_off);
   const uint32_t C = ch->cfg.n_chan, N = ch->cfg.n_fft;
-  if (r.valid_data) {
+  if (r.valid_data || ch->hist.slot0_valid) {
     // the slot holds the newest frame written to it, which is frame_id
-    // whenever frame_off is in range or clamped (history_model.hpp:294-305)
-    const uint64_t slot = (uint64_t)r.frame_id % ch->R;
+    // whenever frame_off is in range or clamped (history_model.hpp:294-305);
+    // with no frame done in this epoch the read lands on slot 0, which still
+    // holds what an earlier epoch wrote there
+    const uint64_t slot =
+        (r.valid_data ? ch->hist.base + r.frame_id : ch->hist.slot0_frame) % ch->R;
     CK(cudaStreamSynchronize(ch->stream));
     CK(cudaMemcpy(vec, ch->ring.p + (slot * N + ((bin & 0xFFFFu) % N)) * C, (size_t)C * 4,
                   cudaMemcpyDeviceToHost));

@@ -102,6 +102,7 @@ class RdStats(C.Structure):
         ("align_timeout", C.c_uint32), ("align_fault", C.c_uint32),
         ("cfar_det", C.c_uint64), ("cfar_sup", C.c_uint64), ("cfar_frames", C.c_uint64),
         ("packets", C.c_uint64), ("flits", C.c_uint64), ("next_seq", C.c_uint32),
+        ("hist_depth", C.c_uint32), ("hist_epoch", C.c_uint32),
     ]
 
     def as_dict(self) -> dict:
@@ -183,6 +184,10 @@ def declare_rd(lib) -> None:
     _proto(lib, "rd_chain_stats", I32, [VP, P(RdStats)])
     _proto(lib, "rd_chain_read_history", I32, [VP, U32, U32, VP, P(U32), P(U32)])
     _proto(lib, "rd_chain_reset", I32, [VP, VP])
+    _proto(lib, "rd_chain_set_history_depth", I32, [VP, U32])
+    _proto(lib, "rd_chain_state_size", U64, [VP])
+    _proto(lib, "rd_chain_save_state", I32, [VP, VP, U64])
+    _proto(lib, "rd_chain_load_state", I32, [VP, VP, U64])
     _proto(lib, "rd_egress_merge", I32, [P(RdEgressSource), U32, U32, U32, VP, U64, VP, VP, VP])
     _proto(lib, "rd_batch_egress", I32, [VP, U32, VP, U64, VP, VP, VP])
     _proto(lib, "rd_route_path", I32, [U32, U32, U32, U32, VP])
@@ -230,7 +235,8 @@ EXPORTED = [
     "rd_chain_set_weights", "rd_chain_set_pairs", "rd_chain_process",
     "rd_chain_process_device", "rd_chain_fetch", "rd_chain_last_launches",
     "rd_chain_flush_cov", "rd_chain_set_profiling", "rd_chain_kernel_times", "rd_chain_stats",
-    "rd_chain_reset", "rd_chain_set_launch_frames", "rd_chain_footprint", "rd_chain_doppler",
+    "rd_chain_reset", "rd_chain_set_history_depth", "rd_chain_state_size", "rd_chain_save_state", "rd_chain_load_state",
+    "rd_chain_set_launch_frames", "rd_chain_footprint", "rd_chain_doppler",
     "rd_egress_merge", "rd_route_path",
     "rd_batch_create", "rd_batch_destroy", "rd_batch_run", "rd_batch_run_sequential",
     "rd_batch_fetch", "rd_batch_set_outputs", "rd_batch_results", "rd_batch_tune", "rd_batch_tune_cached", "rd_batch_egress", "rd_server_create",

@@ -128,6 +128,19 @@ class Chain:
         abi.check(self.L, self.L.rd_chain_fetch(self.h, C.byref(out.c)), "rd_chain_fetch")
         return out.result()
 
+    def save_state(self) -> bytes:
+        """rd_chain_save_state: the stream's state as bytes (checkpoint)."""
+        n = int(self.L.rd_chain_state_size(self.h))
+        buf = C.create_string_buffer(n)
+        abi.check(self.L, self.L.rd_chain_save_state(self.h, buf, n), "rd_chain_save_state")
+        return buf.raw
+
+    def load_state(self, blob: bytes) -> None:
+        """rd_chain_load_state: continue the stream a save_state captured."""
+        buf = C.create_string_buffer(blob, len(blob))
+        abi.check(self.L, self.L.rd_chain_load_state(self.h, buf, len(blob)),
+                  "rd_chain_load_state")
+
     def last_launches(self) -> int:
         return int(self.L.rd_chain_last_launches(self.h))
 
@@ -153,6 +166,10 @@ class Chain:
         abi.check(self.L, self.L.rd_chain_doppler(self.h, n_frames, scale_sched, ptr(out),
                                                   ptr(fl)), "rd_chain_doppler")
         return out, fl
+
+    def set_history_depth(self, frames: int) -> None:
+        abi.check(self.L, self.L.rd_chain_set_history_depth(self.h, frames),
+                  "rd_chain_set_history_depth")
 
     def read_history(self, bin_: int, frame_off: int):
         vec = np.zeros(self.cfg.n_chan, np.uint32)

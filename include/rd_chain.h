@@ -164,6 +164,8 @@ typedef struct rd_stats {
   /* packets */
   uint64_t packets, flits;
   uint32_t next_seq;         /* per-VC packet sequence number (16 bits) */
+  /* history depth in frames and the depth changes so far (history_model.hpp:364-365) */
+  uint32_t hist_depth, hist_epoch;
 } rd_stats;
 
 typedef struct rd_chain rd_chain;
@@ -243,6 +245,28 @@ rd_status rd_chain_stats(const rd_chain* ch, rd_stats* st);
  * models are reset by constructing new ones). The device part is enqueued
  * on `stream` (NULL: the legacy stream), so it can be captured in a graph. */
 rd_status rd_chain_reset(rd_chain* ch, void* stream);
+
+/* hist::Model::request_depth (history_model.hpp:260-266, 435-451): the
+ * history keeps `frames` frames from now on (clamped to 1..hist_frames). The
+ * change lands at once - a call boundary is always a safe boundary, no
+ * antenna being mid-frame - and discards the history: the depth epoch
+ * advances, the frame count and slots restart, so reads report no data until
+ * new frames arrive. Counters are kept. */
+rd_status rd_chain_set_history_depth(rd_chain* ch, uint32_t frames);
+
+/* Checkpoint and resume of a stream (no reference counterpart): the state a
+ * call leaves for the next - PFB delay line, the last hist_frames frames of
+ * the history ring, the covariance accumulators and window counters, the
+ * device and host counters and the packet sequence - as one byte blob.
+ * rd_chain_state_size gives its size (0 for NULL). rd_chain_save_state
+ * waits for the chain's work, then writes it (RD_EINVAL when cap is short).
+ * rd_chain_load_state restores it into a chain created with the same
+ * rd_config and pair count, and given the same coefficients and weights; the
+ * chain then continues the saved stream bit for bit. RD_EINVAL for a blob of
+ * another configuration or a damaged one. Host memory, synchronous. */
+uint64_t rd_chain_state_size(const rd_chain* ch);
+rd_status rd_chain_save_state(rd_chain* ch, void* buf, uint64_t cap);
+rd_status rd_chain_load_state(rd_chain* ch, const void* buf, uint64_t len);
 
 /* Frames per kernel launch, 1..max_frames (default max_frames). Results do
  * not depend on it; the batch autotuner varies it. Longer launches fill more

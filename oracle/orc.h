@@ -43,6 +43,7 @@ int orc_chain_flush_cov(orc_chain* ch, rd_output* out);
 int orc_chain_stats(const orc_chain* ch, rd_stats* st);
 int orc_chain_read_history(orc_chain* ch, uint32_t bin, uint32_t frame_off,
                            rd_cplx16* vec, uint32_t* frame_id, uint32_t* flags);
+int orc_chain_set_history_depth(orc_chain* ch, uint32_t frames);
 
 /* Per-block oracles, same meaning as the rd_* entry points of rd_chain.h. */
 int orc_pfb_run(uint32_t phases, uint32_t taps, const rd_cplx16* coeff,

@@ -60,6 +60,7 @@ class Oracle:
             ("orc_chain_flush_cov", I32, [VP, P(abi.RdOutput)]),
             ("orc_chain_stats", I32, [VP, P(abi.RdStats)]),
             ("orc_chain_read_history", I32, [VP, U32, U32, VP, P(U32), P(U32)]),
+            ("orc_chain_set_history_depth", I32, [VP, U32]),
             ("orc_pfb_run", I32, [U32, U32, VP, VP, VP, U32, VP, VP]),
             ("orc_fft_run", I32, [U32, U32, U32, I32, VP, U32, VP, VP, VP]),
             ("orc_bf_run", I32, [U32, U32, VP, VP, U64, VP, VP, VP]),
@@ -278,6 +279,9 @@ class OracleChain:
         s = abi.RdStats()
         self.orc.lib.orc_chain_stats(self.h, C.byref(s))
         return s.as_dict()
+
+    def set_history_depth(self, frames: int) -> None:
+        assert self.orc.lib.orc_chain_set_history_depth(self.h, frames) == 0
 
     def read_history(self, bin_, frame_off):
         vec = np.zeros(self.cfg.n_chan, np.uint32)

@@ -718,7 +718,7 @@ typedef struct {
   uint32_t* frame;
   int* in_frame;
   uint32_t frames_done;
-  unsigned done_slot, depth;
+  unsigned done_slot, depth, epoch;
   int skew_prev, framing;
   uint32_t c_overwrite, c_skew, c_wbeat, c_read, c_collision, c_error;
 } histm;
@@ -898,7 +898,32 @@ int orc_chain_create(const rd_config* c, const rd_cplx16* coeff,
     ch->cov_im = calloc((size_t)N * (n_pairs ? n_pairs : 1), sizeof(integ));
   }
   hist_init(&ch->hist, C, N, c->spc, c->hist_frames);
+  ch->st.hist_depth = ch->hist.depth;
   *out = ch;
+  return RD_OK;
+}
+
+/* request_depth + the settle_ that lands it (history_model.hpp:260-266,
+ * 435-451): between calls no antenna is mid-frame, so it lands at once and
+ * discards the history */
+int orc_chain_set_history_depth(orc_chain* ch, uint32_t frames) {
+  histm* h = &ch->hist;
+  unsigned d = frames == 0 ? 1u : frames;
+  if (d > h->frames_max) d = h->frames_max;
+  h->depth = d;
+  h->epoch += 1;
+  h->frames_done = 0;
+  h->done_slot = 0;
+  h->skew_prev = 0;
+  for (unsigned a = 0; a < h->n_ant; ++a) {
+    h->beat[a] = 0;
+    h->slot[a] = 0;
+    h->frame[a] = 0;
+  }
+  for (unsigned i = 0; i < h->frames_max; ++i) h->resident[i] = 0xFFFFFFFFu;
+  ch->st.hist_frames_done = 0;
+  ch->st.hist_depth = h->depth;
+  ch->st.hist_epoch = h->epoch;
   return RD_OK;
 }
 
@@ -1131,7 +1156,8 @@ int orc_chain_process(orc_chain* ch, const rd_cplx16* adc, uint64_t n, uint64_t 
       unsigned fl;
       hist_read(&ch->hist, bin, 0, NULL, &fid, &fl);
       hflags_any |= fl;
-      if (fid != (uint32_t)(ch->frame + f)) { hflags_any |= 0x100; }
+      /* the frame just written: the model's ids count from the depth epoch */
+      if (fid != ch->hist.frames_done - 1u) { hflags_any |= 0x100; }
     }
     /* align: N/2 beats of bin pairs, all lanes present (align_model.hpp:321-359) */
     sat_bump(&ch->st.align_beats, N / 2);

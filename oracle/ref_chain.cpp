@@ -162,6 +162,7 @@ int orc_chain_create(const rd_config* c, const rd_cplx16* coeff,
   ac.groups = 4;
   if (!hc.valid() || !ac.valid()) return RD_EINVAL;
   orc_chain* ch = new orc_chain(*c, hc, ac);
+  ch->st.hist_depth = ch->hist.depth();
   const unsigned N = c->n_fft, T = c->taps, C = c->n_chan, B = c->n_beams;
   std::vector<Complex> cf(N * T);
   for (unsigned i = 0; i < N * T; ++i) cf[i] = cx(coeff[i]);
@@ -391,6 +392,8 @@ int orc_chain_process(orc_chain* ch, const rd_cplx16* adc, uint64_t n,
   ch->st.hist_errors = ch->hist.error_count();
   ch->st.hist_overwrites = ch->hist.overwrite_count();
   ch->st.hist_skew = ch->hist.skew_count();
+  ch->st.hist_depth = ch->hist.depth();
+  ch->st.hist_epoch = ch->hist.epoch();
   const algn::Model::Counters ac = ch->align.counters();
   ch->st.align_beats = ac.beats;
   ch->st.align_missing = ac.missing;
@@ -447,6 +450,14 @@ int orc_chain_flush_cov(orc_chain* ch, rd_output* out) {
 
 int orc_chain_stats(const orc_chain* ch, rd_stats* st) {
   *st = ch->st;
+  return RD_OK;
+}
+
+int orc_chain_set_history_depth(orc_chain* ch, uint32_t frames) {
+  ch->hist.request_depth(frames);  // lands at once: no antenna is mid-frame
+  ch->st.hist_frames_done = ch->hist.frames_done();
+  ch->st.hist_depth = ch->hist.depth();
+  ch->st.hist_epoch = ch->hist.epoch();
   return RD_OK;
 }
 

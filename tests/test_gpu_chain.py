@@ -317,3 +317,84 @@ def test_event_truncation_reports(gpulib, port):
     ch = gc.Chain(cfg, coeff, w, (px, py))
     with pytest.raises(RuntimeError, match="RD_ETRUNC"):
         ch.process(x, cap_events=5)
+
+
+@pytest.mark.parametrize("name,split,rest", [("tiny", 37, 50), ("medium", 45, 70)])
+def test_checkpoint_resume(gpulib, port, name, split, rest):
+    # a stream saved after `split` frames (inside a covariance window, with
+    # the delay line and history full) and restored into a new chain of the
+    # same configuration continues bit for bit: the next call's events,
+    # packets, windows and counters equal the oracle's uninterrupted stream,
+    # and so do the history reads and the Doppler map of the restored ring
+    p = sc.preset(name, cov_window=16)
+    cfg = sc.make_config(p, max_frames=32)
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    o = port.chain(cfg, coeff, w, px, py)
+    x1 = sc.adc(p, split * p.n_fft)
+    x2 = sc.adc(p, rest * p.n_fft, start=split * p.n_fft)
+    o.process(x1, taps=False, threads=8)
+    want = o.process(x2, taps=False, threads=8)
+    a = gc.Chain(cfg, coeff, w, (px, py))
+    a.process(x1)
+    blob = a.save_state()
+    assert len(blob) == gpulib.rd_chain_state_size(a.h)
+    a.close()
+    b = gc.Chain(cfg, coeff, w, (px, py))
+    b.load_state(blob)
+    got = b.process(x2)
+    assert diff(got, want, CHAIN_KEYS) == []
+    assert diff_stats(b.stats(), o.stats()) == []
+    # the restored ring: the history reads and the Doppler map equal a
+    # stream that never stopped
+    c = gc.Chain(cfg, coeff, w, (px, py))
+    c.process(x1)
+    c.process(x2)
+    H = cfg.hist_frames
+    for bin_, off in ((0, 0), (p.n_fft - 1, 1), (3, H - 3)):
+        vb, vc = b.read_history(bin_, off), c.read_history(bin_, off)
+        assert all(np.array_equal(u, v) if isinstance(u, np.ndarray) else u == v
+                   for u, v in zip(vb, vc)), (bin_, off)
+    db, dc = b.doppler(H), c.doppler(H)
+    assert np.array_equal(db[0], dc[0]) and np.array_equal(db[1], dc[1])
+    # a blob of another configuration, or cut short, is refused
+    cfg2 = sc.make_config(p, max_frames=16)
+    d = gc.Chain(cfg2, coeff, w, (px, py))
+    assert gpulib.rd_chain_load_state(d.h, blob, len(blob)) == abi.RD_EINVAL
+    assert gpulib.rd_chain_load_state(b.h, blob, len(blob) - 1) == abi.RD_EINVAL
+    bad = bytearray(blob)
+    bad[0] ^= 1
+    assert gpulib.rd_chain_load_state(b.h, bytes(bad), len(bad)) == abi.RD_EINVAL
+    small = (gc.C.c_char * 16)()
+    assert gpulib.rd_chain_save_state(b.h, small, 16) == abi.RD_EINVAL
+    for ch in (b, c, d):
+        ch.close()
+
+
+def test_history_depth_changes(gpulib, port):
+    # rd_chain_set_history_depth against the oracle (which the reference's
+    # own history model pins, tests/test_oracle.py): depth changes between
+    # calls, reads right after a change and after new frames, the counters,
+    # the epoch; and every call's events and windows unchanged by them
+    from test_oracle import _depth_script
+    p = sc.preset("tiny")
+    cfg = sc.make_config(p, max_frames=8)
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    g = gc.Chain(cfg, coeff, w, (px, py))
+    o = port.chain(cfg, coeff, w, px, py)
+
+    def reads(_):
+        for off in range(0, p.hist_frames + 1):
+            for bin_ in (0, 7, p.n_fft - 1):
+                vg, fg, lg = g.read_history(bin_, off)
+                vo, fo, lo = o.read_history(bin_, off)
+                assert (np.array_equal(vg, vo), fg, lg) == (True, fo, lo), (bin_, off)
+
+    _depth_script(g, o, p, reads)
+    assert g.stats()["hist_epoch"] == 6
+    # a reset returns the depth a new chain has
+    g.L.rd_chain_reset(g.h, None)
+    s = g.stats()
+    assert (s["hist_depth"], s["hist_epoch"], s["hist_frames_done"]) == (p.hist_frames, 0, 0)
+    g.close()

@@ -231,3 +231,46 @@ def test_port_matches_reference_bank_swaps(port, refo, name):
     assert diff_stats(a.stats(), b.stats()) == []
     fa, fb = a.flush_cov(), b.flush_cov()
     assert diff(fa, fb, ("cov_windows", "cov_acc")) == []
+
+
+def _depth_script(a, b, p, step_reads):
+    """Frames, depth changes and reads applied to two chains alike; every read
+    and the statistics after every step must agree."""
+    H = p.hist_frames
+    start = 0
+    for what in (("proc", 11), ("depth", 4), ("read",), ("proc", 1), ("read",), ("proc", 6),
+                 ("depth", 1), ("read",), ("proc", 3), ("depth", 2), ("proc", 5),
+                 ("depth", H + 9), ("read",), ("proc", 13), ("depth", 0), ("depth", 3),
+                 ("proc", 2)):
+        if what[0] == "proc":
+            x = sc.adc(p, what[1] * p.n_fft, start=start * p.n_fft)
+            a.process(x), b.process(x)
+            start += what[1]
+        elif what[0] == "depth":
+            a.set_history_depth(what[1]), b.set_history_depth(what[1])
+        step_reads(what)
+        assert diff_stats(a.stats(), b.stats()) == [], what
+
+
+def test_history_depth_changes(port, refo):
+    # hist::Model::request_depth (history_model.hpp:260-266, 435-451): the
+    # restatement against the reference's own model through depth changes
+    # (to 4, 1, 2, above the maximum, 0, 3) between frames - reads right
+    # after a change (no frame done: slot 0 as an earlier epoch left it), the
+    # epoch, depth and frame counters, collisions and stale flags
+    p = sc.preset("tiny")
+    cfg = sc.make_config(p)
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    a = port.chain(cfg, coeff, w, px, py)
+    b = refo.chain(cfg, coeff, w, px, py)
+
+    def reads(_):
+        for off in range(0, p.hist_frames + 1):
+            for bin_ in (0, 7, p.n_fft - 1):
+                assert [np.asarray(v).tolist() for v in a.read_history(bin_, off)] == \
+                       [np.asarray(v).tolist() for v in b.read_history(bin_, off)], (bin_, off)
+
+    _depth_script(a, b, p, reads)
+    s = a.stats()
+    assert (s["hist_depth"], s["hist_epoch"]) == (3, 6)
