@@ -119,6 +119,10 @@ struct HistMirror {
   // every antenna finished the next frame (write_beat x M each, then settle_)
   void write_frame() {
     sat_bump(&c_wbeat, (uint64_t)n_ant * (n / lanes));
+    // the antennas finish a frame one after another: at depth 1 the first to
+    // finish is a whole depth ahead of the frame count until the last one
+    // does, a skew episode per frame (history_model.hpp:425-431)
+    if (depth <= 1u && n_ant > 1u) sat_bump(&c_skew, 1);
     if (frames_done >= depth) sat_bump(&c_overwrite, 1);
     frames_done += 1;
     if (frames_done != 1) done_slot = (done_slot + 1 == depth) ? 0u : done_slot + 1u;
