@@ -233,6 +233,11 @@ struct rd_chain {
   // carries the next one out
   DevBuf<long long> acc_re, acc_im, cov_out;
   uint32_t acc_cur = 0;
+  // the beat-stream covariance engine: pairs, and [2][pairs][re, im] open
+  // window accumulators (ping-pong)
+  uint32_t eng_pairs = 0;
+  DevBuf<long long> eng_acc;
+  uint32_t eng_cur = 0;
   DevBuf<unsigned> sticky, satcnt, win_flags;
   DevBuf<uint32_t> counts, detsup, mask;   // CFAR per-frame decisions
   DevBuf<unsigned long long> totals;       // CFAR events per 8-frame group and per 64 groups
@@ -497,6 +502,16 @@ rd_status rd_chain_create(const rd_config* cfg, rd_chain** out) {
       return RD_ENOMEM;
     }
   }
+  // the beat-stream covariance engine reads the beamformer's outputs
+  ch->eng_pairs = std::min<uint32_t>(c.engine_pairs, B >= 2u ? B / 2u : 1u);
+  if (ch->eng_pairs) {
+    if (bad(ch->beams_bn.ensure((size_t)F * N * B)) ||
+        bad(ch->eng_acc.ensure(4u * ch->eng_pairs))) {
+      rd_chain_destroy(ch);
+      return RD_ENOMEM;
+    }
+    cudaMemset(ch->eng_acc.p, 0, 4u * ch->eng_pairs * sizeof(long long));
+  }
   {
     std::vector<uint32_t> tp(5u * N);
     uint32_t words = 0;
@@ -536,6 +551,7 @@ void rd_chain_destroy(rd_chain* ch) {
   if (ch->stream) cudaStreamSynchronize(ch->stream);
   ch->coeff_t.release(); ch->coeff2.release(); ch->coeff_dp.release(); ch->weights.release(); ch->w_limbs.release(); ch->w_frag.release(); ch->w_t5.release(); ch->tail[0].release(); ch->tail[1].release();
   ch->ring.release(); ch->power.release(); ch->beams_bn.release(); ch->stage.release();
+  ch->eng_acc.release();
   ch->stage2.release();
   ch->stage3.release();
   if (ch->copy_stream) cudaStreamSynchronize(ch->copy_stream);
@@ -741,6 +757,24 @@ static rd_status run_chunk(rd_chain* ch, const uint32_t* adc, uint64_t ld, uint3
       launch_beam(bp, s);
   }
   ch->launches++;
+
+  if (ch->eng_pairs) {  // the beat-stream covariance engine over this launch's beats
+    EngineParams ep{};
+    ep.beams = ch->beams_bn.p;
+    ep.N = N;
+    ep.B = B;
+    ep.pairs = ch->eng_pairs;
+    ep.beats = (uint64_t)F * (N / 2u);
+    const uint64_t done = ch->frame * (N / 2u);  // beats before this launch
+    ep.count0 = (uint32_t)(done % N);
+    ep.n_seg = (uint32_t)((ep.count0 + ep.beats + N - 1u) / N);
+    ep.acc_in = ch->eng_acc.p + (size_t)ch->eng_cur * 2u * ch->eng_pairs;
+    ep.acc_out = ch->eng_acc.p + (size_t)(ch->eng_cur ^ 1u) * 2u * ch->eng_pairs;
+    ep.stats = st;
+    launch_engine(ep, s);
+    ch->eng_cur ^= 1u;
+    ch->launches++;
+  }
 
   if (c.cov_source != RD_COV_OFF && ch->P) {
     const uint32_t wl = c.cov_window ? c.cov_window : 1u;
@@ -1301,6 +1335,8 @@ rd_status rd_chain_reset(rd_chain* ch, void* stream) {
     CK(cudaMemsetAsync(ch->sticky.p, 0, k * 4, s));
     CK(cudaMemsetAsync(ch->satcnt.p, 0, 2 * k * 4, s));
   }
+  if (ch->eng_pairs) CK(cudaMemsetAsync(ch->eng_acc.p, 0, 4u * ch->eng_pairs * sizeof(long long), s));
+  ch->eng_cur = 0;
   ch->tail_cur = 0;
   ch->acc_cur = 0;
   ch->frame = 0;
@@ -1339,8 +1375,9 @@ namespace {
 constexpr char kStateMagic[8] = {'r', 'd', 's', 't', 'a', 't', 'e', '1'};
 
 // The blob: this header, then DevStats, the current delay line, the current
-// covariance accumulators (re, im), sticky flags, saturation counts, and the
-// last `ring_frames` frames of the history ring, oldest first.
+// covariance accumulators (re, im), sticky flags, saturation counts, the
+// beat-stream engine's open-window accumulators, and the last `ring_frames`
+// frames of the history ring, oldest first.
 struct StateHeader {
   char magic[8];
   uint32_t version, cfg_bytes;
@@ -1350,11 +1387,11 @@ struct StateHeader {
   uint32_t cov_count, cov_window_id, align_seq, pad;
   HistMirror hist;
   rd_stats host_st;
-  uint64_t tail_words, acc_words, total_bytes;
+  uint64_t tail_words, acc_words, eng_words, total_bytes;
 };
 
 struct StateSizes {
-  uint64_t tail_words, acc_words, ring_frames, frame_words, total;
+  uint64_t tail_words, acc_words, eng_words, ring_frames, frame_words, total;
 };
 
 StateSizes state_sizes(const rd_chain* ch) {
@@ -1365,8 +1402,9 @@ StateSizes state_sizes(const rd_chain* ch) {
   z.acc_words = ch->P ? (uint64_t)c.n_fft * ch->P : 0u;
   z.ring_frames = std::min<uint64_t>(std::min<uint64_t>(c.hist_frames, ch->R), ch->frame);
   z.frame_words = (uint64_t)c.n_fft * c.n_chan;
+  z.eng_words = 2u * (uint64_t)ch->eng_pairs;
   z.total = sizeof(StateHeader) + sizeof(DevStats) + z.tail_words * 4 + z.acc_words * 16 +
-            z.acc_words * 4 * 3 + z.ring_frames * z.frame_words * 4;
+            z.acc_words * 4 * 3 + z.eng_words * 8 + z.ring_frames * z.frame_words * 4;
   return z;
 }
 
@@ -1416,6 +1454,7 @@ rd_status rd_chain_save_state(rd_chain* ch, void* buf, uint64_t cap) {
   h.host_st = ch->host_st;
   h.tail_words = z.tail_words;
   h.acc_words = z.acc_words;
+  h.eng_words = z.eng_words;
   h.total_bytes = z.total;
   std::memcpy(p, &h, sizeof(h));
   p += sizeof(h);
@@ -1433,6 +1472,11 @@ rd_status rd_chain_save_state(rd_chain* ch, void* buf, uint64_t cap) {
     p += k * 4;
     CK(cudaMemcpy(p, ch->satcnt.p, 2 * k * 4, cudaMemcpyDeviceToHost));
     p += 2 * k * 4;
+  }
+  if (z.eng_words) {  // the engine's open window
+    CK(cudaMemcpy(p, ch->eng_acc.p + (size_t)ch->eng_cur * z.eng_words, z.eng_words * 8,
+                  cudaMemcpyDeviceToHost));
+    p += z.eng_words * 8;
   }
   const size_t fb = z.frame_words * 4;
   return ring_runs(ch, z.ring_frames, [&](uint64_t slot, uint64_t at, uint64_t run) -> rd_status {
@@ -1459,10 +1503,12 @@ rd_status rd_chain_load_state(rd_chain* ch, const void* buf, uint64_t len) {
   const uint64_t ring_frames =
       std::min<uint64_t>(std::min<uint64_t>(c.hist_frames, ch->R), h.frame);
   const uint64_t acc_words = ch->P ? (uint64_t)c.n_fft * ch->P : 0u;
+  const uint64_t eng_words = 2u * (uint64_t)ch->eng_pairs;
   const uint64_t total = sizeof(StateHeader) + sizeof(DevStats) +
-                         (uint64_t)c.n_chan * D * c.n_fft * 4 + acc_words * 28 +
+                         (uint64_t)c.n_chan * D * c.n_fft * 4 + acc_words * 28 + eng_words * 8 +
                          ring_frames * frame_words * 4;
   if (h.tail_words != (uint64_t)c.n_chan * D * c.n_fft || h.acc_words != acc_words ||
+      h.eng_words != eng_words ||
       h.ring_frames != ring_frames || h.total_bytes != total || len < total)
     return fail(RD_EINVAL, "rd_chain_load_state: damaged or truncated state (%llu of %llu bytes)",
                 (unsigned long long)len, (unsigned long long)total);
@@ -1484,6 +1530,11 @@ rd_status rd_chain_load_state(rd_chain* ch, const void* buf, uint64_t len) {
     CK(cudaMemcpy(ch->satcnt.p, p, 2 * k * 4, cudaMemcpyHostToDevice));
     p += 2 * k * 4;
   }
+  if (eng_words) {
+    CK(cudaMemcpy(ch->eng_acc.p, p, eng_words * 8, cudaMemcpyHostToDevice));
+    p += eng_words * 8;
+  }
+  ch->eng_cur = 0;
   ch->tail_cur = 0;
   ch->acc_cur = 0;
   ch->frame = h.frame;
@@ -1525,6 +1576,10 @@ uint64_t rd_chain_footprint(const rd_config* cfg, uint64_t frames_per_call) {
     const uint64_t wl = c.cov_window ? c.cov_window : 1;
     b += (frames_per_call / wl + 1) * (N * P * 16 + 4);       // closed windows of a call
   }
+  if (c.engine_pairs) {  // the beat-stream engine: beam outputs, open windows
+    if (c.cov_source != RD_COV_BEAM) b += F * N * B * 4;
+    b += 4 * std::min<uint64_t>(c.engine_pairs, B >= 2 ? B / 2 : 1) * 8;
+  }
   const uint64_t cap = frames_per_call * B * (2 + N / 16);    // default event capacity
   b += cap * (sizeof(rd_event) + (uint64_t)rd_detection_flits(c.packet_w) *
                                      rd_flit_words(c.packet_w) * 4);
@@ -1556,6 +1611,12 @@ rd_status rd_chain_stats(const rd_chain* ch, rd_stats* st) {
   st->hist_skew = ch->hist.c_skew;
   st->hist_depth = ch->hist.depth;
   st->hist_epoch = ch->hist.epoch;
+  if (ch->eng_pairs) {  // windows of n_fft beats, n_fft / 2 beats a frame, no flush
+    const uint64_t N = ch->cfg.n_fft, beats = ch->frame * (N / 2u);
+    st->engine_window = beats >= N ? (uint32_t)((beats / N - 1u) & 0xFFFFu) : 0u;
+    st->engine_samples = beats >= N ? (uint32_t)N : 0u;
+    st->engine_sat = ds.eng_sat ? 1u : 0u;
+  }
   st->cfar_det = ds.cfar_det;
   st->cfar_sup = ds.cfar_sup;
   st->cfar_frames = ch->frame * ch->cfg.n_beams;

@@ -58,7 +58,21 @@ struct DevStats {
   unsigned long long events_call;    // events of the current call
   unsigned long long scan_scratch[4];
   unsigned dev_timeout;              // a bounded device wait gave up (tcgen05 kernels)
+  unsigned eng_sat;                  // beat-stream engine: some pair's integrator saturated
 };
+
+// ---- the beat-stream covariance engine (k_engine.cu) ------------------------
+struct EngineParams {
+  const uint32_t* beams;      // [F][N][B] packed beamformer outputs of the launch
+  uint32_t N, B, pairs;       // FFT size (window length in beats), beams, engine pairs
+  uint64_t beats;             // beats of the launch: F x N / 2
+  uint32_t count0;            // beats already in the open window
+  uint32_t n_seg;             // window segments the launch touches
+  const long long* acc_in;    // [pairs][re, im] the open window's accumulators
+  long long* acc_out;         // [pairs][re, im] after the launch (the other buffer)
+  DevStats* stats;
+};
+void launch_engine(const EngineParams& p, cudaStream_t s);
 
 // ---- front end: PFB + FFT + corner turn into the spectrum ring ------------
 struct FrontParams {

@@ -41,7 +41,8 @@ class RdConfig(C.Structure):
         "cfar_enable", "cfar_mode", "cfar_out_mode", "guard_lead", "guard_lag",
         "ref_lead", "ref_lag", "alpha", "max_guard", "max_ref",
         "cov_source", "cov_mode", "cov_exp_k", "cov_window", "cov_acc_w",
-        "cov_n_pairs", "packet_w", "src_id", "dest", "vc", "max_frames", "form")]
+        "cov_n_pairs", "packet_w", "src_id", "dest", "vc", "max_frames", "form",
+        "engine_pairs")]
 
     def as_dict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -103,6 +104,8 @@ class RdStats(C.Structure):
         ("cfar_det", C.c_uint64), ("cfar_sup", C.c_uint64), ("cfar_frames", C.c_uint64),
         ("packets", C.c_uint64), ("flits", C.c_uint64), ("next_seq", C.c_uint32),
         ("hist_depth", C.c_uint32), ("hist_epoch", C.c_uint32),
+        ("engine_window", C.c_uint32), ("engine_samples", C.c_uint32),
+        ("engine_sat", C.c_uint32),
     ]
 
     def as_dict(self) -> dict:

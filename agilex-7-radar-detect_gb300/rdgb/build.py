@@ -16,6 +16,7 @@ from . import abi
 CSRC = abi.PKG_ROOT / "csrc"
 SOURCES = ["k_frontend.cu", "k_front_fast.cu", "k_front_fast_256.cu", "k_front_fast_1024.cu",
            "k_backend.cu", "k_beam_tc.cu", "k_beam_t5.cu", "k_cov_tc.cu", "k_cov_t5.cu", "k_pfb_rows.cu",
+           "k_engine.cu",
            "cfar_static.cu", "batch.cu", "server.cu", "fabric.cu", "api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O3", "--expt-relaxed-constexpr"]

@@ -98,6 +98,12 @@ typedef struct rd_config {
   /* engine */
   uint32_t max_frames;    /* frames per internal launch (sizes device state) */
   uint32_t form;          /* RD_FORM_* of the beamformer */
+  /* the RTL's telemetry-only beat-stream covariance engine (covar_model.hpp:
+   * 318-416 as benchmark_sim_top.sv:1124-1200 wires it): pairs of beams
+   * (2p, 2p+1) mod n_beams of every beamformer beat's even bin, 40-bit block
+   * integrators over n_fft beats; 0 leaves it out, more than n_beams / 2
+   * (1 for one beam) is clamped. Its telemetry is in rd_stats. */
+  uint32_t engine_pairs;
 } rd_config;
 
 /* One CFAR event as the chain emits it. w[] holds the 176-bit event of
@@ -166,6 +172,9 @@ typedef struct rd_stats {
   uint32_t next_seq;         /* per-VC packet sequence number (16 bits) */
   /* history depth in frames and the depth changes so far (history_model.hpp:364-365) */
   uint32_t hist_depth, hist_epoch;
+  /* the beat-stream covariance engine's telemetry (benchmark_sim_top.sv:1197-1199):
+   * pair 0's last closed window id and sample count, any pair's sticky saturation */
+  uint32_t engine_window, engine_samples, engine_sat;
 } rd_stats;
 
 typedef struct rd_chain rd_chain;

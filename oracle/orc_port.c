@@ -872,7 +872,21 @@ struct orc_chain {
   uint32_t align_seq;
   uint64_t frame;
   rd_stats st;
+  /* the beat-stream covariance engine: pairs (2p, 2p+1) mod B */
+  unsigned eng_pairs;
+  integ eng_re[128], eng_im[128];
 };
+
+/* The RTL's telemetry-only beat-stream covariance engine (covar::Engine,
+ * covar_model.hpp:318-416, as benchmark_sim_top.sv:1124-1200 wires it): one
+ * source vector per beamformer beat - the beams of the beat's bin_par 0, the
+ * even bin 2g of beat g - pairs (2p, 2p+1) mod B, 40-bit block integrators
+ * over n_fft beats, no flush. The multiplier pipeline only delays when a
+ * product lands; between calls the clock runs on, so every beat has landed. */
+static unsigned engine_pair_count(const rd_config* c) {
+  const unsigned most = c->n_beams >= 2 ? c->n_beams / 2u : 1u;
+  return c->engine_pairs < most ? c->engine_pairs : most;
+}
 
 int orc_chain_create(const rd_config* c, const rd_cplx16* coeff,
                      const rd_cplx16* weights, const uint32_t* pair_x,
@@ -899,6 +913,7 @@ int orc_chain_create(const rd_config* c, const rd_cplx16* coeff,
   }
   hist_init(&ch->hist, C, N, c->spc, c->hist_frames);
   ch->st.hist_depth = ch->hist.depth;
+  ch->eng_pairs = engine_pair_count(c);
   *out = ch;
   return RD_OK;
 }
@@ -1181,6 +1196,30 @@ int orc_chain_process(orc_chain* ch, const rd_cplx16* adc, uint64_t n, uint64_t 
     x.cov_hdr = calloc(max_w, sizeof(integ_result));
     x.cov_wflags = calloc(max_w, sizeof(unsigned));
     parallel_for(N, threads, ph_cov, &x);
+  }
+
+  if (ch->eng_pairs) { /* the beat-stream engine, beat by beat in the beamformer's order */
+    const unsigned Pe = ch->eng_pairs;
+    for (uint64_t f = 0; f < F; ++f)
+      for (unsigned g = 0; g < N / 2u; ++g) {
+        const unsigned bin = 2u * g;
+        for (unsigned p = 0; p < Pe; ++p) {
+          const cpx a = unpack(x.beams[(f * B + (2u * p) % B) * N + bin]);
+          const cpx b = unpack(x.beams[(f * B + (2u * p + 1u) % B) * N + bin]);
+          wide re, im;
+          cross_power(a, b, &re, &im);
+          integ_result rr = {0, 0, 0, 0, 0}, ri = {0, 0, 0, 0, 0};
+          const int er = integ_step(&ch->eng_re[p], 40, N, 0, 0, 1, re, 0, &rr);
+          integ_step(&ch->eng_im[p], 40, N, 0, 0, 1, im, 0, &ri);
+          if (p == 0 && er) {
+            ch->st.engine_window = rr.window_id;
+            ch->st.engine_samples = rr.sample_count;
+          }
+        }
+      }
+    unsigned sat = 0;
+    for (unsigned p = 0; p < Pe; ++p) sat |= ch->eng_re[p].sticky | ch->eng_im[p].sticky;
+    ch->st.engine_sat = sat != 0;
   }
 
   parallel_for(F * B, threads, ph_cfar, &x);

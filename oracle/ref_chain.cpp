@@ -126,10 +126,27 @@ struct orc_chain {
   covar::Config ccfg;
   uint64_t frame = 0;
   rd_stats st;
+  // the RTL's beat-stream covariance engine as benchmark_sim_top.sv:1124-1200
+  // instantiates it (N_SRC = BEAM_PAR = n_beams, pairs (2p, 2p+1) mod n_beams,
+  // ACC_W = COVAR_POWER_W = 40, WINDOW_W = 16, CMULT_PIPE_STAGES = MULT_PIPE
+  // = 4, window FFT_SIZE beats, block mode, enable all, no flush)
+  std::vector<covar::Engine> eng;  // empty, or one engine
+  covar::Config ecfg;
+  unsigned eng_pairs = 0;
 
   orc_chain(const rd_config& c, const hist::Config& hc, const algn::Config& ac)
       : cfg(c), hist(hc), align(ac) {
     std::memset(&st, 0, sizeof(st));
+  }
+
+  // one clock of the engine; pair 0's registered result becomes the telemetry
+  void engine_step(bool valid, const std::vector<Complex>& src) {
+    const std::vector<bool> en(eng_pairs, true);
+    const std::vector<covar::PairResult> r = eng[0].step(ecfg, en, valid, src, false, false);
+    if (r[0].valid) {
+      st.engine_window = r[0].re.window_id;
+      st.engine_samples = r[0].re.sample_count;
+    }
   }
 };
 
@@ -163,6 +180,18 @@ int orc_chain_create(const rd_config* c, const rd_cplx16* coeff,
   if (!hc.valid() || !ac.valid()) return RD_EINVAL;
   orc_chain* ch = new orc_chain(*c, hc, ac);
   ch->st.hist_depth = ch->hist.depth();
+  {
+    const unsigned most = c->n_beams >= 2 ? c->n_beams / 2u : 1u;
+    ch->eng_pairs = std::min(c->engine_pairs, most);
+    if (ch->eng_pairs) {
+      ch->eng.emplace_back(c->n_beams, ch->eng_pairs, 40u, 16u, 4u);
+      for (unsigned p = 0; p < ch->eng_pairs; ++p)
+        ch->eng[0].set_table(p, covar::PairEntry{(2u * p) % c->n_beams, (2u * p + 1u) % c->n_beams});
+      ch->ecfg.window_len = c->n_fft;
+      ch->ecfg.mode = covar::Mode::kBlock;
+      ch->eng[0].reset(ch->ecfg);
+    }
+  }
   const unsigned N = c->n_fft, T = c->taps, C = c->n_chan, B = c->n_beams;
   std::vector<Complex> cf(N * T);
   for (unsigned i = 0; i < N * T; ++i) cf[i] = cx(coeff[i]);
@@ -285,6 +314,11 @@ int orc_chain_process(orc_chain* ch, const rd_cplx16* adc, uint64_t n,
       for (unsigned l = 0; l < 2; ++l)
         for (unsigned a = 0; a < C; ++a) bfin[l][a] = ab.data[l * C + a];
       const bf::BeamBeat bb = ch->bfm.step(bfin);
+      if (ch->eng_pairs) {  // the beat's bin_par 0 beams into the engine
+        std::vector<Complex> esrc(B);
+        for (unsigned b = 0; b < B; ++b) esrc[b] = bb.y[b][0];
+        ch->engine_step(true, esrc);
+      }
       for (unsigned l = 0; l < 2; ++l) {
         const unsigned bin = 2 * g + l;
         if (out->tap_spectrum)
@@ -383,6 +417,14 @@ int orc_chain_process(orc_chain* ch, const rd_cplx16* adc, uint64_t n,
     }
     ch->frame++;
     ch->st.frames++;
+  }
+  if (ch->eng_pairs) {  // the clock runs on after the call: every product lands
+    const std::vector<Complex> idle(B);
+    for (int k = 0; k < 4; ++k) ch->engine_step(false, idle);
+    bool sat = false;
+    for (unsigned p = 0; p < ch->eng_pairs; ++p)
+      sat = sat || ch->eng[0].re(p).sat_sticky() || ch->eng[0].im(p).sat_sticky();
+    ch->st.engine_sat = sat ? 1u : 0u;
   }
   // counters mirrored from the block models
   ch->st.hist_frames_done = ch->hist.frames_done();

@@ -398,3 +398,52 @@ def test_history_depth_changes(gpulib, port):
     s = g.stats()
     assert (s["hist_depth"], s["hist_epoch"], s["hist_frames_done"]) == (p.hist_frames, 0, 0)
     g.close()
+
+
+@pytest.mark.parametrize("case,form", [("tiny", abi.RD_FORM_CUDA_CORE),
+                                       ("medium", abi.RD_FORM_CUDA_CORE),
+                                       ("medium", abi.RD_FORM_TENSOR),
+                                       ("saturating", abi.RD_FORM_CUDA_CORE)])
+def test_beat_stream_engine(gpulib, port, case, form):
+    # the RTL's beat-stream covariance engine against the oracle (pinned to
+    # the reference's covar::Engine, tests/test_oracle.py) over a stream cut
+    # into uneven calls and launches: pair 0's last window id and count and
+    # the saturation flag after every call, the chain's own outputs unchanged;
+    # then a checkpoint inside an open engine window resumes exactly
+    from test_oracle import _engine_case
+    rng = np.random.default_rng(5)
+    p, cfg, w, x = _engine_case(case, rng)
+    cfg.form = form
+    cfg.max_frames = 3
+    px, py = sc.pair_table(p)
+    coeff = sc.coefficients(p.n_fft, p.taps)
+    g = gc.Chain(cfg, coeff, w, (px, py))
+    o = port.chain(cfg, coeff, w, px, py)
+    frames = x.shape[1] // p.n_fft
+    cuts = [0] + sorted(rng.choice(np.arange(1, frames), size=min(3, frames - 1),
+                                   replace=False).tolist()) + [frames]
+    keys = ("engine_window", "engine_samples", "engine_sat")
+    for lo, hi in zip(cuts, cuts[1:]):
+        xs = np.ascontiguousarray(x[:, lo * p.n_fft:hi * p.n_fft])
+        rg, ro = g.process(xs), o.process(xs, taps=False, threads=8)
+        assert diff(rg, ro, CHAIN_KEYS) == [], (lo, hi)
+        sg, so = g.stats(), o.stats()
+        assert [sg[k] for k in keys] == [so[k] for k in keys], (lo, hi)
+        assert diff_stats(sg, so) == [], (lo, hi)
+    if case == "saturating":
+        assert g.stats()["engine_sat"] == 1
+    # a checkpoint with an engine window open carries its accumulators
+    g2 = gc.Chain(cfg, coeff, w, (px, py))
+    o2 = port.chain(cfg, coeff, w, px, py)
+    half = max(1, frames // 2)
+    if (half * p.n_fft // 2) % p.n_fft == 0 and frames > half + 1:
+        half += 1  # inside a window
+    x1, x2 = np.ascontiguousarray(x[:, :half * p.n_fft]), np.ascontiguousarray(x[:, half * p.n_fft:])
+    g2.process(x1), o2.process(x1, taps=False, threads=8)
+    blob = g2.save_state()
+    g3 = gc.Chain(cfg, coeff, w, (px, py))
+    g3.load_state(blob)
+    g3.process(x2), o2.process(x2, taps=False, threads=8)
+    assert diff_stats(g3.stats(), o2.stats()) == []
+    for ch in (g, g2, g3):
+        ch.close()

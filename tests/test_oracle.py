@@ -274,3 +274,59 @@ def test_history_depth_changes(port, refo):
     _depth_script(a, b, p, reads)
     s = a.stats()
     assert (s["hist_depth"], s["hist_epoch"]) == (3, 6)
+
+
+def _engine_case(case, rng):
+    """(preset, config, weights, input) for the beat-stream engine's checks."""
+    if case == "tiny":
+        p = sc.preset("tiny")
+        cfg = sc.make_config(p)
+        cfg.engine_pairs = 1
+        return p, cfg, sc.steering_weights(p.n_chan, p.n_beams), sc.adc(p, 37 * p.n_fft)
+    if case == "medium":
+        p = sc.preset("medium")
+        cfg = sc.make_config(p)
+        cfg.engine_pairs = 5
+        return p, cfg, sc.steering_weights(p.n_chan, p.n_beams), sc.adc(p, 9 * p.n_fft)
+    # 1024 points, no FFT scaling and full-scale noise put the spectrum at
+    # 16-bit full scale; every beam is channel 0 (weight 32767), so a pair's
+    # cross power is |x|^2 ~ 2^31 a beat and 1024 beats pass the 40-bit
+    # integrators' range; 3 beams make the pair table wrap
+    p = sc.preset("full", n_chan=4, n_beams=3, taps=4, cov_source=abi.RD_COV_OFF)
+    cfg = sc.make_config(p)
+    cfg.scale_sched = 0
+    cfg.engine_pairs = 7  # clamped to n_beams / 2 = 1
+    w = np.zeros(p.n_beams * p.n_chan, np.uint32)
+    w[::p.n_chan] = sc.pack(32767, 0)
+    x = rng.integers(0, 2**32, size=(p.n_chan, 6 * p.n_fft), dtype=np.uint64).astype(np.uint32)
+    return p, cfg, w, x
+
+
+@pytest.mark.parametrize("case", ["tiny", "medium", "saturating"])
+def test_engine_port_matches_reference(port, refo, case):
+    # the RTL's beat-stream covariance engine (covar::Engine run as
+    # benchmark_sim_top.sv:1124-1200 wires it, inside the reference-backed
+    # oracle) against its restatement in the C oracle: the telemetry after
+    # every call of a stream cut into uneven calls
+    rng = np.random.default_rng(5)
+    p, cfg, w, x = _engine_case(case, rng)
+    px, py = sc.pair_table(p)
+    coeff = sc.coefficients(p.n_fft, p.taps)
+    a = port.chain(cfg, coeff, w, px, py)
+    b = refo.chain(cfg, coeff, w, px, py)
+    frames = x.shape[1] // p.n_fft
+    cuts = [0] + sorted(rng.choice(np.arange(1, frames), size=min(3, frames - 1),
+                                   replace=False).tolist()) + [frames]
+    for lo, hi in zip(cuts, cuts[1:]):
+        xs = np.ascontiguousarray(x[:, lo * p.n_fft:hi * p.n_fft])
+        a.process(xs, taps=False), b.process(xs, taps=False)
+        sa, sb = a.stats(), b.stats()
+        assert [sa[k] for k in ("engine_window", "engine_samples", "engine_sat")] == \
+               [sb[k] for k in ("engine_window", "engine_samples", "engine_sat")], (lo, hi)
+        assert diff_stats(sa, sb) == [], (lo, hi)
+    s = a.stats()
+    beats = frames * p.n_fft // 2
+    assert s["engine_samples"] == (p.n_fft if beats >= p.n_fft else 0)
+    assert s["engine_window"] == (beats // p.n_fft - 1 if beats >= p.n_fft else 0)
+    if case == "saturating":
+        assert s["engine_sat"] == 1
