@@ -246,12 +246,13 @@ def tiled_adc(p, n: int, block: int = 65536):
 
 
 def workload_input(torch, p, cpis: int, distinct: int, seed: int):
-    """[C][cpis x cpi_samples] ADC samples in page-locked host memory: the
-    first `distinct` CPIs of one seeded stream, repeated up to `cpis`."""
+    """[C][cpis x cpi_samples] ADC samples in page-locked host memory (plain
+    memory without a GPU): the first `distinct` CPIs of one seeded stream,
+    repeated up to `cpis`."""
     from rdgb import scenario as sc
 
     n = cpis * p.cpi_samples
-    host = torch.empty((p.n_chan, n), dtype=torch.int32, pin_memory=True)
+    host = torch.empty((p.n_chan, n), dtype=torch.int32, pin_memory=torch.cuda.is_available())
     h = host.numpy().view(np.uint32)
     d = min(distinct, cpis)
     h[:, :d * p.cpi_samples] = sc.adc(p, d * p.cpi_samples, seed=seed)
@@ -567,6 +568,18 @@ def run_reference(a, rank: int, world: int) -> None:
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(torch, dist, x: float) -> float:
+    """The largest of every rank's x - a job's time is its slowest rank's -
+    or x itself without a process group. NCCL reduces CUDA tensors, gloo CPU
+    ones."""
+    if not dist:
+        return x
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_gpu(a, rank: int, world: int, local: int) -> None:
     import torch
 
@@ -631,11 +644,7 @@ def run_gpu(a, rank: int, world: int, local: int) -> None:
                                      "avg_ms": kt[i].total_ms / max(kt[i].launches, 1),
                                      "total_ms": kt[i].total_ms} for i in range(nk.value)}
     chain.L.rd_chain_set_profiling(chain.h, 0)
-    t_max = total_ms
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
+    t_max = max_over_ranks(torch, dist, total_ms)
     value = world * samples * a.steps / (t_max / 1e3) / 1e6
 
     # roofline of the dominant kernel, and of every kernel of the chain
@@ -697,11 +706,7 @@ def run_gpu(a, rank: int, world: int, local: int) -> None:
         words = (cfg.packet_w + 5 + 31) // 32
         d2h = (out.c.n_events * 32 + out.c.n_flits * words * 4 +
                out.c.n_cov_windows * (16 + p.n_fft * chain.n_pairs * 16))
-        e2e_ms = ms
-        if dist:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_ms = float(t.item())
+        e2e_ms = max_over_ranks(torch, dist, ms)
         e2e = {"value": round(world * samples / (e2e_ms / 1e3) / 1e6, 3), "unit": UNIT,
                "h2d_bytes_per_step": samples * 4, "d2h_bytes_per_step": int(d2h),
                "ms_per_step": round(e2e_ms, 3),
