@@ -917,6 +917,21 @@ class Chain {
     return status(rd_chain_process(h_, adc, n, ld, out));
   }
   rd_status flush_cov(rd_output* out) { return status(rd_chain_flush_cov(h_, out)); }
+  // hist::Model::request_depth (history_model.hpp:260-266): lands at once
+  rd_status request_depth(uint32_t frames) {
+    return status(rd_chain_set_history_depth(h_, frames));
+  }
+  rd_status reset() { return status(rd_chain_reset(h_, nullptr)); }
+  // checkpoint / resume: the stream's state as bytes, and back into a chain
+  // of the same configuration (empty on failure; see rdgb::last_status)
+  std::vector<uint8_t> save_state() {
+    std::vector<uint8_t> b(h_ ? rd_chain_state_size(h_) : 0u);
+    if (!h_ || status(rd_chain_save_state(h_, b.data(), b.size())) != RD_OK) b.clear();
+    return b;
+  }
+  rd_status load_state(const std::vector<uint8_t>& b) {
+    return status(rd_chain_load_state(h_, b.data(), b.size()));
+  }
   rd_stats stats() const {
     rd_stats s{};
     detail::record(rd_chain_stats(h_, &s));

@@ -263,6 +263,30 @@ void check_chain() {
   put("ch_events", ev);
   put("ch_flits", fl);
   put("ch_cov", acc);
+
+  // checkpoint: one chain takes the first half, saves, a new chain loads the
+  // state and takes the rest (its events go out for comparison)
+  const uint64_t h = (n / cfg.n_fft / 2) * cfg.n_fft;
+  rdgb::Chain c1(cfg, coeff, w), c2(cfg, coeff, w);
+  std::vector<rd_event> ev2(cap);
+  std::vector<uint32_t> fl2(fl.capacity());
+  std::vector<rd_cov_window> win2(nw);
+  std::vector<int64_t> acc2(static_cast<size_t>(nw) * cfg.n_fft * pairs * 2);
+  rd_output o2{};
+  o2.events = ev2.data();
+  o2.cap_events = cap;
+  o2.flits = fl2.data();
+  o2.cap_flits = cap * rd_detection_flits(cfg.packet_w);
+  o2.cov_windows = win2.data();
+  o2.cap_cov_windows = nw;
+  o2.cov_acc = acc2.data();
+  bool ck = c1.valid() && c2.valid() && c1.process(adc.data(), h, n, &o2) == RD_OK;
+  const std::vector<uint8_t> blob = c1.save_state();
+  ck = ck && !blob.empty() && c2.load_state(blob) == RD_OK;
+  ck = ck && c2.process(adc.data() + h, n - h, n, &o2) == RD_OK;
+  ev2.resize(ck ? o2.n_events : 0);
+  note("checkpoint", ck && c2.stats().frames == n / cfg.n_fft);
+  put("ck_events", ev2);
 }
 
 int loaders(int argc, char** argv) {

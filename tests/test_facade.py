@@ -256,3 +256,11 @@ def test_facade_vs_oracle(gpulib, port, prog, tmp_path, form):
     assert np.array_equal(_out(d, "ch_flits", np.uint32), ro["flits"].reshape(-1))
     assert np.array_equal(_out(d, "ch_cov", np.int64), ro["cov_acc"].reshape(-1))
     assert os.path.getsize(d / "ch_cov.out") > 0
+    # the checkpointed stream: the second half's events as one stream's
+    # second call
+    h = (adc.shape[1] // p.n_fft // 2) * p.n_fft
+    o2 = port.chain(c2, coeff, w, px, py)
+    o2.process(np.ascontiguousarray(adc[:, :h]), taps=False, threads=4)
+    r2 = o2.process(np.ascontiguousarray(adc[:, h:]), taps=False, threads=4)
+    got2 = np.fromfile(d / "ck_events.out", dtype=abi.EVENT_DTYPE)
+    assert len(got2) > 0 and np.array_equal(got2, r2["events"])
