@@ -447,3 +447,37 @@ def test_beat_stream_engine(gpulib, port, case, form):
     assert diff_stats(g3.stats(), o2.stats()) == []
     for ch in (g, g2, g3):
         ch.close()
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_depth_and_engine_random(gpulib, port, seed):
+    # the random streams of test_oracle.py's reference check, on the GPU:
+    # engine on, depth changes between uneven calls and launches, both forms
+    rng = np.random.default_rng(900 + seed)
+    name = ["tiny", "ref_tiny", "medium", "tiny"][seed]
+    p = sc.preset(name)
+    cfg = sc.make_config(p, max_frames=int(rng.integers(2, 9)),
+                         form=abi.RD_FORM_TENSOR if seed == 2 else abi.RD_FORM_CUDA_CORE)
+    cfg.engine_pairs = int(rng.integers(1, p.n_beams + 3))
+    if seed == 3:
+        cfg.scale_sched = 0
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    g = gc.Chain(cfg, coeff, w, (px, py))
+    o = port.chain(cfg, coeff, w, px, py)
+    start = 0
+    for _ in range(6):
+        if rng.integers(0, 2):
+            d = int(rng.integers(0, p.hist_frames + 3))
+            g.set_history_depth(d), o.set_history_depth(d)
+        nf = int(rng.integers(1, 20 if p.n_fft <= 64 else 6))
+        x = sc.adc(p, nf * p.n_fft, start=start * p.n_fft)
+        rg, ro = g.process(x), o.process(x, taps=False, threads=4)
+        assert diff(rg, ro, CHAIN_KEYS) == []
+        assert diff_stats(g.stats(), o.stats()) == []
+        for off in (0, 1, p.hist_frames - 1, p.hist_frames + 2):
+            vg, fg, lg = g.read_history(3, off)
+            vo, fo, lo = o.read_history(3, off)
+            assert (np.array_equal(vg, vo), fg, lg) == (True, fo, lo), off
+        start += nf
+    g.close()

@@ -330,3 +330,36 @@ def test_engine_port_matches_reference(port, refo, case):
     assert s["engine_window"] == (beats // p.n_fft - 1 if beats >= p.n_fft else 0)
     if case == "saturating":
         assert s["engine_sat"] == 1
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_depth_and_engine_random_vs_reference(port, refo, seed):
+    # random streams through both oracles with the beat-stream engine on
+    # (random pair counts, beams and window lengths) and random history depth
+    # changes between uneven calls: every read, every counter and the
+    # engine's telemetry agree with the reference's own models
+    rng = np.random.default_rng(900 + seed)
+    name = ["tiny", "ref_tiny", "medium", "tiny"][seed]
+    p = sc.preset(name)
+    cfg = sc.make_config(p)
+    cfg.engine_pairs = int(rng.integers(1, p.n_beams + 3))
+    if seed == 3:
+        cfg.scale_sched = 0  # unscaled FFT: large beams
+    px, py = sc.pair_table(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    a = port.chain(cfg, coeff, w, px, py)
+    b = refo.chain(cfg, coeff, w, px, py)
+    start = 0
+    for _ in range(6):
+        if rng.integers(0, 2):
+            d = int(rng.integers(0, p.hist_frames + 3))
+            a.set_history_depth(d), b.set_history_depth(d)
+        nf = int(rng.integers(1, 20 if p.n_fft <= 64 else 6))
+        x = sc.adc(p, nf * p.n_fft, start=start * p.n_fft)
+        ra, rb = a.process(x, taps=False), b.process(x, taps=False)
+        assert diff(ra, rb, CHAIN_KEYS) == []
+        assert diff_stats(a.stats(), b.stats()) == []
+        for off in (0, 1, p.hist_frames - 1, p.hist_frames + 2):
+            assert [np.asarray(v).tolist() for v in a.read_history(3, off)] == \
+                   [np.asarray(v).tolist() for v in b.read_history(3, off)], off
+        start += nf
