@@ -33,6 +33,10 @@ from pathlib import Path
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "agilex-7-radar-detect_gb300"))
+# 32 hardware work queues instead of the default 8, set before the CUDA
+# context exists: the batch's 32 streams and the server's streams otherwise
+# share 8 queues and wait on one another's launches (batched 17.2 -> 14.4 ms)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 import numpy as np  # noqa: E402
 

@@ -311,6 +311,10 @@ rd_status rd_chain_read_history(rd_chain* ch, uint32_t bin, uint32_t frame_off,
  * scenario is a chain; a run resets every chain and processes one input per
  * scenario, the scenarios spread largest-first over `n_streams` concurrent
  * streams, all of it captured once into a CUDA graph and replayed. */
+/* Concurrency across the batch's streams (and the server's) needs the
+ * device's hardware work queues: set CUDA_DEVICE_MAX_CONNECTIONS=32 in the
+ * environment before the process creates its CUDA context (the default 8
+ * makes streams share queues and wait on one another's launches). */
 typedef struct rd_batch rd_batch;
 typedef struct {
   uint32_t n_streams;          /* concurrent streams (0: autotune) */
