@@ -289,6 +289,26 @@ __device__ __forceinline__ void for_taps(const FrontParams& p, int T, unsigned f
   }
 }
 
+// The corner-turn tile's row skew: tile row r (frame fb, bin: r = fb N + bin)
+// starts at word r (CB + 1) + tile_skew<N>(r). The natural-order stores of a
+// warp go to bit-reversed bins, rows a power of two apart; with CB + 1 = 9 or
+// 17 words a row, up to 16 (spc 2) or 8 (spc 1) lanes of a store met in one
+// bank at N = 1024, 4 or 2 at N = 256. One pad word after every 32 rows
+// spreads them over the banks (one word a bank for CB 2^k >= 2). N is a
+// multiple of 32 there, so the skew of fb N + bin is the skew of fb N plus the
+// skew of bin. The smaller sizes keep the plain layout: it is conflict-free or
+// no worse.
+template <int N>
+__host__ __device__ __forceinline__ constexpr unsigned tile_skew(unsigned r) {
+  return N >= 256 ? r >> 5 : 0u;
+}
+
+// the tile's words: FB frames of N rows, CB + 1 words a row, plus the skew pads
+template <int N>
+__host__ __device__ __forceinline__ constexpr size_t tile_words(unsigned FB, unsigned CB) {
+  return (size_t)FB * N * (CB + 1u) + tile_skew<N>(FB * N);
+}
+
 // One pass over IPP items: PFB into registers (EXT: the PFB pass's outputs,
 // k_pfb_rows.cu, loaded), the lane sub-stages, the merge, natural-order
 // outputs into the corner-turn tile. Returns whether any value of the pass
@@ -457,10 +477,12 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
       } else {
         bfly<FL, false>(e, o, shm, ovf, fm);
       }
-      const int bin = (int)bitrev((unsigned)j, NL);
+      const unsigned bin = bitrev((unsigned)j, NL);
+      // rows bin and bin + M; M is a multiple of 32 wherever the skew is on
+      const unsigned row = bin * cbp + tile_skew<N>(bin);
       if (ok) {
-        tile_row[bin * cbp] = pk(e);
-        tile_row[(bin + M) * cbp] = pk(o);
+        tile_row[row] = pk(e);
+        tile_row[row + M * cbp + tile_skew<N>(M)] = pk(o);
       }
     }
     if (FL) sf |= fm << (2 * NL);
@@ -469,7 +491,7 @@ __device__ __forceinline__ bool front_pass_body(const FrontParams& p, int T, int
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int bin = (int)bitrev((unsigned)(base + j), NL);
-      if (ok) tile_row[bin * cbp] = b[xw(ioff, base) ^ xk(j)];
+      if (ok) tile_row[bin * cbp + tile_skew<N>(bin)] = b[xw(ioff, base) ^ xk(j)];
     }
   }
   if (FL && ok) sf_out |= sf;
@@ -512,7 +534,7 @@ __global__ void __launch_bounds__(256, EXT ? 4 : 3) k_front_fast(FrontParams p, 
   // N = 1024: in shared memory they cost a CTA per SM)
   const int2* s_tw = p.tw2;
   uint32_t* s_buf = sm;                   // [2][IPP][N]
-  uint32_t* s_tile = s_buf + 2 * IPP * N; // [FB][N][CB+1]
+  uint32_t* s_tile = s_buf + 2 * IPP * N; // [FB][N][CB+1], rows skewed (tile_skew)
   const unsigned cbp = CB + 1u;
   const int tid = threadIdx.x;
   const int item = tid / TPI, t = tid % TPI;
@@ -546,7 +568,7 @@ __global__ void __launch_bounds__(256, EXT ? 4 : 3) k_front_fast(FrontParams p, 
     const unsigned fb = it / CB, cc = it % CB;
     const unsigned f = f0 + fb, c = c0 + cc;
     const bool ok = it < n_items && f < p.F && c < p.C;
-    uint32_t* tile_row = s_tile + (size_t)fb * N * cbp + cc;
+    uint32_t* tile_row = s_tile + (size_t)fb * N * cbp + tile_skew<N>(fb * N) + cc;
     const bool big = front_pass_body<NL, SPC, TT, false, SH1, EXT>(p, T, q, tl, ok, f, c, s_tw, buf0,
                                                               buf1, ioff, tile_row, cbp, pfl, psat, sf);
     if (big)  // the exact path: saturation and per-sub-stage flags
@@ -569,7 +591,7 @@ __global__ void __launch_bounds__(256, EXT ? 4 : 3) k_front_fast(FrontParams p, 
         if (f < p.F) {
           unsigned slot = p.ring_base + f;
           if (slot >= p.ring_frames) slot -= p.ring_frames;
-          p.ring[((size_t)slot * N + bin) * p.C + c] = s_tile[r * cbp + cc];
+          p.ring[((size_t)slot * N + bin) * p.C + c] = s_tile[r * cbp + tile_skew<N>(r) + cc];
         }
       }
   } else {
@@ -581,7 +603,8 @@ __global__ void __launch_bounds__(256, EXT ? 4 : 3) k_front_fast(FrontParams p, 
       if (f < p.F && c < p.C) {
         unsigned slot = p.ring_base + f;
         if (slot >= p.ring_frames) slot -= p.ring_frames;
-        p.ring[((size_t)slot * N + bin) * p.C + c] = s_tile[((size_t)fb * N + bin) * cbp + cc];
+        const unsigned r = fb * N + bin;
+        p.ring[((size_t)slot * N + bin) * p.C + c] = s_tile[(size_t)r * cbp + tile_skew<N>(r) + cc];
       }
     }
   }
@@ -605,7 +628,7 @@ void launch_fast(const FrontParams& p, cudaStream_t s) {
   while (FB * CB < (unsigned)IPP) FB *= 2;   // at least one full pass of items
   while (FB * CB * N > 8192u && FB > 1u) FB /= 2;
   while (FB * CB * N > 8192u && CB > 1u) CB /= 2;
-  const size_t smem = (2u * IPP * N + (size_t)FB * N * (CB + 1u)) * sizeof(uint32_t);
+  const size_t smem = (2u * IPP * N + tile_words<N>(FB, CB)) * sizeof(uint32_t);
   static PerDevice attr;
   attr.once([] {
     cudaFuncSetAttribute(k_front_fast<NL, SPC, TT, SH1, EXT>,
