@@ -2,14 +2,15 @@
 checkout exists; the GPU host only reads the committed .npz files).
 
   block_vectors.npz  the reference's own golden vectors, parsed from
-                     model/vectors: fxp_ops.vec (1457 ops), cmult.vec (864
+                     model/vectors: fxp_ops.vec (1457 ops), fxp_accum.vec
+                     (251 accumulator steps in 19 sequences), cmult.vec (864
                      products), fft64.vec (36 records, N=64, spc=2) and the
                      ten pfb_<set>_<geometry>.{coeff,vec} files (96 beats each)
   chain_<name>.npz   seeded chain scenarios run through oracle/_ref (the
                      composition driver over the reference's model/cpp
                      headers): inputs, configuration and every output
 
-    python tests/golden/make_golden.py [--reference /path/to/reference]
+    python tests/golden/make_golden.py [--reference /path/to/reference] [--blocks-only]
 """
 from __future__ import annotations
 
@@ -54,6 +55,31 @@ def parse_fxp_ops(path: Path) -> dict:
         "w": np.array([int(r[5]) for r in rows], np.uint32),
         "y": np.array([int(r[6]) for r in rows], np.int64),
         "flags": np.array([int(r[7]) for r in rows], np.uint8),
+    }
+
+
+def parse_fxp_accum(path: Path) -> dict:
+    """fxp_accum.vec: sequences of saturating accumulator steps (fxp::Acc,
+    fxp.hpp:384-420), each from a cleared accumulator at its step 0; per
+    step the width, the addend, the value after it, the step's flags, the
+    sticky flags and the flagged-step count (fxp_vectors.hpp:73-90)."""
+    rows = list(_lines(path))
+    names, seq = [], []
+    for r in rows:
+        if int(r[1]) == 0:
+            names.append(r[0])
+        assert names and r[0] == names[-1], r
+        seq.append(len(names) - 1)
+    return {
+        "names": np.array(names),
+        "seq": np.array(seq, np.uint32),
+        "step": np.array([int(r[1]) for r in rows], np.uint32),
+        "w": np.array([int(r[2]) for r in rows], np.uint32),
+        "x": np.array([int(r[3]) for r in rows], np.int64),
+        "y": np.array([int(r[4]) for r in rows], np.int64),
+        "step_flags": np.array([int(r[5]) for r in rows], np.uint8),
+        "sticky": np.array([int(r[6]) for r in rows], np.uint8),
+        "count": np.array([int(r[7]) for r in rows], np.uint32),
     }
 
 
@@ -106,6 +132,8 @@ def block_vectors(ref: Path) -> dict:
     out = {}
     for k, a in parse_fxp_ops(v / "fxp_ops.vec").items():
         out[f"fxp_{k}"] = a
+    for k, a in parse_fxp_accum(v / "fxp_accum.vec").items():
+        out[f"accum_{k}"] = a
     for k, a in parse_cmult(v / "cmult.vec").items():
         out[f"cmult_{k}"] = a
     for k, a in parse_fft(v / "fft64.vec").items():
@@ -189,13 +217,17 @@ def chain_fixtures() -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=str(orc.REF_SOURCES))
+    ap.add_argument("--blocks-only", action="store_true",
+                    help="write block_vectors.npz alone (the chain fixtures stay as they are)")
     args = ap.parse_args()
     ref = Path(args.reference)
     orc.REF_SOURCES = ref
-    orc.build("port")
-    orc.build("ref")
     np.savez_compressed(HERE / "block_vectors.npz", **block_vectors(ref))
     print("block_vectors.npz written")
+    if args.blocks_only:
+        return
+    orc.build("port")
+    orc.build("ref")
     chain_fixtures()
 
 

@@ -72,6 +72,36 @@ def event_fields(ev: np.ndarray) -> dict:
             "sum": f(129, 47)}
 
 
+def accum_replay(fxp, z) -> tuple:
+    """Replays the saturating-accumulator sequences of fxp_accum.vec (fxp::Acc,
+    fxp.hpp:384-420: wrap-add, then saturate and flag at the accumulator
+    width; sticky flags OR'd, a count of flagged steps - the step
+    covar::Integrator takes in block mode, covar_model.hpp:204-262) through an
+    add-and-saturate primitive `fxp` (the oracle's or the GPU's, the call
+    signature of rd_fxp_apply). Every sequence starts from a cleared
+    accumulator; step k of all sequences goes in one call. Returns the value,
+    step flags, sticky flags and count after every row."""
+    seq, step, w, x = z["accum_seq"], z["accum_step"], z["accum_w"], z["accum_x"]
+    n = len(x)
+    assert all(step[i] == (step[i - 1] + 1 if seq[i] == seq[i - 1] else 0) for i in range(1, n))
+    n_seq = len(z["accum_names"])
+    acc = np.zeros(n_seq, np.int64)
+    sticky = np.zeros(n_seq, np.uint8)
+    cnt = np.zeros(n_seq, np.uint32)
+    y, fl = np.zeros(n, np.int64), np.zeros(n, np.uint8)
+    st, ct = np.zeros(n, np.uint8), np.zeros(n, np.uint32)
+    for k in range(int(step.max()) + 1):
+        rows = np.nonzero(step == k)[0]
+        s = seq[rows]
+        op = np.full(len(rows), abi.OP_CODE["add_sat"], np.uint32)
+        yk, fk = fxp(op, acc[s], x[rows], np.zeros(len(rows), np.uint32), w[rows])
+        acc[s] = yk
+        sticky[s] |= fk
+        cnt[s] += (fk != 0).astype(np.uint32)  # saturates at 2^32 - 1; never near here
+        y[rows], fl[rows], st[rows], ct[rows] = yk, fk, sticky[s], cnt[s]
+    return y, fl, st, ct
+
+
 def rnd(rng, n):
     return rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
 

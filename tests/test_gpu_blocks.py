@@ -3,7 +3,7 @@ vectors and the CPU oracle on seeded random and directed cases. Bit-exact."""
 import numpy as np
 import pytest
 
-from helpers import event_fields
+from helpers import accum_replay, event_fields
 from rdgb import abi, chain as gc, scenario as sc
 
 pytestmark = pytest.mark.gpu
@@ -18,6 +18,17 @@ def test_fxp_ops_vectors(gpulib, blockvec):
     y, fl = gc.fxp(z["fxp_op"], z["fxp_a"], z["fxp_b"], z["fxp_sh"], z["fxp_w"])
     assert np.array_equal(y, z["fxp_y"])
     assert np.array_equal(fl, z["fxp_flags"])
+
+
+def test_fxp_accum_vectors(gpulib, blockvec):
+    # the saturating accumulator sequences of fxp_accum.vec, step by step
+    # through the GPU's add-and-saturate
+    z = blockvec
+    y, fl, st, ct = accum_replay(gc.fxp, z)
+    assert np.array_equal(y, z["accum_y"])
+    assert np.array_equal(fl, z["accum_step_flags"])
+    assert np.array_equal(st, z["accum_sticky"])
+    assert np.array_equal(ct, z["accum_count"])
 
 
 def test_cmult_vectors(gpulib, blockvec):

@@ -6,8 +6,8 @@ import numpy as np
 import pytest
 
 from conftest import load_chain_fixture
-from helpers import (CHAIN_KEYS, TAP_KEYS, banks, cfg_from_fixture, diff, diff_stats,
-                     fixture_stats, weight_sets)
+from helpers import (CHAIN_KEYS, TAP_KEYS, accum_replay, banks, cfg_from_fixture, diff,
+                     diff_stats, fixture_stats, weight_sets)
 from rdgb import abi, scenario as sc
 from rdgb.twiddle import DIGEST, TWIDDLES
 
@@ -33,6 +33,19 @@ def test_fxp_ops_vectors(port, blockvec):
     assert len(y) == 1457
     assert np.array_equal(y, z["fxp_y"])
     assert np.array_equal(fl, z["fxp_flags"])
+
+
+def test_fxp_accum_vectors(port, blockvec):
+    # fxp_accum.vec: 19 sequences, 251 steps, widths 16-40, climbs into either
+    # rail, recoveries, the acc_w growth policy's edge cases
+    z = blockvec
+    y, fl, st, ct = accum_replay(port.fxp, z)
+    assert len(y) == 251
+    assert np.array_equal(y, z["accum_y"])
+    assert np.array_equal(fl, z["accum_step_flags"])
+    assert np.array_equal(st, z["accum_sticky"])
+    assert np.array_equal(ct, z["accum_count"])
+    assert (ct > 0).any() and (z["accum_sticky"] == 1).any() and (z["accum_sticky"] == 2).any()
 
 
 def test_cmult_vectors(port, blockvec):
