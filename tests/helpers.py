@@ -106,6 +106,60 @@ def rnd(rng, n):
     return rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
 
 
+# ---- directed and metamorphic cases of the reference's block tests ---------
+# (sim/tests/test_beamformer.cpp, test_cfar.cpp, test_covariance.cpp and
+# test_pipeline_metamorphic.cpp name them; the values below are this suite's)
+
+def rne15(v):
+    """round_sat(v, 15, 16) with ties to even (fxp.hpp:198-231), |v| < 2^47."""
+    v = np.asarray(v, np.int64)
+    q, rem = v >> 15, v & 0x7FFF
+    return np.clip(q + (rem > 0x4000) + ((rem == 0x4000) & (q & 1)), -32768, 32767)
+
+
+def hadamard_case(n_ant: int, frames: int, rng) -> tuple:
+    """A Sylvester-Hadamard weight bank (real, +-32767; beams = antennas) and
+    inputs that are each one bank row times a small s: the row's beam gets
+    round_sat(A x 32767 x s, 15, 16) and every other beam exactly 0 (the rows
+    are orthogonal and every product is exact). Returns (w, x, row, s)."""
+    h = np.array([[1]], np.int64)
+    while len(h) < n_ant:
+        h = np.block([[h, h], [h, -h]])
+    assert len(h) == n_ant
+    w = sc.pack((h * 32767).reshape(-1), np.zeros(n_ant * n_ant, np.int64))
+    row = rng.integers(0, n_ant, frames)
+    s = rng.integers(-400, 401, frames)
+    x = sc.pack((h[row] * s[:, None]).reshape(-1), np.zeros(frames * n_ant, np.int64))
+    return w, x, row, s
+
+
+def cfar_config(mode, out, gl, gg, rl, rg, alpha, mg=4, mr=16, enable=1) -> abi.RdConfig:
+    c = sc.make_config(sc.preset("tiny"))
+    c.cfar_mode, c.cfar_out_mode, c.cfar_enable = mode, out, enable
+    c.guard_lead, c.guard_lag, c.ref_lead, c.ref_lag = gl, gg, rl, rg
+    c.alpha, c.max_guard, c.max_ref = alpha, mg, mr
+    return c
+
+
+def clutter_edge_cells(n: int = 128, edge: int = 64, lo: int = 100, hi: int = 2000) -> np.ndarray:
+    """A clutter step: `lo` below bin `edge`, `hi` from it on. With guard 2,
+    reference 8 per side and alpha 1.5, CA-CFAR averages both sides and
+    detects the first high cells (their lagging reference cells are low);
+    GO-CFAR takes the greater mean (cfar_model.hpp:268-273) and detects
+    nothing."""
+    c = np.full(n, lo, np.int64)
+    c[edge:] = hi
+    return c
+
+
+def orthogonal_pair(x: np.ndarray) -> np.ndarray:
+    """j x for packed {im, re} samples whose imaginary part is not -32768:
+    x conj(j x) = -j |x|^2, a cross power with real part 0."""
+    re, im = sc.unpack(x)
+    assert (im != -32768).all()
+    return sc.pack(-im, re)
+
+
 def banks(p, rng):
     """Coefficient banks that take the PFB's three integer paths: a small-norm
     bank (byte-limb dot products), a full-range random one (int64 sums), one

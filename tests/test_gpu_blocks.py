@@ -3,7 +3,8 @@ vectors and the CPU oracle on seeded random and directed cases. Bit-exact."""
 import numpy as np
 import pytest
 
-from helpers import accum_replay, event_fields
+from helpers import (accum_replay, cfar_config, clutter_edge_cells, event_fields, hadamard_case,
+                     orthogonal_pair, rne15)
 from rdgb import abi, chain as gc, scenario as sc
 
 pytestmark = pytest.mark.gpu
@@ -297,3 +298,62 @@ def test_packetize_vs_oracle(gpulib, port, pw):
     # every flit has odd parity (packet_model.hpp:221-226)
     pop = np.array([sum(bin(int(v)).count("1") for v in row) for row in g])
     assert (pop % 2 == 1).all()
+
+
+# ---- directed and metamorphic cases of the reference's block tests (their
+# oracle-side twins are in test_oracle.py)
+
+def test_hadamard_bank_directed(gpulib, port):
+    A, frames = 16, 200
+    w, x, row, s = hadamard_case(A, frames, np.random.default_rng(21))
+    g = gc.bf(A, A, w, x)
+    for a, b in zip(g, port.bf(A, A, w, x)):
+        assert np.array_equal(a, b)
+    yr, yi = sc.unpack(g[0].reshape(frames, A))
+    want = np.zeros((frames, A), np.int64)
+    want[np.arange(frames), row] = rne15(A * 32767 * s)
+    assert np.array_equal(yr, want) and not yi.any() and not g[2].any()
+
+
+def test_cfar_clutter_edge_ca_vs_go(gpulib, port):
+    cells = clutter_edge_cells()
+    got = {}
+    for mode in (abi.RD_CFAR_CA, abi.RD_CFAR_GO):
+        cfg = cfar_config(mode, abi.RD_CFAR_EVENTS, 2, 2, 8, 8, 384)
+        ev = gc.cfar(cells, 128, cfg, [0])
+        assert np.array_equal(ev, port.cfar(cells, 128, cfg, [0]))
+        got[mode] = event_fields(ev)
+    ca, go = got[abi.RD_CFAR_CA], got[abi.RD_CFAR_GO]
+    det_ca = set(ca["bin"][ca["kind"] == 0].tolist())
+    assert det_ca and det_ca <= set(range(64, 72))
+    assert not (go["kind"] == 0).any()
+
+
+@pytest.mark.parametrize("mode", [abi.RD_CFAR_CA, abi.RD_CFAR_GO])
+def test_cfar_halving_invariance(gpulib, port, mode):
+    rng = np.random.default_rng(22 + mode)
+    n, frames = 256, 12
+    half = rng.integers(0, 4000, frames * n).astype(np.int64)
+    half[rng.integers(0, half.size, 60)] *= 30
+    cfg = cfar_config(mode, abi.RD_CFAR_DENSE, 2, 3, 8, 12, 900)
+    ea = gc.cfar(half, n, cfg, np.arange(frames))
+    eb = gc.cfar(2 * half, n, cfg, np.arange(frames))
+    assert np.array_equal(ea, port.cfar(half, n, cfg, np.arange(frames)))
+    assert np.array_equal(eb, port.cfar(2 * half, n, cfg, np.arange(frames)))
+    a, b = event_fields(ea), event_fields(eb)
+    assert (a["kind"] == 0).sum() > 20
+    for k in ("kind", "bin", "frame_id", "ref_cnt", "det", "sup"):
+        assert np.array_equal(a[k], b[k]), k
+    assert np.array_equal(2 * a["cut"], b["cut"]) and np.array_equal(2 * a["sum"], b["sum"])
+
+
+def test_cross_power_orthogonal(gpulib, port):
+    rng = np.random.default_rng(23)
+    x = rnd(rng, 4000)
+    re, im = sc.unpack(x)
+    x = sc.pack(re, np.where(im == -32768, 0, im))
+    y = orthogonal_pair(x)
+    c = gc.cross_power(x, y)
+    assert np.array_equal(c, port.cross_power(x, y))
+    c = c.reshape(-1, 2)
+    assert not c[:, 0].any() and np.array_equal(c[:, 1], -gc.power(x))

@@ -481,3 +481,22 @@ def test_depth_and_engine_random(gpulib, port, seed):
             assert (np.array_equal(vg, vo), fg, lg) == (True, fo, lo), off
         start += nf
     g.close()
+
+
+@pytest.mark.parametrize("form", [abi.RD_FORM_CUDA_CORE, abi.RD_FORM_TENSOR])
+def test_exp_covariance_every_k(gpulib, port, form):
+    # the exponential covariance mode at every k = 0..15 (test_covariance.cpp
+    # sweeps them), in two calls, against the oracle
+    p = sc.preset("tiny", cov_window=5)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    px, py = sc.pair_table(p)
+    x = sc.adc(p, 40 * p.n_fft)
+    for k in range(16):
+        cfg = sc.make_config(p, max_frames=16, form=form)
+        cfg.cov_mode, cfg.cov_exp_k, cfg.cov_acc_w = abi.RD_COV_EXP, k, 40
+        g, o = gc.Chain(cfg, coeff, w, (px, py)), port.chain(cfg, coeff, w, px, py)
+        for lo, hi in ((0, 17), (17, 40)):
+            xs = x[:, lo * p.n_fft:hi * p.n_fft]
+            assert diff(g.process(xs), o.process(xs, threads=2)) == [], (k, lo)
+            assert diff_stats(g.stats(), o.stats()) == [], (k, lo)
+        assert diff(g.flush_cov(), o.flush_cov(), ("cov_windows", "cov_acc")) == [], k

@@ -6,8 +6,9 @@ import numpy as np
 import pytest
 
 from conftest import load_chain_fixture
-from helpers import (CHAIN_KEYS, TAP_KEYS, accum_replay, banks, cfg_from_fixture, diff,
-                     diff_stats, fixture_stats, weight_sets)
+from helpers import (CHAIN_KEYS, TAP_KEYS, accum_replay, banks, cfar_config, cfg_from_fixture,
+                     clutter_edge_cells, diff, diff_stats, event_fields, fixture_stats,
+                     hadamard_case, orthogonal_pair, rnd, rne15, weight_sets)
 from rdgb import abi, scenario as sc
 from rdgb.twiddle import DIGEST, TWIDDLES
 
@@ -376,3 +377,71 @@ def test_depth_and_engine_random_vs_reference(port, refo, seed):
             assert [np.asarray(v).tolist() for v in a.read_history(3, off)] == \
                    [np.asarray(v).tolist() for v in b.read_history(3, off)], off
         start += nf
+
+
+# ---- directed and metamorphic cases of the reference's block tests, on the
+# oracle (their GPU twins are in test_gpu_blocks.py and test_gpu_chain.py)
+
+def test_hadamard_bank_directed(port):
+    # test_beamformer.cpp's orthogonal bank: each input is one bank row, so
+    # one beam carries it and the others are exactly zero
+    A, frames = 16, 200
+    w, x, row, s = hadamard_case(A, frames, np.random.default_rng(21))
+    y, _, fl = port.bf(A, A, w, x)
+    yr, yi = sc.unpack(y.reshape(frames, A))
+    want = np.zeros((frames, A), np.int64)
+    want[np.arange(frames), row] = rne15(A * 32767 * s)
+    assert np.array_equal(yr, want) and not yi.any() and not fl.any()
+
+
+def test_cfar_clutter_edge_ca_vs_go(port):
+    cells = clutter_edge_cells()
+    ca = event_fields(port.cfar(cells, 128, cfar_config(abi.RD_CFAR_CA, abi.RD_CFAR_EVENTS,
+                                                        2, 2, 8, 8, 384), [0]))
+    go = event_fields(port.cfar(cells, 128, cfar_config(abi.RD_CFAR_GO, abi.RD_CFAR_EVENTS,
+                                                        2, 2, 8, 8, 384), [0]))
+    det_ca = set(ca["bin"][ca["kind"] == 0].tolist())
+    assert det_ca and det_ca <= set(range(64, 72))
+    assert not (go["kind"] == 0).any()
+
+
+@pytest.mark.parametrize("mode", [abi.RD_CFAR_CA, abi.RD_CFAR_GO])
+def test_cfar_halving_invariance(port, mode):
+    # test_pipeline_metamorphic.cpp: exact halving of every cell leaves the
+    # detections as they are (the threshold test is homogeneous)
+    rng = np.random.default_rng(22 + mode)
+    n, frames = 256, 12
+    half = rng.integers(0, 4000, frames * n).astype(np.int64)
+    half[rng.integers(0, half.size, 60)] *= 30
+    cfg = cfar_config(mode, abi.RD_CFAR_DENSE, 2, 3, 8, 12, 900)
+    a = event_fields(port.cfar(half, n, cfg, np.arange(frames)))
+    b = event_fields(port.cfar(2 * half, n, cfg, np.arange(frames)))
+    assert (a["kind"] == 0).sum() > 20
+    for k in ("kind", "bin", "frame_id", "ref_cnt", "det", "sup"):
+        assert np.array_equal(a[k], b[k]), k
+    assert np.array_equal(2 * a["cut"], b["cut"]) and np.array_equal(2 * a["sum"], b["sum"])
+
+
+def test_cross_power_orthogonal(port):
+    rng = np.random.default_rng(23)
+    x = rnd(rng, 4000)
+    re, im = sc.unpack(x)
+    x = sc.pack(re, np.where(im == -32768, 0, im))
+    c = port.cross_power(x, orthogonal_pair(x)).reshape(-1, 2)
+    assert not c[:, 0].any() and np.array_equal(c[:, 1], -port.power(x))
+
+
+def test_exp_covariance_every_k_vs_reference(port, refo):
+    # test_covariance.cpp sweeps the exponential mode's k = 0..15
+    p = sc.preset("tiny", cov_window=5)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    px, py = sc.pair_table(p)
+    x = sc.adc(p, 40 * p.n_fft)
+    for k in range(16):
+        cfg = sc.make_config(p)
+        cfg.cov_mode, cfg.cov_exp_k, cfg.cov_acc_w = abi.RD_COV_EXP, k, 40
+        a, b = port.chain(cfg, coeff, w, px, py), refo.chain(cfg, coeff, w, px, py)
+        ra, rb = a.process(x, threads=2), b.process(x)
+        assert diff(ra, rb) == [], k
+        assert diff_stats(a.stats(), b.stats()) == [], k
+        assert diff(a.flush_cov(), b.flush_cov(), ("cov_windows", "cov_acc")) == [], k
