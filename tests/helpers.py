@@ -152,6 +152,38 @@ def clutter_edge_cells(n: int = 128, edge: int = 64, lo: int = 100, hi: int = 20
     return c
 
 
+def delayed_input(x: np.ndarray, frames: int, n_fft: int) -> np.ndarray:
+    """The ADC input [C][n] behind `frames` frames of zeros."""
+    return np.concatenate([np.zeros((x.shape[0], frames * n_fft), np.uint32), x], axis=1)
+
+
+def check_delayed(a: dict, b: dict, d: int, n_beams: int, window: int) -> None:
+    """Delay invariance (test_pipeline_metamorphic.cpp): `b` is the chain's
+    output for its input behind d zero frames, `a` for the input alone. The
+    delay line starts at zero, so the zero frames leave no trace: they add
+    one CFAR summary event per beam and frame (no detection, cfar_model.hpp
+    run_frame) and all-zero covariance windows (d a multiple of the window);
+    after them every event and window equals `a`'s with the frame ids, end
+    frames and window ids moved on by the delay."""
+    fa, fb = event_fields(a["events"]), event_fields(b["events"])
+    lead = d * n_beams
+    assert len(fb["kind"]) == len(fa["kind"]) + lead
+    assert (fb["kind"][:lead] == 3).all() and not fb["det"][:lead].any()
+    for k in fa:
+        if k != "frame_id":
+            assert np.array_equal(fa[k], fb[k][lead:]), k
+    assert np.array_equal((fa["frame_id"] + d) & 0xFFFF, fb["frame_id"][lead:])
+    assert d % window == 0
+    nz = d // window
+    assert not b["cov_acc"][:nz].any()
+    assert np.array_equal(a["cov_acc"], b["cov_acc"][nz:])
+    wa, wb = a["cov_windows"], b["cov_windows"][nz:]
+    for k in ("sample_count", "flushed", "truncated", "sat_flags"):
+        assert np.array_equal(wa[k], wb[k]), k
+    assert np.array_equal(wa["end_frame"] + d, wb["end_frame"])
+    assert np.array_equal((wa["window_id"] + nz) & 0xFFFF, wb["window_id"])
+
+
 def orthogonal_pair(x: np.ndarray) -> np.ndarray:
     """j x for packed {im, re} samples whose imaginary part is not -32768:
     x conj(j x) = -j |x|^2, a cross power with real part 0."""

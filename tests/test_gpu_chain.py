@@ -6,8 +6,8 @@ import numpy as np
 import pytest
 
 from conftest import load_chain_fixture
-from helpers import (CHAIN_KEYS, TAP_KEYS, cfg_from_fixture, diff, diff_stats, event_fields,
-                     fixture_stats)
+from helpers import (CHAIN_KEYS, TAP_KEYS, cfg_from_fixture, check_delayed, delayed_input, diff,
+                     diff_stats, event_fields, fixture_stats)
 from rdgb import abi, chain as gc, scenario as sc
 
 pytestmark = pytest.mark.gpu
@@ -500,3 +500,32 @@ def test_exp_covariance_every_k(gpulib, port, form):
             assert diff(g.process(xs), o.process(xs, threads=2)) == [], (k, lo)
             assert diff_stats(g.stats(), o.stats()) == [], (k, lo)
         assert diff(g.flush_cov(), o.flush_cov(), ("cov_windows", "cov_acc")) == [], k
+
+
+def _run_calls(ch, x, n_fft, calls):
+    """Runs x in calls of the given frame counts; the outputs concatenated."""
+    outs, f0 = [], 0
+    for nf in calls:
+        outs.append(ch.process(x[:, f0 * n_fft:(f0 + nf) * n_fft]))
+        f0 += nf
+    assert f0 * n_fft == x.shape[1]
+    return {k: np.concatenate([o[k] for o in outs]) for k in ("events", "cov_windows", "cov_acc")}
+
+
+@pytest.mark.parametrize("name,form,calls", [("tiny", abi.RD_FORM_CUDA_CORE, (7, 30, 19)),
+                                             ("medium", abi.RD_FORM_TENSOR, (5, 29, 22))])
+def test_delay_invariance(gpulib, port, name, form, calls):
+    # test_pipeline_metamorphic.cpp: the input behind 16 zero frames, run in
+    # uneven calls over short launches, leaves every output as it was
+    p = sc.preset(name, cov_window=8)
+    cfg = sc.make_config(p, max_frames=12, form=form)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    px, py = sc.pair_table(p)
+    x = sc.adc(p, 40 * p.n_fft)
+    xd = delayed_input(x, 16, p.n_fft)
+    a = gc.Chain(cfg, coeff, w, (px, py)).process(x)
+    b = _run_calls(gc.Chain(cfg, coeff, w, (px, py)), xd, p.n_fft, calls)
+    assert (event_fields(a["events"])["kind"] == 0).any()
+    check_delayed(a, b, 16, p.n_beams, 8)
+    o = port.chain(cfg, coeff, w, px, py).process(xd, threads=2)
+    assert diff(b, o, ("events", "cov_windows", "cov_acc")) == []

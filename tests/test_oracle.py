@@ -7,8 +7,9 @@ import pytest
 
 from conftest import load_chain_fixture
 from helpers import (CHAIN_KEYS, TAP_KEYS, accum_replay, banks, cfar_config, cfg_from_fixture,
-                     clutter_edge_cells, diff, diff_stats, event_fields, fixture_stats,
-                     hadamard_case, orthogonal_pair, rnd, rne15, weight_sets)
+                     check_delayed, clutter_edge_cells, delayed_input, diff, diff_stats,
+                     event_fields, fixture_stats, hadamard_case, orthogonal_pair, rnd, rne15,
+                     weight_sets)
 from rdgb import abi, scenario as sc
 from rdgb.twiddle import DIGEST, TWIDDLES
 
@@ -445,3 +446,16 @@ def test_exp_covariance_every_k_vs_reference(port, refo):
         assert diff(ra, rb) == [], k
         assert diff_stats(a.stats(), b.stats()) == [], k
         assert diff(a.flush_cov(), b.flush_cov(), ("cov_windows", "cov_acc")) == [], k
+
+
+def test_delay_invariance(port):
+    # test_pipeline_metamorphic.cpp: the input behind zero frames
+    p = sc.preset("tiny", cov_window=8)
+    cfg = sc.make_config(p)
+    coeff, w = sc.coefficients(p.n_fft, p.taps), sc.steering_weights(p.n_chan, p.n_beams)
+    px, py = sc.pair_table(p)
+    x = sc.adc(p, 60 * p.n_fft)
+    a = port.chain(cfg, coeff, w, px, py).process(x)
+    b = port.chain(cfg, coeff, w, px, py).process(delayed_input(x, 16, p.n_fft))
+    assert (event_fields(a["events"])["kind"] == 0).any()
+    check_delayed(a, b, 16, p.n_beams, 8)
