@@ -283,8 +283,16 @@ def test_serving_admission_by_budget(gpulib):
     assert srv.close_stream(a) == abi.RD_OK
     st3, _ = srv.open(cfg, co, w)
     assert st3 == abi.RD_OK
-    # the queue holds two requests; the third is pushed back
     x = sc.adc(p, 4096)
+    # malformed requests are refused before they take a queue slot: no such
+    # stream, samples that are not whole frames, more than a request may
+    # hold, none at all
+    assert srv.submit(999, x)[0] == abi.RD_EINVAL
+    assert srv.submit(b, x[:, :4096 - p.n_fft // 2])[0] == abi.RD_EINVAL
+    assert b"a multiple of" in gc.lib().rd_last_error()
+    assert srv.submit(b, sc.adc(p, 8192))[0] == abi.RD_EINVAL
+    assert srv.submit(b, x[:, :0])[0] == abi.RD_EINVAL
+    # the queue holds two requests; the third is pushed back
     assert srv.submit(b, x)[0] == abi.RD_OK
     assert srv.submit(b, x)[0] == abi.RD_OK
     assert srv.submit(b, x)[0] == abi.RD_EAGAIN
