@@ -9,6 +9,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "fxp.cuh"
@@ -1389,6 +1390,8 @@ struct StateHeader {
   rd_stats host_st;
   uint64_t tail_words, acc_words, eng_words, total_bytes;
 };
+// the header travels as raw bytes: no member may own memory
+static_assert(std::is_trivially_copyable<StateHeader>::value, "the state header must be plain data");
 
 struct StateSizes {
   uint64_t tail_words, acc_words, eng_words, ring_frames, frame_words, total;
@@ -1439,7 +1442,8 @@ rd_status rd_chain_save_state(rd_chain* ch, void* buf, uint64_t cap) {
   CK(cudaStreamSynchronize(ch->stream));
   if (ch->out_stream) CK(cudaStreamSynchronize(ch->out_stream));
   unsigned char* p = static_cast<unsigned char*>(buf);
-  StateHeader h{};
+  StateHeader h;
+  std::memset(static_cast<void*>(&h), 0, sizeof(h));  // padding too: equal states, equal blobs
   std::memcpy(h.magic, kStateMagic, 8);
   h.version = 1;
   h.cfg_bytes = sizeof(rd_config);
