@@ -86,3 +86,32 @@ def test_no_cpu_fallback(lib):
     assert b"device" in lib.rd_last_error()
     x = np.zeros(64, np.uint32)
     assert lib.rd_fft_run(64, 2, 0xFFFFFFFF, 1, abi.ptr(x), 1, abi.ptr(x), None, None) == abi.RD_EDEVICE
+
+
+def test_footprint(lib):
+    """rd_chain_footprint, the figure the server admits streams against: 0
+    for an invalid configuration; linear in the launch size, by exactly the
+    per-frame buffers of the data layout (spectrum ring, power cells, CFAR
+    counts and emit mask, PFB pass outputs); more with covariance on and
+    with the tensor form's operands; never below the resident buffers."""
+    bad = sc.make_config(sc.preset("tiny"))
+    bad.n_fft = 12
+    assert lib.rd_chain_footprint(C.byref(bad), 16) == 0
+    for name in ("tiny", "medium", "full"):
+        p = sc.preset(name)
+        N, Cn, B, D, H = p.n_fft, p.n_chan, p.n_beams, p.taps - 1, p.hist_frames
+
+        def fp(frames, form=abi.RD_FORM_CUDA_CORE, cov=True, per_call=16):
+            cfg = sc.make_config(p, max_frames=frames, form=form)
+            if not cov:
+                cfg.cov_source = abi.RD_COV_OFF
+            return lib.rd_chain_footprint(C.byref(cfg), per_call)
+
+        per_frame = N * Cn * 4 + B * N * 4 + B * 20 + B * ((N + 31) // 32) * 4 + Cn * N * 4
+        assert fp(1024) - fp(256) == 768 * per_frame, name
+        assert fp(4096) - fp(1024) == 3072 * per_frame, name
+        for f in (256, 4096):
+            resident = (f + H) * N * Cn * 4 + f * B * N * 4 + 2 * Cn * D * N * 4
+            assert fp(f) > resident, (name, f)
+            assert fp(f, form=abi.RD_FORM_TENSOR) > fp(f) > fp(f, cov=False), (name, f)
+            assert fp(f, per_call=256) >= fp(f, per_call=16), (name, f)
